@@ -1,0 +1,197 @@
+/*
+ * qgw_gpu.h -- C ABI of libqgw_gpu.so, the GB300 (sm_103a) time-stepping
+ * engine of the multi-layer quasi-geostrophic model qgw.
+ *
+ * The reference program keeps its whole state in globals and advances it
+ * with four C functions that the driver calls directly:
+ *
+ *   invert_pv(q, psi)        src/elliptic.h:149   (called at src/qg.c:167,188)
+ *   timestep(q)              src/timestep.h:386   (called at src/qg.c:197)
+ *   rhs(q, f)                src/dynamics.h:47    (inside timestep)
+ *   adjust_timestep(psi)     src/timestep.h:341   (inside timestep)
+ *
+ * plus the host-side set-up read_params (src/extra.h:118),
+ * compute_eigmode (src/eigmode.h:87) and check_timestep (src/timestep.h:290).
+ * This header replaces that global-state interface with an opaque run handle.
+ * A host driver that used to call the functions above calls the entry points
+ * below instead; fields cross the boundary in the reference's own array
+ * layout, so output code written against the reference stays unchanged.
+ *
+ * Array layout at the boundary ("reference layout"): a 3-D field is
+ * (nl, ny+2, nx+2) row-major doubles with a one-point ghost/wall ring,
+ * element (i, j, k) at k*(ny+2)*(nx+2) + j*(nx+2) + i, exactly the idx()
+ * macro of src/domain.h:62.  For a closed basin (bc_fac >= 0) the interior
+ * sizes are nx = NX-1, ny = NY-1 (src/domain.h:71-74).
+ *
+ * Conventions: every entry point returns 0 on success or a negative
+ * qgw_status; nothing in the library calls exit().  All device memory is
+ * owned by the library; host arrays are owned by the caller and are only
+ * read/written during the call that receives them.  One run handle may be
+ * used from one host thread at a time.
+ */
+#ifndef QGW_GPU_H
+#define QGW_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QGW_ABI_VERSION 1
+
+/* Largest number of layers a params struct can describe.  The reference
+ * sizes its dh/N2 arrays with nl_max = 1000 (src/qg.c:45); the GPU kernels
+ * accept nl <= QGW_NL_GPU_MAX. */
+#define QGW_NL_MAX 64
+#define QGW_NL_GPU_MAX 32
+
+typedef enum qgw_status {
+  QGW_OK = 0,
+  QGW_ERR_PARAM = -1,       /* invalid or unsupported parameter            */
+  QGW_ERR_FILE = -2,        /* params file missing (reference: exit(0))    */
+  QGW_ERR_CUDA = -3,        /* a CUDA runtime call failed                  */
+  QGW_ERR_NOMEM = -4,       /* device or host allocation failed            */
+  QGW_ERR_NAN = -5,         /* NaN/Inf detected in the state               */
+  QGW_ERR_UNSUPPORTED = -6, /* configuration outside what the kernels do   */
+  QGW_ERR_EIGEN = -7,       /* stretching-matrix eigensolver failed        */
+  QGW_ERR_STATE = -8,       /* call out of order (e.g. step before set_q)  */
+  QGW_ERR_ADMISSION = -9,   /* pool: request does not fit the HBM budget   */
+  QGW_ERR_TIMEOUT = -10,    /* a bounded device wait gave up               */
+  QGW_ERR_NOT_READY = -11   /* pool: result not available yet              */
+} qgw_status;
+
+typedef enum qgw_precision {
+  QGW_FP64 = 0,  /* plain FP64: the drop-in step                           */
+  QGW_FP32C = 1  /* FP32 arithmetic, q kept as an FP32 hi+lo pair           */
+} qgw_precision;
+
+/* Every key the reference registers from params.in (src/qg.c:113-137),
+ * with the reference's defaults (src/qg.c:57-83, src/forcing.h:13-14,38-39),
+ * plus one optional extra key `dt` (fixed time step; 0 = adaptive, the
+ * reference behaviour).  The reference parser ignores unknown keys, so a
+ * params.in carrying `dt` still drives the reference unchanged. */
+typedef struct qgw_params {
+  int NX, NY, nl, n_hyper;
+  double Lx;
+  double dh[QGW_NL_MAX];
+  double N2[QGW_NL_MAX];
+  double tau0, forc_mode, f0, beta, nu, nu_hyper, hEkb, Ld;
+  double h_topo, w_topo, bc_fac, tend, dt_out;
+  double dt_forc, dt_forc_period, sigma_f, k_f, cfl;
+  double dt;  /* extra key: fixed dt when > 0 */
+} qgw_params;
+
+/* Time-stepping scalars of a run (the reference globals t, dt, dt0, dt1,
+ * DT_max, src/qg.c:63-69 and src/timestep.h:286). */
+typedef struct qgw_time {
+  double t, dt, dt0, dt1, DT_max;
+} qgw_time;
+
+typedef struct qgw_step_info {
+  qgw_time time;   /* after the last step taken                        */
+  int steps_taken; /* <= nsteps; fewer when a stop condition was hit    */
+  int stop_reason; /* 0 = nsteps done, 1 = reached t_out, 2 = reached tend */
+  int nonfinite;   /* 1 if a NaN/Inf was seen in the CFL reduction       */
+} qgw_step_info;
+
+/* FP64 domain diagnostics (no reference counterpart in C; the energy and
+ * enstrophy formulas follow test/test_energy_injection.py:24-25).  All sums
+ * are over interior points and weighted by Delta^2/(Lx*Ly). */
+typedef struct qgw_budget_out {
+  double ke;          /* sum_k dh_k/H * 1/2 |grad psi_k|^2 (one-sided, as CFL) */
+  double energy;      /* -sum_k dh_k/H * psi_k q_k  (test_energy_injection.py) */
+  double enstrophy;   /* sum_k dh_k/H * q_k^2                                  */
+  double wind_work;   /* -dh_0/H * psi_0 * forcing_q  (rate of energy input)   */
+} qgw_budget_out;
+
+typedef struct qgw_run qgw_run;
+
+/* ---- host-side set-up (no GPU needed) ---------------------------------- */
+
+/* Fill p with the reference defaults (src/qg.c:57-83). */
+void qgw_params_default(qgw_params* p);
+
+/* Parse a params.in file into p (which should hold defaults first).
+ * Same grammar as read_params, src/extra.h:118-153: lines `key = value` or
+ * `key = [a, b, ...]`, spaces ignored, unknown keys and comments ignored.
+ * Returns QGW_ERR_FILE where the reference calls exit(0). */
+int qgw_params_read(qgw_params* p, const char* path);
+
+/* Vertical modes of the stretching matrix: replaces compute_eigmode,
+ * src/eigmode.h:87-271 (LAPACKE_dgeev there, a symmetric-tridiagonal
+ * Jacobi solver here; the Flierl normalisation makes both give the same
+ * result).  cl2m, cm2l are nl*nl row-major, iRd2 has nl entries. */
+int qgw_eigmode(const qgw_params* p, double* cl2m, double* cm2l, double* iRd2);
+
+/* Maximum and initial time step: replaces check_timestep,
+ * src/timestep.h:290-326, including its operator-precedence quirks. */
+int qgw_check_timestep(const qgw_params* p, double* DT_max, double* dt);
+
+/* Topography on the reference layout (ny+2, nx+2): init_vars,
+ * src/domain.h:200-207. */
+int qgw_topo(const qgw_params* p, double* topo);
+
+/* ---- one run on one GPU ------------------------------------------------ */
+
+/* Create a run on the current CUDA device.  cl2m/cm2l/iRd2 may be NULL, in
+ * which case qgw_eigmode() is used.  topo may be NULL (flat bottom, or the
+ * analytic shelf of qgw_topo() when h_topo != 0); otherwise it is a
+ * (ny+2, nx+2) reference-layout array.  The time scalars start as the
+ * reference's init_timestep leaves them (src/timestep.h:328-339), or at the
+ * fixed dt when p->dt > 0.  q starts at zero. */
+int qgw_create(const qgw_params* p, const double* cl2m, const double* cm2l,
+               const double* iRd2, const double* topo, int precision,
+               qgw_run** out);
+
+/* Release the run and its device memory. */
+void qgw_destroy(qgw_run* run);
+
+/* Copy q in (reference layout; ghost values are ignored).  Replaces the
+ * restart read of q, src/qg.c:160-164.  Clears the AB3 history. */
+int qgw_set_q(qgw_run* run, const double* q);
+
+/* Same, from a device pointer holding the reference layout. */
+int qgw_set_q_device(qgw_run* run, const double* q_dev);
+
+/* Read and overwrite the time scalars (t, dt, dt0, dt1, DT_max). */
+int qgw_get_time(qgw_run* run, qgw_time* out);
+int qgw_set_time(qgw_run* run, const qgw_time* in);
+
+/* Advance up to nsteps reference time steps (timestep(), src/timestep.h:386).
+ * t_out is the next output time used by the dt snapping of
+ * adjust_timestep (src/timestep.h:369-381); pass 0 for none.  Mirrors the
+ * driver loop src/qg.c:181-199: before each step, stop if t >= tend
+ * (tend <= 0: no limit) or |t - t_out| < 1e-9*dt.  Work stays on the device
+ * between steps; the call returns after the last step has finished. */
+int qgw_step(qgw_run* run, int nsteps, double t_out, double tend,
+             qgw_step_info* info);
+
+/* Recompute psi from the current q (invert_pv, src/elliptic.h:149). */
+int qgw_invert(qgw_run* run);
+
+/* Copy psi and/or q out in the reference layout (either may be NULL).  The
+ * ghost ring is what the reference holds after invert_pv:
+ * psi = 0, q = 2*bc_fac/Delta^2 * psi_adjacent (src/domain.h:308-348).
+ * psi is the inversion of the current q (qgw_invert is implied). */
+int qgw_get(qgw_run* run, double* psi, double* q);
+
+/* FP64 diagnostics of the current state (implies qgw_invert). */
+int qgw_budget(qgw_run* run, qgw_budget_out* out);
+
+/* Device bytes held by a run of these parameters (admission control). */
+int qgw_footprint(const qgw_params* p, int precision, size_t* bytes);
+
+/* Launch sequencing for measurement: the CUDA stream the run uses
+ * (cudaStream_t as void*) and the number of kernels one step launches. */
+void* qgw_stream(qgw_run* run);
+int qgw_kernels_per_step(qgw_run* run);
+
+const char* qgw_strerror(int status);
+int qgw_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QGW_GPU_H */

@@ -1,0 +1,43 @@
+/*
+ * oracle_math.h -- CPU numerics shared by the oracle (test infrastructure
+ * only: used by tests/, the smoke check and the CPU baseline of bench.py,
+ * never by the product library).
+ *
+ * - DST-I (FFTW's RODFT00 definition, the transform the reference plans at
+ *   src/elliptic.h:136-139):  Y_k = 2 sum_{j=0}^{n-1} X_j sin(pi (j+1)(k+1)/(n+1)).
+ *   Two implementations: a direct O(n^2) sum with an exactly reduced sine
+ *   table, and an O(n log n) one through a half-length complex FFT (used when
+ *   n+1 is a power of two).
+ * - eigen-decomposition of a real tridiagonal matrix whose off-diagonal
+ *   products are positive (the reference's stretching matrix,
+ *   src/eigmode.h:105-119), by diagonal similarity to a symmetric matrix and
+ *   cyclic Jacobi rotations.
+ */
+#ifndef QGW_ORACLE_MATH_H
+#define QGW_ORACLE_MATH_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* In-place DST-I of `howmany` rows of length n, rows `stride` doubles apart,
+ * elements `dist` doubles apart within a row. */
+void om_dst1_direct(int n, int howmany, double* data, int stride, int dist);
+void om_dst1_fast(int n, int howmany, double* data, int stride, int dist);
+/* Fast when n+1 is a power of two, direct otherwise. */
+void om_dst1(int n, int howmany, double* data, int stride, int dist);
+
+/* 2-D DST-I of a row-major (n0 rows, n1 columns) array in place. */
+void om_dst2(int n0, int n1, double* data, int fast);
+
+/* Eigen-decomposition of a row-major n x n matrix a that is tridiagonal
+ * with a[i][i+1]*a[i+1][i] > 0 (or both zero).  Outputs as LAPACK dgeev with
+ * row-major storage: eigenvalues w (unsorted), right eigenvectors in the
+ * columns of vr, left eigenvectors in the columns of vl, each column of unit
+ * 2-norm.  Returns 0, or -1 when a is not of that form. */
+int om_tridiag_eig(int n, const double* a, double* w, double* vl, double* vr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
