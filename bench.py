@@ -1,0 +1,425 @@
+#!/usr/bin/env python3
+"""Benchmark of the qgw time step on GB300.
+
+Workload: the closed double-gyre basin at NX = NY = 1024 (1023^2 interior
+points) with 10 stretched layers, biharmonic viscosity 1e9 m^4/s, fixed
+dt = 600 s, seeded Gaussian q of std 1e-7 s^-1 (synthetic data).  One bench
+step is one model time step (the reference's timestep(), src/timestep.h:386).
+
+Metric: layer-gridpoint-steps/s = nl * (NX-1)^2 * steps / seconds, for the
+plain FP64 path (``value``), with the FP32-compensated path reported beside it
+(``fp32c``).  ``value`` is device-timed with the state resident in HBM;
+``e2e`` goes through the C ABI with host buffers: every step copies q in
+from pinned memory (qgw_put_q), steps, and copies q out (qgw_get).
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+``--impl reference`` times the reference's CPU step instead: the C
+restatement of the reference step (oracle/qgw_port.c), one full-size model
+step per worker per bench step, on every host core (independent replicas:
+the reference's MPI build cannot run without MPI).  Under torchrun every rank
+runs an independent replica (no collective on the data path; the barrier and
+the max over ranks are for timing only).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+HBM_FALLBACK_GBS = 6800.0
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nx", type=int, default=1024)
+    ap.add_argument("--nl", type=int, default=10)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp32c", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=0, help="0: same as --steps")
+    return ap.parse_args()
+
+
+def workload(nx, nl):
+    from qgw_gb300 import configs
+    return configs.cfg2(nx, nl)
+
+
+def lgp_of(p):
+    from qgw_gb300 import configs
+    return configs.lgp(p)
+
+
+# ------------------------------------------------------------- CPU baseline
+def _port_worker_init(nx, nl, seed):
+    global _PORT
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from qgw_gb300 import configs
+    p = workload(nx, nl)
+    _PORT = oracle.Port(p)
+    _PORT.set_q(configs.noise_ic(p, seed))
+    _PORT.fix_dt(600.0)
+
+
+def _port_worker_step(n):
+    t0 = time.perf_counter()
+    _PORT.step(n)
+    return time.perf_counter() - t0
+
+
+def cpu_pool(nx, nl, workers):
+    import multiprocessing as mp
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build(ref=False)  # the port only: the reference sources never travel
+    ctx = mp.get_context("spawn")
+    return ctx.Pool(workers, initializer=_port_worker_init, initargs=(nx, nl, 12345))
+
+
+def cpu_measure(pool, workers, lgp, steps, warmup):
+    """Aggregate lgp-steps/s of `workers` concurrent full-size runs."""
+    for _ in range(warmup):
+        pool.map(_port_worker_step, [1] * workers)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        pool.map(_port_worker_step, [1] * workers)
+    wall = time.perf_counter() - t0
+    return workers * lgp * steps / wall, wall
+
+
+# ------------------------------------------------------------------ clocks
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.gpu = gpu_index
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-i", str(self.gpu), "-lms", "50"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [l.strip().split(",") for l in self.f.read().splitlines() if l.strip()]
+        sm, mx, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                power.append(float(r[3]))
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w_max": max(power) if power else None}
+
+
+# --------------------------------------------------------------- roofline
+def bytes_per_lgp(precision):
+    """Algorithmic HBM bytes per layer-gridpoint of each step kernel:
+    rows forward reads q, f0, f1, f2 and writes q and the spectral field;
+    columns read/write the spectral field (+ the FP64 Helmholtz table);
+    rows inverse read the spectral field and write psi; the RHS reads psi and
+    q and writes f0."""
+    if precision == 0:
+        return [48.0, 24.0, 16.0, 24.0]
+    return [32.0, 8.0, 8.0, 12.0]
+
+
+def fp64_ops_per_lgp(nl, M, nsweep):
+    """FP64-pipe instructions (add, mul and fma each count one) per
+    layer-gridpoint of each kernel, from the kernels' arithmetic: DST-I of
+    length M-1 = pre-processing 2 + complex FFT of M/2 points (radix-8 first
+    pass 52/8 per point, later passes 80/8, radix-4/2 tails) / 2 + split 3 +
+    prefix sum 1."""
+    H = M // 2
+    rem, passes = H, []
+    while rem >= 8:
+        passes.append(8)
+        rem //= 8
+    if rem > 1:
+        passes.append(rem)
+    fft = 0.0
+    for i, R in enumerate(passes):
+        base = {8: 52, 4: 16, 2: 4}[R]
+        tw = 0 if i == 0 else 4 * (R - 1)
+        fft += (base + tw) / R
+    dst = 2 + fft / 2 + 3 + 1
+    k1 = 3 + nl + dst
+    k2 = 2 * dst + 1
+    k3 = dst + nl
+    k4 = 4.4 + 10 + 2 + (4 * nsweep * 1.2 + 1 if nsweep else 0) + 2 + 0.5
+    return [k1, k2, k3, k4]
+
+
+def read_measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+def read_traffic(precision):
+    """Per-launch DRAM traffic of the dominant kernel from the committed ncu
+    summary (profiles/traffic.json), if present."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get("fp64" if precision == 0 else "fp32c")
+    except (OSError, ValueError):
+        return None
+
+
+KERNEL_NAMES = ["rows_fwd (AB3 + projection + x-DST)", "cols (y-DST, Helmholtz, inverse y-DST)",
+                "rows_inv (inverse x-DST + back-projection)", "rhs (Jacobian, viscosity, forcing, CFL)"]
+
+
+# -------------------------------------------------------------------- ours
+def run_ours(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+    from qgw_gb300 import build, capi, configs
+
+    torch.cuda.set_device(local_rank)
+    build.build()
+    p = workload(args.nx, args.nl)
+    lgp = lgp_of(p)
+    q0 = configs.noise_ic(p, 2000)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    def timed(precision, K, W, clocks=None):
+        run = capi.Run(p, precision)
+        run.set_q(q0)
+        run.fix_dt(600.0)
+        run.step(W)
+        stream = torch.cuda.ExternalStream(run.stream())
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        barrier()
+        torch.cuda.synchronize()
+        if clocks:
+            clocks.start()
+        e0.record(stream)
+        info = run.step(K)
+        e1.record(stream)
+        e1.synchronize()
+        cl = clocks.stop() if clocks else None
+        torch.cuda.synchronize()
+        barrier()
+        assert info.steps_taken == K, (info.steps_taken, K)
+        ms = max_over_ranks(e0.elapsed_time(e1))
+        kms = run.profile_kernels(5)
+        return run, ms, kms, cl
+
+    K, W = args.steps, args.warmup
+    clocks = Clocks(local_rank)
+    run64, ms64, kms64, cl = timed(0, K, W, clocks)
+    value = world * lgp * K / (ms64 / 1e3)
+
+    hbm_peak, peak_kind = read_measured_peaks()
+    fp64_peak, fp32_peak = capi.probe_fp_rates()
+    M = args.nx
+    nsweep = 3  # n_hyper = 4: n_hyper/2 + 1 Laplacian sweeps
+    bpl = bytes_per_lgp(0)
+    dom = max(range(4), key=lambda k: kms64[k])
+    achieved = bpl[dom] * lgp / (kms64[dom] / 1e3) / 1e9
+    ops = fp64_ops_per_lgp(args.nl, M, nsweep)
+    fp64_rate = ops[dom] * 2 * lgp / (kms64[dom] / 1e3) / 1e12  # one FMA slot = 2 flops
+    roofline = {"bound": "hbm", "kernel": KERNEL_NAMES[dom], "achieved": achieved, "peak": hbm_peak,
+                "unit": "GB/s", "frac": achieved / hbm_peak, "peak_source": peak_kind,
+                "traffic": read_traffic(0), "bytes_per_lgp": bpl[dom],
+                "kernel_ms": kms64[dom], "all_kernels_ms": kms64}
+    roofline_fp64 = {"bound": "fp64", "kernel": KERNEL_NAMES[dom], "achieved": fp64_rate,
+                     "peak": fp64_peak, "unit": "TFLOP/s (FMA-slot equivalent)",
+                     "frac": fp64_rate / fp64_peak if fp64_peak > 0 else None,
+                     "ops_per_lgp_model": ops[dom],
+                     "step_frac": sum(o * 2 * lgp for o in ops) / (ms64 / K / 1e3) / 1e12 / fp64_peak
+                     if fp64_peak > 0 else None,
+                     "peak_source": "measured live (qgw_probe_fp_rates)"}
+
+    # e2e: per step, q in from pinned host memory, one step, q out
+    E = args.e2e_steps or K
+    shape = run64.shape
+    qh = torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    qo = torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    run64.get(q=qh, want=("q",))
+    for _ in range(2):
+        run64.put_q(qh)
+        run64.step(1)
+        run64.get(q=qo, want=("q",))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(E):
+        run64.put_q(qh)
+        run64.step(1)
+        run64.get(q=qo, want=("q",))
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    interior_bytes = args.nl * (args.nx - 1) ** 2 * 8
+    e2e = {"value": world * lgp * E / e2e_s, "unit": "lgp-steps/s", "steps": E,
+           "h2d_bytes_per_step": interior_bytes, "d2h_bytes_per_step": interior_bytes,
+           "api": "qgw_put_q + qgw_step(1) + qgw_get(q) per step, pinned host buffers"}
+    run64.close()
+
+    fp32c = None
+    if not args.no_fp32c:
+        run32, ms32, kms32, _ = timed(1, K, W)
+        run32.close()
+        v32 = world * lgp * K / (ms32 / 1e3)
+        b32 = bytes_per_lgp(1)
+        dom32 = max(range(4), key=lambda k: kms32[k])
+        ach32 = b32[dom32] * lgp / (kms32[dom32] / 1e3) / 1e9
+        step_bytes = sum(b32) * lgp / (ms32 / K / 1e3) / 1e9
+        # accuracy against the FP64 path after 10 and 100 steps
+        errs = {}
+        for n in (10, 100):
+            outs = []
+            for prec in (0, 1):
+                r = capi.Run(p, prec)
+                r.set_q(q0)
+                r.fix_dt(600.0)
+                r.step(n)
+                outs.append(r.get())
+                r.close()
+            (psi64, q64), (psi32, q32) = outs
+            errs[f"rel_l2_q_{n}"] = float(np.linalg.norm(q32 - q64) / np.linalg.norm(q64))
+            errs[f"rel_l2_psi_{n}"] = float(np.linalg.norm(psi32 - psi64) / np.linalg.norm(psi64))
+        fp32c = {"value": v32, "unit": "lgp-steps/s", "ms_per_step": ms32 / K, "speedup_vs_fp64": v32 / value,
+                 "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[dom32], "achieved": ach32, "peak": hbm_peak,
+                              "unit": "GB/s", "frac": ach32 / hbm_peak, "traffic": read_traffic(1),
+                              "all_kernels_ms": kms32, "step_achieved_gbs": step_bytes,
+                              "step_frac": step_bytes / hbm_peak},
+                 "error_vs_fp64": errs, "dtype": "f32 (q as f32 hi+lo)"}
+
+    if rank != 0:
+        return None
+    cpu = None
+    if getattr(args, "_cpu", None) is not None:
+        cpu = args._cpu
+    launches = K * 4 + 3
+    out = {
+        "metric": "layer-gridpoint-steps/s at 1024^2 x 10 layers (plain FP64 step)",
+        "value": value, "unit": "lgp-steps/s", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": ms64 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded Gaussian q, std 1e-7 s^-1)",
+        "config": {"workload": f"closed double-gyre basin NX=NY={args.nx}, nl={args.nl}, biharmonic 1e9, "
+                               f"dt=600 s, fixed-dt mode", "NX": args.nx, "nl": args.nl,
+                   "lgp_per_step": lgp, "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": f"inputs larger than L2: FP64 working set "
+                         f"{7 * args.nl * (args.nx - 1) * args.nx * 8 / 1e6:.0f} MB per step"},
+        "roofline": roofline, "roofline_fp64": roofline_fp64,
+        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": cl,
+        "fp32c": fp32c,
+        "fp64_tflops_measured": fp64_peak, "fp32_tflops_measured": fp32_peak,
+    }
+    return out
+
+
+def run_reference(args):
+    p = workload(args.nx, args.nl)
+    lgp = lgp_of(p)
+    workers = os.cpu_count() or 1
+    pool = cpu_pool(args.nx, args.nl, workers)
+    value, wall = cpu_measure(pool, workers, lgp, args.steps, args.warmup)
+    pool.close()
+    pool.join()
+    cpu = {"value": value, "unit": "lgp-steps/s", "cores": workers, "kind": "port",
+           "sample": f"{workers} concurrent full-size runs ({args.nx}^2 x {args.nl}), one model step each "
+                     f"per bench step, {args.steps} timed + {args.warmup} warm-up bench steps; the C "
+                     f"restatement of the reference step (oracle/qgw_port.c), O(n log n) DST"}
+    return {
+        "impl": "reference",
+        "metric": "layer-gridpoint-steps/s at 1024^2 x 10 layers (plain FP64 step)",
+        "value": value, "unit": "lgp-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"closed double-gyre basin NX=NY={args.nx}, nl={args.nl}, biharmonic 1e9, "
+                               f"dt=600 s", "NX": args.nx, "nl": args.nl, "lgp_per_step": lgp,
+                   "parallelism": f"{workers} independent CPU replicas"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": value, "unit": "lgp-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        print(json.dumps(run_reference(args)))
+        return 0
+    # CPU baseline first, before any CUDA context exists (spawned workers)
+    args._cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        p = workload(args.nx, args.nl)
+        workers = os.cpu_count() or 1
+        pool = cpu_pool(args.nx, args.nl, workers)
+        v, wall = cpu_measure(pool, workers, lgp_of(p), steps=2, warmup=1)
+        pool.close()
+        pool.join()
+        args._cpu = {"value": v, "unit": "lgp-steps/s", "cores": workers, "kind": "port",
+                     "sample": f"{workers} concurrent full-size runs, 1 warm-up + 2 timed model steps each "
+                               f"({wall:.1f} s); oracle/qgw_port.c, the C restatement of the reference step"}
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group(backend="nccl", init_method="env://")
+    out = run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

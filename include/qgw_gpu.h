@@ -120,9 +120,9 @@ void qgw_params_default(qgw_params* p);
 int qgw_params_read(qgw_params* p, const char* path);
 
 /* Vertical modes of the stretching matrix: replaces compute_eigmode,
- * src/eigmode.h:87-271 (LAPACKE_dgeev there, a symmetric-tridiagonal
- * Jacobi solver here; the Flierl normalisation makes both give the same
- * result).  cl2m, cm2l are nl*nl row-major, iRd2 has nl entries. */
+ * src/eigmode.h:87-271 (LAPACKE_dgeev there, the implicit-QL
+ * symmetric-tridiagonal solver here; the Flierl normalisation makes both
+ * give the same result).  cl2m, cm2l are nl*nl row-major, iRd2 has nl entries. */
 int qgw_eigmode(const qgw_params* p, double* cl2m, double* cm2l, double* iRd2);
 
 /* Maximum and initial time step: replaces check_timestep,
@@ -155,6 +155,12 @@ int qgw_set_q(qgw_run* run, const double* q);
 /* Same, from a device pointer holding the reference layout. */
 int qgw_set_q_device(qgw_run* run, const double* q_dev);
 
+/* Replace q but keep the AB3 history: the reference's timestep(q)
+ * (src/timestep.h:386) works on the caller's q array while f0/f1/f2 stay in
+ * globals, so a driver that owns q on the host calls qgw_put_q, qgw_step(1),
+ * qgw_get(NULL, q) per step.  Requires a prior qgw_set_q. */
+int qgw_put_q(qgw_run* run, const double* q);
+
 /* Read and overwrite the time scalars (t, dt, dt0, dt1, DT_max). */
 int qgw_get_time(qgw_run* run, qgw_time* out);
 int qgw_set_time(qgw_run* run, const qgw_time* in);
@@ -174,7 +180,8 @@ int qgw_invert(qgw_run* run);
 /* Copy psi and/or q out in the reference layout (either may be NULL).  The
  * ghost ring is what the reference holds after invert_pv:
  * psi = 0, q = 2*bc_fac/Delta^2 * psi_adjacent (src/domain.h:308-348).
- * psi is the inversion of the current q (qgw_invert is implied). */
+ * psi is the inversion of the current q (qgw_invert is implied when psi is
+ * requested, or for q when bc_fac != 0). */
 int qgw_get(qgw_run* run, double* psi, double* q);
 
 /* FP64 diagnostics of the current state (implies qgw_invert). */
@@ -187,6 +194,16 @@ int qgw_footprint(const qgw_params* p, int precision, size_t* bytes);
  * (cudaStream_t as void*) and the number of kernels one step launches. */
 void* qgw_stream(qgw_run* run);
 int qgw_kernels_per_step(qgw_run* run);
+
+/* Run nsteps steps with CUDA events between the four kernels of each step
+ * and return each kernel's mean duration in ms: ms4[0] rows forward
+ * (AB3 + projection + x-DST), ms4[1] columns (y-DST, Helmholtz divide,
+ * inverse y-DST), ms4[2] rows inverse (x-DST + back-projection), ms4[3] RHS. */
+int qgw_profile_kernels(qgw_run* run, int nsteps, float* ms4);
+
+/* Measured FMA throughput of the current device in TFLOP/s (FP64 and FP32,
+ * independent FMA chains): the arithmetic roofs of the FP64 kernels. */
+int qgw_probe_fp_rates(double* fp64_tflops, double* fp32_tflops);
 
 const char* qgw_strerror(int status);
 int qgw_abi_version(void);

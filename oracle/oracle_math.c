@@ -262,7 +262,7 @@ int om_tridiag_eig(int n, const double* a, double* w, double* vl, double* vr) {
     const double up = a[i * n + i + 1], lo = a[(i + 1) * n + i];
     const double pr = up * lo;
     if (pr > 0.0) {
-      d[i + 1] = d[i] * sqrt(lo / up);
+      d[i + 1] = d[i] * sqrt(up / lo); /* d_i^2 up = d_{i+1}^2 lo */
       const double off = (up > 0 ? 1.0 : -1.0) * sqrt(pr);
       s[i * n + i + 1] = off;
       s[(i + 1) * n + i] = off;

@@ -1,0 +1,239 @@
+"""ctypes binding of libqgw_gpu.so (include/qgw_gpu.h).
+
+``Run`` mirrors the reference's step interface on one GPU run:
+
+    reference (src/)                      this binding
+    read_params(params, "params.in")      read_params(path) -> dict-like struct
+    compute_eigmode()                     eigmode(params)
+    check_timestep()                      check_timestep(params)
+    invert_pv(q, psi)                     Run.invert()
+    timestep(q)                           Run.step(n)
+    q, psi globals                        Run.get() / Run.set_q()
+
+The library is loaded from the package's ``lib/`` directory; there is no
+fallback: a missing or unloadable library raises ``ImportError``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Dict, Optional
+
+import numpy as np
+
+from .params import QgwBudget, QgwParams, QgwStepInfo, QgwTime, halo_shape, to_struct
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libqgw_gpu.so")
+
+FP64 = 0
+FP32C = 1
+
+STATUS = {
+    0: "ok", -1: "invalid parameter", -2: "params file not found", -3: "CUDA runtime error",
+    -4: "out of memory", -5: "non-finite value in the state", -6: "configuration not supported",
+    -7: "eigensolver failed", -8: "call out of order", -9: "request exceeds the HBM budget",
+    -10: "device wait timed out", -11: "result not ready",
+}
+
+# Every entry point declared in include/qgw_gpu.h (checked by the CPU tests).
+EXPORTS = [
+    "qgw_params_default", "qgw_params_read", "qgw_eigmode", "qgw_check_timestep", "qgw_topo",
+    "qgw_create", "qgw_destroy", "qgw_set_q", "qgw_set_q_device", "qgw_put_q", "qgw_get_time", "qgw_set_time",
+    "qgw_step", "qgw_invert", "qgw_get", "qgw_budget", "qgw_footprint", "qgw_stream",
+    "qgw_kernels_per_step", "qgw_profile_kernels", "qgw_probe_fp_rates", "qgw_strerror", "qgw_abi_version",
+]
+
+
+class QgwError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        super().__init__(f"{where}: {STATUS.get(status, 'unknown')} ({status})")
+        self.status = status
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the library once; raises ImportError when it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: run qgw_gb300.build.build() first")
+    lib = ctypes.CDLL(path)
+    P, D, I, V = ctypes.POINTER, ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_void_p
+    pp = P(QgwParams)
+    lib.qgw_params_default.argtypes = [pp]
+    lib.qgw_params_default.restype = None
+    lib.qgw_params_read.argtypes = [pp, ctypes.c_char_p]
+    lib.qgw_eigmode.argtypes = [pp, D, D, D]
+    lib.qgw_check_timestep.argtypes = [pp, D, D]
+    lib.qgw_topo.argtypes = [pp, D]
+    lib.qgw_create.argtypes = [pp, D, D, D, D, I, P(V)]
+    lib.qgw_destroy.argtypes = [V]
+    lib.qgw_destroy.restype = None
+    lib.qgw_set_q.argtypes = [V, D]
+    lib.qgw_set_q_device.argtypes = [V, V]
+    lib.qgw_put_q.argtypes = [V, D]
+    lib.qgw_get_time.argtypes = [V, P(QgwTime)]
+    lib.qgw_set_time.argtypes = [V, P(QgwTime)]
+    lib.qgw_step.argtypes = [V, I, ctypes.c_double, ctypes.c_double, P(QgwStepInfo)]
+    lib.qgw_invert.argtypes = [V]
+    lib.qgw_get.argtypes = [V, D, D]
+    lib.qgw_budget.argtypes = [V, P(QgwBudget)]
+    lib.qgw_footprint.argtypes = [pp, I, P(ctypes.c_size_t)]
+    lib.qgw_stream.argtypes = [V]
+    lib.qgw_stream.restype = V
+    lib.qgw_kernels_per_step.argtypes = [V]
+    lib.qgw_profile_kernels.argtypes = [V, I, P(ctypes.c_float)]
+    lib.qgw_probe_fp_rates.argtypes = [D, D]
+    lib.qgw_strerror.argtypes = [I]
+    lib.qgw_strerror.restype = ctypes.c_char_p
+    lib.qgw_abi_version.argtypes = []
+    _lib = lib
+    return lib
+
+
+def _check(rc: int, where: str):
+    if rc != 0:
+        raise QgwError(rc, where)
+
+
+def _dp(a: Optional[np.ndarray]):
+    if a is None:
+        return None
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def read_params(path: str) -> QgwParams:
+    lib = load()
+    s = QgwParams()
+    lib.qgw_params_default(ctypes.byref(s))
+    _check(lib.qgw_params_read(ctypes.byref(s), path.encode()), "qgw_params_read")
+    return s
+
+
+def eigmode(params: Dict[str, object]):
+    lib = load()
+    s = to_struct(params)
+    nl = s.nl
+    a, b, c = np.empty((nl, nl)), np.empty((nl, nl)), np.empty(nl)
+    _check(lib.qgw_eigmode(ctypes.byref(s), _dp(a), _dp(b), _dp(c)), "qgw_eigmode")
+    return a, b, c
+
+
+def check_timestep(params: Dict[str, object]):
+    lib = load()
+    s = to_struct(params)
+    DT, dt = ctypes.c_double(), ctypes.c_double()
+    _check(lib.qgw_check_timestep(ctypes.byref(s), ctypes.byref(DT), ctypes.byref(dt)), "qgw_check_timestep")
+    return DT.value, dt.value
+
+
+def probe_fp_rates():
+    """Measured (FP64, FP32) FMA throughput of the current GPU in TFLOP/s."""
+    lib = load()
+    a, b = ctypes.c_double(), ctypes.c_double()
+    _check(lib.qgw_probe_fp_rates(ctypes.byref(a), ctypes.byref(b)), "qgw_probe_fp_rates")
+    return a.value, b.value
+
+
+def footprint(params: Dict[str, object], precision: int = FP64) -> int:
+    lib = load()
+    s = to_struct(params)
+    b = ctypes.c_size_t()
+    _check(lib.qgw_footprint(ctypes.byref(s), int(precision), ctypes.byref(b)), "qgw_footprint")
+    return int(b.value)
+
+
+class Run:
+    """One qgw run resident on the current CUDA device."""
+
+    def __init__(self, params: Dict[str, object], precision: int = FP64,
+                 topo: Optional[np.ndarray] = None, modes=None):
+        self.lib = load()
+        self.params = params
+        self.precision = precision
+        self._s = to_struct(params)
+        self.shape = halo_shape(params)
+        h = ctypes.c_void_p()
+        cl = cm = ird = None
+        if modes is not None:
+            cl, cm, ird = (np.ascontiguousarray(m, dtype=np.float64) for m in modes)
+        tp = None if topo is None else np.ascontiguousarray(topo, dtype=np.float64)
+        _check(self.lib.qgw_create(ctypes.byref(self._s), _dp(cl), _dp(cm), _dp(ird), _dp(tp),
+                                   int(precision), ctypes.byref(h)), "qgw_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.qgw_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_q(self, q: np.ndarray):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        if q.shape != self.shape:
+            raise ValueError(f"q has shape {q.shape}, expected {self.shape}")
+        _check(self.lib.qgw_set_q(self.h, _dp(q)), "qgw_set_q")
+
+    def put_q(self, q: np.ndarray):
+        """Replace q, keeping the AB3 history (per-step host driver)."""
+        _check(self.lib.qgw_put_q(self.h, _dp(q)), "qgw_put_q")
+
+    def set_q_device(self, ptr: int):
+        _check(self.lib.qgw_set_q_device(self.h, ctypes.c_void_p(ptr)), "qgw_set_q_device")
+
+    def time(self) -> Dict[str, float]:
+        t = QgwTime()
+        _check(self.lib.qgw_get_time(self.h, ctypes.byref(t)), "qgw_get_time")
+        return {"t": t.t, "dt": t.dt, "dt0": t.dt0, "dt1": t.dt1, "DT_max": t.DT_max}
+
+    def set_time(self, t=0.0, dt=0.0, dt0=None, dt1=None, DT_max=None):
+        tm = QgwTime(t, dt, dt if dt0 is None else dt0, dt if dt1 is None else dt1,
+                     dt if DT_max is None else DT_max)
+        _check(self.lib.qgw_set_time(self.h, ctypes.byref(tm)), "qgw_set_time")
+
+    def fix_dt(self, dt: float):
+        self.set_time(0.0, dt, dt, dt, dt)
+
+    def step(self, n: int = 1, t_out: float = 0.0, tend: float = 0.0) -> QgwStepInfo:
+        info = QgwStepInfo()
+        _check(self.lib.qgw_step(self.h, int(n), float(t_out), float(tend), ctypes.byref(info)), "qgw_step")
+        return info
+
+    def invert(self):
+        _check(self.lib.qgw_invert(self.h), "qgw_invert")
+
+    def get(self, psi: Optional[np.ndarray] = None, q: Optional[np.ndarray] = None, want=("psi", "q")):
+        if psi is None and "psi" in want:
+            psi = np.empty(self.shape)
+        if q is None and "q" in want:
+            q = np.empty(self.shape)
+        _check(self.lib.qgw_get(self.h, _dp(psi), _dp(q)), "qgw_get")
+        return psi, q
+
+    def budget(self) -> Dict[str, float]:
+        b = QgwBudget()
+        _check(self.lib.qgw_budget(self.h, ctypes.byref(b)), "qgw_budget")
+        return {"ke": b.ke, "energy": b.energy, "enstrophy": b.enstrophy, "wind_work": b.wind_work}
+
+    def stream(self) -> int:
+        return int(self.lib.qgw_stream(self.h) or 0)
+
+    def profile_kernels(self, nsteps: int):
+        ms = (ctypes.c_float * 4)()
+        _check(self.lib.qgw_profile_kernels(self.h, int(nsteps), ms), "qgw_profile_kernels")
+        return [float(x) for x in ms]

@@ -1,0 +1,610 @@
+// api.cu -- the C ABI of libqgw_gpu.so (include/qgw_gpu.h): run creation,
+// boundary copies in the reference layout, the device-resident step loop
+// and diagnostics.  All device memory of a run is allocated in qgw_create
+// and released in qgw_destroy.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "../../include/qgw_gpu.h"
+#include "dst_tables.h"
+#include "host.h"
+#include "kernels.h"
+#include "qgw_device.cuh"
+
+using qgw::DevState;
+using qgw::DstGeom;
+using qgw::StepArgs;
+
+struct qgw_run {
+  int precision = 0;
+  qgw_params p{};
+  int nx = 0, ny = 0, nl = 0, pitch = 0;
+  size_t lstride = 0;
+  double Delta = 0, Ly = 0, norm = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<void*> allocs;
+  DevState* d_state = nullptr;
+  DevState* h_state = nullptr;  // pinned
+  double* d_stage = nullptr;    // FP64 staging field (compensated path)
+  double* d_wts = nullptr;
+  double* d_part = nullptr;
+  double* d_bout = nullptr;
+  int budget_blocks = 0;
+  StepArgs<double> a64{};
+  StepArgs<float> a32{};
+  std::vector<double> cl2m, cm2l, iRd2;
+  bool has_q = false;
+};
+
+namespace {
+
+int cuda_fail(cudaError_t e) {
+  if (e == cudaSuccess) return QGW_OK;
+  if (e == cudaErrorMemoryAllocation) return QGW_ERR_NOMEM;
+  return QGW_ERR_CUDA;
+}
+#define CK(x)                                  \
+  do {                                         \
+    cudaError_t e_ = (x);                      \
+    if (e_ != cudaSuccess) return cuda_fail(e_); \
+  } while (0)
+
+bool pow2(int v) { return v >= 4 && (v & (v - 1)) == 0; }
+
+template <typename T>
+int dalloc(qgw_run* r, T** out, size_t count) {
+  void* ptr = nullptr;
+  cudaError_t e = cudaMalloc(&ptr, count * sizeof(T) + 16);
+  if (e != cudaSuccess) return cuda_fail(e);
+  r->allocs.push_back(ptr);
+  e = cudaMemsetAsync(ptr, 0, count * sizeof(T) + 16, r->stream);
+  if (e != cudaSuccess) return cuda_fail(e);
+  *out = (T*)ptr;
+  return QGW_OK;
+}
+
+template <typename T>
+int upload(qgw_run* r, T** out, const std::vector<double>& host) {
+  std::vector<T> tmp(host.begin(), host.end());
+  int rc = dalloc(r, out, tmp.size());
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(*out, tmp.data(), tmp.size() * sizeof(T), cudaMemcpyHostToDevice, r->stream));
+  return cudaStreamSynchronize(r->stream) == cudaSuccess ? QGW_OK : QGW_ERR_CUDA;
+}
+
+// choose the modes per row block and the columns per column block so that
+// each block's two work buffers stay within the shared-memory budget
+void choose_groups(int nl, int Mx, int My, size_t elem, int* G1, int* CT) {
+  const size_t budget = 96 * 1024;
+  int g = (int)(budget / (2 * (size_t)Mx * elem));
+  if (g < 1) g = 1;
+  if (g > 16) g = 16;
+  const int ngroups = (nl + g - 1) / g;
+  *G1 = (nl + ngroups - 1) / ngroups;
+  int ct = (int)(budget / (2 * (size_t)My * elem));
+  if (ct < 1) ct = 1;
+  if (ct > 16) ct = 16;
+  *CT = ct;
+}
+
+template <typename T>
+int setup_args(qgw_run* r, StepArgs<T>& a) {
+  const qgw_params& p = r->p;
+  a.nx = r->nx;
+  a.ny = r->ny;
+  a.nl = r->nl;
+  a.pitch = r->pitch;
+  a.lstride = (long long)r->lstride;
+  a.gx = qgw::make_geom(r->nx + 1);
+  a.gy = qgw::make_geom(r->ny + 1);
+  int rc;
+  // DST tables for x and y
+  for (int dim = 0; dim < 2; ++dim) {
+    const int M = dim == 0 ? r->nx + 1 : r->ny + 1;
+    qgw::DstTablesHost th = qgw::build_dst_tables(M);
+    T *tw, *pre, *spl;
+    if ((rc = upload<T>(r, &tw, th.tw))) return rc;
+    if ((rc = upload<T>(r, &pre, th.pre))) return rc;
+    if ((rc = upload<T>(r, &spl, th.spl))) return rc;
+    qgw::DstTables<T>& t = dim == 0 ? a.tx : a.ty;
+    t.tw = (const qgw::C2<T>*)tw;
+    t.pre = (const qgw::C2<T>*)pre;
+    t.spl = (const qgw::C2<T>*)spl;
+  }
+  T *cl, *cm;
+  if ((rc = upload<T>(r, &cl, r->cl2m))) return rc;
+  if ((rc = upload<T>(r, &cm, r->cm2l))) return rc;
+  a.cl2m = cl;
+  a.cm2l = cm;
+  double* ird;
+  if ((rc = upload<double>(r, &ird, r->iRd2))) return rc;
+  a.iRd2 = ird;
+  const size_t field = (size_t)r->nl * r->lstride;
+  if ((rc = dalloc(r, &a.q, field))) return rc;
+  a.qlo = nullptr;
+  if (r->precision == QGW_FP32C && (rc = dalloc(r, &a.qlo, field))) return rc;
+  if ((rc = dalloc(r, &a.psi, field))) return rc;
+  if ((rc = dalloc(r, &a.spec, field))) return rc;
+  if ((rc = dalloc(r, &a.fab, 3 * field))) return rc;
+  std::vector<double> Lsq(r->nx), Ksq(r->ny);
+  for (int k = 0; k < r->nx; ++k) { const double L = M_PI * (k + 1) / p.Lx; Lsq[k] = L * L; }
+  for (int j = 0; j < r->ny; ++j) { const double K = M_PI * (j + 1) / p.Lx; Ksq[j] = K * K; }
+  double *dL, *dK;
+  if ((rc = upload<double>(r, &dL, Lsq))) return rc;
+  if ((rc = upload<double>(r, &dK, Ksq))) return rc;
+  a.Lsq = dL;
+  a.Ksq = dK;
+  a.hinv = nullptr;
+  if (r->precision == QGW_FP64) {
+    // 1 / (fact * norm), fact = -(sq(L[i]) + sq(K[j]) + iRd2[k]) as in
+    // invert_pv, src/elliptic.h:195-200 and the /norm of :207-211
+    std::vector<double> h(field, 0.0);
+    for (int m = 0; m < r->nl; ++m)
+      for (int j = 0; j < r->ny; ++j)
+        for (int k = 0; k < r->nx; ++k) {
+          const double fact = -(Lsq[k] + Ksq[j] + r->iRd2[m]);
+          h[(size_t)m * r->lstride + (size_t)j * r->pitch + k] = 1.0 / (fact * r->norm);
+        }
+    double* dh;
+    if ((rc = upload<double>(r, &dh, h))) return rc;
+    a.hinv = dh;
+  }
+  std::vector<double> wind(r->ny);
+  for (int j = 0; j < r->ny; ++j) wind[j] = qgw_host_wind(&p, j + 1);
+  T* dw;
+  if ((rc = upload<T>(r, &dw, wind))) return rc;
+  a.wind = dw;
+  a.topo = nullptr;
+  a.state = r->d_state;
+  a.Delta = r->Delta;
+  a.norm = r->norm;
+  a.cfl = p.cfl;
+  a.inv12d2 = 1.0 / (12. * r->Delta * r->Delta);
+  a.b2d = p.beta / (2 * r->Delta);
+  a.nu_d2 = p.nu / (r->Delta * r->Delta);
+  a.has_nu = p.nu != 0;
+  const double nuh = qgw_host_nu_hyper(&p);
+  // calc_diff runs n_hyper/2+1 Laplacian sweeps (src/dynamics.h:25); the
+  // term is nu_hyper * lap_n_diff, identically zero when nu_hyper == 0
+  int sweeps = p.n_hyper >= 0 ? p.n_hyper / 2 + 1 : 0;
+  if (nuh == 0) sweeps = 0;
+  if (sweeps > 7) return QGW_ERR_UNSUPPORTED;
+  a.nsweep = sweeps;
+  a.nuh_scaled = sweeps ? nuh / std::pow(r->Delta, 2.0 * sweeps) : 0.0;
+  a.cbc = 2 * p.bc_fac / (r->Delta * r->Delta);
+  for (int s = 0; s < 8; ++s) a.gh[s] = (s >= 1) ? 2 * p.bc_fac * std::pow(r->Delta, 2.0 * s - 2) : 0.0;
+  const double dhb = p.dh[r->nl - 1];
+  a.drag_d2 = -p.hEkb * p.f0 / (2 * dhb) / (r->Delta * r->Delta);
+  a.has_drag = p.hEkb != 0;
+  a.topo_fac = p.f0 / dhb;
+  a.has_topo = 0;
+  a.has_wind = p.tau0 != 0;
+  choose_groups(r->nl, r->nx + 1, r->ny + 1, sizeof(T), &a.G1, &a.CT);
+  a.low_k64 = 8;
+  return QGW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qgw_abi_version(void) { return QGW_ABI_VERSION; }
+
+const char* qgw_strerror(int s) {
+  switch (s) {
+    case QGW_OK: return "ok";
+    case QGW_ERR_PARAM: return "invalid parameter";
+    case QGW_ERR_FILE: return "params file not found";
+    case QGW_ERR_CUDA: return "CUDA runtime error";
+    case QGW_ERR_NOMEM: return "out of memory";
+    case QGW_ERR_NAN: return "non-finite value in the state";
+    case QGW_ERR_UNSUPPORTED: return "configuration not supported by the GPU kernels";
+    case QGW_ERR_EIGEN: return "stretching-matrix eigensolver failed";
+    case QGW_ERR_STATE: return "call out of order";
+    case QGW_ERR_ADMISSION: return "request exceeds the HBM budget";
+    case QGW_ERR_TIMEOUT: return "device wait timed out";
+    case QGW_ERR_NOT_READY: return "result not ready";
+    default: return "unknown status";
+  }
+}
+
+int qgw_footprint(const qgw_params* p, int precision, size_t* bytes) {
+  if (!p || !bytes) return QGW_ERR_PARAM;
+  const size_t nx = p->NX - (p->bc_fac >= 0 ? 1 : 0), ny = p->NY - (p->bc_fac >= 0 ? 1 : 0);
+  const size_t field = (size_t)p->nl * ny * (nx + 1);
+  size_t b;
+  if (precision == QGW_FP64) b = field * 8 * 7;  // q psi spec f0 f1 f2 hinv
+  else b = field * 4 * 7 + field * 8;            // q_hi q_lo psi spec f0 f1 f2 + FP64 staging
+  *bytes = b + (size_t)(nx + ny) * 64 + (1 << 20);
+  return QGW_OK;
+}
+
+int qgw_create(const qgw_params* pin, const double* cl2m, const double* cm2l, const double* iRd2,
+               const double* topo, int precision, qgw_run** out) {
+  if (!pin || !out) return QGW_ERR_PARAM;
+  *out = nullptr;
+  if (precision != QGW_FP64 && precision != QGW_FP32C) return QGW_ERR_PARAM;
+  const qgw_params& p = *pin;
+  if (p.bc_fac < 0) return QGW_ERR_UNSUPPORTED;            // periodic basin
+  if (p.k_f != 0 || p.dt_forc_period != 0) return QGW_ERR_UNSUPPORTED;  // stochastic / 4-D forcing
+  if (!pow2(p.NX) || !pow2(p.NY) || p.NX > 8192 || p.NY > 8192) return QGW_ERR_UNSUPPORTED;
+  if (p.nl < 1 || p.nl > QGW_NL_GPU_MAX) return QGW_ERR_UNSUPPORTED;
+  if (!(p.Lx > 0) || !(p.cfl > 0)) return QGW_ERR_PARAM;
+  qgw_run* r = new qgw_run();
+  r->precision = precision;
+  r->p = p;
+  r->nx = p.NX - 1;
+  r->ny = p.NY - 1;
+  r->nl = p.nl;
+  r->pitch = r->nx + 1;
+  r->lstride = (size_t)r->ny * r->pitch;
+  r->Delta = p.Lx / p.NX;
+  r->Ly = p.NY * r->Delta;
+  r->norm = 4.0 * (r->nx + 1) * (r->ny + 1);
+  r->cl2m.resize((size_t)r->nl * r->nl);
+  r->cm2l.resize((size_t)r->nl * r->nl);
+  r->iRd2.resize(r->nl);
+  int rc = QGW_OK;
+  if (cl2m && cm2l && iRd2) {
+    std::memcpy(r->cl2m.data(), cl2m, sizeof(double) * r->nl * r->nl);
+    std::memcpy(r->cm2l.data(), cm2l, sizeof(double) * r->nl * r->nl);
+    std::memcpy(r->iRd2.data(), iRd2, sizeof(double) * r->nl);
+  } else if ((rc = qgw_eigmode(&p, r->cl2m.data(), r->cm2l.data(), r->iRd2.data()))) {
+    delete r;
+    return rc;
+  }
+  auto fail = [&](int code) {
+    qgw_destroy(r);
+    return code;
+  };
+  if (cudaGetDevice(&r->device) != cudaSuccess) return fail(QGW_ERR_CUDA);
+  if (cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(QGW_ERR_CUDA);
+  if (cudaMallocHost(&r->h_state, sizeof(DevState)) != cudaSuccess) return fail(QGW_ERR_NOMEM);
+  if ((rc = dalloc(r, &r->d_state, 1))) return fail(rc);
+  if (precision == QGW_FP64) {
+    if ((rc = setup_args<double>(r, r->a64))) return fail(rc);
+  } else {
+    if ((rc = setup_args<float>(r, r->a32))) return fail(rc);
+    if ((rc = dalloc(r, &r->d_stage, (size_t)r->nl * r->lstride))) return fail(rc);
+  }
+  // topography: explicit array, or the analytic shelf when h_topo != 0
+  std::vector<double> th;
+  const double* tsrc = topo;
+  if (!tsrc && p.h_topo != 0) {
+    th.resize((size_t)(r->nx + 2) * (r->ny + 2));
+    qgw_topo(&p, th.data());
+    tsrc = th.data();
+  }
+  if (tsrc) {
+    bool nz = false;
+    const size_t n2 = (size_t)(r->nx + 2) * (r->ny + 2);
+    for (size_t s = 0; s < n2 && !nz; ++s) nz = tsrc[s] != 0;
+    if (nz) {
+      std::vector<double> tv(tsrc, tsrc + n2);
+      double* dt;
+      if ((rc = upload<double>(r, &dt, tv))) return fail(rc);
+      r->a64.topo = dt;
+      r->a64.has_topo = 1;
+      r->a32.topo = dt;
+      r->a32.has_topo = 1;
+    }
+  }
+  // FP64 diagnostics buffers
+  std::vector<double> w(r->nl);
+  double H = 0;
+  for (int k = 0; k < r->nl; ++k) H += p.dh[k];
+  for (int k = 0; k < r->nl; ++k) w[k] = p.dh[k] / H;
+  if ((rc = upload<double>(r, &r->d_wts, w))) return fail(rc);
+  r->budget_blocks = 304;
+  if ((rc = dalloc(r, &r->d_part, (size_t)4 * r->budget_blocks))) return fail(rc);
+  if ((rc = dalloc(r, &r->d_bout, 4))) return fail(rc);
+  // initial time scalars: init_timestep (src/timestep.h:328-339), or the
+  // fixed dt of the optional `dt` key
+  DevState s{};
+  double DT, dt0;
+  if ((rc = qgw_check_timestep(&p, &DT, &dt0))) return fail(rc);
+  if (p.dt > 0) { DT = p.dt; dt0 = p.dt; }
+  s.t = 0; s.dt = dt0; s.dt0 = dt0; s.dt1 = dt0; s.DT_max = DT;
+  if (cudaMemcpyAsync(r->d_state, &s, sizeof(s), cudaMemcpyHostToDevice, r->stream) != cudaSuccess)
+    return fail(QGW_ERR_CUDA);
+  cudaError_t e = precision == QGW_FP64 ? qgw::prepare_f64(r->a64) : qgw::prepare_f32c(r->a32);
+  if (e != cudaSuccess) return fail(cuda_fail(e));
+  if (cudaStreamSynchronize(r->stream) != cudaSuccess) return fail(QGW_ERR_CUDA);
+  *out = r;
+  return QGW_OK;
+}
+
+void qgw_destroy(qgw_run* r) {
+  if (!r) return;
+  if (r->stream) cudaStreamSynchronize(r->stream);
+  for (void* ptr : r->allocs) cudaFree(ptr);
+  if (r->h_state) cudaFreeHost(r->h_state);
+  if (r->stream) cudaStreamDestroy(r->stream);
+  delete r;
+}
+
+void* qgw_stream(qgw_run* r) { return r ? (void*)r->stream : nullptr; }
+int qgw_kernels_per_step(qgw_run* r) { return r ? 4 : 0; }
+
+static cudaMemcpy3DParms copy_params(qgw_run* r, const void* src, bool src_ref, void* dst, bool dst_ref,
+                                     size_t elem) {
+  // reference layout: (nl, ny+2, nx+2), interior at (1, 1); device layout:
+  // (nl, ny, pitch), interior at (0, 0)
+  cudaMemcpy3DParms c{};
+  const size_t rw = (size_t)(r->nx + 2) * elem, dw = (size_t)r->pitch * elem;
+  if (src_ref) {
+    c.srcPtr = make_cudaPitchedPtr((void*)src, rw, r->nx + 2, r->ny + 2);
+    c.srcPos = make_cudaPos(elem, 1, 0);
+  } else {
+    c.srcPtr = make_cudaPitchedPtr((void*)src, dw, r->pitch, r->ny);
+    c.srcPos = make_cudaPos(0, 0, 0);
+  }
+  if (dst_ref) {
+    c.dstPtr = make_cudaPitchedPtr(dst, rw, r->nx + 2, r->ny + 2);
+    c.dstPos = make_cudaPos(elem, 1, 0);
+  } else {
+    c.dstPtr = make_cudaPitchedPtr(dst, dw, r->pitch, r->ny);
+    c.dstPos = make_cudaPos(0, 0, 0);
+  }
+  c.extent = make_cudaExtent((size_t)r->nx * elem, r->ny, r->nl);
+  c.kind = cudaMemcpyDefault;
+  return c;
+}
+
+static int reset_history(qgw_run* r) {
+  const size_t field = (size_t)r->nl * r->lstride;
+  void* fab = r->precision == QGW_FP64 ? (void*)r->a64.fab : (void*)r->a32.fab;
+  const size_t esz = r->precision == QGW_FP64 ? 8 : 4;
+  CK(cudaMemsetAsync(fab, 0, 3 * field * esz, r->stream));
+  // pending = 0, step_index = 0, maxbits = 0, done_blocks = 0
+  DevState* d = r->d_state;
+  CK(cudaMemsetAsync(&d->maxbits, 0, sizeof(unsigned long long), r->stream));
+  CK(cudaMemsetAsync(&d->done_blocks, 0, sizeof(unsigned int), r->stream));
+  CK(cudaMemsetAsync(&d->pending, 0, sizeof(int), r->stream));
+  CK(cudaMemsetAsync(&d->step_index, 0, sizeof(int), r->stream));
+  CK(cudaMemsetAsync(&d->nonfinite, 0, sizeof(int), r->stream));
+  return QGW_OK;
+}
+
+static int set_q_impl(qgw_run* r, const double* q, bool device_src) {
+  if (!r || !q) return QGW_ERR_PARAM;
+  (void)device_src;
+  if (r->precision == QGW_FP64) {
+    cudaMemcpy3DParms c = copy_params(r, q, true, r->a64.q, false, sizeof(double));
+    CK(cudaMemcpy3DAsync(&c, r->stream));
+  } else {
+    cudaMemcpy3DParms c = copy_params(r, q, true, r->d_stage, false, sizeof(double));
+    CK(cudaMemcpy3DAsync(&c, r->stream));
+    qgw::enqueue_split_f64(r->d_stage, r->a32.q, r->a32.qlo, (size_t)r->nl * r->lstride, r->stream);
+  }
+  int rc = reset_history(r);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(r->stream));
+  CK(cudaGetLastError());
+  r->has_q = true;
+  return QGW_OK;
+}
+
+int qgw_set_q(qgw_run* r, const double* q) { return set_q_impl(r, q, false); }
+int qgw_set_q_device(qgw_run* r, const double* q) { return set_q_impl(r, q, true); }
+
+int qgw_put_q(qgw_run* r, const double* q) {
+  if (!r || !q) return QGW_ERR_PARAM;
+  if (!r->has_q) return QGW_ERR_STATE;
+  if (r->precision == QGW_FP64) {
+    cudaMemcpy3DParms c = copy_params(r, q, true, r->a64.q, false, sizeof(double));
+    CK(cudaMemcpy3DAsync(&c, r->stream));
+  } else {
+    cudaMemcpy3DParms c = copy_params(r, q, true, r->d_stage, false, sizeof(double));
+    CK(cudaMemcpy3DAsync(&c, r->stream));
+    qgw::enqueue_split_f64(r->d_stage, r->a32.q, r->a32.qlo, (size_t)r->nl * r->lstride, r->stream);
+  }
+  CK(cudaStreamSynchronize(r->stream));
+  CK(cudaGetLastError());
+  return QGW_OK;
+}
+
+int qgw_get_time(qgw_run* r, qgw_time* out) {
+  if (!r || !out) return QGW_ERR_PARAM;
+  CK(cudaMemcpyAsync(r->h_state, r->d_state, sizeof(DevState), cudaMemcpyDeviceToHost, r->stream));
+  CK(cudaStreamSynchronize(r->stream));
+  out->t = r->h_state->t;
+  out->dt = r->h_state->dt;
+  out->dt0 = r->h_state->dt0;
+  out->dt1 = r->h_state->dt1;
+  out->DT_max = r->h_state->DT_max;
+  return QGW_OK;
+}
+
+int qgw_set_time(qgw_run* r, const qgw_time* in) {
+  if (!r || !in) return QGW_ERR_PARAM;
+  double v[5] = {in->t, in->dt, in->dt0, in->dt1, in->DT_max};
+  CK(cudaMemcpyAsync(r->d_state, v, sizeof(v), cudaMemcpyHostToDevice, r->stream));
+  CK(cudaStreamSynchronize(r->stream));
+  return QGW_OK;
+}
+
+static void enqueue_invert(qgw_run* r) {
+  if (r->precision == QGW_FP64) qgw::enqueue_invert_f64(r->a64, r->stream);
+  else qgw::enqueue_invert_f32c(r->a32, r->stream);
+}
+
+int qgw_step(qgw_run* r, int nsteps, double t_out, double tend, qgw_step_info* info) {
+  if (!r) return QGW_ERR_PARAM;
+  if (!r->has_q) return QGW_ERR_STATE;
+  if (nsteps < 0) return QGW_ERR_PARAM;
+  qgw::enqueue_begin(r->d_state, t_out, tend, r->stream);
+  const int chunk = 256;
+  int launched = 0;
+  while (launched < nsteps) {
+    const int n = (nsteps - launched) < chunk ? (nsteps - launched) : chunk;
+    for (int s = 0; s < n; ++s) {
+      if (r->precision == QGW_FP64) qgw::enqueue_step_f64(r->a64, r->stream);
+      else qgw::enqueue_step_f32c(r->a32, r->stream);
+    }
+    launched += n;
+    if (launched < nsteps) {
+      // stop launching once the device loop has ended
+      CK(cudaMemcpyAsync(r->h_state, r->d_state, sizeof(DevState), cudaMemcpyDeviceToHost, r->stream));
+      CK(cudaStreamSynchronize(r->stream));
+      if (!r->h_state->active) break;
+    }
+  }
+  if (r->precision == QGW_FP64) qgw::enqueue_flush_f64(r->a64, r->stream);
+  else qgw::enqueue_flush_f32c(r->a32, r->stream);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(r->h_state, r->d_state, sizeof(DevState), cudaMemcpyDeviceToHost, r->stream));
+  CK(cudaStreamSynchronize(r->stream));
+  const DevState& s = *r->h_state;
+  if (info) {
+    info->time.t = s.t;
+    info->time.dt = s.dt;
+    info->time.dt0 = s.dt0;
+    info->time.dt1 = s.dt1;
+    info->time.DT_max = s.DT_max;
+    info->steps_taken = s.steps_taken;
+    info->stop_reason = s.stop_reason;
+    info->nonfinite = s.nonfinite;
+  }
+  return s.nonfinite ? QGW_ERR_NAN : QGW_OK;
+}
+
+int qgw_invert(qgw_run* r) {
+  if (!r) return QGW_ERR_PARAM;
+  if (!r->has_q) return QGW_ERR_STATE;
+  enqueue_invert(r);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(r->stream));
+  return QGW_OK;
+}
+
+int qgw_get(qgw_run* r, double* psi, double* q) {
+  if (!r) return QGW_ERR_PARAM;
+  if (!r->has_q) return QGW_ERR_STATE;
+  // psi is the inversion of the current q; q alone needs it only for the
+  // ghost values of a no-slip or partial-slip wall
+  if (psi || r->p.bc_fac != 0) enqueue_invert(r);
+  const size_t field = (size_t)r->nl * r->lstride;
+  if (psi) {
+    const void* src = r->a64.psi;
+    if (r->precision != QGW_FP64) {
+      qgw::enqueue_join_f64(r->a32.psi, nullptr, r->d_stage, field, r->stream);
+      src = r->d_stage;
+    }
+    cudaMemcpy3DParms c = copy_params(r, src, false, psi, true, sizeof(double));
+    CK(cudaMemcpy3DAsync(&c, r->stream));
+  }
+  std::vector<double> psi_tmp;
+  if (q) {
+    const void* src = r->a64.q;
+    if (r->precision != QGW_FP64) {
+      CK(cudaStreamSynchronize(r->stream));
+      qgw::enqueue_join_f64(r->a32.q, r->a32.qlo, r->d_stage, field, r->stream);
+      src = r->d_stage;
+    }
+    cudaMemcpy3DParms c = copy_params(r, src, false, q, true, sizeof(double));
+    CK(cudaMemcpy3DAsync(&c, r->stream));
+  }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(r->stream));
+  // ghost rings as adjust_bc leaves them after invert_pv
+  // (src/elliptic.h:225-226, src/domain.h:308-348)
+  const int nxp2 = r->nx + 2, nyp2 = r->ny + 2;
+  const size_t L = (size_t)nxp2 * nyp2;
+  const double c = 2 * r->p.bc_fac / (r->Delta * r->Delta);
+  const double* ps = psi;
+  if (q && !psi && c != 0) {
+    psi_tmp.resize(L * r->nl);
+    cudaMemcpy3DParms cp = copy_params(r, r->precision == QGW_FP64 ? (const void*)r->a64.psi : (const void*)r->d_stage,
+                                       false, psi_tmp.data(), true, sizeof(double));
+    if (r->precision != QGW_FP64) qgw::enqueue_join_f64(r->a32.psi, nullptr, r->d_stage, field, r->stream);
+    CK(cudaMemcpy3DAsync(&cp, r->stream));
+    CK(cudaStreamSynchronize(r->stream));
+    ps = psi_tmp.data();
+  }
+  for (int k = 0; k < r->nl; ++k) {
+    double* P = psi ? psi + k * L : nullptr;
+    double* Q = q ? q + k * L : nullptr;
+    const double* PS = ps ? ps + k * L : nullptr;
+    for (int i = 0; i < nxp2; ++i) {
+      for (int jj : {0, nyp2 - 1}) {
+        if (P) P[(size_t)jj * nxp2 + i] = 0.0;
+        if (Q) {
+          const int ja = jj == 0 ? 1 : nyp2 - 2;
+          const bool corner = (i == 0 || i == nxp2 - 1);
+          Q[(size_t)jj * nxp2 + i] = (corner || c == 0) ? 0.0 : c * PS[(size_t)ja * nxp2 + i];
+        }
+      }
+    }
+    for (int j = 0; j < nyp2; ++j) {
+      for (int ii : {0, nxp2 - 1}) {
+        if (P) P[(size_t)j * nxp2 + ii] = 0.0;
+        if (Q) {
+          const int ia = ii == 0 ? 1 : nxp2 - 2;
+          const bool corner = (j == 0 || j == nyp2 - 1);
+          Q[(size_t)j * nxp2 + ii] = (corner || c == 0) ? 0.0 : c * PS[(size_t)j * nxp2 + ia];
+        }
+      }
+    }
+  }
+  return QGW_OK;
+}
+
+int qgw_budget(qgw_run* r, qgw_budget_out* out) {
+  if (!r || !out) return QGW_ERR_PARAM;
+  if (!r->has_q) return QGW_ERR_STATE;
+  enqueue_invert(r);
+  const double scale = r->Delta * r->Delta / (r->p.Lx * r->Ly);
+  if (r->precision == QGW_FP64)
+    qgw::enqueue_budget_f64(r->a64, r->d_wts, r->d_part, r->budget_blocks, scale, r->d_bout, r->stream);
+  else
+    qgw::enqueue_budget_f32c(r->a32, r->d_wts, r->d_part, r->budget_blocks, scale, r->d_bout, r->stream);
+  double v[4];
+  CK(cudaMemcpyAsync(v, r->d_bout, sizeof(v), cudaMemcpyDeviceToHost, r->stream));
+  CK(cudaStreamSynchronize(r->stream));
+  CK(cudaGetLastError());
+  out->ke = v[0];
+  out->energy = v[1];
+  out->enstrophy = v[2];
+  out->wind_work = v[3];
+  return QGW_OK;
+}
+
+// Measurement helper: runs nsteps steps with CUDA events between the four
+// kernels of each step on the run's stream and returns the mean duration of
+// each kernel in ms (ms4[0..3]: rows forward, columns, rows inverse, RHS).
+int qgw_profile_kernels(qgw_run* r, int nsteps, float* ms4) {
+  if (!r || !ms4 || nsteps < 1) return QGW_ERR_PARAM;
+  if (!r->has_q) return QGW_ERR_STATE;
+  std::vector<cudaEvent_t> ev(5 * (size_t)nsteps);
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  qgw::enqueue_begin(r->d_state, 0.0, 0.0, r->stream);
+  for (int s = 0; s < nsteps; ++s) {
+    CK(cudaEventRecord(ev[5 * s], r->stream));
+    for (int k = 0; k < 4; ++k) {
+      if (r->precision == QGW_FP64) qgw::enqueue_step_kernel_f64(r->a64, k, r->stream);
+      else qgw::enqueue_step_kernel_f32c(r->a32, k, r->stream);
+      CK(cudaEventRecord(ev[5 * s + k + 1], r->stream));
+    }
+  }
+  if (r->precision == QGW_FP64) qgw::enqueue_flush_f64(r->a64, r->stream);
+  else qgw::enqueue_flush_f32c(r->a32, r->stream);
+  CK(cudaStreamSynchronize(r->stream));
+  for (int k = 0; k < 4; ++k) ms4[k] = 0;
+  for (int s = 0; s < nsteps; ++s)
+    for (int k = 0; k < 4; ++k) {
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, ev[5 * s + k], ev[5 * s + k + 1]));
+      ms4[k] += ms / nsteps;
+    }
+  for (auto& e : ev) cudaEventDestroy(e);
+  return QGW_OK;
+}
+
+}  // extern "C"

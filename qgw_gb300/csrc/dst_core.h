@@ -1,0 +1,239 @@
+// dst_core.h -- building blocks of the batched DST-I used by the PV
+// inversion (the reference takes it from FFTW's RODFT00 plans,
+// src/elliptic.h:136-139,174,204).
+//
+// Definition (FFTW RODFT00, unnormalised), length n = M-1, M = 2H = 2^p:
+//     Y_k = 2 sum_{j=1}^{M-1} x_j sin(pi j k / M),   k = 1..M-1.
+// Method (published: the sine transform through a half-length complex FFT,
+// e.g. Press et al., Numerical Recipes, section 12.3):
+//   1. y_0 = 0, y_j = (s_j + 1/2) x_j + (s_j - 1/2) x_{M-j},  s_j = sin(pi j/M)
+//   2. Z = FFT_H(z),  z_m = y_{2m} + i y_{2m+1}          (Stockham autosort)
+//   3. with A = Z_k, B = conj Z_{H-k}, (c, s) = (cos, sin)(2 pi k / M):
+//        2R_k = (A+B).re + (c (A-B).im - s (A-B).re)
+//        -2I_k = (c (A-B).re + s (A-B).im) - (A+B).im
+//      Y_{2k} = -2 I_k,  Y_{2k+1} = R_0 + sum_{k'=1..k} 2 R_{k'} (prefix sum)
+//
+// Every function below is one independent work item of one phase; a phase
+// may run its items in any order or in parallel (the CUDA kernels spread
+// them over a thread block, the CPU unit test runs them in a loop).  Rows
+// are stored contiguously: row r of a buffer starts at r * ld reals.
+//
+// Buffer formats (reals):
+//   input   x_j at index j-1 (j = 1..M-1); index M-1 is padding
+//   work    H complex values = M reals
+//   output  Y_k at index k-1 (k = 1..M-1)  -- same as the input format,
+//           so a DST output can feed the next DST directly.
+#pragma once
+
+#include <stdint.h>
+
+#ifdef __CUDACC__
+#define QGW_HD __host__ __device__ __forceinline__
+#define QGW_ALIGN(n) __align__(n)
+#else
+#define QGW_HD inline
+#define QGW_ALIGN(n) alignas(n)
+#endif
+
+namespace qgw {
+
+template <typename T> struct C2;
+template <> struct QGW_ALIGN(16) C2<double> { double x, y; };
+template <> struct QGW_ALIGN(8) C2<float> { float x, y; };
+
+// fused multiply-add on both host and device
+QGW_HD double fmaT(double a, double b, double c) {
+#ifdef __CUDA_ARCH__
+  return __fma_rn(a, b, c);
+#else
+  return __builtin_fma(a, b, c);
+#endif
+}
+QGW_HD float fmaT(float a, float b, float c) {
+#ifdef __CUDA_ARCH__
+  return __fmaf_rn(a, b, c);
+#else
+  return __builtin_fmaf(a, b, c);
+#endif
+}
+
+// Static shape of one DST length.
+struct DstGeom {
+  int M;          // DST length + 1 (power of two, >= 4)
+  int H;          // M / 2, complex FFT length
+  int npass;      // Stockham passes
+  int radix[8];   // radix of each pass (8, then 4 or 2); first pass has Ns = 1
+  int chunk;      // prefix-sum chunk length (values per work item)
+  int nchunk;     // H / chunk (<= 32)
+};
+
+inline DstGeom make_geom(int M) {
+  DstGeom g{};
+  g.M = M;
+  g.H = M / 2;
+  int rem = g.H, p = 0;
+  while (rem >= 8) { g.radix[p++] = 8; rem /= 8; }
+  if (rem == 4) g.radix[p++] = 4;
+  else if (rem == 2) g.radix[p++] = 2;
+  g.npass = p;
+  g.chunk = g.H >= 256 ? g.H / 32 : (g.H >= 8 ? 8 : g.H);
+  g.nchunk = g.H / g.chunk;
+  return g;
+}
+
+// Tables (host-computed in FP64, stored per real type):
+//   tw[m]  = (cos, -sin)(2 pi m / H),            m < H     (FFT twiddles)
+//   pre[j] = (s_j + 1/2, s_j - 1/2), s_j = sin(pi j/M), j <= H
+//   spl[k] = (cos, sin)(2 pi k / M),             k <= H/2
+template <typename T> struct DstTables {
+  const C2<T>* tw;
+  const C2<T>* pre;
+  const C2<T>* spl;
+};
+
+// ---- phase 1: pre-processing, items j = 1..H per row -------------------
+// reads x (input format) of row r, writes y (work format) of row r.
+template <typename T>
+QGW_HD void dst_pre_item(const T* __restrict__ x, T* __restrict__ y, int j, const DstGeom& g,
+                         const C2<T>* __restrict__ pre) {
+  const T a = x[j - 1];
+  const T b = x[g.M - j - 1];
+  const C2<T> w = pre[j];
+  y[j] = fmaT(w.x, a, w.y * b);
+  y[g.M - j] = fmaT(w.y, a, w.x * b);
+  if (j == 1) y[0] = T(0);
+}
+
+// ---- phase 2: Stockham radix-R pass, items b = 0..H/R-1 per row ---------
+template <typename T> QGW_HD C2<T> cmul(C2<T> a, C2<T> w) {
+  C2<T> r;
+  r.x = fmaT(a.x, w.x, -(a.y * w.y));
+  r.y = fmaT(a.x, w.y, a.y * w.x);
+  return r;
+}
+template <typename T> QGW_HD C2<T> cadd(C2<T> a, C2<T> b) { C2<T> r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename T> QGW_HD C2<T> csub(C2<T> a, C2<T> b) { C2<T> r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+// -i * a
+template <typename T> QGW_HD C2<T> cmi(C2<T> a) { C2<T> r; r.x = a.y; r.y = -a.x; return r; }
+
+template <typename T> QGW_HD void dft2(C2<T>* v) {
+  const C2<T> a = v[0], b = v[1];
+  v[0] = cadd(a, b);
+  v[1] = csub(a, b);
+}
+
+template <typename T> QGW_HD void dft4(C2<T>* v) {
+  const C2<T> c0 = cadd(v[0], v[2]), c1 = csub(v[0], v[2]);
+  const C2<T> d0 = cadd(v[1], v[3]), d1 = cmi(csub(v[1], v[3]));
+  v[0] = cadd(c0, d0);
+  v[2] = csub(c0, d0);
+  v[1] = cadd(c1, d1);
+  v[3] = csub(c1, d1);
+}
+
+// forward DFT of length 8 (52 real operations with FMA)
+template <typename T> QGW_HD void dft8(C2<T>* v) {
+  const T s = T(0.70710678118654752440);
+  C2<T> a[4], b[4];
+  for (int r = 0; r < 4; ++r) { a[r] = cadd(v[r], v[r + 4]); b[r] = csub(v[r], v[r + 4]); }
+  // even outputs: DFT4(a)
+  {
+    const C2<T> c0 = cadd(a[0], a[2]), c1 = csub(a[0], a[2]);
+    const C2<T> d0 = cadd(a[1], a[3]), d1 = cmi(csub(a[1], a[3]));
+    v[0] = cadd(c0, d0);
+    v[4] = csub(c0, d0);
+    v[2] = cadd(c1, d1);
+    v[6] = csub(c1, d1);
+  }
+  // odd outputs: DFT4(b0, W b1, W^2 b2, W^3 b3), W = (1 - i)/sqrt 2,
+  // with the 1/sqrt 2 folded into the final FMAs
+  {
+    C2<T> p1, p3;
+    p1.x = b[1].x + b[1].y; p1.y = b[1].y - b[1].x;     // sqrt2 * W b1
+    p3.x = b[3].y - b[3].x; p3.y = -(b[3].x + b[3].y);  // sqrt2 * W^3 b3
+    const C2<T> u2 = cmi(b[2]);
+    const C2<T> c0 = cadd(b[0], u2), c1 = csub(b[0], u2);
+    const C2<T> P = cadd(p1, p3), D = csub(p1, p3);
+    // X1 = c0 + s P, X5 = c0 - s P, X3 = c1 - i s D, X7 = c1 + i s D
+    v[1].x = fmaT(s, P.x, c0.x);  v[1].y = fmaT(s, P.y, c0.y);
+    v[5].x = fmaT(-s, P.x, c0.x); v[5].y = fmaT(-s, P.y, c0.y);
+    v[3].x = fmaT(s, D.y, c1.x);  v[3].y = fmaT(-s, D.x, c1.y);
+    v[7].x = fmaT(-s, D.y, c1.x); v[7].y = fmaT(s, D.x, c1.y);
+  }
+}
+
+template <int R, typename T>
+QGW_HD void stockham_item(const C2<T>* __restrict__ src, C2<T>* __restrict__ dst, int b, int Ns, int H,
+                          const C2<T>* __restrict__ tw) {
+  const int stride = H / R;
+  C2<T> v[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) v[q] = src[b + q * stride];
+  const int k = b & (Ns - 1);
+  if (Ns > 1) {
+    const int step = k * (H / (Ns * R));
+#pragma unroll
+    for (int q = 1; q < R; ++q) v[q] = cmul(v[q], tw[q * step]);
+  }
+  if (R == 8) dft8(v);
+  else if (R == 4) dft4(v);
+  else dft2(v);
+  const int base = (b - k) * R + k;
+#pragma unroll
+  for (int q = 0; q < R; ++q) dst[base + q * Ns] = v[q];
+}
+
+template <typename T>
+QGW_HD void stockham_dispatch(int R, const C2<T>* src, C2<T>* dst, int b, int Ns, int H, const C2<T>* tw) {
+  if (R == 8) stockham_item<8, T>(src, dst, b, Ns, H, tw);
+  else if (R == 4) stockham_item<4, T>(src, dst, b, Ns, H, tw);
+  else stockham_item<2, T>(src, dst, b, Ns, H, tw);
+}
+
+// ---- phase 3: split, items k = 0..H/2 per row --------------------------
+// reads the FFT result Z (work format) and writes the output format, with
+// the odd outputs still as increments (2R_k; R_0 at index 0).
+template <typename T>
+QGW_HD void dst_split_item(const C2<T>* __restrict__ Z, T* __restrict__ out, int k, const DstGeom& g,
+                           const C2<T>* __restrict__ spl) {
+  const int H = g.H;
+  if (k == 0) {
+    const C2<T> a = Z[0];
+    out[0] = a.x + a.y;  // R_0
+    return;
+  }
+  const C2<T> A = Z[k];
+  const C2<T> Bc = Z[H - k];
+  const T br = Bc.x, bi = -Bc.y;
+  const C2<T> cs = spl[k];
+  const T sr = A.x + br, si = A.y + bi, dr = A.x - br, di = A.y - bi;
+  const T P = fmaT(cs.x, di, -(cs.y * dr));
+  const T Q = fmaT(cs.x, dr, cs.y * di);
+  out[2 * k] = sr + P;          // 2 R_k
+  out[2 * k - 1] = Q - si;      // Y_{2k} = -2 I_k
+  if (2 * k != H) {
+    out[2 * (H - k)] = sr - P;      // 2 R_{H-k}
+    out[2 * (H - k) - 1] = Q + si;  // Y_{2(H-k)}
+  }
+}
+
+// ---- phase 4: prefix sum of the odd outputs (indices 0, 2, 4, ...) ------
+// 4a: items c = 0..nchunk-1: inclusive scan inside chunk c, returns total
+template <typename T>
+QGW_HD T dst_scan_chunk(T* out, int c, const DstGeom& g) {
+  T acc = T(0);
+  const int k0 = c * g.chunk;
+  for (int t = 0; t < g.chunk; ++t) {
+    acc = (t == 0) ? out[2 * k0] : acc + out[2 * (k0 + t)];
+    out[2 * (k0 + t)] = acc;
+  }
+  return acc;
+}
+// 4c: items c = 1..nchunk-1: add the exclusive prefix of chunk totals
+template <typename T>
+QGW_HD void dst_scan_fix(T* out, int c, T prefix, const DstGeom& g) {
+  const int k0 = c * g.chunk;
+  for (int t = 0; t < g.chunk; ++t) out[2 * (k0 + t)] += prefix;
+}
+
+}  // namespace qgw

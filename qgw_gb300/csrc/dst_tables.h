@@ -1,0 +1,52 @@
+// dst_tables.h -- host construction of the DST-I tables of dst_core.h, in
+// FP64 with exactly reduced angles (one libm rounding per entry).
+#pragma once
+
+#include <cmath>
+#include <vector>
+
+#include "dst_core.h"
+
+namespace qgw {
+
+// sin(pi * m / N) for integer m, reduced exactly to [0, pi/2]
+inline double sinpi_frac(long m, long N) {
+  long r = m % (2 * N);
+  if (r < 0) r += 2 * N;
+  double sg = 1.0;
+  if (r >= N) { r -= N; sg = -1.0; }
+  if (2 * r > N) r = N - r;
+  return sg * std::sin(M_PI * (double)r / (double)N);
+}
+// cos(pi m / N) = sin(pi (2m + N) / (2N))
+inline double cospi_frac(long m, long N) { return sinpi_frac(2 * m + N, 2 * N); }
+
+struct DstTablesHost {
+  std::vector<double> tw, pre, spl;  // interleaved (x, y) pairs
+};
+
+// tw: H entries, pre: H+1 entries, spl: H/2+1 entries
+inline DstTablesHost build_dst_tables(int M) {
+  const int H = M / 2;
+  DstTablesHost t;
+  t.tw.resize(2 * (size_t)H);
+  for (int m = 0; m < H; ++m) {
+    // 2 pi m / H = pi (2m) / H
+    t.tw[2 * m] = cospi_frac(2L * m, H);
+    t.tw[2 * m + 1] = -sinpi_frac(2L * m, H);
+  }
+  t.pre.resize(2 * (size_t)(H + 1));
+  for (int j = 0; j <= H; ++j) {
+    const double s = sinpi_frac(j, M);
+    t.pre[2 * j] = s + 0.5;
+    t.pre[2 * j + 1] = s - 0.5;
+  }
+  t.spl.resize(2 * (size_t)(H / 2 + 1));
+  for (int k = 0; k <= H / 2; ++k) {
+    t.spl[2 * k] = cospi_frac(2L * k, M);
+    t.spl[2 * k + 1] = sinpi_frac(2L * k, M);
+  }
+  return t;
+}
+
+}  // namespace qgw

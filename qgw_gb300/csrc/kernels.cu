@@ -1,0 +1,693 @@
+// kernels.cu -- the four kernels of one qgw time step on GB300 (sm_103a),
+// for the plain FP64 path (T = double) and the compensated FP32 path
+// (T = float, q held as hi + lo).
+//
+// One reference step (timestep, src/timestep.h:386-439) is
+//   K1 rows   : apply the pending AB3 update of the previous step, project
+//               layers onto vertical modes, forward DST-I along x
+//   K2 columns: forward DST-I along y, Helmholtz divide, inverse DST-I
+//               along y                                  (invert_pv core)
+//   K3 rows   : inverse DST-I along x, back-project modes onto layers -> psi
+//   K4 tiles  : RHS (Arakawa Jacobian, beta, viscosity, hyperviscosity,
+//               wind, bottom drag, topography) -> f0, CFL maximum; the last
+//               block advances dt/t and computes the AB3 coefficients
+// The AB3 update q += c0 f0 + c1 f1 + c2 f2 needs the CFL-limited dt of the
+// same step, i.e. a reduction over all of psi, so it is applied by the next
+// step's K1 (or by the flush kernel at the end of a call), which saves one
+// full pass over q, f0, f1, f2.
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+#include "qgw_device.cuh"
+
+namespace qgw {
+
+constexpr int NT = 256;          // threads per block in every step kernel
+constexpr int GMAX = 16;         // max modes per block in the row kernels
+constexpr int TX = 32, TY = 16;  // RHS tile (interior points)
+constexpr double TEPS = 1e-9;    // src/timestep.h:288
+constexpr double HUGEV = 1e30;   // src/qg.c:43
+
+// --------------------------------------------------------------- DST block
+// Batched DST-I of nrows rows (row r at A + r*ld, input format) by the whole
+// block; B is the second work buffer.  Returns the buffer with the output.
+template <typename T>
+__device__ T* dst_block(T* A, T* B, int nrows, int ld, const DstGeom& g, const DstTables<T>& tb,
+                        T* tot) {
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int H = g.H, lgH = __ffs(H) - 1;
+  for (int w = tid; w < nrows * H; w += nth) {
+    const int r = w >> lgH, j = (w & (H - 1)) + 1;
+    dst_pre_item<T>(A + r * ld, B + r * ld, j, g, tb.pre);
+  }
+  __syncthreads();
+  T* src = B;
+  T* dst = A;
+  int Ns = 1;
+  for (int p = 0; p < g.npass; ++p) {
+    const int R = g.radix[p];
+    const int nb = H / R, lgnb = __ffs(nb) - 1;
+    for (int w = tid; w < nrows * nb; w += nth) {
+      const int r = w >> lgnb, b = w & (nb - 1);
+      stockham_dispatch<T>(R, (const C2<T>*)(src + r * ld), (C2<T>*)(dst + r * ld), b, Ns, H, tb.tw);
+    }
+    __syncthreads();
+    Ns *= R;
+    T* t = src; src = dst; dst = t;
+  }
+  const int ns = H / 2 + 1;
+  for (int w = tid; w < nrows * ns; w += nth) {
+    const int r = w / ns, k = w - r * ns;
+    dst_split_item<T>((const C2<T>*)(src + r * ld), dst + r * ld, k, g, tb.spl);
+  }
+  __syncthreads();
+  const int nc = g.nchunk;
+  for (int w = tid; w < nrows * nc; w += nth) {
+    const int r = w / nc, c = w - r * nc;
+    tot[r * 32 + c] = dst_scan_chunk<T>(dst + r * ld, c, g);
+  }
+  __syncthreads();
+  const int warp = tid >> 5, lane = tid & 31, nwarp = nth >> 5;
+  for (int r = warp; r < nrows; r += nwarp) {
+    T incl = lane < nc ? tot[r * 32 + lane] : T(0);
+    for (int o = 1; o < 32; o <<= 1) {
+      const T u = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += u;
+    }
+    T ex = __shfl_up_sync(0xffffffffu, incl, 1);
+    if (lane == 0) ex = T(0);
+    __syncwarp();
+    if (lane < nc) tot[r * 32 + lane] = ex;
+  }
+  __syncthreads();
+  for (int w = tid; w < nrows * nc; w += nth) {
+    const int r = w / nc, c = w - r * nc;
+    if (c > 0) dst_scan_fix<T>(dst + r * ld, c, tot[r * 32 + c], g);
+  }
+  __syncthreads();
+  return dst;
+}
+
+__device__ __forceinline__ void slabs(int si, int& s0, int& s1, int& s2) {
+  const int m = si % 3;
+  s0 = (3 - m) % 3;
+  s1 = (4 - m) % 3;
+  s2 = (5 - m) % 3;
+}
+
+// Compensated add of an increment d to (hi, lo).
+__device__ __forceinline__ void comp_add(float& hi, float& lo, float d) {
+  const float s = hi + d;
+  const float bp = s - hi;
+  const float err = (hi - (s - bp)) + (d - bp);
+  const float l2 = lo + err;
+  const float h2 = s + l2;
+  lo = l2 - (h2 - s);
+  hi = h2;
+}
+
+// ------------------------------------------------------------------ K1
+// One block per row j.  Mode groups are processed in turn by the same block:
+// the AB3 update is applied (and q written) while forming the first group,
+// and later groups re-read the updated q written by the same thread, so no
+// block ever reads a q value another block may be updating.
+template <typename T, bool COMP>
+__global__ void __launch_bounds__(NT) k_rows_fwd(StepArgs<T> a, int step_mode) {
+  DevState* st = a.state;
+  if (step_mode && !st->active) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ T tot[GMAX * 32];
+  const int j = blockIdx.x;
+  const int ld = a.gx.M;
+  T* A = (T*)smem_raw;
+  T* B = A + (size_t)a.G1 * ld;
+  const bool ab3 = step_mode && st->pending;
+  int s0 = 0, s1 = 0, s2 = 0;
+  slabs(st->step_index, s0, s1, s2);
+  const double c0 = st->c0, c1 = st->c1, c2 = st->c2;
+  const size_t fs = (size_t)a.nl * a.lstride;
+  const T* f0 = a.fab + s0 * fs;
+  const T* f1 = a.fab + s1 * fs;
+  const T* f2 = a.fab + s2 * fs;
+  const T* cl = a.cl2m;
+  for (int m0 = 0; m0 < a.nl; m0 += a.G1) {
+    const int G = min(a.G1, a.nl - m0);
+    const bool upd = ab3 && m0 == 0;
+    for (int i = threadIdx.x; i < a.nx; i += NT) {
+      T acc[GMAX];
+      for (int l = 0; l < a.nl; ++l) {
+        const size_t o = (size_t)l * a.lstride + (size_t)j * a.pitch + i;
+        T v;
+        if (COMP) {
+          float hi = (float)a.q[o];
+          if (upd) {
+            float lo = (float)a.qlo[o];
+            const float d = (float)c0 * (float)f0[o] + (float)c1 * (float)f1[o] + (float)c2 * (float)f2[o];
+            comp_add(hi, lo, d);
+            a.q[o] = (T)hi;
+            a.qlo[o] = (T)lo;
+          }
+          v = (T)hi;
+        } else {
+          v = a.q[o];
+          if (upd) {
+            v = v + (T)c0 * f0[o] + (T)c1 * f1[o] + (T)c2 * f2[o];
+            a.q[o] = v;
+          }
+        }
+#pragma unroll
+        for (int gg = 0; gg < GMAX; ++gg)
+          if (gg < G) {
+            const T c = cl[(m0 + gg) * a.nl + l];
+            acc[gg] = (l == 0) ? c * v : fmaT(c, v, acc[gg]);
+          }
+      }
+#pragma unroll
+      for (int gg = 0; gg < GMAX; ++gg)
+        if (gg < G) A[gg * ld + i] = acc[gg];
+    }
+    __syncthreads();
+    T* O = dst_block<T>(A, B, G, ld, a.gx, a.tx, tot);
+    for (int gg = 0; gg < G; ++gg) {
+      T* dstrow = a.spec + (size_t)(m0 + gg) * a.lstride + (size_t)j * a.pitch;
+      for (int i = threadIdx.x; i < a.nx; i += NT) dstrow[i] = O[gg * ld + i];
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ K2
+template <typename T, bool COMP>
+__global__ void __launch_bounds__(NT) k_cols(StepArgs<T> a, int step_mode) {
+  DevState* st = a.state;
+  if (step_mode && !st->active) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ T tot[GMAX * 32];
+  const int k0 = blockIdx.x * a.CT;
+  const int m = blockIdx.y;
+  const int CTb = min(a.CT, a.nx - k0);
+  const int ld = a.gy.M;
+  T* A = (T*)smem_raw;
+  T* B = A + (size_t)a.CT * ld;
+  T* S = a.spec + (size_t)m * a.lstride;
+  const int ny = a.ny;
+  for (int w = threadIdx.x; w < ny * CTb; w += NT) {
+    const int jj = w / CTb, c = w - jj * CTb;
+    A[c * ld + jj] = S[(size_t)jj * a.pitch + k0 + c];
+  }
+  __syncthreads();
+  T* O = dst_block<T>(A, B, CTb, ld, a.gy, a.ty, tot);
+  const double iRd2 = a.iRd2[m];
+  for (int w = threadIdx.x; w < ny * CTb; w += NT) {
+    const int jj = w / CTb, c = w - jj * CTb;
+    const int k = k0 + c;
+    if (!COMP) {
+      O[c * ld + jj] *= (T)a.hinv[(size_t)m * a.lstride + (size_t)jj * a.pitch + k];
+    } else if (m == 0 && jj < a.low_k64 && k < a.low_k64) {
+      // barotropic mode, lowest wavenumbers: divide in FP64
+      const double fact = -(a.Lsq[k] + a.Ksq[jj] + iRd2);
+      O[c * ld + jj] = (T)((double)O[c * ld + jj] / fact / a.norm);
+    } else {
+      const float fact = -(((float)a.Lsq[k] + (float)a.Ksq[jj]) + (float)iRd2);
+      O[c * ld + jj] = (T)((float)O[c * ld + jj] / (fact * (float)a.norm));
+    }
+  }
+  __syncthreads();
+  T* Oth = (O == A) ? B : A;
+  T* O2 = dst_block<T>(O, Oth, CTb, ld, a.gy, a.ty, tot);
+  for (int w = threadIdx.x; w < ny * CTb; w += NT) {
+    const int jj = w / CTb, c = w - jj * CTb;
+    S[(size_t)jj * a.pitch + k0 + c] = O2[c * ld + jj];
+  }
+}
+
+// ------------------------------------------------------------------ K3
+template <typename T, bool COMP>
+__global__ void __launch_bounds__(NT) k_rows_inv(StepArgs<T> a, int step_mode) {
+  DevState* st = a.state;
+  if (step_mode && !st->active) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ T tot[GMAX * 32];
+  const int j = blockIdx.x;
+  const int ld = a.gx.M;
+  T* A = (T*)smem_raw;
+  T* B = A + (size_t)a.G1 * ld;
+  const T* cm = a.cm2l;
+  for (int m0 = 0; m0 < a.nl; m0 += a.G1) {
+    const int G = min(a.G1, a.nl - m0);
+    for (int gg = 0; gg < G; ++gg) {
+      const T* srow = a.spec + (size_t)(m0 + gg) * a.lstride + (size_t)j * a.pitch;
+      for (int i = threadIdx.x; i < a.nx; i += NT) A[gg * ld + i] = srow[i];
+    }
+    __syncthreads();
+    T* O = dst_block<T>(A, B, G, ld, a.gx, a.tx, tot);
+    for (int i = threadIdx.x; i < a.nx; i += NT) {
+      for (int l = 0; l < a.nl; ++l) {
+        const size_t o = (size_t)l * a.lstride + (size_t)j * a.pitch + i;
+        T acc = (m0 == 0) ? T(0) : a.psi[o];
+        for (int gg = 0; gg < G; ++gg) acc = fmaT(cm[l * a.nl + m0 + gg], O[gg * ld + i], acc);
+        a.psi[o] = acc;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ K4
+__device__ __forceinline__ unsigned long long absbits(double v) {
+  return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL;
+}
+__device__ __forceinline__ unsigned long long absbits(float v) {
+  // widen exactly to double so that both paths reduce the same quantity
+  return absbits((double)v);
+}
+
+// adjust_timestep's dt rule (src/timestep.h:341-383) and the AB3
+// coefficients (src/timestep.h:398-405), by one thread.
+__device__ void scalar_update(DevState* st, double Delta, double cfl) {
+  const unsigned long long bits = atomicMax(&st->maxbits, 0ULL);
+  const bool bad = bits >= 0x7ff0000000000000ULL;
+  double dt_max = HUGEV;
+  const double maxabs = __longlong_as_double((long long)bits);
+  if (!bad && maxabs != 0.0) {
+    const double u = maxabs / Delta;
+    const double dl = cfl * Delta / u;
+    if (dl < dt_max) dt_max = dl;
+  }
+  const double t = st->t;
+  double dt = st->dt;
+  st->dt1 = st->dt0;
+  st->dt0 = dt;
+  if (dt < dt_max) dt = 2. * dt;
+  if (dt > st->DT_max) dt = st->DT_max;
+  if (dt > dt_max) dt = dt_max;
+  const double t_out = st->t_out;
+  if (t_out > t + TEPS) {
+    const unsigned int n_step = (unsigned int)((t_out - t) / dt);
+    if (n_step == 0)
+      dt = t_out - t;
+    else {
+      const double d1 = (t_out - t) / n_step;
+      if (d1 > dt * (1. + TEPS))
+        dt = (t_out - t) / (n_step + 1);
+      else if (d1 < dt)
+        dt = d1;
+    }
+  }
+  st->dt = dt;
+  const double dt0 = st->dt0, dt1 = st->dt1;
+  st->c0 = dt * (2 * dt * dt + 3 * dt * (2 * dt0 + dt1) + 6 * dt0 * (dt0 + dt1)) / (6 * dt0 * (dt0 + dt1));
+  st->c1 = dt * dt * (-dt / 3 - dt0 / 2 - dt1 / 2) / (dt0 * dt1);
+  st->c2 = dt * dt * (dt / 3 + dt0 / 2) / (dt1 * (dt0 + dt1));
+  st->pending = 1;
+  const double tn = t + dt;
+  st->t = tn;
+  st->step_index += 1;
+  st->steps_taken += 1;
+  st->first = 0;
+  if (bad) {
+    st->active = 0; st->stop_reason = 3; st->nonfinite = 1;
+  } else if (st->tend > 0 && !(tn < st->tend)) {
+    st->active = 0; st->stop_reason = 2;
+  } else if (fabs(tn - t_out) < TEPS * dt) {
+    st->active = 0; st->stop_reason = 1;
+  }
+  st->maxbits = 0ULL;
+  st->done_blocks = 0u;
+}
+
+template <typename T, bool COMP>
+__global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
+  DevState* st = a.state;
+  if (!st->active) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int k = blockIdx.z;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  const int r = a.nsweep > 0 ? a.nsweep : 1;
+  const int W = TX + 2 * r, Hh = TY + 2 * r;
+  const int nx = a.nx, ny = a.ny;
+  T* ps = (T*)smem_raw;                 // W*Hh, psi with halo r
+  T* L0 = ps + W * Hh;                  // chain ping-pong
+  T* L1 = L0 + W * Hh;
+  T* qs = L1 + W * Hh;                  // (TX+2)*(TY+2)
+  T* dyp = qs + (TX + 2) * (TY + 2);    // (TX+2)*TY
+  T* dyq = dyp + (TX + 2) * TY;
+  T* dxp = dyq + (TX + 2) * TY;         // TX*(TY+2)
+  T* dxq = dxp + TX * (TY + 2);
+  __shared__ unsigned long long wmax[NT / 32];
+  __shared__ int is_last;
+
+  const T* psiL = a.psi + (size_t)k * a.lstride;
+  const T* qL = a.q + (size_t)k * a.lstride;
+#define PS(x, y) ps[((y) + r) * W + (x) + r]
+  for (int w = threadIdx.x; w < W * Hh; w += NT) {
+    const int x = w % W - r, y = w / W - r;
+    const int gi = i0 + x, gj = j0 + y;
+    T v = T(0);
+    if (gi >= 0 && gi < nx && gj >= 0 && gj < ny) v = psiL[(size_t)gj * a.pitch + gi];
+    ps[w] = v;
+  }
+  __syncthreads();
+  const T cbc = (T)a.cbc;
+  // q with one ghost point: adjust_bc(q, 1, psi), src/domain.h:308-348
+#define QS(x, y) qs[((y) + 1) * (TX + 2) + (x) + 1]
+  for (int w = threadIdx.x; w < (TX + 2) * (TY + 2); w += NT) {
+    const int x = w % (TX + 2) - 1, y = w / (TX + 2) - 1;
+    const int gi = i0 + x, gj = j0 + y;
+    const bool inx = gi >= 0 && gi < nx, iny = gj >= 0 && gj < ny;
+    T v = T(0);
+    if (inx && iny) v = qL[(size_t)gj * a.pitch + gi];
+    else if (iny && gi == -1) v = cbc * PS(x + 1, y);
+    else if (iny && gi == nx) v = cbc * PS(x - 1, y);
+    else if (inx && gj == -1) v = cbc * PS(x, y + 1);
+    else if (inx && gj == ny) v = cbc * PS(x, y - 1);
+    qs[w] = v;
+  }
+  // hyperviscosity chain (calc_diff, src/dynamics.h:13-44) on the tile with
+  // a shrinking halo; sweeps are unscaled (no 1/Delta^2), the scale is in
+  // nuh_scaled and in the ghost factors gh[s]
+  const T* Lp = ps;
+  T* Lc = L0;
+  for (int s = 1; s <= a.nsweep; ++s) {
+    __syncthreads();
+    const int rr = r - s;
+    const int Ws = TX + 2 * rr, Hs = TY + 2 * rr;
+    const T ghs = (T)a.gh[s];
+    for (int w = threadIdx.x; w < Ws * Hs; w += NT) {
+      const int x = w % Ws - rr, y = w / Ws - rr;
+      const int gi = i0 + x, gj = j0 + y;
+      const bool inx = gi >= 0 && gi < nx, iny = gj >= 0 && gj < ny;
+      const int o = (y + r) * W + x + r;
+      T v = T(0);
+      if (inx && iny) {
+        const T sum = (Lp[o + 1] + Lp[o - 1]) + (Lp[o + W] + Lp[o - W]);
+        v = fmaT(T(-4), Lp[o], sum);
+      } else if (iny && gi == -1) v = ghs * PS(x + 1, y);
+      else if (iny && gi == nx) v = ghs * PS(x - 1, y);
+      else if (inx && gj == -1) v = ghs * PS(x, y + 1);
+      else if (inx && gj == ny) v = ghs * PS(x, y - 1);
+      Lc[o] = v;
+    }
+    Lp = Lc;
+    Lc = (Lc == L0) ? L1 : L0;
+  }
+  __syncthreads();
+  // centred differences shared between neighbouring Jacobian evaluations
+  for (int w = threadIdx.x; w < (TX + 2) * TY; w += NT) {
+    const int x = w % (TX + 2) - 1, y = w / (TX + 2);
+    dyp[w] = PS(x, y + 1) - PS(x, y - 1);
+    dyq[w] = QS(x, y + 1) - QS(x, y - 1);
+  }
+  for (int w = threadIdx.x; w < TX * (TY + 2); w += NT) {
+    const int x = w % TX, y = w / TX - 1;
+    dxp[w] = PS(x + 1, y) - PS(x - 1, y);
+    dxq[w] = QS(x + 1, y) - QS(x - 1, y);
+  }
+  __syncthreads();
+#define DY(arr, x, y) arr[(y) * (TX + 2) + (x) + 1]
+#define DX(arr, x, y) arr[((y) + 1) * TX + (x)]
+  const size_t fs = (size_t)a.nl * a.lstride;
+  int s0, s1, s2;
+  slabs(st->step_index + 1, s0, s1, s2);
+  T* fout = a.fab + s0 * fs + (size_t)k * a.lstride;
+  const bool bottom = (k == a.nl - 1);
+  unsigned long long mymax = 0ULL;
+  for (int w = threadIdx.x; w < TX * TY; w += NT) {
+    const int x = w % TX, y = w / TX;
+    const int gi = i0 + x, gj = j0 + y;
+    if (gi >= nx || gj >= ny) continue;
+    // Arakawa Jacobian J(psi, q) (jacobian_lev, src/domain.h:17-27) with the
+    // centred differences shared: 2 products + 8 fused terms
+    T J = DX(dxp, x, y) * DY(dyq, x, y);
+    J = fmaT(-DY(dyp, x, y), DX(dxq, x, y), J);
+    J = fmaT(PS(x + 1, y), DY(dyq, x + 1, y), J);
+    J = fmaT(-PS(x - 1, y), DY(dyq, x - 1, y), J);
+    J = fmaT(-PS(x, y + 1), DX(dxq, x, y + 1), J);
+    J = fmaT(PS(x, y - 1), DX(dxq, x, y - 1), J);
+    J = fmaT(QS(x, y + 1), DX(dxp, x, y + 1), J);
+    J = fmaT(-QS(x, y - 1), DX(dxp, x, y - 1), J);
+    J = fmaT(-QS(x + 1, y), DY(dyp, x + 1, y), J);
+    J = fmaT(QS(x - 1, y), DY(dyp, x - 1, y), J);
+    // rhs, src/dynamics.h:55-58: -J - beta psi_x + nu lap q + nu_h lap^n psi
+    T f = fmaT((T)(-a.inv12d2), J, -((T)a.b2d * DX(dxp, x, y)));
+    if (a.has_nu) {
+      const T lq = fmaT(T(-4), QS(x, y), (QS(x + 1, y) + QS(x - 1, y)) + (QS(x, y + 1) + QS(x, y - 1)));
+      f = fmaT((T)a.nu_d2, lq, f);
+    }
+    if (a.nsweep > 0) f = fmaT((T)a.nuh_scaled, Lp[(y + r) * W + x + r], f);
+    // surface wind (src/dynamics.h:66) and bottom drag + topography (:67-69)
+    if (k == 0 && a.has_wind) f += a.wind[gj];
+    if (bottom) {
+      if (a.has_drag) {
+        const T lp = fmaT(T(-4), PS(x, y), (PS(x + 1, y) + PS(x - 1, y)) + (PS(x, y + 1) + PS(x, y - 1)));
+        f = fmaT((T)a.drag_d2, lp, f);
+      }
+      if (a.has_topo) {
+        // J(psi, topo) on the ghosted topography grid (reference layout)
+        const int tp = nx + 2;
+        const double* tb = a.topo + (size_t)(gj + 1) * tp + (gi + 1);
+#define TP(dx, dy) ((T)tb[(dy) * tp + (dx)])
+        const T jt = (DX(dxp, x, y) * (TP(0, 1) - TP(0, -1)) - DY(dyp, x, y) * (TP(1, 0) - TP(-1, 0))
+                      + PS(x + 1, y) * (TP(1, 1) - TP(1, -1)) - PS(x - 1, y) * (TP(-1, 1) - TP(-1, -1))
+                      - PS(x, y + 1) * (TP(1, 1) - TP(-1, 1)) + PS(x, y - 1) * (TP(1, -1) - TP(-1, -1))
+                      + TP(0, 1) * (PS(x + 1, y + 1) - PS(x - 1, y + 1))
+                      - TP(0, -1) * (PS(x + 1, y - 1) - PS(x - 1, y - 1))
+                      - TP(1, 0) * (PS(x + 1, y + 1) - PS(x + 1, y - 1))
+                      + TP(-1, 0) * (PS(x - 1, y + 1) - PS(x - 1, y - 1)));
+#undef TP
+        f = fmaT(-(T)(a.inv12d2 * a.topo_fac), jt, f);
+      }
+    }
+    fout[(size_t)gj * a.pitch + gi] = f;
+    // CFL (adjust_timestep, src/timestep.h:346-359): one-sided differences
+    const T du = PS(x + 1, y) - PS(x, y);
+    const T dv = PS(x, y + 1) - PS(x, y);
+    const unsigned long long bu = absbits(du), bv = absbits(dv);
+    const unsigned long long bm = bu > bv ? bu : bv;
+    mymax = bm > mymax ? bm : mymax;
+  }
+#undef DY
+#undef DX
+#undef PS
+#undef QS
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long u = __shfl_xor_sync(0xffffffffu, mymax, o);
+    mymax = u > mymax ? u : mymax;
+  }
+  if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = mymax;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long bm = 0ULL;
+    for (int w = 0; w < NT / 32; ++w) bm = wmax[w] > bm ? wmax[w] : bm;
+    atomicMax(&st->maxbits, bm);
+    __threadfence();
+    const unsigned int total = gridDim.x * gridDim.y * gridDim.z;
+    const unsigned int ticket = atomicAdd(&st->done_blocks, 1u);
+    is_last = (ticket == total - 1);
+  }
+  __syncthreads();
+  if (is_last && threadIdx.x == 0) {
+    __threadfence();
+    scalar_update(st, a.Delta, a.cfl);
+  }
+}
+
+// ------------------------------------------------------- small kernels
+__global__ void k_begin(DevState* st, double t_out, double tend) {
+  st->t_out = t_out;
+  st->tend = tend;
+  st->first = 1;
+  st->steps_taken = 0;
+  st->stop_reason = 0;
+  st->active = (tend > 0 && !(st->t < tend)) ? 0 : 1;
+}
+
+template <typename T, bool COMP>
+__global__ void __launch_bounds__(NT) k_flush(StepArgs<T> a) {
+  DevState* st = a.state;
+  if (!st->pending) return;
+  int s0, s1, s2;
+  slabs(st->step_index, s0, s1, s2);
+  const double c0 = st->c0, c1 = st->c1, c2 = st->c2;
+  const size_t fs = (size_t)a.nl * a.lstride;
+  const T* f0 = a.fab + s0 * fs;
+  const T* f1 = a.fab + s1 * fs;
+  const T* f2 = a.fab + s2 * fs;
+  const size_t n = (size_t)a.nl * a.ny * a.nx;
+  for (size_t w = blockIdx.x * (size_t)NT + threadIdx.x; w < n; w += (size_t)gridDim.x * NT) {
+    const size_t row = w / a.nx;
+    const int i = (int)(w - row * a.nx);
+    const size_t o = row * a.pitch + i;
+    if (COMP) {
+      float hi = (float)a.q[o], lo = (float)a.qlo[o];
+      const float d = (float)c0 * (float)f0[o] + (float)c1 * (float)f1[o] + (float)c2 * (float)f2[o];
+      comp_add(hi, lo, d);
+      a.q[o] = (T)hi;
+      a.qlo[o] = (T)lo;
+    } else {
+      a.q[o] = a.q[o] + (T)c0 * f0[o] + (T)c1 * f1[o] + (T)c2 * f2[o];
+    }
+  }
+}
+
+__global__ void k_end(DevState* st) { st->pending = 0; }
+
+// FP32c <-> FP64 conversions for the boundary copies
+__global__ void k_split_f64(const double* src, float* hi, float* lo, size_t n) {
+  for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < n; w += (size_t)gridDim.x * blockDim.x) {
+    const double x = src[w];
+    const float h = (float)x;
+    hi[w] = h;
+    lo[w] = (float)(x - (double)h);
+  }
+}
+__global__ void k_join_f64(const float* hi, const float* lo, double* dst, size_t n) {
+  for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < n; w += (size_t)gridDim.x * blockDim.x)
+    dst[w] = (double)hi[w] + (lo ? (double)lo[w] : 0.0);
+}
+
+// FP64 diagnostics: per-block partial sums, then one block adds them up in a
+// fixed order (bit-reproducible).
+template <typename T>
+__global__ void __launch_bounds__(NT) k_budget_partial(StepArgs<T> a, const double* wts, double* part) {
+  __shared__ double red[4][NT];
+  double ke = 0, en = 0, ens = 0, ww = 0;
+  const size_t n = (size_t)a.nl * a.ny * a.nx;
+  for (size_t w = blockIdx.x * (size_t)NT + threadIdx.x; w < n; w += (size_t)gridDim.x * NT) {
+    const size_t row = w / a.nx;
+    const int i = (int)(w - row * a.nx);
+    const int l = (int)(row / a.ny);
+    const int j = (int)(row - (size_t)l * a.ny);
+    const size_t o = row * a.pitch + i;
+    const double p = (double)a.psi[o];
+    const double qv = (double)a.q[o] + (a.qlo ? (double)a.qlo[o] : 0.0);
+    const double pe = (i + 1 < a.nx) ? (double)a.psi[o + 1] : 0.0;
+    const double pn = (j + 1 < a.ny) ? (double)a.psi[o + a.pitch] : 0.0;
+    const double u = (pe - p) / a.Delta, v = (pn - p) / a.Delta;
+    const double wl = wts[l];
+    ke += wl * 0.5 * (u * u + v * v);
+    en -= wl * p * qv;
+    ens += wl * qv * qv;
+    if (l == 0 && a.wind) ww -= wl * p * (double)a.wind[j];
+  }
+  red[0][threadIdx.x] = ke; red[1][threadIdx.x] = en; red[2][threadIdx.x] = ens; red[3][threadIdx.x] = ww;
+  __syncthreads();
+  for (int s = NT / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+      for (int c = 0; c < 4; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) part[blockIdx.x * 4 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+__global__ void k_budget_final(const double* part, int nblk, double scale, double* out) {
+  if (threadIdx.x < 4) {
+    double s = 0;
+    for (int b = 0; b < nblk; ++b) s += part[b * 4 + threadIdx.x];
+    out[threadIdx.x] = s * scale;
+  }
+}
+
+// ------------------------------------------------------------- launchers
+template <typename T, bool COMP>
+static size_t smem_rows(const StepArgs<T>& a) { return (size_t)2 * a.G1 * a.gx.M * sizeof(T); }
+template <typename T, bool COMP>
+static size_t smem_cols(const StepArgs<T>& a) { return (size_t)2 * a.CT * a.gy.M * sizeof(T); }
+template <typename T>
+static size_t smem_rhs(const StepArgs<T>& a) {
+  const int r = a.nsweep > 0 ? a.nsweep : 1;
+  const size_t W = TX + 2 * r, Hh = TY + 2 * r;
+  return sizeof(T) * (3 * W * Hh + (TX + 2) * (TY + 2) + 2 * (TX + 2) * TY + 2 * TX * (TY + 2));
+}
+
+template <typename T, bool COMP>
+static cudaError_t set_attrs(const StepArgs<T>& a) {
+  cudaError_t e;
+  e = cudaFuncSetAttribute(k_rows_fwd<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_rows<T, COMP>(a));
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_rows_inv<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_rows<T, COMP>(a));
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_cols<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cols<T, COMP>(a));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_rhs<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_rhs<T>(a));
+}
+
+template <typename T, bool COMP>
+static void launch_invert(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
+  k_rows_fwd<T, COMP><<<dim3(a.ny), NT, smem_rows<T, COMP>(a), s>>>(a, step_mode);
+  k_cols<T, COMP><<<dim3((a.nx + a.CT - 1) / a.CT, a.nl), NT, smem_cols<T, COMP>(a), s>>>(a, step_mode);
+  k_rows_inv<T, COMP><<<dim3(a.ny), NT, smem_rows<T, COMP>(a), s>>>(a, step_mode);
+}
+
+template <typename T, bool COMP>
+static void launch_rhs(const StepArgs<T>& a, cudaStream_t s) {
+  k_rhs<T, COMP><<<dim3((a.nx + TX - 1) / TX, (a.ny + TY - 1) / TY, a.nl), NT, smem_rhs<T>(a), s>>>(a);
+}
+
+template <typename T, bool COMP>
+static void launch_flush(const StepArgs<T>& a, cudaStream_t s) {
+  const size_t n = (size_t)a.nl * a.ny * a.nx;
+  int blocks = (int)((n + NT - 1) / NT);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  k_flush<T, COMP><<<blocks, NT, 0, s>>>(a);
+  k_end<<<1, 1, 0, s>>>(a.state);
+}
+
+// ---- entry points used by api.cu (see kernels.h)
+cudaError_t prepare_f64(const StepArgs<double>& a) { return set_attrs<double, false>(a); }
+cudaError_t prepare_f32c(const StepArgs<float>& a) { return set_attrs<float, true>(a); }
+
+void enqueue_begin(DevState* st, double t_out, double tend, cudaStream_t s) { k_begin<<<1, 1, 0, s>>>(st, t_out, tend); }
+
+void enqueue_step_f64(const StepArgs<double>& a, cudaStream_t s) {
+  launch_invert<double, false>(a, 1, s);
+  launch_rhs<double, false>(a, s);
+}
+void enqueue_step_f32c(const StepArgs<float>& a, cudaStream_t s) {
+  launch_invert<float, true>(a, 1, s);
+  launch_rhs<float, true>(a, s);
+}
+void enqueue_invert_f64(const StepArgs<double>& a, cudaStream_t s) { launch_invert<double, false>(a, 0, s); }
+void enqueue_invert_f32c(const StepArgs<float>& a, cudaStream_t s) { launch_invert<float, true>(a, 0, s); }
+void enqueue_flush_f64(const StepArgs<double>& a, cudaStream_t s) { launch_flush<double, false>(a, s); }
+void enqueue_flush_f32c(const StepArgs<float>& a, cudaStream_t s) { launch_flush<float, true>(a, s); }
+
+void enqueue_step_kernel_f64(const StepArgs<double>& a, int which, cudaStream_t s) {
+  if (which == 0) k_rows_fwd<double, false><<<dim3(a.ny), NT, smem_rows<double, false>(a), s>>>(a, 1);
+  if (which == 1) k_cols<double, false><<<dim3((a.nx + a.CT - 1) / a.CT, a.nl), NT, smem_cols<double, false>(a), s>>>(a, 1);
+  if (which == 2) k_rows_inv<double, false><<<dim3(a.ny), NT, smem_rows<double, false>(a), s>>>(a, 1);
+  if (which == 3) launch_rhs<double, false>(a, s);
+}
+void enqueue_step_kernel_f32c(const StepArgs<float>& a, int which, cudaStream_t s) {
+  if (which == 0) k_rows_fwd<float, true><<<dim3(a.ny), NT, smem_rows<float, true>(a), s>>>(a, 1);
+  if (which == 1) k_cols<float, true><<<dim3((a.nx + a.CT - 1) / a.CT, a.nl), NT, smem_cols<float, true>(a), s>>>(a, 1);
+  if (which == 2) k_rows_inv<float, true><<<dim3(a.ny), NT, smem_rows<float, true>(a), s>>>(a, 1);
+  if (which == 3) launch_rhs<float, true>(a, s);
+}
+
+void enqueue_split_f64(const double* src, float* hi, float* lo, size_t n, cudaStream_t s) {
+  k_split_f64<<<1024, 256, 0, s>>>(src, hi, lo, n);
+}
+void enqueue_join_f64(const float* hi, const float* lo, double* dst, size_t n, cudaStream_t s) {
+  k_join_f64<<<1024, 256, 0, s>>>(hi, lo, dst, n);
+}
+
+template <typename T>
+static void budget_impl(const StepArgs<T>& a, const double* wts, double* part, int nblk, double scale, double* out,
+                        cudaStream_t s) {
+  k_budget_partial<T><<<nblk, NT, 0, s>>>(a, wts, part);
+  k_budget_final<<<1, 32, 0, s>>>(part, nblk, scale, out);
+}
+void enqueue_budget_f64(const StepArgs<double>& a, const double* w, double* part, int nblk, double scale, double* out,
+                        cudaStream_t s) { budget_impl<double>(a, w, part, nblk, scale, out, s); }
+void enqueue_budget_f32c(const StepArgs<float>& a, const double* w, double* part, int nblk, double scale, double* out,
+                         cudaStream_t s) { budget_impl<float>(a, w, part, nblk, scale, out, s); }
+
+size_t smem_bytes_rows_f64(const StepArgs<double>& a) { return smem_rows<double, false>(a); }
+size_t smem_bytes_cols_f64(const StepArgs<double>& a) { return smem_cols<double, false>(a); }
+size_t smem_bytes_rhs_f64(const StepArgs<double>& a) { return smem_rhs<double>(a); }
+size_t smem_bytes_rows_f32c(const StepArgs<float>& a) { return smem_rows<float, true>(a); }
+size_t smem_bytes_cols_f32c(const StepArgs<float>& a) { return smem_cols<float, true>(a); }
+size_t smem_bytes_rhs_f32c(const StepArgs<float>& a) { return smem_rhs<float>(a); }
+
+}  // namespace qgw

@@ -1,0 +1,85 @@
+// qgw_device.cuh -- device-side state and kernel argument types of the
+// GB300 time step.
+//
+// Data layout in HBM (one run):
+//   interior-only fields, [nl][ny][pitch] with pitch = nx+1 (the DST length
+//   plus one padding column); reference point (i, j, k) with 1 <= i <= nx,
+//   1 <= j <= ny lives at k*ny*pitch + (j-1)*pitch + (i-1).  Ghost/wall
+//   values are never stored: kernels derive them from the boundary rule of
+//   adjust_bc (src/domain.h:308-348).
+//   q      FP64 (plain) or FP32 hi + FP32 lo (compensated)
+//   psi    streamfunction, same precision as the arithmetic
+//   spec   spectral work field between the row and column passes
+//   fab    3 slabs of the AB3 history (f0/f1/f2 rotate by step index)
+//   hinv   FP64 path only: 1 / (-(L^2 + K^2 + iRd2_m) * norm) per (m, j, k)
+//   topo   (ny+2) x (nx+2) reference layout (only when non-zero)
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "dst_core.h"
+
+namespace qgw {
+
+// Scalars that evolve on the device (the reference globals t, dt, dt0,
+// dt1 of src/qg.c:63-64 and src/timestep.h:286, plus the control flags of
+// the device-side driver loop).
+struct DevState {
+  double t, dt, dt0, dt1, DT_max;
+  double t_out, tend;
+  double c0, c1, c2;               // AB3 coefficients of the pending update
+  unsigned long long maxbits;      // CFL: max |dpsi| over the step, as bits
+  unsigned int done_blocks;        // last-block detection in the RHS kernel
+  int pending;                     // AB3 update computed but not yet applied
+  int active;                      // steps continue while 1
+  int first;                       // first step of the current call
+  int steps_taken;
+  int stop_reason;                 // 0 nsteps, 1 t_out, 2 tend, 3 non-finite
+  int nonfinite;
+  int step_index;                  // RHS evaluations so far (slab rotation)
+  int pad_;
+};
+
+// Everything a step kernel needs, passed by value.
+template <typename T> struct StepArgs {
+  // sizes
+  int nx, ny, nl, pitch;
+  long long lstride;               // ny * pitch
+  DstGeom gx, gy;
+  DstTables<T> tx, ty;
+  // vertical modes (FP64 master copies and T copies)
+  const T* cl2m;                   // nl*nl row-major, mode m row: cl2m[m*nl+l]
+  const T* cm2l;                   // cm2l[l*nl+m]
+  const double* iRd2;
+  // fields
+  T* q;                            // plain: q; compensated: q_hi
+  T* qlo;                          // compensated only
+  T* psi;
+  T* spec;
+  T* fab;                          // 3 slabs of nl*lstride
+  const double* hinv;              // FP64 path
+  const double* Lsq;               // L_{k+1}^2, k < nx
+  const double* Ksq;               // K_{j+1}^2, j < ny
+  const T* wind;                   // per interior row j: forcing_q (layer 0)
+  const double* topo;              // (ny+2)*(nx+2) or null
+  DevState* state;
+  // physics
+  double Delta, norm, cfl;
+  double inv12d2;                  // 1 / (12 Delta^2)
+  double b2d;                      // beta / (2 Delta)
+  double nu_d2;                    // nu / Delta^2
+  double nuh_scaled;               // nu_hyper / Delta^(2S)  (unscaled chain)
+  double drag_d2;                  // -hEkb f0 / (2 dh_{nl-1}) / Delta^2
+  double topo_fac;                 // f0 / dh_{nl-1}
+  double cbc;                      // 2 bc_fac / Delta^2 (ghost rule)
+  double gh[8];                    // ghost factor of chain sweep s: 2 bc Delta^(2s-2)
+  int nsweep;                      // hyperviscosity Laplacian sweeps (0: off)
+  int has_nu, has_topo, has_wind, has_drag;
+  // grouping
+  int G1;                          // modes per block in the row passes
+  int CT;                          // columns per block in the column pass
+  int low_k64;                     // compensated: FP64 divide for mode 0, j,k < low_k64
+};
+
+}  // namespace qgw

@@ -1,0 +1,49 @@
+// CPU check of the device DST-I building blocks (qgw_gb300/csrc/dst_core.h):
+// runs every phase's work items in a plain loop, exactly as the kernels
+// spread them over threads, and exposes the result through a C function.
+#include <vector>
+#include <cstring>
+#include "../../qgw_gb300/csrc/dst_tables.h"
+
+using namespace qgw;
+
+template <typename T>
+static void run(int M, int howmany, T* data) {
+  DstGeom g = make_geom(M);
+  DstTablesHost th = build_dst_tables(M);
+  std::vector<T> tw(th.tw.begin(), th.tw.end()), pre(th.pre.begin(), th.pre.end()),
+      spl(th.spl.begin(), th.spl.end());
+  const C2<T>* TW = (const C2<T>*)tw.data();
+  const C2<T>* PRE = (const C2<T>*)pre.data();
+  const C2<T>* SPL = (const C2<T>*)spl.data();
+  std::vector<T> A(M), B(M);
+  for (int r = 0; r < howmany; ++r) {
+    T* x = data + (size_t)r * (M - 1);
+    for (int j = 0; j < M - 1; ++j) A[j] = x[j];
+    A[M - 1] = T(12345);  // padding must never be read
+    for (int j = 1; j <= g.H; ++j) dst_pre_item<T>(A.data(), B.data(), j, g, PRE);
+    T* src = B.data();
+    T* dst = A.data();
+    int Ns = 1;
+    for (int p = 0; p < g.npass; ++p) {
+      const int R = g.radix[p];
+      for (int b = 0; b < g.H / R; ++b)
+        stockham_dispatch<T>(R, (const C2<T>*)src, (C2<T>*)dst, b, Ns, g.H, TW);
+      Ns *= R;
+      T* t = src; src = dst; dst = t;
+    }
+    // result in src; split into dst
+    for (int k = 0; k <= g.H / 2; ++k) dst_split_item<T>((const C2<T>*)src, dst, k, g, SPL);
+    std::vector<T> tot(g.nchunk);
+    for (int c = 0; c < g.nchunk; ++c) tot[c] = dst_scan_chunk<T>(dst, c, g);
+    T pref = T(0);
+    for (int c = 0; c < g.nchunk; ++c) {
+      if (c > 0) dst_scan_fix<T>(dst, c, pref, g);
+      pref += tot[c];
+    }
+    for (int j = 0; j < M - 1; ++j) x[j] = dst[j];
+  }
+}
+
+extern "C" void dst_core_run_f64(int M, int howmany, double* data) { run<double>(M, howmany, data); }
+extern "C" void dst_core_run_f32(int M, int howmany, float* data) { run<float>(M, howmany, data); }

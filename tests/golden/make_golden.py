@@ -1,0 +1,94 @@
+"""Generate the golden fixtures of tests/golden/ from the REFERENCE ITSELF.
+
+Each case runs the reference's own src/qg.c (compiled in place with the
+oracle shims, oracle/_ref/qgw_ref) from a seeded initial condition and
+stores inputs and outputs as compressed npz.  One case is driven by the
+parameter file the reference ships as test/params_03.in (read here from the
+reference tree; the fixture stores the parsed values, not the file).
+
+Run in the container that holds the reference sources:
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import oracle as O  # noqa: E402
+from qgw_gb300 import configs as C  # noqa: E402
+
+REF_TEST = os.environ.get("QGW_REF_TEST", "/root/reference/test")
+
+
+def parse_params_in(path):
+    """Minimal reader of a params.in for the fixture metadata (the reference
+    parser itself is what the run uses)."""
+    out = {}
+    ints = {"NX", "NY", "nl", "n_hyper"}
+    for line in open(path):
+        line = line.replace(" ", "").strip()
+        if "=" not in line or line.startswith("#"):
+            continue
+        k, v = line.split("=", 1)
+        if v.startswith("["):
+            out[k] = [float(x) for x in v.strip("[]").split(",")]
+        else:
+            try:
+                out[k] = int(v) if k in ints else float(v.rstrip(";"))
+            except ValueError:
+                pass
+    return out
+
+
+def cases():
+    out = []
+    p = C.cfg1(64)
+    out.append(("cfg1_nx64_fixed", p, 100, 1200.0, None))
+    p = C.cfg2(32, 10)
+    out.append(("cfg2_nx32_nl10_fixed", p, 100, 600.0, None))
+    p = C.cfg1(32)
+    p = {k: v for k, v in p.items() if k != "dt"}
+    p.update(tend=1e9, dt_out=86400.0 * 2)
+    out.append(("cfg1_nx32_adaptive", p, 40, None, None))
+    p = C.cfg1(32)
+    p.update(bc_fac=0.6, h_topo=150.0, w_topo=3e5)
+    out.append(("noslip_topo_nx32", p, 50, 1200.0, None))
+    p = C.cfg1(64)
+    p["NY"] = 32
+    out.append(("cfg1_nx64_ny32", p, 30, 1200.0, None))
+    ref03 = os.path.join(REF_TEST, "params_03.in")
+    if os.path.exists(ref03):
+        p = parse_params_in(ref03)
+        p["tend"] = 1e12
+        out.append(("ref_params03", p, 30, None, None))
+    return out
+
+
+def main():
+    O.build(ref=True)
+    if not O.ref_available():
+        raise SystemExit("reference build unavailable")
+    index = {}
+    for name, params, nsteps, dt, topo in cases():
+        seed = 7000 + len(index)
+        q0 = C.noise_ic(params, seed)
+        r = O.run_ref(params, q0, nsteps, dt_fixed=dt, fast_dst=False)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), q0=q0, psi=r["psi"], q=r["q"],
+                            cl2m=r["modes"][0], cm2l=r["modes"][1], iRd2=r["modes"][2])
+        index[name] = {"params": params, "nsteps": nsteps, "dt_fixed": dt, "seed": seed,
+                       "time": r["time"]}
+        print(name, r["time"])
+    with open(os.path.join(HERE, "index.json"), "w") as f:
+        json.dump(index, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()

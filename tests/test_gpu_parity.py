@@ -1,0 +1,188 @@
+"""Parity of the GPU step (through the C ABI) with the oracle.
+
+Tolerances: the plain FP64 path must match the reference's CPU step to
+rel-L2 <= 1e-12 on psi and q after 100 steps (rel-L2 = ||a-b||_2/||b||_2
+over the full reference-layout arrays); the compensated FP32 path must stay
+within 1e-5 of the FP64 result after 100 steps."""
+import numpy as np
+import pytest
+
+import golden_cases as G
+from qgw_gb300 import configs as C
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32C = 1e-5
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / nb if nb > 0 else np.linalg.norm(a - b)
+
+
+def gpu_run(capi, params, q0, nsteps, dt_fixed, precision=0, topo=None, snap=False):
+    r = capi.Run(params, precision, topo=topo)
+    r.set_q(q0)
+    if dt_fixed:
+        r.fix_dt(dt_fixed)
+        done = 0
+        while done < nsteps:
+            info = r.step(nsteps - done)
+            assert info.steps_taken > 0
+            done += info.steps_taken
+    else:
+        # the driver loop of src/qg.c:181-199 with t_out snapping
+        t_out = 0.0
+        done = 0
+        while done < nsteps:
+            tm = r.time()
+            if abs(tm["t"] - t_out) < 1e-9 * tm["dt"]:
+                t_out += params["dt_out"]
+            info = r.step(1, t_out=t_out, tend=params.get("tend", 0.0))
+            done += info.steps_taken
+    psi, q = r.get()
+    tm = r.time()
+    r.close()
+    return psi, q, tm
+
+
+@pytest.mark.parametrize("name", G.names())
+def test_fp64_matches_reference_golden(qgwlib, name):
+    meta, d = G.load(name)
+    p = meta["params"]
+    psi, q, tm = gpu_run(qgwlib, p, d["q0"], meta["nsteps"], meta["dt_fixed"])
+    assert rel(q, d["q"]) <= TOL64, rel(q, d["q"])
+    assert rel(psi, d["psi"]) <= TOL64, rel(psi, d["psi"])
+    assert tm["t"] == pytest.approx(meta["time"]["t"], rel=1e-14)
+    assert tm["dt"] == pytest.approx(meta["time"]["dt"], rel=1e-14)
+
+
+def test_invert_only(qgwlib, oracle_mod):
+    p = C.cfg2(128, 10)
+    q0 = C.noise_ic(p, 5)
+    port = oracle_mod.Port(p)
+    port.set_q(q0)
+    port.invert()
+    psi_o, q_o = port.get()
+    r = qgwlib.Run(p)
+    r.set_q(q0)
+    psi, q = r.get()
+    assert rel(psi, psi_o) <= 1e-13
+    assert rel(q, q_o) == 0.0
+
+
+@pytest.mark.parametrize("case", ["cfg1_256", "cfg2_256_nl10", "noslip_topo_128", "nxny_256x128"])
+def test_fp64_vs_port_100_steps(qgwlib, oracle_mod, case):
+    if case == "cfg1_256":
+        p, dt = C.cfg1(256), 1200.0
+    elif case == "cfg2_256_nl10":
+        p, dt = C.cfg2(256, 10), 600.0
+    elif case == "noslip_topo_128":
+        p, dt = dict(C.cfg1(128), bc_fac=1.0, h_topo=300.0, w_topo=4e5), 1200.0
+    else:
+        p, dt = dict(C.cfg1(256), NY=128), 1200.0
+    q0 = C.noise_ic(p, 1001)
+    o = oracle_mod.run_port(p, q0, 100, dt_fixed=dt)
+    psi, q, tm = gpu_run(qgwlib, p, q0, 100, dt)
+    assert rel(q, o["q"]) <= TOL64, rel(q, o["q"])
+    assert rel(psi, o["psi"]) <= TOL64, rel(psi, o["psi"])
+
+
+def test_fp64_adaptive_dt_vs_port(qgwlib, oracle_mod):
+    p = dict(C.cfg1(128))
+    p.pop("dt")
+    p.update(tend=1e9, dt_out=86400.0 * 2)
+    q0 = C.noise_ic(p, 17)
+    o = oracle_mod.run_port(p, q0, 40)
+    psi, q, tm = gpu_run(qgwlib, p, q0, 40, None)
+    assert tm["t"] == pytest.approx(o["time"]["t"], rel=1e-14)
+    assert tm["dt"] == pytest.approx(o["time"]["dt"], rel=1e-14)
+    assert rel(q, o["q"]) <= TOL64
+    assert rel(psi, o["psi"]) <= TOL64
+
+
+def test_full_size_few_steps_vs_port(qgwlib, oracle_mod):
+    """1024^2 x 10 layers (the measured configuration), 3 steps."""
+    p = C.cfg2(1024, 10)
+    q0 = C.noise_ic(p, 2001)
+    o = oracle_mod.run_port(p, q0, 3, dt_fixed=600.0)
+    psi, q, _ = gpu_run(qgwlib, p, q0, 3, 600.0)
+    assert rel(q, o["q"]) <= TOL64
+    assert rel(psi, o["psi"]) <= TOL64
+
+
+def test_analytic_mode_inversion_full_size(qgwlib):
+    """Known answer: q = sin(a pi x/L) sin(b pi y/L) on one vertical mode m
+    inverts to psi = q / -((a pi/L)^2 + (b pi/L)^2 + iRd2_m) exactly."""
+    p = C.cfg2(1024, 10)
+    cl, cm, ird = qgwlib.eigmode(p)
+    nl, ny2, nx2 = 10, 1025, 1025
+    L = p["Lx"]
+    D = L / 1024
+    x = np.arange(nx2) * D
+    y = np.arange(ny2)[:, None] * D
+    for a, b, m in [(1, 1, 0), (3, 7, 4), (500, 2, 9), (1000, 1001, 3)]:
+        shape = np.sin(a * np.pi * x / L) * np.sin(b * np.pi * y / L)
+        shape[0, :] = shape[-1, :] = 0
+        shape[:, 0] = shape[:, -1] = 0
+        q = cm[:, m][:, None, None] * shape[None]
+        r = qgwlib.Run(p)
+        r.set_q(q)
+        psi, _ = r.get()
+        r.close()
+        expect = q / -((a * np.pi / L) ** 2 + (b * np.pi / L) ** 2 + ird[m])
+        assert rel(psi, expect) <= 1e-12, (a, b, m, rel(psi, expect))
+
+
+def test_fp32c_vs_fp64_100_steps(qgwlib):
+    p = C.cfg2(256, 10)
+    q0 = C.noise_ic(p, 33)
+    psi64, q64, _ = gpu_run(qgwlib, p, q0, 100, 600.0, precision=0)
+    psi32, q32, _ = gpu_run(qgwlib, p, q0, 100, 600.0, precision=1)
+    assert rel(q32, q64) <= TOL32C, rel(q32, q64)
+    assert rel(psi32, psi64) <= TOL32C, rel(psi32, psi64)
+
+
+def test_budget_matches_numpy(qgwlib):
+    p = C.cfg1(128)
+    q0 = C.noise_ic(p, 9)
+    r = qgwlib.Run(p)
+    r.set_q(q0)
+    r.fix_dt(1200.0)
+    r.step(10)
+    b = r.budget()
+    psi, q = r.get()
+    r.close()
+    dh = np.array(p["dh"])
+    w = dh / dh.sum()
+    D = p["Lx"] / p["NX"]
+    scale = D * D / (p["Lx"] * p["Lx"])
+    P, Q = psi[:, 1:-1, 1:-1], q[:, 1:-1, 1:-1]
+    u = (psi[:, 1:-1, 2:] - P) / D
+    v = (psi[:, 2:, 1:-1] - P) / D
+    ke = (w[:, None, None] * 0.5 * (u ** 2 + v ** 2)).sum() * scale
+    en = -(w[:, None, None] * P * Q).sum() * scale
+    ens = (w[:, None, None] * Q * Q).sum() * scale
+    assert b["ke"] == pytest.approx(ke, rel=1e-12)
+    assert b["energy"] == pytest.approx(en, rel=1e-12)
+    assert b["enstrophy"] == pytest.approx(ens, rel=1e-12)
+
+
+def test_step_stops_at_t_out_and_tend(qgwlib):
+    p = dict(C.cfg1(64), dt=1000.0)
+    r = qgwlib.Run(p)
+    r.set_q(C.noise_ic(p, 1))
+    info = r.step(100, t_out=5000.0)
+    assert info.steps_taken == 5 and info.stop_reason == 1
+    info = r.step(100, t_out=0.0, tend=8000.0)
+    assert info.steps_taken == 3 and info.stop_reason == 2
+    assert r.time()["t"] == pytest.approx(8000.0)
+    r.close()
+
+
+def test_unsupported_configs_fail_loudly(qgwlib):
+    for bad in (dict(C.cfg1(64), NX=100), dict(C.cfg1(64), bc_fac=-1.0), dict(C.cfg1(64), k_f=3.0)):
+        with pytest.raises(qgwlib.QgwError) as e:
+            qgwlib.Run(bad)
+        assert e.value.status == -6

