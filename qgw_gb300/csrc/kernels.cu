@@ -600,16 +600,28 @@ static size_t smem_rhs(const StepArgs<T>& a) {
   return sizeof(T) * (3 * W * Hh + (TX + 2) * (TY + 2) + 2 * (TX + 2) * TY + 2 * TX * (TY + 2));
 }
 
+// The dynamic shared-memory limit is a process-wide attribute of each kernel,
+// shared by every run in the process; it is set to the device's opt-in
+// maximum (never lowered) so that runs of different sizes can coexist.
 template <typename T, bool COMP>
 static cudaError_t set_attrs(const StepArgs<T>& a) {
-  cudaError_t e;
-  e = cudaFuncSetAttribute(k_rows_fwd<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_rows<T, COMP>(a));
+  int dev = 0, optin = 0;
+  cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_rows_inv<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_rows<T, COMP>(a));
+  e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_cols<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cols<T, COMP>(a));
+  const size_t static_tot = sizeof(T) * GMAX * 32 + 64;
+  if (smem_rows<T, COMP>(a) + static_tot > (size_t)optin || smem_cols<T, COMP>(a) + static_tot > (size_t)optin ||
+      smem_rhs<T>(a) + 1024 > (size_t)optin)
+    return cudaErrorInvalidValue;
+  const int lim = optin - (int)static_tot;
+  e = cudaFuncSetAttribute(k_rows_fwd<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_rhs<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_rhs<T>(a));
+  e = cudaFuncSetAttribute(k_rows_inv<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_cols<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_rhs<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - 1024);
 }
 
 template <typename T, bool COMP>

@@ -186,3 +186,20 @@ def test_unsupported_configs_fail_loudly(qgwlib):
         with pytest.raises(qgwlib.QgwError) as e:
             qgwlib.Run(bad)
         assert e.value.status == -6
+
+
+def test_runs_of_different_sizes_coexist(qgwlib):
+    """A small run created after a large one must not break the large one
+    (the dynamic shared-memory limit is a per-kernel process-wide setting)."""
+    big = dict(C.cfg2(1024, 10))
+    small = dict(C.cfg1(32))
+    rb = qgwlib.Run(big)
+    rb.set_q(C.noise_ic(big, 1))
+    rb.fix_dt(600.0)
+    rs = qgwlib.Run(small)
+    rs.set_q(C.noise_ic(small, 2))
+    rs.fix_dt(1200.0)
+    assert rs.step(2).steps_taken == 2
+    assert rb.step(2).steps_taken == 2
+    rb.close()
+    rs.close()
