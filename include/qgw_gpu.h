@@ -201,6 +201,25 @@ int qgw_kernels_per_step(qgw_run* run);
  * inverse y-DST), ms4[2] rows inverse (x-DST + back-projection), ms4[3] RHS. */
 int qgw_profile_kernels(qgw_run* run, int nsteps, float* ms4);
 
+/* PV inversion without any allocation (no counterpart in the reference,
+ * whose invert_pv, src/elliptic.h:149, allocates nothing only because its
+ * work array is a global made at start-up).  For callers that cannot
+ * allocate device memory -- a host model whose memory manager owns every
+ * device buffer, or a loop that must not call cudaMalloc/cudaFree, which
+ * synchronise the device and can fail under memory pressure.  q_dev and
+ * psi_dev are the caller's device arrays in the reference layout
+ * (nl, NY+1, NX+1); on return (asynchronously, on `stream`) psi_dev holds
+ * psi with a zero ghost ring and q_dev's ghost ring is set as invert_pv sets
+ * it.  cl2m, cm2l, iRd2 are host arrays (e.g. from qgw_eigmode).  Scratch
+ * is one file-scope device array of 32 MiB held by every GPU that loads the
+ * library: sizes beyond nl*(NX+1)*(NY+1) <= 2097152, NX, NY <= 1024 or
+ * nl > 32 are rejected with QGW_ERR_UNSUPPORTED.  The first call on a device
+ * looks up the array's device address (with that device current) and should
+ * come before any stream capture.  Calls share the array: calls that
+ * overlap on the GPU, or come from several host threads at once, race. */
+int qgw_invert_pv_noalloc(const qgw_params* p, const double* cl2m, const double* cm2l,
+                          const double* iRd2, double* q_dev, double* psi_dev, void* stream);
+
 /* Measured FMA throughput of the current device in TFLOP/s (FP64 and FP32,
  * independent FMA chains): the arithmetic roofs of the FP64 kernels. */
 int qgw_probe_fp_rates(double* fp64_tflops, double* fp32_tflops);
