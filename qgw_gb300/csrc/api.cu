@@ -187,6 +187,37 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   a.has_wind = p.tau0 != 0;
   choose_groups(r->nl, r->nx + 1, r->ny + 1, sizeof(T), &a.G1, &a.CT);
   a.low_k64 = 8;
+  // compensated path: psi's FP32 round-off is white in wavenumber while psi
+  // itself is dominated by the largest scales, so Laplacians of psi taken
+  // by stencils lose ~(k_max/k_min)^2 of relative accuracy at grid scale.
+  // The discrete Laplacian zeta is therefore formed spectrally (exact
+  // symbol) and feeds the hyperviscosity chain and the bottom drag.
+  a.G3 = a.G1;
+  a.zeta_mode = 0;
+  a.spec2 = nullptr;
+  a.zeta = nullptr;
+  if (r->precision == QGW_FP32C && (a.nsweep > 0 || a.has_drag)) {
+    a.zeta_mode = 1;
+    if ((rc = dalloc(r, &a.spec2, field))) return rc;
+    if ((rc = dalloc(r, &a.zeta, field))) return rc;
+    const size_t budget = 96 * 1024;
+    int g3 = (int)(budget / (4 * (size_t)(r->nx + 1) * sizeof(T)));
+    g3 = g3 < 1 ? 1 : (g3 > 8 ? 8 : g3);
+    const int ng = (r->nl + g3 - 1) / g3;
+    a.G3 = (r->nl + ng - 1) / ng;
+    int ct = (int)(budget / (3 * (size_t)(r->ny + 1) * sizeof(T)));
+    a.CT = ct < 1 ? 1 : (ct > 16 ? 16 : ct);
+    std::vector<double> sx(r->nx), sy(r->ny);
+    for (int k = 0; k < r->nx; ++k) { const double s = std::sin(M_PI * (k + 1) / (2.0 * (r->nx + 1))); sx[k] = s * s; }
+    for (int j = 0; j < r->ny; ++j) { const double s = std::sin(M_PI * (j + 1) / (2.0 * (r->ny + 1))); sy[j] = s * s; }
+    double *dsx, *dsy;
+    if ((rc = upload<double>(r, &dsx, sx))) return rc;
+    if ((rc = upload<double>(r, &dsy, sy))) return rc;
+    a.sx2 = dsx;
+    a.sy2 = dsy;
+    a.lx2 = -4.0 / (r->Delta * r->Delta);
+    a.ly2 = a.lx2;
+  }
   return QGW_OK;
 }
 
@@ -220,7 +251,7 @@ int qgw_footprint(const qgw_params* p, int precision, size_t* bytes) {
   const size_t field = (size_t)p->nl * ny * (nx + 1);
   size_t b;
   if (precision == QGW_FP64) b = field * 8 * 7;  // q psi spec f0 f1 f2 hinv
-  else b = field * 4 * 7 + field * 8;            // q_hi q_lo psi spec f0 f1 f2 + FP64 staging
+  else b = field * 4 * 9 + field * 8;            // q_hi q_lo psi spec spec2 zeta f0 f1 f2 + FP64 staging
   *bytes = b + (size_t)(nx + ny) * 64 + (1 << 20);
   return QGW_OK;
 }

@@ -198,6 +198,11 @@ __global__ void __launch_bounds__(NT) k_cols(StepArgs<T> a, int step_mode) {
   __syncthreads();
   T* O = dst_block<T>(A, B, CTb, ld, a.gy, a.ty, tot);
   const double iRd2 = a.iRd2[m];
+  // zeta mode: C receives the spectral discrete Laplacian of psi,
+  // lambda(k, j) * psi_hat with lambda = -4/Delta^2 (sin^2 kx + sin^2 ky), the
+  // exact symbol of the 5-point Laplacian with zero ghosts in the DST basis
+  T* C = (T*)smem_raw + (size_t)2 * a.CT * ld;
+  const bool zm = COMP && a.zeta_mode;
   for (int w = threadIdx.x; w < ny * CTb; w += NT) {
     const int jj = w / CTb, c = w - jj * CTb;
     const int k = k0 + c;
@@ -211,6 +216,10 @@ __global__ void __launch_bounds__(NT) k_cols(StepArgs<T> a, int step_mode) {
       const float fact = -(((float)a.Lsq[k] + (float)a.Ksq[jj]) + (float)iRd2);
       O[c * ld + jj] = (T)((float)O[c * ld + jj] / (fact * (float)a.norm));
     }
+    if (zm) {
+      const float lam = (float)a.lx2 * (float)a.sx2[k] + (float)a.ly2 * (float)a.sy2[jj];
+      C[c * ld + jj] = (T)(lam * (float)O[c * ld + jj]);
+    }
   }
   __syncthreads();
   T* Oth = (O == A) ? B : A;
@@ -219,9 +228,21 @@ __global__ void __launch_bounds__(NT) k_cols(StepArgs<T> a, int step_mode) {
     const int jj = w / CTb, c = w - jj * CTb;
     S[(size_t)jj * a.pitch + k0 + c] = O2[c * ld + jj];
   }
+  if (zm) {
+    __syncthreads();
+    T* O3 = dst_block<T>(C, O2 == A ? B : A, CTb, ld, a.gy, a.ty, tot);
+    T* S2 = a.spec2 + (size_t)m * a.lstride;
+    for (int w = threadIdx.x; w < ny * CTb; w += NT) {
+      const int jj = w / CTb, c = w - jj * CTb;
+      S2[(size_t)jj * a.pitch + k0 + c] = O3[c * ld + jj];
+    }
+  }
 }
 
 // ------------------------------------------------------------------ K3
+// One block per row j; mode groups in turn.  In zeta mode each group also
+// inverse-transforms the spectral zeta rows (rows G..2G-1 of the batch) and
+// back-projects them into zeta.
 template <typename T, bool COMP>
 __global__ void __launch_bounds__(NT) k_rows_inv(StepArgs<T> a, int step_mode) {
   DevState* st = a.state;
@@ -230,23 +251,34 @@ __global__ void __launch_bounds__(NT) k_rows_inv(StepArgs<T> a, int step_mode) {
   __shared__ T tot[GMAX * 32];
   const int j = blockIdx.x;
   const int ld = a.gx.M;
+  const bool zm = COMP && a.zeta_mode;
+  const int Gb = zm ? a.G3 : a.G1;
   T* A = (T*)smem_raw;
-  T* B = A + (size_t)a.G1 * ld;
+  T* B = A + (size_t)(zm ? 2 * Gb : Gb) * ld;
   const T* cm = a.cm2l;
-  for (int m0 = 0; m0 < a.nl; m0 += a.G1) {
-    const int G = min(a.G1, a.nl - m0);
+  for (int m0 = 0; m0 < a.nl; m0 += Gb) {
+    const int G = min(Gb, a.nl - m0);
     for (int gg = 0; gg < G; ++gg) {
       const T* srow = a.spec + (size_t)(m0 + gg) * a.lstride + (size_t)j * a.pitch;
       for (int i = threadIdx.x; i < a.nx; i += NT) A[gg * ld + i] = srow[i];
+      if (zm) {
+        const T* zrow = a.spec2 + (size_t)(m0 + gg) * a.lstride + (size_t)j * a.pitch;
+        for (int i = threadIdx.x; i < a.nx; i += NT) A[(G + gg) * ld + i] = zrow[i];
+      }
     }
     __syncthreads();
-    T* O = dst_block<T>(A, B, G, ld, a.gx, a.tx, tot);
+    T* O = dst_block<T>(A, B, zm ? 2 * G : G, ld, a.gx, a.tx, tot);
     for (int i = threadIdx.x; i < a.nx; i += NT) {
       for (int l = 0; l < a.nl; ++l) {
         const size_t o = (size_t)l * a.lstride + (size_t)j * a.pitch + i;
         T acc = (m0 == 0) ? T(0) : a.psi[o];
         for (int gg = 0; gg < G; ++gg) acc = fmaT(cm[l * a.nl + m0 + gg], O[gg * ld + i], acc);
         a.psi[o] = acc;
+        if (zm) {
+          T zc = (m0 == 0) ? T(0) : a.zeta[o];
+          for (int gg = 0; gg < G; ++gg) zc = fmaT(cm[l * a.nl + m0 + gg], O[(G + gg) * ld + i], zc);
+          a.zeta[o] = zc;
+        }
       }
     }
     __syncthreads();
@@ -339,6 +371,9 @@ __global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
 
   const T* psiL = a.psi + (size_t)k * a.lstride;
   const T* qL = a.q + (size_t)k * a.lstride;
+  const bool zm = COMP && a.zeta_mode;
+  const T* zetaL = zm ? a.zeta + (size_t)k * a.lstride : nullptr;
+  const double d2 = a.Delta * a.Delta;
 #define PS(x, y) ps[((y) + r) * W + (x) + r]
   for (int w = threadIdx.x; w < W * Hh; w += NT) {
     const int x = w % W - r, y = w / W - r;
@@ -380,8 +415,13 @@ __global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
       const int o = (y + r) * W + x + r;
       T v = T(0);
       if (inx && iny) {
-        const T sum = (Lp[o + 1] + Lp[o - 1]) + (Lp[o + W] + Lp[o - W]);
-        v = fmaT(T(-4), Lp[o], sum);
+        if (s == 1 && zm) {
+          // sweep 1 from the spectral zeta (unscaled: Delta^2 * zeta)
+          v = (T)d2 * zetaL[(size_t)gj * a.pitch + gi];
+        } else {
+          const T sum = (Lp[o + 1] + Lp[o - 1]) + (Lp[o + W] + Lp[o - W]);
+          v = fmaT(T(-4), Lp[o], sum);
+        }
       } else if (iny && gi == -1) v = ghs * PS(x + 1, y);
       else if (iny && gi == nx) v = ghs * PS(x - 1, y);
       else if (inx && gj == -1) v = ghs * PS(x, y + 1);
@@ -439,7 +479,8 @@ __global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
     if (k == 0 && a.has_wind) f += a.wind[gj];
     if (bottom) {
       if (a.has_drag) {
-        const T lp = fmaT(T(-4), PS(x, y), (PS(x + 1, y) + PS(x - 1, y)) + (PS(x, y + 1) + PS(x, y - 1)));
+        const T lp = zm ? (T)d2 * zetaL[(size_t)gj * a.pitch + gi]
+                        : fmaT(T(-4), PS(x, y), (PS(x + 1, y) + PS(x - 1, y)) + (PS(x, y + 1) + PS(x, y - 1)));
         f = fmaT((T)a.drag_d2, lp, f);
       }
       if (a.has_topo) {
@@ -592,7 +633,13 @@ __global__ void k_budget_final(const double* part, int nblk, double scale, doubl
 template <typename T, bool COMP>
 static size_t smem_rows(const StepArgs<T>& a) { return (size_t)2 * a.G1 * a.gx.M * sizeof(T); }
 template <typename T, bool COMP>
-static size_t smem_cols(const StepArgs<T>& a) { return (size_t)2 * a.CT * a.gy.M * sizeof(T); }
+static size_t smem_cols(const StepArgs<T>& a) {
+  return (size_t)((COMP && a.zeta_mode) ? 3 : 2) * a.CT * a.gy.M * sizeof(T);
+}
+template <typename T, bool COMP>
+static size_t smem_rows_inv(const StepArgs<T>& a) {
+  return (COMP && a.zeta_mode) ? (size_t)4 * a.G3 * a.gx.M * sizeof(T) : smem_rows<T, COMP>(a);
+}
 template <typename T>
 static size_t smem_rhs(const StepArgs<T>& a) {
   const int r = a.nsweep > 0 ? a.nsweep : 1;
@@ -612,6 +659,7 @@ static cudaError_t set_attrs(const StepArgs<T>& a) {
   if (e != cudaSuccess) return e;
   const size_t static_tot = sizeof(T) * GMAX * 32 + 64;
   if (smem_rows<T, COMP>(a) + static_tot > (size_t)optin || smem_cols<T, COMP>(a) + static_tot > (size_t)optin ||
+      smem_rows_inv<T, COMP>(a) + static_tot > (size_t)optin ||
       smem_rhs<T>(a) + 1024 > (size_t)optin)
     return cudaErrorInvalidValue;
   const int lim = optin - (int)static_tot;
@@ -628,7 +676,7 @@ template <typename T, bool COMP>
 static void launch_invert(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
   k_rows_fwd<T, COMP><<<dim3(a.ny), NT, smem_rows<T, COMP>(a), s>>>(a, step_mode);
   k_cols<T, COMP><<<dim3((a.nx + a.CT - 1) / a.CT, a.nl), NT, smem_cols<T, COMP>(a), s>>>(a, step_mode);
-  k_rows_inv<T, COMP><<<dim3(a.ny), NT, smem_rows<T, COMP>(a), s>>>(a, step_mode);
+  k_rows_inv<T, COMP><<<dim3(a.ny), NT, smem_rows_inv<T, COMP>(a), s>>>(a, step_mode);
 }
 
 template <typename T, bool COMP>
@@ -667,13 +715,13 @@ void enqueue_flush_f32c(const StepArgs<float>& a, cudaStream_t s) { launch_flush
 void enqueue_step_kernel_f64(const StepArgs<double>& a, int which, cudaStream_t s) {
   if (which == 0) k_rows_fwd<double, false><<<dim3(a.ny), NT, smem_rows<double, false>(a), s>>>(a, 1);
   if (which == 1) k_cols<double, false><<<dim3((a.nx + a.CT - 1) / a.CT, a.nl), NT, smem_cols<double, false>(a), s>>>(a, 1);
-  if (which == 2) k_rows_inv<double, false><<<dim3(a.ny), NT, smem_rows<double, false>(a), s>>>(a, 1);
+  if (which == 2) k_rows_inv<double, false><<<dim3(a.ny), NT, smem_rows_inv<double, false>(a), s>>>(a, 1);
   if (which == 3) launch_rhs<double, false>(a, s);
 }
 void enqueue_step_kernel_f32c(const StepArgs<float>& a, int which, cudaStream_t s) {
   if (which == 0) k_rows_fwd<float, true><<<dim3(a.ny), NT, smem_rows<float, true>(a), s>>>(a, 1);
   if (which == 1) k_cols<float, true><<<dim3((a.nx + a.CT - 1) / a.CT, a.nl), NT, smem_cols<float, true>(a), s>>>(a, 1);
-  if (which == 2) k_rows_inv<float, true><<<dim3(a.ny), NT, smem_rows<float, true>(a), s>>>(a, 1);
+  if (which == 2) k_rows_inv<float, true><<<dim3(a.ny), NT, smem_rows_inv<float, true>(a), s>>>(a, 1);
   if (which == 3) launch_rhs<float, true>(a, s);
 }
 

@@ -57,6 +57,8 @@ template <typename T> struct StepArgs {
   T* qlo;                          // compensated only
   T* psi;
   T* spec;
+  T* spec2;                        // compensated: spectral zeta between K2 and K3
+  T* zeta;                         // compensated: discrete Laplacian of psi
   T* fab;                          // 3 slabs of nl*lstride
   const double* hinv;              // FP64 path
   const double* Lsq;               // L_{k+1}^2, k < nx
@@ -78,6 +80,11 @@ template <typename T> struct StepArgs {
   int has_nu, has_topo, has_wind, has_drag;
   // grouping
   int G1;                          // modes per block in the row passes
+  int G3;                          // modes per block in K3 (zeta doubles the rows)
+  int zeta_mode;                   // 1: K2/K3 also produce zeta, K4 uses it
+  double lx2, ly2;                 // -4/Delta^2 factors of the discrete symbol
+  const double* sx2;               // sin^2(pi k / (2 Mx)), k = 1..nx
+  const double* sy2;               // sin^2(pi j / (2 My)), j = 1..ny
   int CT;                          // columns per block in the column pass
   int low_k64;                     // compensated: FP64 divide for mode 0, j,k < low_k64
 };
