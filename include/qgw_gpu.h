@@ -224,6 +224,19 @@ int qgw_invert_pv_noalloc(const qgw_params* p, const double* cl2m, const double*
  * independent FMA chains): the arithmetic roofs of the FP64 kernels. */
 int qgw_probe_fp_rates(double* fp64_tflops, double* fp32_tflops);
 
+/* ---- netCDF-3 output and restart (host code, no netCDF library) --------
+ * vars.nc as create_nc/write_nc write it (src/netcdf_io.h:38-277): dims
+ * t (unlimited), level, y, x; float variables t, y, x, level, psi, q, the
+ * fields including the wall ring.  qgw_nc_read replaces read_nc
+ * (src/netcdf_io.h:286-382): record `rec` of a variable with `count` values
+ * per record, e.g. "q" (nl*(NY+1)*(NX+1)) or "topo" ((NY+1)*(NX+1)); it
+ * returns the number of values read or a negative status. */
+typedef struct qgw_nc qgw_nc;
+qgw_nc* qgw_nc_create(const char* path, int nl, int ny_out, int nx_out, double Delta);
+int qgw_nc_write(qgw_nc* nc, double t, const double* psi, const double* q);
+void qgw_nc_close(qgw_nc* nc);
+long qgw_nc_read(const char* path, const char* name, int rec, double* out, long count);
+
 const char* qgw_strerror(int status);
 int qgw_abi_version(void);
 

@@ -15,13 +15,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "lib")
 LIB = os.path.join(OUT, "libqgw_gpu.so")
+DRIVER = os.path.join(OUT, "qg_gpu")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"] + ARCH
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall"]
 
 CU_SOURCES = ["kernels.cu", "api.cu", "probe.cu", "noalloc.cu"]
-CXX_SOURCES = ["host.cpp"]
+CXX_SOURCES = ["host.cpp", "ncio.cpp"]
 
 
 def nvcc() -> str:
@@ -41,6 +42,7 @@ def _stale(objs, srcs) -> bool:
         return True
     t = os.path.getmtime(LIB)
     deps = [os.path.join(SRC, f) for f in os.listdir(SRC)]
+    deps += [os.path.join(HERE, "driver", f) for f in os.listdir(os.path.join(HERE, "driver"))]
     deps.append(os.path.join(HERE, "..", "include", "qgw_gpu.h"))
     deps.append(os.path.abspath(__file__))
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
@@ -81,6 +83,14 @@ def build(verbose: bool = False, force: bool = False, ptxas_v: bool = False) -> 
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{' '.join(link)}\n{res.stderr}")
     os.replace(tmp, LIB)
+    # the qg executable on top of the library (rpath: same directory)
+    drv = [("g++", os.path.join(HERE, "driver", "qg_gpu.cpp"), DRIVER)]
+    for cxx, src, out in drv:
+        cmd = [cxx] + CXXFLAGS + [src, "-o", out + ".tmp", "-L", OUT, "-lqgw_gpu", "-Wl,-rpath,$ORIGIN", "-lm"]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"building {out} failed:\n{' '.join(cmd)}\n{res.stderr}")
+        os.replace(out + ".tmp", out)
     return LIB
 
 

@@ -42,6 +42,7 @@ EXPORTS = [
     "qgw_create", "qgw_destroy", "qgw_set_q", "qgw_set_q_device", "qgw_put_q", "qgw_get_time", "qgw_set_time",
     "qgw_step", "qgw_invert", "qgw_get", "qgw_budget", "qgw_footprint", "qgw_stream",
     "qgw_kernels_per_step", "qgw_profile_kernels", "qgw_probe_fp_rates", "qgw_strerror", "qgw_abi_version",
+    "qgw_invert_pv_noalloc", "qgw_nc_create", "qgw_nc_write", "qgw_nc_close", "qgw_nc_read",
 ]
 
 
@@ -91,6 +92,13 @@ def load(path: str = LIB_PATH):
     lib.qgw_strerror.argtypes = [I]
     lib.qgw_strerror.restype = ctypes.c_char_p
     lib.qgw_abi_version.argtypes = []
+    lib.qgw_nc_create.argtypes = [ctypes.c_char_p, I, I, I, ctypes.c_double]
+    lib.qgw_nc_create.restype = V
+    lib.qgw_nc_write.argtypes = [V, ctypes.c_double, D, D]
+    lib.qgw_nc_close.argtypes = [V]
+    lib.qgw_nc_close.restype = None
+    lib.qgw_nc_read.argtypes = [ctypes.c_char_p, ctypes.c_char_p, I, D, ctypes.c_long]
+    lib.qgw_nc_read.restype = ctypes.c_long
     _lib = lib
     return lib
 
@@ -145,6 +153,35 @@ def footprint(params: Dict[str, object], precision: int = FP64) -> int:
     b = ctypes.c_size_t()
     _check(lib.qgw_footprint(ctypes.byref(s), int(precision), ctypes.byref(b)), "qgw_footprint")
     return int(b.value)
+
+
+class NcWriter:
+    """vars.nc in the reference's layout (netCDF-3, written by the library)."""
+
+    def __init__(self, path: str, nl: int, ny_out: int, nx_out: int, Delta: float):
+        self.lib = load()
+        self.h = self.lib.qgw_nc_create(path.encode(), nl, ny_out, nx_out, float(Delta))
+        if not self.h:
+            raise QgwError(-2, "qgw_nc_create")
+
+    def write(self, t: float, psi: np.ndarray, q: np.ndarray):
+        psi = np.ascontiguousarray(psi, dtype=np.float64)
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        _check(self.lib.qgw_nc_write(self.h, float(t), _dp(psi), _dp(q)), "qgw_nc_write")
+
+    def close(self):
+        if self.h:
+            self.lib.qgw_nc_close(self.h)
+            self.h = None
+
+
+def nc_read(path: str, name: str, shape, rec: int = 0) -> np.ndarray:
+    """Record `rec` of a netCDF-3 variable as float64 of the given shape."""
+    out = np.empty(shape, dtype=np.float64)
+    n = load().qgw_nc_read(path.encode(), name.encode(), int(rec), _dp(out), int(out.size))
+    if n < 0:
+        raise QgwError(int(n), f"qgw_nc_read({name})")
+    return out
 
 
 class Run:

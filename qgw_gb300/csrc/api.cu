@@ -82,7 +82,7 @@ int upload(qgw_run* r, T** out, const std::vector<double>& host) {
 // each block's two work buffers stay within the shared-memory budget
 void choose_groups(int nl, int Mx, int My, size_t elem, int* G1, int* CT) {
   const size_t budget = 96 * 1024;
-  int g = (int)(budget / (2 * (size_t)Mx * elem));
+  int g = (int)(budget / (2 * (size_t)qgw::padded_len(Mx) * elem));
   if (g < 1) g = 1;
   if (g > 16) g = 16;
   const int ngroups = (nl + g - 1) / g;
@@ -187,6 +187,10 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   a.has_wind = p.tau0 != 0;
   choose_groups(r->nl, r->nx + 1, r->ny + 1, sizeof(T), &a.G1, &a.CT);
   a.low_k64 = 8;
+  // 16-byte column vectors: rows 16-byte aligned and a whole number of
+  // 32-byte column tiles per row, so a tile never crosses into the next row
+  const int ct = (int)(32 / sizeof(T));
+  a.vec_cols = ((size_t)r->pitch * sizeof(T)) % 16 == 0 && r->pitch % ct == 0;
   // compensated path: psi's FP32 round-off is white in wavenumber while psi
   // itself is dominated by the largest scales, so Laplacians of psi taken
   // by stencils lose ~(k_max/k_min)^2 of relative accuracy at grid scale.
@@ -201,7 +205,7 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
     if ((rc = dalloc(r, &a.spec2, field))) return rc;
     if ((rc = dalloc(r, &a.zeta, field))) return rc;
     const size_t budget = 96 * 1024;
-    int g3 = (int)(budget / (4 * (size_t)(r->nx + 1) * sizeof(T)));
+    int g3 = (int)(budget / (4 * (size_t)qgw::padded_len(r->nx + 1) * sizeof(T)));
     g3 = g3 < 1 ? 1 : (g3 > 8 ? 8 : g3);
     const int ng = (r->nl + g3 - 1) / g3;
     a.G3 = (r->nl + ng - 1) / ng;

@@ -18,7 +18,7 @@
 // them over a thread block, the CPU unit test runs them in a loop).  Rows
 // are stored contiguously: row r of a buffer starts at r * ld reals.
 //
-// Buffer formats (reals):
+// Buffer formats (reals, every access through the padded index pr/pc):
 //   input   x_j at index j-1 (j = 1..M-1); index M-1 is padding
 //   work    H complex values = M reals
 //   output  Y_k at index k-1 (k = 1..M-1)  -- same as the input format,
@@ -56,6 +56,15 @@ QGW_HD float fmaT(float a, float b, float c) {
   return __builtin_fmaf(a, b, c);
 #endif
 }
+
+// Padded layout of a row buffer in shared memory: one pad slot after every
+// 8 complex values (16 reals), so that the stride-8 stores of the first
+// Stockham pass and the transposed column loads hit distinct banks.
+// Complex index e lives at pc(e), real index i at pr(i).
+QGW_HD int pc(int e) { return e + (e >> 3); }
+QGW_HD int pr(int i) { return i + ((i >> 4) << 1); }
+// reals occupied by a padded row of M reals
+QGW_HD int padded_len(int M) { return M + ((M >> 4) << 1) + 2; }
 
 // Static shape of one DST length.
 struct DstGeom {
@@ -96,11 +105,11 @@ template <typename T> struct DstTables {
 template <typename T>
 QGW_HD void dst_pre_item(const T* __restrict__ x, T* __restrict__ y, int j, const DstGeom& g,
                          const C2<T>* __restrict__ pre) {
-  const T a = x[j - 1];
-  const T b = x[g.M - j - 1];
+  const T a = x[pr(j - 1)];
+  const T b = x[pr(g.M - j - 1)];
   const C2<T> w = pre[j];
-  y[j] = fmaT(w.x, a, w.y * b);
-  y[g.M - j] = fmaT(w.y, a, w.x * b);
+  y[pr(j)] = fmaT(w.x, a, w.y * b);
+  y[pr(g.M - j)] = fmaT(w.y, a, w.x * b);
   if (j == 1) y[0] = T(0);
 }
 
@@ -162,25 +171,80 @@ template <typename T> QGW_HD void dft8(C2<T>* v) {
   }
 }
 
+// Radix-8 butterfly whose inputs 1..7 carry twiddles w[1..7]: the products
+// are folded into the first butterfly layer with FMAs, using
+// x_r - w y = 2 x_r - (x_r + w y) for the difference outputs.
+template <typename T> QGW_HD void dft8_tw(C2<T>* v, const C2<T>* w) {
+  C2<T> a[4], b[4];
+  {
+    // r = 0: x_0 has no twiddle
+    const C2<T> y = v[4], t = w[4];
+    a[0].x = fmaT(y.x, t.x, fmaT(-y.y, t.y, v[0].x));
+    a[0].y = fmaT(y.x, t.y, fmaT(y.y, t.x, v[0].y));
+    b[0].x = fmaT(T(2), v[0].x, -a[0].x);
+    b[0].y = fmaT(T(2), v[0].y, -a[0].y);
+  }
+#pragma unroll
+  for (int r = 1; r < 4; ++r) {
+    const C2<T> xr = cmul(v[r], w[r]);
+    const C2<T> y = v[r + 4], t = w[r + 4];
+    a[r].x = fmaT(y.x, t.x, fmaT(-y.y, t.y, xr.x));
+    a[r].y = fmaT(y.x, t.y, fmaT(y.y, t.x, xr.y));
+    b[r].x = fmaT(T(2), xr.x, -a[r].x);
+    b[r].y = fmaT(T(2), xr.y, -a[r].y);
+  }
+  const T s = T(0.70710678118654752440);
+  {
+    const C2<T> c0 = cadd(a[0], a[2]), c1 = csub(a[0], a[2]);
+    const C2<T> d0 = cadd(a[1], a[3]), d1 = cmi(csub(a[1], a[3]));
+    v[0] = cadd(c0, d0);
+    v[4] = csub(c0, d0);
+    v[2] = cadd(c1, d1);
+    v[6] = csub(c1, d1);
+  }
+  {
+    C2<T> p1, p3;
+    p1.x = b[1].x + b[1].y; p1.y = b[1].y - b[1].x;
+    p3.x = b[3].y - b[3].x; p3.y = -(b[3].x + b[3].y);
+    const C2<T> u2 = cmi(b[2]);
+    const C2<T> c0 = cadd(b[0], u2), c1 = csub(b[0], u2);
+    const C2<T> P = cadd(p1, p3), D = csub(p1, p3);
+    v[1].x = fmaT(s, P.x, c0.x);  v[1].y = fmaT(s, P.y, c0.y);
+    v[5].x = fmaT(-s, P.x, c0.x); v[5].y = fmaT(-s, P.y, c0.y);
+    v[3].x = fmaT(s, D.y, c1.x);  v[3].y = fmaT(-s, D.x, c1.y);
+    v[7].x = fmaT(-s, D.y, c1.x); v[7].y = fmaT(s, D.x, c1.y);
+  }
+}
+
 template <int R, typename T>
 QGW_HD void stockham_item(const C2<T>* __restrict__ src, C2<T>* __restrict__ dst, int b, int Ns, int H,
                           const C2<T>* __restrict__ tw) {
   const int stride = H / R;
   C2<T> v[R];
 #pragma unroll
-  for (int q = 0; q < R; ++q) v[q] = src[b + q * stride];
+  for (int q = 0; q < R; ++q) v[q] = src[pc(b + q * stride)];
   const int k = b & (Ns - 1);
   if (Ns > 1) {
     const int step = k * (H / (Ns * R));
+    if (R == 8) {
+      C2<T> w[8];
 #pragma unroll
-    for (int q = 1; q < R; ++q) v[q] = cmul(v[q], tw[q * step]);
+      for (int q = 1; q < 8; ++q) w[q] = tw[q * step];
+      dft8_tw(v, w);
+    } else {
+#pragma unroll
+      for (int q = 1; q < R; ++q) v[q] = cmul(v[q], tw[q * step]);
+      if (R == 4) dft4(v);
+      else dft2(v);
+    }
+  } else {
+    if (R == 8) dft8(v);
+    else if (R == 4) dft4(v);
+    else dft2(v);
   }
-  if (R == 8) dft8(v);
-  else if (R == 4) dft4(v);
-  else dft2(v);
   const int base = (b - k) * R + k;
 #pragma unroll
-  for (int q = 0; q < R; ++q) dst[base + q * Ns] = v[q];
+  for (int q = 0; q < R; ++q) dst[pc(base + q * Ns)] = v[q];
 }
 
 template <typename T>
@@ -202,18 +266,18 @@ QGW_HD void dst_split_item(const C2<T>* __restrict__ Z, T* __restrict__ out, int
     out[0] = a.x + a.y;  // R_0
     return;
   }
-  const C2<T> A = Z[k];
-  const C2<T> Bc = Z[H - k];
+  const C2<T> A = Z[pc(k)];
+  const C2<T> Bc = Z[pc(H - k)];
   const T br = Bc.x, bi = -Bc.y;
   const C2<T> cs = spl[k];
   const T sr = A.x + br, si = A.y + bi, dr = A.x - br, di = A.y - bi;
   const T P = fmaT(cs.x, di, -(cs.y * dr));
   const T Q = fmaT(cs.x, dr, cs.y * di);
-  out[2 * k] = sr + P;          // 2 R_k
-  out[2 * k - 1] = Q - si;      // Y_{2k} = -2 I_k
+  out[pr(2 * k)] = sr + P;          // 2 R_k
+  out[pr(2 * k - 1)] = Q - si;      // Y_{2k} = -2 I_k
   if (2 * k != H) {
-    out[2 * (H - k)] = sr - P;      // 2 R_{H-k}
-    out[2 * (H - k) - 1] = Q + si;  // Y_{2(H-k)}
+    out[pr(2 * (H - k))] = sr - P;      // 2 R_{H-k}
+    out[pr(2 * (H - k) - 1)] = Q + si;  // Y_{2(H-k)}
   }
 }
 
@@ -223,9 +287,10 @@ template <typename T>
 QGW_HD T dst_scan_chunk(T* out, int c, const DstGeom& g) {
   T acc = T(0);
   const int k0 = c * g.chunk;
-  for (int t = 0; t < g.chunk; ++t) {
-    acc = (t == 0) ? out[2 * k0] : acc + out[2 * (k0 + t)];
-    out[2 * (k0 + t)] = acc;
+  acc = out[pr(2 * k0)];
+  for (int t = 1; t < g.chunk; ++t) {
+    acc = acc + out[pr(2 * (k0 + t))];
+    out[pr(2 * (k0 + t))] = acc;
   }
   return acc;
 }
@@ -233,7 +298,7 @@ QGW_HD T dst_scan_chunk(T* out, int c, const DstGeom& g) {
 template <typename T>
 QGW_HD void dst_scan_fix(T* out, int c, T prefix, const DstGeom& g) {
   const int k0 = c * g.chunk;
-  for (int t = 0; t < g.chunk; ++t) out[2 * (k0 + t)] += prefix;
+  for (int t = 0; t < g.chunk; ++t) out[pr(2 * (k0 + t))] += prefix;
 }
 
 }  // namespace qgw

@@ -15,6 +15,10 @@
 // same step, i.e. a reduction over all of psi, so it is applied by the next
 // step's K1 (or by the flush kernel at the end of a call), which saves one
 // full pass over q, f0, f1, f2.
+//
+// Shared-memory rows use the padded layout of dst_core.h (pr/pc); every
+// work loop walks a power-of-two item count per row, so item -> (row, index)
+// is a shift and a mask.
 #include <cuda_runtime.h>
 
 #include "kernels.h"
@@ -23,20 +27,24 @@
 namespace qgw {
 
 constexpr int NT = 256;          // threads per block in every step kernel
-constexpr int GMAX = 16;         // max modes per block in the row kernels
+constexpr int GMAX = 16;         // max rows of one batched DST in a block
 constexpr int TX = 32, TY = 16;  // RHS tile (interior points)
 constexpr double TEPS = 1e-9;    // src/timestep.h:288
 constexpr double HUGEV = 1e30;   // src/qg.c:43
 
+// columns per block of the column kernel: 32 bytes, two 16-byte vectors
+template <typename T> struct ColsPer { static constexpr int value = sizeof(T) == 8 ? 4 : 8; };
+
 // --------------------------------------------------------------- DST block
-// Batched DST-I of nrows rows (row r at A + r*ld, input format) by the whole
-// block; B is the second work buffer.  Returns the buffer with the output.
+// Batched DST-I of nrows rows (row r at A + r*ld, padded input format) by
+// the whole block; B is the second work buffer.  Returns the buffer that
+// holds the output.
 template <typename T>
 __device__ T* dst_block(T* A, T* B, int nrows, int ld, const DstGeom& g, const DstTables<T>& tb,
                         T* tot) {
-  const int tid = threadIdx.x, nth = blockDim.x;
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x, nth = blockDim.x * blockDim.y;
   const int H = g.H, lgH = __ffs(H) - 1;
-  for (int w = tid; w < nrows * H; w += nth) {
+  for (int w = tid; w < (nrows << lgH); w += nth) {
     const int r = w >> lgH, j = (w & (H - 1)) + 1;
     dst_pre_item<T>(A + r * ld, B + r * ld, j, g, tb.pre);
   }
@@ -47,7 +55,7 @@ __device__ T* dst_block(T* A, T* B, int nrows, int ld, const DstGeom& g, const D
   for (int p = 0; p < g.npass; ++p) {
     const int R = g.radix[p];
     const int nb = H / R, lgnb = __ffs(nb) - 1;
-    for (int w = tid; w < nrows * nb; w += nth) {
+    for (int w = tid; w < (nrows << lgnb); w += nth) {
       const int r = w >> lgnb, b = w & (nb - 1);
       stockham_dispatch<T>(R, (const C2<T>*)(src + r * ld), (C2<T>*)(dst + r * ld), b, Ns, H, tb.tw);
     }
@@ -55,21 +63,24 @@ __device__ T* dst_block(T* A, T* B, int nrows, int ld, const DstGeom& g, const D
     Ns *= R;
     T* t = src; src = dst; dst = t;
   }
-  const int ns = H / 2 + 1;
-  for (int w = tid; w < nrows * ns; w += nth) {
-    const int r = w / ns, k = w - r * ns;
+  // split: items k = 0..H/2-1 per row; item 0 also does k = H/2
+  const int lgh = lgH - 1;
+  for (int w = tid; w < (nrows << lgh); w += nth) {
+    const int r = w >> lgh, k = w & ((H >> 1) - 1);
     dst_split_item<T>((const C2<T>*)(src + r * ld), dst + r * ld, k, g, tb.spl);
+    if (k == 0) dst_split_item<T>((const C2<T>*)(src + r * ld), dst + r * ld, H >> 1, g, tb.spl);
   }
   __syncthreads();
-  const int nc = g.nchunk;
-  for (int w = tid; w < nrows * nc; w += nth) {
-    const int r = w / nc, c = w - r * nc;
+  const int nc = g.nchunk, lgnc = __ffs(nc) - 1;
+  for (int w = tid; w < (nrows << lgnc); w += nth) {
+    const int r = w >> lgnc, c = w & (nc - 1);
     tot[r * 32 + c] = dst_scan_chunk<T>(dst + r * ld, c, g);
   }
   __syncthreads();
   const int warp = tid >> 5, lane = tid & 31, nwarp = nth >> 5;
   for (int r = warp; r < nrows; r += nwarp) {
     T incl = lane < nc ? tot[r * 32 + lane] : T(0);
+#pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const T u = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += u;
@@ -80,8 +91,8 @@ __device__ T* dst_block(T* A, T* B, int nrows, int ld, const DstGeom& g, const D
     if (lane < nc) tot[r * 32 + lane] = ex;
   }
   __syncthreads();
-  for (int w = tid; w < nrows * nc; w += nth) {
-    const int r = w / nc, c = w - r * nc;
+  for (int w = tid; w < (nrows << lgnc); w += nth) {
+    const int r = w >> lgnc, c = w & (nc - 1);
     if (c > 0) dst_scan_fix<T>(dst + r * ld, c, tot[r * 32 + c], g);
   }
   __syncthreads();
@@ -110,7 +121,8 @@ __device__ __forceinline__ void comp_add(float& hi, float& lo, float d) {
 // One block per row j.  Mode groups are processed in turn by the same block:
 // the AB3 update is applied (and q written) while forming the first group,
 // and later groups re-read the updated q written by the same thread, so no
-// block ever reads a q value another block may be updating.
+// block ever reads a q value another block may be updating.  The projection
+// accumulates in shared memory (one FMA per layer and mode).
 template <typename T, bool COMP>
 __global__ void __launch_bounds__(NT) k_rows_fwd(StepArgs<T> a, int step_mode) {
   DevState* st = a.state;
@@ -118,13 +130,13 @@ __global__ void __launch_bounds__(NT) k_rows_fwd(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
   const int j = blockIdx.x;
-  const int ld = a.gx.M;
+  const int ld = padded_len(a.gx.M);
   T* A = (T*)smem_raw;
   T* B = A + (size_t)a.G1 * ld;
   const bool ab3 = step_mode && st->pending;
   int s0 = 0, s1 = 0, s2 = 0;
   slabs(st->step_index, s0, s1, s2);
-  const double c0 = st->c0, c1 = st->c1, c2 = st->c2;
+  const T c0 = (T)st->c0, c1 = (T)st->c1, c2 = (T)st->c2;
   const size_t fs = (size_t)a.nl * a.lstride;
   const T* f0 = a.fab + s0 * fs;
   const T* f1 = a.fab + s1 * fs;
@@ -134,7 +146,8 @@ __global__ void __launch_bounds__(NT) k_rows_fwd(StepArgs<T> a, int step_mode) {
     const int G = min(a.G1, a.nl - m0);
     const bool upd = ab3 && m0 == 0;
     for (int i = threadIdx.x; i < a.nx; i += NT) {
-      T acc[GMAX];
+      const int pi = pr(i);
+      for (int gg = 0; gg < G; ++gg) A[gg * ld + pi] = T(0);
       for (int l = 0; l < a.nl; ++l) {
         const size_t o = (size_t)l * a.lstride + (size_t)j * a.pitch + i;
         T v;
@@ -151,90 +164,141 @@ __global__ void __launch_bounds__(NT) k_rows_fwd(StepArgs<T> a, int step_mode) {
         } else {
           v = a.q[o];
           if (upd) {
-            v = v + (T)c0 * f0[o] + (T)c1 * f1[o] + (T)c2 * f2[o];
+            v = v + c0 * f0[o] + c1 * f1[o] + c2 * f2[o];
             a.q[o] = v;
           }
         }
-#pragma unroll
-        for (int gg = 0; gg < GMAX; ++gg)
-          if (gg < G) {
-            const T c = cl[(m0 + gg) * a.nl + l];
-            acc[gg] = (l == 0) ? c * v : fmaT(c, v, acc[gg]);
-          }
+        const T* crow = cl + (size_t)m0 * a.nl + l;
+        for (int gg = 0; gg < G; ++gg) A[gg * ld + pi] = fmaT(__ldg(crow + gg * a.nl), v, A[gg * ld + pi]);
       }
-#pragma unroll
-      for (int gg = 0; gg < GMAX; ++gg)
-        if (gg < G) A[gg * ld + i] = acc[gg];
     }
     __syncthreads();
     T* O = dst_block<T>(A, B, G, ld, a.gx, a.tx, tot);
     for (int gg = 0; gg < G; ++gg) {
       T* dstrow = a.spec + (size_t)(m0 + gg) * a.lstride + (size_t)j * a.pitch;
-      for (int i = threadIdx.x; i < a.nx; i += NT) dstrow[i] = O[gg * ld + i];
+      for (int i = threadIdx.x; i < a.nx; i += NT) dstrow[i] = O[gg * ld + pr(i)];
     }
     __syncthreads();
   }
 }
 
 // ------------------------------------------------------------------ K2
+// CT columns of one mode per block (CT * sizeof(T) = 32 bytes: two 16-byte
+// vectors per row, one thread per row), transposed into shared memory so
+// that each column is a contiguous padded row.
+template <typename T, int CT>
+__device__ __forceinline__ void load_cols(const T* __restrict__ src, T* v) {
+  const uint4* p = reinterpret_cast<const uint4*>(src);
+  uint4 u0 = p[0], u1 = p[1];
+  const T* a0 = reinterpret_cast<const T*>(&u0);
+  const T* a1 = reinterpret_cast<const T*>(&u1);
+#pragma unroll
+  for (int c = 0; c < CT / 2; ++c) { v[c] = a0[c]; v[CT / 2 + c] = a1[c]; }
+}
+template <typename T, int CT>
+__device__ __forceinline__ void store_cols(T* __restrict__ dst, const T* v) {
+  uint4 u0, u1;
+  T* a0 = reinterpret_cast<T*>(&u0);
+  T* a1 = reinterpret_cast<T*>(&u1);
+#pragma unroll
+  for (int c = 0; c < CT / 2; ++c) { a0[c] = v[c]; a1[c] = v[CT / 2 + c]; }
+  uint4* p = reinterpret_cast<uint4*>(dst);
+  p[0] = u0;
+  p[1] = u1;
+}
+
 template <typename T, bool COMP>
 __global__ void __launch_bounds__(NT) k_cols(StepArgs<T> a, int step_mode) {
+  constexpr int CT = ColsPer<T>::value;
   DevState* st = a.state;
   if (step_mode && !st->active) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
-  const int k0 = blockIdx.x * a.CT;
+  const int k0 = blockIdx.x * CT;
   const int m = blockIdx.y;
-  const int CTb = min(a.CT, a.nx - k0);
-  const int ld = a.gy.M;
+  const int CTb = min(CT, a.nx - k0);
+  const int ld = padded_len(a.gy.M);
   T* A = (T*)smem_raw;
-  T* B = A + (size_t)a.CT * ld;
+  T* B = A + (size_t)CT * ld;
+  T* C = B + (size_t)CT * ld;  // zeta mode only
   T* S = a.spec + (size_t)m * a.lstride;
   const int ny = a.ny;
-  for (int w = threadIdx.x; w < ny * CTb; w += NT) {
-    const int jj = w / CTb, c = w - jj * CTb;
-    A[c * ld + jj] = S[(size_t)jj * a.pitch + k0 + c];
+  // 16-byte vectors need 16-byte aligned rows (vec_cols); the last tile then
+  // reads the padding column (index nx < pitch), never past the row
+  const bool vec = a.vec_cols != 0;
+  T v[CT];
+  for (int jj = threadIdx.x; jj < ny; jj += NT) {
+    const T* src = S + (size_t)jj * a.pitch + k0;
+    if (vec) load_cols<T, CT>(src, v);
+    else
+      for (int c = 0; c < CT; ++c) v[c] = c < CTb ? src[c] : T(0);
+    const int pj = pr(jj);
+#pragma unroll
+    for (int c = 0; c < CT; ++c) A[c * ld + pj] = v[c];
   }
   __syncthreads();
-  T* O = dst_block<T>(A, B, CTb, ld, a.gy, a.ty, tot);
+  T* O = dst_block<T>(A, B, CT, ld, a.gy, a.ty, tot);
   const double iRd2 = a.iRd2[m];
-  // zeta mode: C receives the spectral discrete Laplacian of psi,
-  // lambda(k, j) * psi_hat with lambda = -4/Delta^2 (sin^2 kx + sin^2 ky), the
-  // exact symbol of the 5-point Laplacian with zero ghosts in the DST basis
-  T* C = (T*)smem_raw + (size_t)2 * a.CT * ld;
   const bool zm = COMP && a.zeta_mode;
-  for (int w = threadIdx.x; w < ny * CTb; w += NT) {
-    const int jj = w / CTb, c = w - jj * CTb;
-    const int k = k0 + c;
+  for (int jj = threadIdx.x; jj < ny; jj += NT) {
+    const int pj = pr(jj);
     if (!COMP) {
-      O[c * ld + jj] *= (T)a.hinv[(size_t)m * a.lstride + (size_t)jj * a.pitch + k];
-    } else if (m == 0 && jj < a.low_k64 && k < a.low_k64) {
-      // barotropic mode, lowest wavenumbers: divide in FP64
-      const double fact = -(a.Lsq[k] + a.Ksq[jj] + iRd2);
-      O[c * ld + jj] = (T)((double)O[c * ld + jj] / fact / a.norm);
+      const T* hrow = (const T*)(a.hinv + (size_t)m * a.lstride + (size_t)jj * a.pitch + k0);
+      T h[CT];
+      if (vec) load_cols<T, CT>(hrow, h);
+      else
+        for (int c = 0; c < CT; ++c) h[c] = c < CTb ? hrow[c] : T(0);
+#pragma unroll
+      for (int c = 0; c < CT; ++c) O[c * ld + pj] *= h[c];
     } else {
-      const float fact = -(((float)a.Lsq[k] + (float)a.Ksq[jj]) + (float)iRd2);
-      O[c * ld + jj] = (T)((float)O[c * ld + jj] / (fact * (float)a.norm));
-    }
-    if (zm) {
-      const float lam = (float)a.lx2 * (float)a.sx2[k] + (float)a.ly2 * (float)a.sy2[jj];
-      C[c * ld + jj] = (T)(lam * (float)O[c * ld + jj]);
+      const float ksq = (float)a.Ksq[jj];
+#pragma unroll
+      for (int c = 0; c < CT; ++c) {
+        const int k = min(k0 + c, a.nx - 1);
+        float x;
+        if (m == 0 && jj < a.low_k64 && k < a.low_k64) {
+          // barotropic mode, lowest wavenumbers: divide in FP64
+          const double fact = -(a.Lsq[k] + a.Ksq[jj] + iRd2);
+          x = (float)((double)O[c * ld + pj] / fact / a.norm);
+        } else {
+          const float fact = -(((float)a.Lsq[k] + ksq) + (float)iRd2);
+          x = (float)O[c * ld + pj] / (fact * (float)a.norm);
+        }
+        O[c * ld + pj] = (T)x;
+        if (zm) {
+          // spectral discrete Laplacian of psi: lambda(k, j) * psi_hat with
+          // lambda = -4/Delta^2 (sin^2 kx + sin^2 ky), the exact symbol of
+          // the 5-point Laplacian with zero ghosts in the DST basis
+          const float lam = (float)a.lx2 * (float)a.sx2[k] + (float)a.ly2 * (float)a.sy2[jj];
+          C[c * ld + pj] = (T)(lam * x);
+        }
+      }
     }
   }
   __syncthreads();
   T* Oth = (O == A) ? B : A;
-  T* O2 = dst_block<T>(O, Oth, CTb, ld, a.gy, a.ty, tot);
-  for (int w = threadIdx.x; w < ny * CTb; w += NT) {
-    const int jj = w / CTb, c = w - jj * CTb;
-    S[(size_t)jj * a.pitch + k0 + c] = O2[c * ld + jj];
+  T* O2 = dst_block<T>(O, Oth, CT, ld, a.gy, a.ty, tot);
+  for (int jj = threadIdx.x; jj < ny; jj += NT) {
+    const int pj = pr(jj);
+#pragma unroll
+    for (int c = 0; c < CT; ++c) v[c] = c < CTb ? O2[c * ld + pj] : T(0);
+    T* dst = S + (size_t)jj * a.pitch + k0;
+    if (vec) store_cols<T, CT>(dst, v);
+    else
+      for (int c = 0; c < CTb; ++c) dst[c] = v[c];
   }
   if (zm) {
     __syncthreads();
-    T* O3 = dst_block<T>(C, O2 == A ? B : A, CTb, ld, a.gy, a.ty, tot);
+    T* O3 = dst_block<T>(C, O2 == A ? B : A, CT, ld, a.gy, a.ty, tot);
     T* S2 = a.spec2 + (size_t)m * a.lstride;
-    for (int w = threadIdx.x; w < ny * CTb; w += NT) {
-      const int jj = w / CTb, c = w - jj * CTb;
-      S2[(size_t)jj * a.pitch + k0 + c] = O3[c * ld + jj];
+    for (int jj = threadIdx.x; jj < ny; jj += NT) {
+      const int pj = pr(jj);
+#pragma unroll
+      for (int c = 0; c < CT; ++c) v[c] = c < CTb ? O3[c * ld + pj] : T(0);
+      T* dst = S2 + (size_t)jj * a.pitch + k0;
+      if (vec) store_cols<T, CT>(dst, v);
+      else
+        for (int c = 0; c < CTb; ++c) dst[c] = v[c];
     }
   }
 }
@@ -250,7 +314,7 @@ __global__ void __launch_bounds__(NT) k_rows_inv(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
   const int j = blockIdx.x;
-  const int ld = a.gx.M;
+  const int ld = padded_len(a.gx.M);
   const bool zm = COMP && a.zeta_mode;
   const int Gb = zm ? a.G3 : a.G1;
   T* A = (T*)smem_raw;
@@ -260,23 +324,25 @@ __global__ void __launch_bounds__(NT) k_rows_inv(StepArgs<T> a, int step_mode) {
     const int G = min(Gb, a.nl - m0);
     for (int gg = 0; gg < G; ++gg) {
       const T* srow = a.spec + (size_t)(m0 + gg) * a.lstride + (size_t)j * a.pitch;
-      for (int i = threadIdx.x; i < a.nx; i += NT) A[gg * ld + i] = srow[i];
+      for (int i = threadIdx.x; i < a.nx; i += NT) A[gg * ld + pr(i)] = srow[i];
       if (zm) {
         const T* zrow = a.spec2 + (size_t)(m0 + gg) * a.lstride + (size_t)j * a.pitch;
-        for (int i = threadIdx.x; i < a.nx; i += NT) A[(G + gg) * ld + i] = zrow[i];
+        for (int i = threadIdx.x; i < a.nx; i += NT) A[(G + gg) * ld + pr(i)] = zrow[i];
       }
     }
     __syncthreads();
     T* O = dst_block<T>(A, B, zm ? 2 * G : G, ld, a.gx, a.tx, tot);
     for (int i = threadIdx.x; i < a.nx; i += NT) {
+      const int pi = pr(i);
       for (int l = 0; l < a.nl; ++l) {
         const size_t o = (size_t)l * a.lstride + (size_t)j * a.pitch + i;
+        const T* crow = cm + (size_t)l * a.nl + m0;
         T acc = (m0 == 0) ? T(0) : a.psi[o];
-        for (int gg = 0; gg < G; ++gg) acc = fmaT(cm[l * a.nl + m0 + gg], O[gg * ld + i], acc);
+        for (int gg = 0; gg < G; ++gg) acc = fmaT(__ldg(crow + gg), O[gg * ld + pi], acc);
         a.psi[o] = acc;
         if (zm) {
           T zc = (m0 == 0) ? T(0) : a.zeta[o];
-          for (int gg = 0; gg < G; ++gg) zc = fmaT(cm[l * a.nl + m0 + gg], O[(G + gg) * ld + i], zc);
+          for (int gg = 0; gg < G; ++gg) zc = fmaT(__ldg(crow + gg), O[(G + gg) * ld + pi], zc);
           a.zeta[o] = zc;
         }
       }
@@ -348,103 +414,106 @@ __device__ void scalar_update(DevState* st, double Delta, double cfl) {
   st->done_blocks = 0u;
 }
 
-template <typename T, bool COMP>
+// RHS tile of TX x TY points of one layer; block (32, 8); R = halo radius
+// of psi (the number of hyperviscosity sweeps, at least 1).
+template <typename T, bool COMP, int R>
 __global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
   DevState* st = a.state;
   if (!st->active) return;
+  constexpr int W = TX + 2 * R, HH = TY + 2 * R;
+  constexpr int QW = TX + 2, QH = TY + 2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int k = blockIdx.z;
-  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
-  const int r = a.nsweep > 0 ? a.nsweep : 1;
-  const int W = TX + 2 * r, Hh = TY + 2 * r;
-  const int nx = a.nx, ny = a.ny;
-  T* ps = (T*)smem_raw;                 // W*Hh, psi with halo r
-  T* L0 = ps + W * Hh;                  // chain ping-pong
-  T* L1 = L0 + W * Hh;
-  T* qs = L1 + W * Hh;                  // (TX+2)*(TY+2)
-  T* dyp = qs + (TX + 2) * (TY + 2);    // (TX+2)*TY
-  T* dyq = dyp + (TX + 2) * TY;
-  T* dxp = dyq + (TX + 2) * TY;         // TX*(TY+2)
-  T* dxq = dxp + TX * (TY + 2);
+  T* ps = (T*)smem_raw;       // HH x W, psi with halo R
+  T* L0 = ps + W * HH;        // chain ping-pong
+  T* L1 = L0 + W * HH;
+  T* qs = L1 + W * HH;        // QH x QW
+  T* dyp = qs + QW * QH;      // TY x QW
+  T* dyq = dyp + QW * TY;
+  T* dxp = dyq + QW * TY;     // QH x TX
+  T* dxq = dxp + TX * QH;
   __shared__ unsigned long long wmax[NT / 32];
   __shared__ int is_last;
-
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int k = blockIdx.z;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  const int nx = a.nx, ny = a.ny;
   const T* psiL = a.psi + (size_t)k * a.lstride;
   const T* qL = a.q + (size_t)k * a.lstride;
   const bool zm = COMP && a.zeta_mode;
   const T* zetaL = zm ? a.zeta + (size_t)k * a.lstride : nullptr;
-  const double d2 = a.Delta * a.Delta;
-#define PS(x, y) ps[((y) + r) * W + (x) + r]
-  for (int w = threadIdx.x; w < W * Hh; w += NT) {
-    const int x = w % W - r, y = w / W - r;
-    const int gi = i0 + x, gj = j0 + y;
-    T v = T(0);
-    if (gi >= 0 && gi < nx && gj >= 0 && gj < ny) v = psiL[(size_t)gj * a.pitch + gi];
-    ps[w] = v;
-  }
+  const T d2 = (T)(a.Delta * a.Delta);
+#define PS(x, y) ps[((y) + R) * W + (x) + R]
+#define QS(x, y) qs[((y) + 1) * QW + (x) + 1]
+  for (int y = ty; y < HH; y += 8)
+    for (int x = tx; x < W; x += 32) {
+      const int gi = i0 + x - R, gj = j0 + y - R;
+      T v = T(0);
+      if (gi >= 0 && gi < nx && gj >= 0 && gj < ny) v = psiL[(size_t)gj * a.pitch + gi];
+      ps[y * W + x] = v;
+    }
   __syncthreads();
   const T cbc = (T)a.cbc;
   // q with one ghost point: adjust_bc(q, 1, psi), src/domain.h:308-348
-#define QS(x, y) qs[((y) + 1) * (TX + 2) + (x) + 1]
-  for (int w = threadIdx.x; w < (TX + 2) * (TY + 2); w += NT) {
-    const int x = w % (TX + 2) - 1, y = w / (TX + 2) - 1;
-    const int gi = i0 + x, gj = j0 + y;
-    const bool inx = gi >= 0 && gi < nx, iny = gj >= 0 && gj < ny;
-    T v = T(0);
-    if (inx && iny) v = qL[(size_t)gj * a.pitch + gi];
-    else if (iny && gi == -1) v = cbc * PS(x + 1, y);
-    else if (iny && gi == nx) v = cbc * PS(x - 1, y);
-    else if (inx && gj == -1) v = cbc * PS(x, y + 1);
-    else if (inx && gj == ny) v = cbc * PS(x, y - 1);
-    qs[w] = v;
-  }
+  for (int y = ty; y < QH; y += 8)
+    for (int x = tx; x < QW; x += 32) {
+      const int xx = x - 1, yy = y - 1;
+      const int gi = i0 + xx, gj = j0 + yy;
+      const bool inx = gi >= 0 && gi < nx, iny = gj >= 0 && gj < ny;
+      T v = T(0);
+      if (inx && iny) v = qL[(size_t)gj * a.pitch + gi];
+      else if (iny && gi == -1) v = cbc * PS(xx + 1, yy);
+      else if (iny && gi == nx) v = cbc * PS(xx - 1, yy);
+      else if (inx && gj == -1) v = cbc * PS(xx, yy + 1);
+      else if (inx && gj == ny) v = cbc * PS(xx, yy - 1);
+      qs[y * QW + x] = v;
+    }
   // hyperviscosity chain (calc_diff, src/dynamics.h:13-44) on the tile with
   // a shrinking halo; sweeps are unscaled (no 1/Delta^2), the scale is in
-  // nuh_scaled and in the ghost factors gh[s]
+  // nuh_scaled and in the ghost factors gh[s]; in zeta mode the first
+  // sweep is the spectral zeta
   const T* Lp = ps;
   T* Lc = L0;
   for (int s = 1; s <= a.nsweep; ++s) {
     __syncthreads();
-    const int rr = r - s;
-    const int Ws = TX + 2 * rr, Hs = TY + 2 * rr;
     const T ghs = (T)a.gh[s];
-    for (int w = threadIdx.x; w < Ws * Hs; w += NT) {
-      const int x = w % Ws - rr, y = w / Ws - rr;
-      const int gi = i0 + x, gj = j0 + y;
-      const bool inx = gi >= 0 && gi < nx, iny = gj >= 0 && gj < ny;
-      const int o = (y + r) * W + x + r;
-      T v = T(0);
-      if (inx && iny) {
-        if (s == 1 && zm) {
-          // sweep 1 from the spectral zeta (unscaled: Delta^2 * zeta)
-          v = (T)d2 * zetaL[(size_t)gj * a.pitch + gi];
-        } else {
-          const T sum = (Lp[o + 1] + Lp[o - 1]) + (Lp[o + W] + Lp[o - W]);
-          v = fmaT(T(-4), Lp[o], sum);
-        }
-      } else if (iny && gi == -1) v = ghs * PS(x + 1, y);
-      else if (iny && gi == nx) v = ghs * PS(x - 1, y);
-      else if (inx && gj == -1) v = ghs * PS(x, y + 1);
-      else if (inx && gj == ny) v = ghs * PS(x, y - 1);
-      Lc[o] = v;
-    }
+    for (int y = s + ty; y < HH - s; y += 8)
+      for (int x = s + tx; x < W - s; x += 32) {
+        const int xx = x - R, yy = y - R;
+        const int gi = i0 + xx, gj = j0 + yy;
+        const bool inx = gi >= 0 && gi < nx, iny = gj >= 0 && gj < ny;
+        const int o = y * W + x;
+        T v = T(0);
+        if (inx && iny) {
+          if (s == 1 && zm) {
+            v = d2 * zetaL[(size_t)gj * a.pitch + gi];
+          } else {
+            const T sum = (Lp[o + 1] + Lp[o - 1]) + (Lp[o + W] + Lp[o - W]);
+            v = fmaT(T(-4), Lp[o], sum);
+          }
+        } else if (iny && gi == -1) v = ghs * PS(xx + 1, yy);
+        else if (iny && gi == nx) v = ghs * PS(xx - 1, yy);
+        else if (inx && gj == -1) v = ghs * PS(xx, yy + 1);
+        else if (inx && gj == ny) v = ghs * PS(xx, yy - 1);
+        Lc[o] = v;
+      }
     Lp = Lc;
     Lc = (Lc == L0) ? L1 : L0;
   }
   __syncthreads();
   // centred differences shared between neighbouring Jacobian evaluations
-  for (int w = threadIdx.x; w < (TX + 2) * TY; w += NT) {
-    const int x = w % (TX + 2) - 1, y = w / (TX + 2);
-    dyp[w] = PS(x, y + 1) - PS(x, y - 1);
-    dyq[w] = QS(x, y + 1) - QS(x, y - 1);
-  }
-  for (int w = threadIdx.x; w < TX * (TY + 2); w += NT) {
-    const int x = w % TX, y = w / TX - 1;
-    dxp[w] = PS(x + 1, y) - PS(x - 1, y);
-    dxq[w] = QS(x + 1, y) - QS(x - 1, y);
+  for (int y = ty; y < TY; y += 8)
+    for (int x = tx; x < QW; x += 32) {
+      const int xx = x - 1;
+      dyp[y * QW + x] = PS(xx, y + 1) - PS(xx, y - 1);
+      dyq[y * QW + x] = QS(xx, y + 1) - QS(xx, y - 1);
+    }
+  for (int y = ty; y < QH; y += 8) {
+    const int yy = y - 1;
+    dxp[y * TX + tx] = PS(tx + 1, yy) - PS(tx - 1, yy);
+    dxq[y * TX + tx] = QS(tx + 1, yy) - QS(tx - 1, yy);
   }
   __syncthreads();
-#define DY(arr, x, y) arr[(y) * (TX + 2) + (x) + 1]
+#define DY(arr, x, y) arr[(y) * QW + (x) + 1]
 #define DX(arr, x, y) arr[((y) + 1) * TX + (x)]
   const size_t fs = (size_t)a.nl * a.lstride;
   int s0, s1, s2;
@@ -452,8 +521,8 @@ __global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
   T* fout = a.fab + s0 * fs + (size_t)k * a.lstride;
   const bool bottom = (k == a.nl - 1);
   unsigned long long mymax = 0ULL;
-  for (int w = threadIdx.x; w < TX * TY; w += NT) {
-    const int x = w % TX, y = w / TX;
+  const int x = tx;
+  for (int y = ty; y < TY; y += 8) {
     const int gi = i0 + x, gj = j0 + y;
     if (gi >= nx || gj >= ny) continue;
     // Arakawa Jacobian J(psi, q) (jacobian_lev, src/domain.h:17-27) with the
@@ -474,12 +543,12 @@ __global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
       const T lq = fmaT(T(-4), QS(x, y), (QS(x + 1, y) + QS(x - 1, y)) + (QS(x, y + 1) + QS(x, y - 1)));
       f = fmaT((T)a.nu_d2, lq, f);
     }
-    if (a.nsweep > 0) f = fmaT((T)a.nuh_scaled, Lp[(y + r) * W + x + r], f);
+    if (a.nsweep > 0) f = fmaT((T)a.nuh_scaled, Lp[(y + R) * W + x + R], f);
     // surface wind (src/dynamics.h:66) and bottom drag + topography (:67-69)
     if (k == 0 && a.has_wind) f += a.wind[gj];
     if (bottom) {
       if (a.has_drag) {
-        const T lp = zm ? (T)d2 * zetaL[(size_t)gj * a.pitch + gi]
+        const T lp = zm ? d2 * zetaL[(size_t)gj * a.pitch + gi]
                         : fmaT(T(-4), PS(x, y), (PS(x + 1, y) + PS(x - 1, y)) + (PS(x, y + 1) + PS(x, y - 1)));
         f = fmaT((T)a.drag_d2, lp, f);
       }
@@ -515,9 +584,10 @@ __global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
     const unsigned long long u = __shfl_xor_sync(0xffffffffu, mymax, o);
     mymax = u > mymax ? u : mymax;
   }
-  if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = mymax;
+  const int tid = tx + ty * 32;
+  if ((tid & 31) == 0) wmax[tid >> 5] = mymax;
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     unsigned long long bm = 0ULL;
     for (int w = 0; w < NT / 32; ++w) bm = wmax[w] > bm ? wmax[w] : bm;
     atomicMax(&st->maxbits, bm);
@@ -527,11 +597,12 @@ __global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
     is_last = (ticket == total - 1);
   }
   __syncthreads();
-  if (is_last && threadIdx.x == 0) {
+  if (is_last && tid == 0) {
     __threadfence();
     scalar_update(st, a.Delta, a.cfl);
   }
 }
+
 
 // ------------------------------------------------------- small kernels
 __global__ void k_begin(DevState* st, double t_out, double tend) {
@@ -631,21 +702,26 @@ __global__ void k_budget_final(const double* part, int nblk, double scale, doubl
 
 // ------------------------------------------------------------- launchers
 template <typename T, bool COMP>
-static size_t smem_rows(const StepArgs<T>& a) { return (size_t)2 * a.G1 * a.gx.M * sizeof(T); }
+static size_t smem_rows(const StepArgs<T>& a) { return (size_t)2 * a.G1 * padded_len(a.gx.M) * sizeof(T); }
 template <typename T, bool COMP>
 static size_t smem_cols(const StepArgs<T>& a) {
-  return (size_t)((COMP && a.zeta_mode) ? 3 : 2) * a.CT * a.gy.M * sizeof(T);
+  return (size_t)((COMP && a.zeta_mode) ? 3 : 2) * ColsPer<T>::value * padded_len(a.gy.M) * sizeof(T);
 }
 template <typename T, bool COMP>
 static size_t smem_rows_inv(const StepArgs<T>& a) {
-  return (COMP && a.zeta_mode) ? (size_t)4 * a.G3 * a.gx.M * sizeof(T) : smem_rows<T, COMP>(a);
+  return (COMP && a.zeta_mode) ? (size_t)4 * a.G3 * padded_len(a.gx.M) * sizeof(T) : smem_rows<T, COMP>(a);
 }
 template <typename T>
-static size_t smem_rhs(const StepArgs<T>& a) {
-  const int r = a.nsweep > 0 ? a.nsweep : 1;
+static size_t smem_rhs_r(int r) {
   const size_t W = TX + 2 * r, Hh = TY + 2 * r;
   return sizeof(T) * (3 * W * Hh + (TX + 2) * (TY + 2) + 2 * (TX + 2) * TY + 2 * TX * (TY + 2));
 }
+template <typename T>
+static int rhs_halo(const StepArgs<T>& a) { return a.nsweep > 0 ? a.nsweep : 1; }
+template <typename T>
+static size_t smem_rhs(const StepArgs<T>& a) { return smem_rhs_r<T>(rhs_halo(a)); }
+
+constexpr int RHS_RMAX = 4;  // n_hyper <= 6
 
 // The dynamic shared-memory limit is a process-wide attribute of each kernel,
 // shared by every run in the process; it is set to the device's opt-in
@@ -659,7 +735,7 @@ static cudaError_t set_attrs(const StepArgs<T>& a) {
   if (e != cudaSuccess) return e;
   const size_t static_tot = sizeof(T) * GMAX * 32 + 64;
   if (smem_rows<T, COMP>(a) + static_tot > (size_t)optin || smem_cols<T, COMP>(a) + static_tot > (size_t)optin ||
-      smem_rows_inv<T, COMP>(a) + static_tot > (size_t)optin ||
+      smem_rows_inv<T, COMP>(a) + static_tot > (size_t)optin || rhs_halo(a) > RHS_RMAX ||
       smem_rhs<T>(a) + 1024 > (size_t)optin)
     return cudaErrorInvalidValue;
   const int lim = optin - (int)static_tot;
@@ -669,19 +745,46 @@ static cudaError_t set_attrs(const StepArgs<T>& a) {
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k_cols<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_rhs<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - 1024);
+  const int rl = optin - 1024;
+  if ((e = cudaFuncSetAttribute(k_rhs<T, COMP, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, rl)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(k_rhs<T, COMP, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, rl)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(k_rhs<T, COMP, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, rl)) != cudaSuccess)
+    return e;
+  return cudaFuncSetAttribute(k_rhs<T, COMP, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, rl);
+}
+
+template <typename T, bool COMP>
+static void launch_k1(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
+  k_rows_fwd<T, COMP><<<dim3(a.ny), NT, smem_rows<T, COMP>(a), s>>>(a, step_mode);
+}
+template <typename T, bool COMP>
+static void launch_k2(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
+  constexpr int CT = ColsPer<T>::value;
+  k_cols<T, COMP><<<dim3((a.nx + CT - 1) / CT, a.nl), NT, smem_cols<T, COMP>(a), s>>>(a, step_mode);
+}
+template <typename T, bool COMP>
+static void launch_k3(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
+  k_rows_inv<T, COMP><<<dim3(a.ny), NT, smem_rows_inv<T, COMP>(a), s>>>(a, step_mode);
+}
+template <typename T, bool COMP>
+static void launch_rhs(const StepArgs<T>& a, cudaStream_t s) {
+  const dim3 grid((a.nx + TX - 1) / TX, (a.ny + TY - 1) / TY, a.nl), blk(32, 8);
+  const size_t sm = smem_rhs(a);
+  switch (rhs_halo(a)) {
+    case 1: k_rhs<T, COMP, 1><<<grid, blk, sm, s>>>(a); break;
+    case 2: k_rhs<T, COMP, 2><<<grid, blk, sm, s>>>(a); break;
+    case 3: k_rhs<T, COMP, 3><<<grid, blk, sm, s>>>(a); break;
+    default: k_rhs<T, COMP, 4><<<grid, blk, sm, s>>>(a); break;
+  }
 }
 
 template <typename T, bool COMP>
 static void launch_invert(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
-  k_rows_fwd<T, COMP><<<dim3(a.ny), NT, smem_rows<T, COMP>(a), s>>>(a, step_mode);
-  k_cols<T, COMP><<<dim3((a.nx + a.CT - 1) / a.CT, a.nl), NT, smem_cols<T, COMP>(a), s>>>(a, step_mode);
-  k_rows_inv<T, COMP><<<dim3(a.ny), NT, smem_rows_inv<T, COMP>(a), s>>>(a, step_mode);
-}
-
-template <typename T, bool COMP>
-static void launch_rhs(const StepArgs<T>& a, cudaStream_t s) {
-  k_rhs<T, COMP><<<dim3((a.nx + TX - 1) / TX, (a.ny + TY - 1) / TY, a.nl), NT, smem_rhs<T>(a), s>>>(a);
+  launch_k1<T, COMP>(a, step_mode, s);
+  launch_k2<T, COMP>(a, step_mode, s);
+  launch_k3<T, COMP>(a, step_mode, s);
 }
 
 template <typename T, bool COMP>
@@ -691,6 +794,14 @@ static void launch_flush(const StepArgs<T>& a, cudaStream_t s) {
   if (blocks > 152 * 8) blocks = 152 * 8;
   k_flush<T, COMP><<<blocks, NT, 0, s>>>(a);
   k_end<<<1, 1, 0, s>>>(a.state);
+}
+
+template <typename T, bool COMP>
+static void launch_one(const StepArgs<T>& a, int which, cudaStream_t s) {
+  if (which == 0) launch_k1<T, COMP>(a, 1, s);
+  if (which == 1) launch_k2<T, COMP>(a, 1, s);
+  if (which == 2) launch_k3<T, COMP>(a, 1, s);
+  if (which == 3) launch_rhs<T, COMP>(a, s);
 }
 
 // ---- entry points used by api.cu (see kernels.h)
@@ -711,19 +822,8 @@ void enqueue_invert_f64(const StepArgs<double>& a, cudaStream_t s) { launch_inve
 void enqueue_invert_f32c(const StepArgs<float>& a, cudaStream_t s) { launch_invert<float, true>(a, 0, s); }
 void enqueue_flush_f64(const StepArgs<double>& a, cudaStream_t s) { launch_flush<double, false>(a, s); }
 void enqueue_flush_f32c(const StepArgs<float>& a, cudaStream_t s) { launch_flush<float, true>(a, s); }
-
-void enqueue_step_kernel_f64(const StepArgs<double>& a, int which, cudaStream_t s) {
-  if (which == 0) k_rows_fwd<double, false><<<dim3(a.ny), NT, smem_rows<double, false>(a), s>>>(a, 1);
-  if (which == 1) k_cols<double, false><<<dim3((a.nx + a.CT - 1) / a.CT, a.nl), NT, smem_cols<double, false>(a), s>>>(a, 1);
-  if (which == 2) k_rows_inv<double, false><<<dim3(a.ny), NT, smem_rows_inv<double, false>(a), s>>>(a, 1);
-  if (which == 3) launch_rhs<double, false>(a, s);
-}
-void enqueue_step_kernel_f32c(const StepArgs<float>& a, int which, cudaStream_t s) {
-  if (which == 0) k_rows_fwd<float, true><<<dim3(a.ny), NT, smem_rows<float, true>(a), s>>>(a, 1);
-  if (which == 1) k_cols<float, true><<<dim3((a.nx + a.CT - 1) / a.CT, a.nl), NT, smem_cols<float, true>(a), s>>>(a, 1);
-  if (which == 2) k_rows_inv<float, true><<<dim3(a.ny), NT, smem_rows_inv<float, true>(a), s>>>(a, 1);
-  if (which == 3) launch_rhs<float, true>(a, s);
-}
+void enqueue_step_kernel_f64(const StepArgs<double>& a, int which, cudaStream_t s) { launch_one<double, false>(a, which, s); }
+void enqueue_step_kernel_f32c(const StepArgs<float>& a, int which, cudaStream_t s) { launch_one<float, true>(a, which, s); }
 
 void enqueue_split_f64(const double* src, float* hi, float* lo, size_t n, cudaStream_t s) {
   k_split_f64<<<1024, 256, 0, s>>>(src, hi, lo, n);
