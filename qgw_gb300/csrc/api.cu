@@ -140,6 +140,11 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   if ((rc = upload<double>(r, &dK, Ksq))) return rc;
   a.Lsq = dL;
   a.Ksq = dK;
+  float *fL, *fK;
+  if ((rc = upload<float>(r, &fL, Lsq))) return rc;
+  if ((rc = upload<float>(r, &fK, Ksq))) return rc;
+  a.Lsqf = fL;
+  a.Ksqf = fK;
   a.hinv = nullptr;
   if (r->precision == QGW_FP64) {
     // 1 / (fact * norm), fact = -(sq(L[i]) + sq(K[j]) + iRd2[k]) as in
@@ -219,6 +224,11 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
     if ((rc = upload<double>(r, &dsy, sy))) return rc;
     a.sx2 = dsx;
     a.sy2 = dsy;
+    float *fsx, *fsy;
+    if ((rc = upload<float>(r, &fsx, sx))) return rc;
+    if ((rc = upload<float>(r, &fsy, sy))) return rc;
+    a.sx2f = fsx;
+    a.sy2f = fsy;
     a.lx2 = -4.0 / (r->Delta * r->Delta);
     a.ly2 = a.lx2;
   }

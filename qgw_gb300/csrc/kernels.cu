@@ -240,6 +240,7 @@ __global__ void __launch_bounds__(NT) k_cols(StepArgs<T> a, int step_mode) {
   T* O = dst_block<T>(A, B, CT, ld, a.gy, a.ty, tot);
   const double iRd2 = a.iRd2[m];
   const bool zm = COMP && a.zeta_mode;
+  const float ird2f = (float)iRd2, normf = (float)a.norm, lx2f = (float)a.lx2, ly2f = (float)a.ly2;
   for (int jj = threadIdx.x; jj < ny; jj += NT) {
     const int pj = pr(jj);
     if (!COMP) {
@@ -251,7 +252,7 @@ __global__ void __launch_bounds__(NT) k_cols(StepArgs<T> a, int step_mode) {
 #pragma unroll
       for (int c = 0; c < CT; ++c) O[c * ld + pj] *= h[c];
     } else {
-      const float ksq = (float)a.Ksq[jj];
+      const float ksq = a.Ksqf[jj], sy = a.sy2f[jj];
 #pragma unroll
       for (int c = 0; c < CT; ++c) {
         const int k = min(k0 + c, a.nx - 1);
@@ -261,15 +262,15 @@ __global__ void __launch_bounds__(NT) k_cols(StepArgs<T> a, int step_mode) {
           const double fact = -(a.Lsq[k] + a.Ksq[jj] + iRd2);
           x = (float)((double)O[c * ld + pj] / fact / a.norm);
         } else {
-          const float fact = -(((float)a.Lsq[k] + ksq) + (float)iRd2);
-          x = (float)O[c * ld + pj] / (fact * (float)a.norm);
+          const float fact = -((a.Lsqf[k] + ksq) + ird2f);
+          x = (float)O[c * ld + pj] / (fact * normf);
         }
         O[c * ld + pj] = (T)x;
         if (zm) {
           // spectral discrete Laplacian of psi: lambda(k, j) * psi_hat with
           // lambda = -4/Delta^2 (sin^2 kx + sin^2 ky), the exact symbol of
           // the 5-point Laplacian with zero ghosts in the DST basis
-          const float lam = (float)a.lx2 * (float)a.sx2[k] + (float)a.ly2 * (float)a.sy2[jj];
+          const float lam = lx2f * a.sx2f[k] + ly2f * sy;
           C[c * ld + pj] = (T)(lam * x);
         }
       }
@@ -355,9 +356,14 @@ __global__ void __launch_bounds__(NT) k_rows_inv(StepArgs<T> a, int step_mode) {
 __device__ __forceinline__ unsigned long long absbits(double v) {
   return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL;
 }
-__device__ __forceinline__ unsigned long long absbits(float v) {
-  // widen exactly to double so that both paths reduce the same quantity
-  return absbits((double)v);
+// |v| as bits in the arithmetic width (non-negative floats order like their
+// bit patterns); a float maximum is widened to double bits once per block
+__device__ __forceinline__ unsigned long long absbits_native(double v) { return absbits(v); }
+__device__ __forceinline__ unsigned int absbits_native(float v) { return __float_as_uint(v) & 0x7fffffffu; }
+template <typename T> __device__ __forceinline__ unsigned long long widen_absbits(unsigned long long b) { return b; }
+template <> __device__ __forceinline__ unsigned long long widen_absbits<float>(unsigned long long b) {
+  // NaN and Inf stay above every finite value after widening
+  return absbits((double)__uint_as_float((unsigned int)b));
 }
 
 // adjust_timestep's dt rule (src/timestep.h:341-383) and the AB3
@@ -441,43 +447,52 @@ __global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
   const T* qL = a.q + (size_t)k * a.lstride;
   const bool zm = COMP && a.zeta_mode;
   const T* zetaL = zm ? a.zeta + (size_t)k * a.lstride : nullptr;
+  // every double parameter converted once (conversions run on the FP64 pipe)
   const T d2 = (T)(a.Delta * a.Delta);
+  const T cbc = (T)a.cbc;
+  const T m_inv12 = (T)(-a.inv12d2), b2d = (T)a.b2d, nu_d2 = (T)a.nu_d2, nuh = (T)a.nuh_scaled;
+  const T drag = (T)a.drag_d2, topo_c = -(T)(a.inv12d2 * a.topo_fac);
 #define PS(x, y) ps[((y) + R) * W + (x) + R]
 #define QS(x, y) qs[((y) + 1) * QW + (x) + 1]
-  for (int y = ty; y < HH; y += 8)
-    for (int x = tx; x < W; x += 32) {
-      const int gi = i0 + x - R, gj = j0 + y - R;
-      T v = T(0);
-      if (gi >= 0 && gi < nx && gj >= 0 && gj < ny) v = psiL[(size_t)gj * a.pitch + gi];
-      ps[y * W + x] = v;
-    }
+  const int tid = tx + ty * 32;
+  for (int w = tid; w < HH * W; w += NT) {
+    const int y = w / W, x = w - y * W;
+    const int gi = i0 + x - R, gj = j0 + y - R;
+    T v = T(0);
+    if (gi >= 0 && gi < nx && gj >= 0 && gj < ny) v = psiL[(size_t)gj * a.pitch + gi];
+    ps[w] = v;
+  }
   __syncthreads();
-  const T cbc = (T)a.cbc;
   // q with one ghost point: adjust_bc(q, 1, psi), src/domain.h:308-348
-  for (int y = ty; y < QH; y += 8)
-    for (int x = tx; x < QW; x += 32) {
-      const int xx = x - 1, yy = y - 1;
-      const int gi = i0 + xx, gj = j0 + yy;
-      const bool inx = gi >= 0 && gi < nx, iny = gj >= 0 && gj < ny;
-      T v = T(0);
-      if (inx && iny) v = qL[(size_t)gj * a.pitch + gi];
-      else if (iny && gi == -1) v = cbc * PS(xx + 1, yy);
-      else if (iny && gi == nx) v = cbc * PS(xx - 1, yy);
-      else if (inx && gj == -1) v = cbc * PS(xx, yy + 1);
-      else if (inx && gj == ny) v = cbc * PS(xx, yy - 1);
-      qs[y * QW + x] = v;
-    }
+  for (int w = tid; w < QH * QW; w += NT) {
+    const int y = w / QW, x = w - y * QW;
+    const int xx = x - 1, yy = y - 1;
+    const int gi = i0 + xx, gj = j0 + yy;
+    const bool inx = gi >= 0 && gi < nx, iny = gj >= 0 && gj < ny;
+    T v = T(0);
+    if (inx && iny) v = qL[(size_t)gj * a.pitch + gi];
+    else if (iny && gi == -1) v = cbc * PS(xx + 1, yy);
+    else if (iny && gi == nx) v = cbc * PS(xx - 1, yy);
+    else if (inx && gj == -1) v = cbc * PS(xx, yy + 1);
+    else if (inx && gj == ny) v = cbc * PS(xx, yy - 1);
+    qs[w] = v;
+  }
   // hyperviscosity chain (calc_diff, src/dynamics.h:13-44) on the tile with
   // a shrinking halo; sweeps are unscaled (no 1/Delta^2), the scale is in
   // nuh_scaled and in the ghost factors gh[s]; in zeta mode the first
-  // sweep is the spectral zeta
+  // sweep is the spectral zeta.  Unrolled over s so that every region
+  // width is a compile-time constant.
   const T* Lp = ps;
   T* Lc = L0;
-  for (int s = 1; s <= a.nsweep; ++s) {
-    __syncthreads();
-    const T ghs = (T)a.gh[s];
-    for (int y = s + ty; y < HH - s; y += 8)
-      for (int x = s + tx; x < W - s; x += 32) {
+#pragma unroll
+  for (int s = 1; s <= R; ++s) {
+    if (s <= a.nsweep) {
+      __syncthreads();
+      const T ghs = (T)a.gh[s];
+      const int Ws = W - 2 * s, Hs = HH - 2 * s;
+      for (int w = tid; w < Ws * Hs; w += NT) {
+        const int yr = w / Ws, xr = w - yr * Ws;
+        const int x = xr + s, y = yr + s;
         const int xx = x - R, yy = y - R;
         const int gi = i0 + xx, gj = j0 + yy;
         const bool inx = gi >= 0 && gi < nx, iny = gj >= 0 && gj < ny;
@@ -496,21 +511,23 @@ __global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
         else if (inx && gj == ny) v = ghs * PS(xx, yy - 1);
         Lc[o] = v;
       }
-    Lp = Lc;
-    Lc = (Lc == L0) ? L1 : L0;
+      Lp = Lc;
+      Lc = (Lc == L0) ? L1 : L0;
+    }
   }
   __syncthreads();
   // centred differences shared between neighbouring Jacobian evaluations
-  for (int y = ty; y < TY; y += 8)
-    for (int x = tx; x < QW; x += 32) {
-      const int xx = x - 1;
-      dyp[y * QW + x] = PS(xx, y + 1) - PS(xx, y - 1);
-      dyq[y * QW + x] = QS(xx, y + 1) - QS(xx, y - 1);
-    }
-  for (int y = ty; y < QH; y += 8) {
+  for (int w = tid; w < TY * QW; w += NT) {
+    const int y = w / QW, x = w - y * QW;
+    const int xx = x - 1;
+    dyp[w] = PS(xx, y + 1) - PS(xx, y - 1);
+    dyq[w] = QS(xx, y + 1) - QS(xx, y - 1);
+  }
+  for (int w = tid; w < QH * TX; w += NT) {
+    const int y = w / TX, x = w - y * TX;
     const int yy = y - 1;
-    dxp[y * TX + tx] = PS(tx + 1, yy) - PS(tx - 1, yy);
-    dxq[y * TX + tx] = QS(tx + 1, yy) - QS(tx - 1, yy);
+    dxp[w] = PS(x + 1, yy) - PS(x - 1, yy);
+    dxq[w] = QS(x + 1, yy) - QS(x - 1, yy);
   }
   __syncthreads();
 #define DY(arr, x, y) arr[(y) * QW + (x) + 1]
@@ -520,7 +537,7 @@ __global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
   slabs(st->step_index + 1, s0, s1, s2);
   T* fout = a.fab + s0 * fs + (size_t)k * a.lstride;
   const bool bottom = (k == a.nl - 1);
-  unsigned long long mymax = 0ULL;
+  decltype(absbits_native(T(0))) mymax_n = 0;
   const int x = tx;
   for (int y = ty; y < TY; y += 8) {
     const int gi = i0 + x, gj = j0 + y;
@@ -538,19 +555,19 @@ __global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
     J = fmaT(-QS(x + 1, y), DY(dyp, x + 1, y), J);
     J = fmaT(QS(x - 1, y), DY(dyp, x - 1, y), J);
     // rhs, src/dynamics.h:55-58: -J - beta psi_x + nu lap q + nu_h lap^n psi
-    T f = fmaT((T)(-a.inv12d2), J, -((T)a.b2d * DX(dxp, x, y)));
+    T f = fmaT(m_inv12, J, -(b2d * DX(dxp, x, y)));
     if (a.has_nu) {
       const T lq = fmaT(T(-4), QS(x, y), (QS(x + 1, y) + QS(x - 1, y)) + (QS(x, y + 1) + QS(x, y - 1)));
-      f = fmaT((T)a.nu_d2, lq, f);
+      f = fmaT(nu_d2, lq, f);
     }
-    if (a.nsweep > 0) f = fmaT((T)a.nuh_scaled, Lp[(y + R) * W + x + R], f);
+    if (a.nsweep > 0) f = fmaT(nuh, Lp[(y + R) * W + x + R], f);
     // surface wind (src/dynamics.h:66) and bottom drag + topography (:67-69)
     if (k == 0 && a.has_wind) f += a.wind[gj];
     if (bottom) {
       if (a.has_drag) {
         const T lp = zm ? d2 * zetaL[(size_t)gj * a.pitch + gi]
                         : fmaT(T(-4), PS(x, y), (PS(x + 1, y) + PS(x - 1, y)) + (PS(x, y + 1) + PS(x, y - 1)));
-        f = fmaT((T)a.drag_d2, lp, f);
+        f = fmaT(drag, lp, f);
       }
       if (a.has_topo) {
         // J(psi, topo) on the ghosted topography grid (reference layout)
@@ -565,17 +582,18 @@ __global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
                       - TP(1, 0) * (PS(x + 1, y + 1) - PS(x + 1, y - 1))
                       + TP(-1, 0) * (PS(x - 1, y + 1) - PS(x - 1, y - 1)));
 #undef TP
-        f = fmaT(-(T)(a.inv12d2 * a.topo_fac), jt, f);
+        f = fmaT(topo_c, jt, f);
       }
     }
     fout[(size_t)gj * a.pitch + gi] = f;
     // CFL (adjust_timestep, src/timestep.h:346-359): one-sided differences
     const T du = PS(x + 1, y) - PS(x, y);
     const T dv = PS(x, y + 1) - PS(x, y);
-    const unsigned long long bu = absbits(du), bv = absbits(dv);
-    const unsigned long long bm = bu > bv ? bu : bv;
-    mymax = bm > mymax ? bm : mymax;
+    const auto bu = absbits_native(du), bv = absbits_native(dv);
+    const auto bm = bu > bv ? bu : bv;
+    mymax_n = bm > mymax_n ? bm : mymax_n;
   }
+  unsigned long long mymax = widen_absbits<T>(mymax_n);
 #undef DY
 #undef DX
 #undef PS
@@ -584,7 +602,6 @@ __global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
     const unsigned long long u = __shfl_xor_sync(0xffffffffu, mymax, o);
     mymax = u > mymax ? u : mymax;
   }
-  const int tid = tx + ty * 32;
   if ((tid & 31) == 0) wmax[tid >> 5] = mymax;
   __syncthreads();
   if (tid == 0) {

@@ -85,6 +85,11 @@ template <typename T> struct StepArgs {
   double lx2, ly2;                 // -4/Delta^2 factors of the discrete symbol
   const double* sx2;               // sin^2(pi k / (2 Mx)), k = 1..nx
   const double* sy2;               // sin^2(pi j / (2 My)), j = 1..ny
+  // FP32 copies of the per-wavenumber tables (compensated path)
+  const float* Lsqf;
+  const float* Ksqf;
+  const float* sx2f;
+  const float* sy2f;
   int CT;                          // (unused by the kernels; kept for layout)
   int vec_cols;                    // rows are 16-byte aligned: 16-byte column loads
   int low_k64;                     // compensated: FP64 divide for mode 0, j,k < low_k64
