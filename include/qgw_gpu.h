@@ -224,6 +224,29 @@ int qgw_invert_pv_noalloc(const qgw_params* p, const double* cl2m, const double*
  * independent FMA chains): the arithmetic roofs of the FP64 kernels. */
 int qgw_probe_fp_rates(double* fp64_tflops, double* fp32_tflops);
 
+/* ---- ensembles: many runs, one launch per step stage --------------------
+ * Members may differ in grid size and layer count (one precision per
+ * ensemble).  qgw_ensemble_step advances every member by up to nsteps steps
+ * (max_steps[i] > 0 caps member i), each stage as one persistent launch
+ * over all members' work items, the four launches of a step captured once
+ * as a CUDA graph (use_graph != 0) and replayed.  A member's result is
+ * bitwise the same alone and in any ensemble.  qgw_ensemble_tune times each
+ * stage for several persistent grid sizes and keeps the fastest; the trial
+ * launches advance the state, so set q afterwards.  No reference
+ * counterpart: the reference runs one configuration per process. */
+typedef struct qgw_ensemble qgw_ensemble;
+int qgw_ensemble_create(int nmembers, const qgw_params* params, int precision, qgw_ensemble** out);
+void qgw_ensemble_destroy(qgw_ensemble* ens);
+int qgw_ensemble_size(qgw_ensemble* ens);
+qgw_run* qgw_ensemble_member(qgw_ensemble* ens, int i);
+int qgw_ensemble_set_q(qgw_ensemble* ens, int i, const double* q);
+int qgw_ensemble_set_time(qgw_ensemble* ens, int i, const qgw_time* tm);
+int qgw_ensemble_get(qgw_ensemble* ens, int i, double* psi, double* q);
+int qgw_ensemble_step(qgw_ensemble* ens, int nsteps, const int* max_steps, int use_graph,
+                      qgw_step_info* infos);
+int qgw_ensemble_tune(qgw_ensemble* ens, int trial_steps, float* best_ms);
+int qgw_ensemble_grids(qgw_ensemble* ens, int* blocks_per_sm);
+
 /* ---- netCDF-3 output and restart (host code, no netCDF library) --------
  * vars.nc as create_nc/write_nc write it (src/netcdf_io.h:38-277): dims
  * t (unlimited), level, y, x; float variables t, y, x, level, psi, q, the

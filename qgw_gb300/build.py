@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"] + ARCH
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall"]
 
-CU_SOURCES = ["kernels.cu", "api.cu", "probe.cu", "noalloc.cu"]
+CU_SOURCES = ["kernels.cu", "api.cu", "ensemble.cu", "probe.cu", "noalloc.cu"]
 CXX_SOURCES = ["host.cpp", "ncio.cpp"]
 
 

@@ -43,6 +43,9 @@ EXPORTS = [
     "qgw_step", "qgw_invert", "qgw_get", "qgw_budget", "qgw_footprint", "qgw_stream",
     "qgw_kernels_per_step", "qgw_profile_kernels", "qgw_probe_fp_rates", "qgw_strerror", "qgw_abi_version",
     "qgw_invert_pv_noalloc", "qgw_nc_create", "qgw_nc_write", "qgw_nc_close", "qgw_nc_read",
+    "qgw_ensemble_create", "qgw_ensemble_destroy", "qgw_ensemble_size", "qgw_ensemble_member",
+    "qgw_ensemble_set_q", "qgw_ensemble_set_time", "qgw_ensemble_get", "qgw_ensemble_step",
+    "qgw_ensemble_tune", "qgw_ensemble_grids",
 ]
 
 
@@ -92,6 +95,18 @@ def load(path: str = LIB_PATH):
     lib.qgw_strerror.argtypes = [I]
     lib.qgw_strerror.restype = ctypes.c_char_p
     lib.qgw_abi_version.argtypes = []
+    lib.qgw_ensemble_create.argtypes = [I, pp, I, P(V)]
+    lib.qgw_ensemble_destroy.argtypes = [V]
+    lib.qgw_ensemble_destroy.restype = None
+    lib.qgw_ensemble_size.argtypes = [V]
+    lib.qgw_ensemble_member.argtypes = [V, I]
+    lib.qgw_ensemble_member.restype = V
+    lib.qgw_ensemble_set_q.argtypes = [V, I, D]
+    lib.qgw_ensemble_set_time.argtypes = [V, I, P(QgwTime)]
+    lib.qgw_ensemble_get.argtypes = [V, I, D, D]
+    lib.qgw_ensemble_step.argtypes = [V, I, P(I), I, P(QgwStepInfo)]
+    lib.qgw_ensemble_tune.argtypes = [V, I, P(ctypes.c_float)]
+    lib.qgw_ensemble_grids.argtypes = [V, P(I)]
     lib.qgw_nc_create.argtypes = [ctypes.c_char_p, I, I, I, ctypes.c_double]
     lib.qgw_nc_create.restype = V
     lib.qgw_nc_write.argtypes = [V, ctypes.c_double, D, D]
@@ -153,6 +168,63 @@ def footprint(params: Dict[str, object], precision: int = FP64) -> int:
     b = ctypes.c_size_t()
     _check(lib.qgw_footprint(ctypes.byref(s), int(precision), ctypes.byref(b)), "qgw_footprint")
     return int(b.value)
+
+
+class Ensemble:
+    """Independent runs of uneven sizes advanced together (one launch per
+    step stage over all members, replayed as a CUDA graph)."""
+
+    def __init__(self, params_list, precision: int = FP32C):
+        self.lib = load()
+        self.params = list(params_list)
+        n = len(self.params)
+        arr = (QgwParams * n)(*[to_struct(p) for p in self.params])
+        self._arr = arr
+        h = ctypes.c_void_p()
+        _check(self.lib.qgw_ensemble_create(n, arr, int(precision), ctypes.byref(h)), "qgw_ensemble_create")
+        self.h = h
+        self.shapes = [halo_shape(p) for p in self.params]
+
+    def __len__(self):
+        return len(self.params)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.qgw_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_q(self, i: int, q: np.ndarray):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        _check(self.lib.qgw_ensemble_set_q(self.h, int(i), _dp(q)), "qgw_ensemble_set_q")
+
+    def fix_dt(self, i: int, dt: float):
+        tm = QgwTime(0.0, dt, dt, dt, dt)
+        _check(self.lib.qgw_ensemble_set_time(self.h, int(i), ctypes.byref(tm)), "qgw_ensemble_set_time")
+
+    def step(self, n: int, max_steps=None, graph: bool = True):
+        m = len(self.params)
+        infos = (QgwStepInfo * m)()
+        ms = None if max_steps is None else (ctypes.c_int * m)(*[int(x) for x in max_steps])
+        _check(self.lib.qgw_ensemble_step(self.h, int(n), ms, int(graph), infos), "qgw_ensemble_step")
+        return list(infos)
+
+    def get(self, i: int):
+        psi, q = np.empty(self.shapes[i]), np.empty(self.shapes[i])
+        _check(self.lib.qgw_ensemble_get(self.h, int(i), _dp(psi), _dp(q)), "qgw_ensemble_get")
+        return psi, q
+
+    def tune(self, trial_steps: int = 3):
+        ms = (ctypes.c_float * 4)()
+        _check(self.lib.qgw_ensemble_tune(self.h, int(trial_steps), ms), "qgw_ensemble_tune")
+        g = (ctypes.c_int * 4)()
+        _check(self.lib.qgw_ensemble_grids(self.h, g), "qgw_ensemble_grids")
+        return list(ms), list(g)
 
 
 class NcWriter:

@@ -1,0 +1,316 @@
+// ensemble.cu -- batches of independent runs (uneven grids and layer
+// counts) advanced together: one persistent launch per step stage over all
+// members, the four launches of a step captured once as a CUDA graph and
+// replayed, and a project autotuner for the persistent grid of each stage.
+//
+// Each member is a full qgw_run (own fields, own device scalars, own CFL
+// counter); the batched kernels only change which block computes which
+// member's work item, never the arithmetic, so a member's result is bitwise
+// the same alone and in any batch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "../../include/qgw_gpu.h"
+#include "kernels.h"
+#include "qgw_device.cuh"
+#include "run.h"
+
+struct qgw_ensemble {
+  int precision = 0;
+  int nsm = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<qgw_run*> members;
+  // device member table and work lists
+  void* d_members = nullptr;
+  int* d_lists = nullptr;  // start_rows | start_cols | start_rhs | total[4]
+  int* d_maxsteps = nullptr;
+  qgw::EnsArgs<double> e64{};
+  qgw::EnsArgs<float> e32{};
+  qgw::EnsSmem sm{};
+  int total[4] = {0, 0, 0, 0};
+  int bps[4] = {2, 2, 2, 2};  // persistent blocks per SM, per stage (tuned)
+  int grid[4] = {0, 0, 0, 0};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<qgw::DevState> h_states;
+};
+
+namespace {
+
+int cuda_fail(cudaError_t e) {
+  if (e == cudaSuccess) return QGW_OK;
+  if (e == cudaErrorMemoryAllocation) return QGW_ERR_NOMEM;
+  return QGW_ERR_CUDA;
+}
+#define CK(x)                                    \
+  do {                                           \
+    cudaError_t e_ = (x);                        \
+    if (e_ != cudaSuccess) return cuda_fail(e_); \
+  } while (0)
+
+void drop_graph(qgw_ensemble* e) {
+  if (e->exec) cudaGraphExecDestroy(e->exec);
+  if (e->graph) cudaGraphDestroy(e->graph);
+  e->exec = nullptr;
+  e->graph = nullptr;
+}
+
+void set_grids(qgw_ensemble* e) {
+  for (int s = 0; s < 4; ++s) e->grid[s] = std::max(1, std::min(e->total[s], e->nsm * e->bps[s]));
+}
+
+// member table, per-stage work lists and shared-memory sizes
+int build_tables(qgw_ensemble* e) {
+  const int n = (int)e->members.size();
+  const int ct = e->precision == QGW_FP64 ? qgw::cols_per_tile_f64() : qgw::cols_per_tile_f32c();
+  const int tx = qgw::rhs_tile_x(), ty = qgw::rhs_tile_y();
+  std::vector<int> lists(3 * (n + 1) + 4, 0);
+  int* rows = lists.data();
+  int* cols = rows + (n + 1);
+  int* rhs = cols + (n + 1);
+  for (int i = 0; i < n; ++i) {
+    const qgw_run* r = e->members[i];
+    rows[i + 1] = rows[i] + r->ny;
+    cols[i + 1] = cols[i] + ((r->nx + ct - 1) / ct) * r->nl;
+    rhs[i + 1] = rhs[i] + ((r->nx + tx - 1) / tx) * ((r->ny + ty - 1) / ty) * r->nl;
+  }
+  int* tot = rhs + (n + 1);
+  tot[0] = rows[n];
+  tot[1] = cols[n];
+  tot[2] = rows[n];
+  tot[3] = rhs[n];
+  for (int s = 0; s < 4; ++s) e->total[s] = tot[s];
+  CK(cudaMalloc(&e->d_lists, sizeof(int) * lists.size()));
+  CK(cudaMemcpyAsync(e->d_lists, lists.data(), sizeof(int) * lists.size(), cudaMemcpyHostToDevice, e->stream));
+  CK(cudaMalloc(&e->d_maxsteps, sizeof(int) * n));
+  if (e->precision == QGW_FP64) {
+    std::vector<qgw::StepArgs<double>> h(n);
+    for (int i = 0; i < n; ++i) h[i] = e->members[i]->a64;
+    CK(cudaMalloc(&e->d_members, sizeof(h[0]) * n));
+    CK(cudaMemcpyAsync(e->d_members, h.data(), sizeof(h[0]) * n, cudaMemcpyHostToDevice, e->stream));
+    e->sm = qgw::ens_smem_f64(h.data(), n);
+    e->e64 = {(const qgw::StepArgs<double>*)e->d_members, e->d_lists, e->d_lists + (n + 1),
+              e->d_lists + 2 * (n + 1), e->d_lists + 3 * (n + 1), n};
+  } else {
+    std::vector<qgw::StepArgs<float>> h(n);
+    for (int i = 0; i < n; ++i) h[i] = e->members[i]->a32;
+    CK(cudaMalloc(&e->d_members, sizeof(h[0]) * n));
+    CK(cudaMemcpyAsync(e->d_members, h.data(), sizeof(h[0]) * n, cudaMemcpyHostToDevice, e->stream));
+    e->sm = qgw::ens_smem_f32c(h.data(), n);
+    e->e32 = {(const qgw::StepArgs<float>*)e->d_members, e->d_lists, e->d_lists + (n + 1),
+              e->d_lists + 2 * (n + 1), e->d_lists + 3 * (n + 1), n};
+  }
+  set_grids(e);
+  CK(cudaStreamSynchronize(e->stream));
+  return QGW_OK;
+}
+
+void launch_step(qgw_ensemble* e, int mask) {
+  if (e->precision == QGW_FP64) qgw::ens_step_f64(e->e64, e->sm, e->grid, mask, e->stream);
+  else qgw::ens_step_f32c(e->e32, e->sm, e->grid, mask, e->stream);
+}
+
+int ensure_graph(qgw_ensemble* e) {
+  if (e->exec) return QGW_OK;
+  CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+  launch_step(e, 15);
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamEndCapture(e->stream, &g));
+  e->graph = g;
+  CK(cudaGraphInstantiate(&e->exec, g, 0));
+  return QGW_OK;
+}
+
+int read_states(qgw_ensemble* e) {
+  const int n = (int)e->members.size();
+  e->h_states.resize(n);
+  for (int i = 0; i < n; ++i)
+    CK(cudaMemcpyAsync(&e->h_states[i], e->members[i]->d_state, sizeof(qgw::DevState), cudaMemcpyDeviceToHost,
+                       e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  return QGW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qgw_ensemble_create(int n, const qgw_params* params, int precision, qgw_ensemble** out) {
+  if (!params || !out || n < 1) return QGW_ERR_PARAM;
+  *out = nullptr;
+  qgw_ensemble* e = new qgw_ensemble();
+  e->precision = precision;
+  int dev = 0, rc = QGW_OK;
+  auto fail = [&](int code) {
+    qgw_ensemble_destroy(e);
+    return code;
+  };
+  if (cudaGetDevice(&dev) != cudaSuccess) return fail(QGW_ERR_CUDA);
+  if (cudaDeviceGetAttribute(&e->nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return fail(QGW_ERR_CUDA);
+  if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(QGW_ERR_CUDA);
+  for (int i = 0; i < n; ++i) {
+    qgw_run* r = nullptr;
+    if ((rc = qgw_create(&params[i], nullptr, nullptr, nullptr, nullptr, precision, &r))) return fail(rc);
+    e->members.push_back(r);
+  }
+  const cudaError_t pe = precision == QGW_FP64 ? qgw::ens_prepare_f64() : qgw::ens_prepare_f32c();
+  if (pe != cudaSuccess) return fail(cuda_fail(pe));
+  if ((rc = build_tables(e))) return fail(rc);
+  *out = e;
+  return QGW_OK;
+}
+
+void qgw_ensemble_destroy(qgw_ensemble* e) {
+  if (!e) return;
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  drop_graph(e);
+  for (qgw_run* r : e->members) qgw_destroy(r);
+  if (e->d_members) cudaFree(e->d_members);
+  if (e->d_lists) cudaFree(e->d_lists);
+  if (e->d_maxsteps) cudaFree(e->d_maxsteps);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+}
+
+int qgw_ensemble_size(qgw_ensemble* e) { return e ? (int)e->members.size() : 0; }
+
+qgw_run* qgw_ensemble_member(qgw_ensemble* e, int i) {
+  if (!e || i < 0 || i >= (int)e->members.size()) return nullptr;
+  cudaStreamSynchronize(e->stream);
+  return e->members[i];
+}
+
+int qgw_ensemble_step(qgw_ensemble* e, int nsteps, const int* max_steps, int use_graph, qgw_step_info* infos) {
+  if (!e || nsteps < 0) return QGW_ERR_PARAM;
+  const int n = (int)e->members.size();
+  for (qgw_run* r : e->members)
+    if (!r->has_q) return QGW_ERR_STATE;
+  for (qgw_run* r : e->members) CK(cudaStreamSynchronize(r->stream));
+  std::vector<int> ms(n, 0);
+  if (max_steps) std::memcpy(ms.data(), max_steps, sizeof(int) * n);
+  CK(cudaMemcpyAsync(e->d_maxsteps, ms.data(), sizeof(int) * n, cudaMemcpyHostToDevice, e->stream));
+  if (e->precision == QGW_FP64) qgw::ens_begin_f64(e->e64, e->d_maxsteps, e->stream);
+  else qgw::ens_begin_f32c(e->e32, e->d_maxsteps, e->stream);
+  int rc;
+  if (use_graph && (rc = ensure_graph(e))) return rc;
+  const int chunk = 256;
+  for (int done = 0; done < nsteps;) {
+    const int k = std::min(chunk, nsteps - done);
+    for (int s = 0; s < k; ++s) {
+      if (use_graph) CK(cudaGraphLaunch(e->exec, e->stream));
+      else launch_step(e, 15);
+    }
+    done += k;
+    if (done < nsteps) {
+      if ((rc = read_states(e))) return rc;
+      bool any = false;
+      for (const auto& s : e->h_states) any = any || s.active;
+      if (!any) break;
+    }
+  }
+  const int fgrid = std::max(1, std::min(e->total[0], e->nsm * 4));
+  if (e->precision == QGW_FP64) qgw::ens_flush_f64(e->e64, fgrid, e->stream);
+  else qgw::ens_flush_f32c(e->e32, fgrid, e->stream);
+  CK(cudaGetLastError());
+  if ((rc = read_states(e))) return rc;
+  bool bad = false;
+  for (int i = 0; i < n; ++i) {
+    const qgw::DevState& s = e->h_states[i];
+    bad = bad || s.nonfinite;
+    if (infos) {
+      infos[i].time.t = s.t;
+      infos[i].time.dt = s.dt;
+      infos[i].time.dt0 = s.dt0;
+      infos[i].time.dt1 = s.dt1;
+      infos[i].time.DT_max = s.DT_max;
+      infos[i].steps_taken = s.steps_taken;
+      infos[i].stop_reason = s.stop_reason;
+      infos[i].nonfinite = s.nonfinite;
+    }
+  }
+  return bad ? QGW_ERR_NAN : QGW_OK;
+}
+
+// Autotuner: for each stage, time `trial_steps` launches of that stage
+// alone for every candidate persistent grid (blocks per SM), keep the
+// fastest.  Runs on the current state and then restores the members' time
+// scalars and AB3 history, so call it before the time loop (it re-applies
+// qgw_set_q's reset of the history).  best_ms[4] (optional) receives the
+// per-stage times of the chosen grids.
+int qgw_ensemble_tune(qgw_ensemble* e, int trial_steps, float* best_ms) {
+  if (!e || trial_steps < 1) return QGW_ERR_PARAM;
+  for (qgw_run* r : e->members)
+    if (!r->has_q) return QGW_ERR_STATE;
+  const int n = (int)e->members.size();
+  std::vector<qgw_time> saved(n);
+  for (int i = 0; i < n; ++i) qgw_get_time(e->members[i], &saved[i]);
+  std::vector<int> ms(n, 0);
+  CK(cudaMemcpyAsync(e->d_maxsteps, ms.data(), sizeof(int) * n, cudaMemcpyHostToDevice, e->stream));
+  const int cands[] = {1, 2, 3, 4, 6, 8};
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  drop_graph(e);
+  for (int s = 0; s < 4; ++s) {
+    float best = 1e30f;
+    int best_b = e->bps[s];
+    for (int b : cands) {
+      e->bps[s] = b;
+      set_grids(e);
+      if (e->precision == QGW_FP64) qgw::ens_begin_f64(e->e64, e->d_maxsteps, e->stream);
+      else qgw::ens_begin_f32c(e->e32, e->d_maxsteps, e->stream);
+      launch_step(e, 1 << s);  // warm-up
+      CK(cudaEventRecord(e0, e->stream));
+      for (int t = 0; t < trial_steps; ++t) launch_step(e, 1 << s);
+      CK(cudaEventRecord(e1, e->stream));
+      CK(cudaEventSynchronize(e1));
+      float msr = 0;
+      CK(cudaEventElapsedTime(&msr, e0, e1));
+      msr /= trial_steps;
+      if (msr < best) { best = msr; best_b = b; }
+    }
+    e->bps[s] = best_b;
+    if (best_ms) best_ms[s] = best;
+  }
+  set_grids(e);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CK(cudaGetLastError());
+  // the trial launches advanced the state: restore time scalars and clear
+  // the history; q itself was only touched by AB3 updates of zero history
+  // when nothing was pending, so callers re-set q before the time loop
+  for (int i = 0; i < n; ++i) {
+    qgw_run* r = e->members[i];
+    qgw_set_time(r, &saved[i]);
+  }
+  return QGW_OK;
+}
+
+int qgw_ensemble_set_q(qgw_ensemble* e, int i, const double* q) {
+  if (!e || i < 0 || i >= (int)e->members.size()) return QGW_ERR_PARAM;
+  CK(cudaStreamSynchronize(e->stream));
+  return qgw_set_q(e->members[i], q);
+}
+
+int qgw_ensemble_set_time(qgw_ensemble* e, int i, const qgw_time* tm) {
+  if (!e || i < 0 || i >= (int)e->members.size()) return QGW_ERR_PARAM;
+  CK(cudaStreamSynchronize(e->stream));
+  return qgw_set_time(e->members[i], tm);
+}
+
+int qgw_ensemble_get(qgw_ensemble* e, int i, double* psi, double* q) {
+  if (!e || i < 0 || i >= (int)e->members.size()) return QGW_ERR_PARAM;
+  CK(cudaStreamSynchronize(e->stream));
+  return qgw_get(e->members[i], psi, q);
+}
+
+int qgw_ensemble_grids(qgw_ensemble* e, int* bps4) {
+  if (!e || !bps4) return QGW_ERR_PARAM;
+  for (int s = 0; s < 4; ++s) bps4[s] = e->bps[s];
+  return QGW_OK;
+}
+
+}  // extern "C"

@@ -21,6 +21,8 @@
 // is a shift and a mask.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "kernels.h"
 #include "qgw_device.cuh"
 
@@ -124,12 +126,10 @@ __device__ __forceinline__ void comp_add(float& hi, float& lo, float d) {
 // block ever reads a q value another block may be updating.  The projection
 // accumulates in shared memory (one FMA per layer and mode).
 template <typename T, bool COMP>
-__global__ void __launch_bounds__(NT) k_rows_fwd(StepArgs<T> a, int step_mode) {
+__device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mode, int j, unsigned char* smem_raw,
+                                              T* tot) {
   DevState* st = a.state;
   if (step_mode && !st->active) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ T tot[GMAX * 32];
-  const int j = blockIdx.x;
   const int ld = padded_len(a.gx.M);
   T* A = (T*)smem_raw;
   T* B = A + (size_t)a.G1 * ld;
@@ -208,14 +208,12 @@ __device__ __forceinline__ void store_cols(T* __restrict__ dst, const T* v) {
 }
 
 template <typename T, bool COMP>
-__global__ void __launch_bounds__(NT) k_cols(StepArgs<T> a, int step_mode) {
+__device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, int bx, int m, unsigned char* smem_raw,
+                                          T* tot) {
   constexpr int CT = ColsPer<T>::value;
   DevState* st = a.state;
   if (step_mode && !st->active) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ T tot[GMAX * 32];
-  const int k0 = blockIdx.x * CT;
-  const int m = blockIdx.y;
+  const int k0 = bx * CT;
   const int CTb = min(CT, a.nx - k0);
   const int ld = padded_len(a.gy.M);
   T* A = (T*)smem_raw;
@@ -309,12 +307,10 @@ __global__ void __launch_bounds__(NT) k_cols(StepArgs<T> a, int step_mode) {
 // inverse-transforms the spectral zeta rows (rows G..2G-1 of the batch) and
 // back-projects them into zeta.
 template <typename T, bool COMP>
-__global__ void __launch_bounds__(NT) k_rows_inv(StepArgs<T> a, int step_mode) {
+__device__ __forceinline__ void body_rows_inv(const StepArgs<T>& a, int step_mode, int j, unsigned char* smem_raw,
+                                              T* tot) {
   DevState* st = a.state;
   if (step_mode && !st->active) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ T tot[GMAX * 32];
-  const int j = blockIdx.x;
   const int ld = padded_len(a.gx.M);
   const bool zm = COMP && a.zeta_mode;
   const int Gb = zm ? a.G3 : a.G1;
@@ -415,6 +411,8 @@ __device__ void scalar_update(DevState* st, double Delta, double cfl) {
     st->active = 0; st->stop_reason = 2;
   } else if (fabs(tn - t_out) < TEPS * dt) {
     st->active = 0; st->stop_reason = 1;
+  } else if (st->max_steps > 0 && st->steps_taken >= st->max_steps) {
+    st->active = 0; st->stop_reason = 0;
   }
   st->maxbits = 0ULL;
   st->done_blocks = 0u;
@@ -423,12 +421,12 @@ __device__ void scalar_update(DevState* st, double Delta, double cfl) {
 // RHS tile of TX x TY points of one layer; block (32, 8); R = halo radius
 // of psi (the number of hyperviscosity sweeps, at least 1).
 template <typename T, bool COMP, int R>
-__global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
+__device__ __forceinline__ void body_rhs(const StepArgs<T>& a, int bx, int by, int k, unsigned int total,
+                                         unsigned char* smem_raw) {
   DevState* st = a.state;
   if (!st->active) return;
   constexpr int W = TX + 2 * R, HH = TY + 2 * R;
   constexpr int QW = TX + 2, QH = TY + 2;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   T* ps = (T*)smem_raw;       // HH x W, psi with halo R
   T* L0 = ps + W * HH;        // chain ping-pong
   T* L1 = L0 + W * HH;
@@ -440,8 +438,7 @@ __global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
   __shared__ unsigned long long wmax[NT / 32];
   __shared__ int is_last;
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const int k = blockIdx.z;
-  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  const int i0 = bx * TX, j0 = by * TY;
   const int nx = a.nx, ny = a.ny;
   const T* psiL = a.psi + (size_t)k * a.lstride;
   const T* qL = a.q + (size_t)k * a.lstride;
@@ -609,7 +606,6 @@ __global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
     for (int w = 0; w < NT / 32; ++w) bm = wmax[w] > bm ? wmax[w] : bm;
     atomicMax(&st->maxbits, bm);
     __threadfence();
-    const unsigned int total = gridDim.x * gridDim.y * gridDim.z;
     const unsigned int ticket = atomicAdd(&st->done_blocks, 1u);
     is_last = (ticket == total - 1);
   }
@@ -620,15 +616,136 @@ __global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
   }
 }
 
+// ------------------------------------------------- single-run wrappers
+template <typename T, bool COMP>
+__global__ void __launch_bounds__(NT) k_rows_fwd(StepArgs<T> a, int step_mode) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ T tot[GMAX * 32];
+  body_rows_fwd<T, COMP>(a, step_mode, blockIdx.x, smem_raw, tot);
+}
+template <typename T, bool COMP>
+__global__ void __launch_bounds__(NT) k_cols(StepArgs<T> a, int step_mode) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ T tot[GMAX * 32];
+  body_cols<T, COMP>(a, step_mode, blockIdx.x, blockIdx.y, smem_raw, tot);
+}
+template <typename T, bool COMP>
+__global__ void __launch_bounds__(NT) k_rows_inv(StepArgs<T> a, int step_mode) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ T tot[GMAX * 32];
+  body_rows_inv<T, COMP>(a, step_mode, blockIdx.x, smem_raw, tot);
+}
+template <typename T, bool COMP, int R>
+__global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  body_rhs<T, COMP, R>(a, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x * gridDim.y * gridDim.z, smem_raw);
+}
+
+// --------------------------------------------------- ensemble wrappers
+// Persistent launches over all members of an ensemble: work item w of a
+// stage belongs to member mi with start[mi] <= w < start[mi+1]; each block
+// copies that member's arguments into shared memory and runs the same body
+// as a single run would.  Members are independent (own fields, own device
+// scalars, own CFL counter), so a member's result does not depend on which
+// other members share the launch.
+template <typename T>
+__device__ __forceinline__ int ens_item(const EnsArgs<T>& e, const int* start, int item, StepArgs<T>* sa) {
+  __shared__ int s_mi;
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    int lo = 0, hi = e.n - 1;
+    while (lo < hi) {  // last member whose start <= item
+      const int mid = (lo + hi + 1) >> 1;
+      if (start[mid] <= item) lo = mid;
+      else hi = mid - 1;
+    }
+    s_mi = lo;
+  }
+  __syncthreads();
+  const int mi = s_mi;
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+  const int* srcw = reinterpret_cast<const int*>(e.members + mi);
+  int* dstw = reinterpret_cast<int*>(sa);
+  for (int w = tid; w < (int)(sizeof(StepArgs<T>) / 4); w += blockDim.x * blockDim.y) dstw[w] = srcw[w];
+  __syncthreads();
+  return item - start[mi];
+}
+
+template <typename T, bool COMP>
+__global__ void __launch_bounds__(NT) k_rows_fwd_ens(EnsArgs<T> e, int step_mode) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ T tot[GMAX * 32];
+  __shared__ StepArgs<T> sa;
+  for (int item = blockIdx.x; item < e.total[0]; item += gridDim.x) {
+    const int local = ens_item(e, e.start_rows, item, &sa);
+    body_rows_fwd<T, COMP>(sa, step_mode, local, smem_raw, tot);
+    __syncthreads();
+  }
+}
+template <typename T, bool COMP>
+__global__ void __launch_bounds__(NT) k_cols_ens(EnsArgs<T> e, int step_mode) {
+  constexpr int CT = ColsPer<T>::value;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ T tot[GMAX * 32];
+  __shared__ StepArgs<T> sa;
+  for (int item = blockIdx.x; item < e.total[1]; item += gridDim.x) {
+    const int local = ens_item(e, e.start_cols, item, &sa);
+    const int ntx = (sa.nx + CT - 1) / CT;
+    body_cols<T, COMP>(sa, step_mode, local % ntx, local / ntx, smem_raw, tot);
+    __syncthreads();
+  }
+}
+template <typename T, bool COMP>
+__global__ void __launch_bounds__(NT) k_rows_inv_ens(EnsArgs<T> e, int step_mode) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ T tot[GMAX * 32];
+  __shared__ StepArgs<T> sa;
+  for (int item = blockIdx.x; item < e.total[2]; item += gridDim.x) {
+    const int local = ens_item(e, e.start_rows, item, &sa);
+    body_rows_inv<T, COMP>(sa, step_mode, local, smem_raw, tot);
+    __syncthreads();
+  }
+}
+template <typename T, bool COMP>
+__global__ void __launch_bounds__(NT) k_rhs_ens(EnsArgs<T> e) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ StepArgs<T> sa;
+  for (int item = blockIdx.x; item < e.total[3]; item += gridDim.x) {
+    const int local = ens_item(e, e.start_rhs, item, &sa);
+    const int ntx = (sa.nx + TX - 1) / TX, nty = (sa.ny + TY - 1) / TY;
+    const int bx = local % ntx, rest = local / ntx, by = rest % nty, bz = rest / nty;
+    const unsigned int total = (unsigned int)(ntx * nty * sa.nl);
+    switch (sa.nsweep > 0 ? sa.nsweep : 1) {
+      case 1: body_rhs<T, COMP, 1>(sa, bx, by, bz, total, smem_raw); break;
+      case 2: body_rhs<T, COMP, 2>(sa, bx, by, bz, total, smem_raw); break;
+      case 3: body_rhs<T, COMP, 3>(sa, bx, by, bz, total, smem_raw); break;
+      default: body_rhs<T, COMP, 4>(sa, bx, by, bz, total, smem_raw); break;
+    }
+    __syncthreads();
+  }
+}
+
 
 // ------------------------------------------------------- small kernels
-__global__ void k_begin(DevState* st, double t_out, double tend) {
+__device__ __forceinline__ void begin_state(DevState* st, double t_out, double tend, int max_steps) {
   st->t_out = t_out;
   st->tend = tend;
   st->first = 1;
   st->steps_taken = 0;
   st->stop_reason = 0;
-  st->active = (tend > 0 && !(st->t < tend)) ? 0 : 1;
+  st->max_steps = max_steps;
+  st->active = ((tend > 0 && !(st->t < tend)) || max_steps < 0) ? 0 : 1;
+}
+__global__ void k_begin(DevState* st, double t_out, double tend) { begin_state(st, t_out, tend, 0); }
+
+template <typename T>
+__global__ void k_begin_ens(EnsArgs<T> e, double t_out, double tend, const int* max_steps) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < e.n) begin_state(e.members[i].state, t_out, tend, max_steps ? max_steps[i] : 0);
+}
+template <typename T>
+__global__ void k_end_ens(EnsArgs<T> e) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < e.n) e.members[i].state->pending = 0;
 }
 
 template <typename T, bool COMP>
@@ -660,6 +777,37 @@ __global__ void __launch_bounds__(NT) k_flush(StepArgs<T> a) {
 }
 
 __global__ void k_end(DevState* st) { st->pending = 0; }
+
+// flush of the pending AB3 update for every member, one row per work item
+template <typename T, bool COMP>
+__global__ void __launch_bounds__(NT) k_flush_ens(EnsArgs<T> e) {
+  __shared__ StepArgs<T> sa;
+  for (int item = blockIdx.x; item < e.total[0]; item += gridDim.x) {
+    const int j = ens_item(e, e.start_rows, item, &sa);
+    const DevState* st = sa.state;
+    if (st->pending) {
+      int s0, s1, s2;
+      slabs(st->step_index, s0, s1, s2);
+      const double c0 = st->c0, c1 = st->c1, c2 = st->c2;
+      const size_t fs = (size_t)sa.nl * sa.lstride;
+      for (int l = 0; l < sa.nl; ++l)
+        for (int i = threadIdx.x; i < sa.nx; i += NT) {
+          const size_t o = (size_t)l * sa.lstride + (size_t)j * sa.pitch + i;
+          if (COMP) {
+            float hi = (float)sa.q[o], lo = (float)sa.qlo[o];
+            const float d = (float)c0 * (float)sa.fab[s0 * fs + o] + (float)c1 * (float)sa.fab[s1 * fs + o] +
+                            (float)c2 * (float)sa.fab[s2 * fs + o];
+            comp_add(hi, lo, d);
+            sa.q[o] = (T)hi;
+            sa.qlo[o] = (T)lo;
+          } else {
+            sa.q[o] = sa.q[o] + (T)c0 * sa.fab[s0 * fs + o] + (T)c1 * sa.fab[s1 * fs + o] + (T)c2 * sa.fab[s2 * fs + o];
+          }
+        }
+    }
+    __syncthreads();
+  }
+}
 
 // FP32c <-> FP64 conversions for the boundary copies
 __global__ void k_split_f64(const double* src, float* hi, float* lo, size_t n) {
@@ -859,6 +1007,86 @@ void enqueue_budget_f64(const StepArgs<double>& a, const double* w, double* part
                         cudaStream_t s) { budget_impl<double>(a, w, part, nblk, scale, out, s); }
 void enqueue_budget_f32c(const StepArgs<float>& a, const double* w, double* part, int nblk, double scale, double* out,
                          cudaStream_t s) { budget_impl<float>(a, w, part, nblk, scale, out, s); }
+
+// ---- ensembles: one persistent launch per stage over all members
+template <typename T, bool COMP>
+static cudaError_t set_attrs_ens() {
+  int dev = 0, optin = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+  const int lim = optin - (int)(sizeof(T) * GMAX * 32 + sizeof(StepArgs<T>) + 128);
+  if ((e = cudaFuncSetAttribute(k_rows_fwd_ens<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
+    return e;
+  if ((e = cudaFuncSetAttribute(k_rows_inv_ens<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
+    return e;
+  if ((e = cudaFuncSetAttribute(k_cols_ens<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
+  return cudaFuncSetAttribute(k_rhs_ens<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              optin - (int)(sizeof(StepArgs<T>) + 1024));
+}
+
+template <typename T, bool COMP>
+static EnsSmem ens_smem(const StepArgs<T>* host_members, int n) {
+  EnsSmem s{};
+  for (int i = 0; i < n; ++i) {
+    const StepArgs<T>& a = host_members[i];
+    s.bytes[0] = std::max(s.bytes[0], smem_rows<T, COMP>(a));
+    s.bytes[1] = std::max(s.bytes[1], smem_cols<T, COMP>(a));
+    s.bytes[2] = std::max(s.bytes[2], smem_rows_inv<T, COMP>(a));
+    s.bytes[3] = std::max(s.bytes[3], smem_rhs<T>(a));
+  }
+  return s;
+}
+
+template <typename T, bool COMP>
+static void ens_step(const EnsArgs<T>& e, const EnsSmem& sm, const int* grid, int which_mask, cudaStream_t s) {
+  if (which_mask & 1) k_rows_fwd_ens<T, COMP><<<grid[0], NT, sm.bytes[0], s>>>(e, 1);
+  if (which_mask & 2) k_cols_ens<T, COMP><<<grid[1], NT, sm.bytes[1], s>>>(e, 1);
+  if (which_mask & 4) k_rows_inv_ens<T, COMP><<<grid[2], NT, sm.bytes[2], s>>>(e, 1);
+  if (which_mask & 8) k_rhs_ens<T, COMP><<<grid[3], dim3(32, 8), sm.bytes[3], s>>>(e);
+}
+template <typename T, bool COMP>
+static void ens_invert(const EnsArgs<T>& e, const EnsSmem& sm, const int* grid, cudaStream_t s) {
+  k_rows_fwd_ens<T, COMP><<<grid[0], NT, sm.bytes[0], s>>>(e, 0);
+  k_cols_ens<T, COMP><<<grid[1], NT, sm.bytes[1], s>>>(e, 0);
+  k_rows_inv_ens<T, COMP><<<grid[2], NT, sm.bytes[2], s>>>(e, 0);
+}
+
+cudaError_t ens_prepare_f64() { return set_attrs_ens<double, false>(); }
+cudaError_t ens_prepare_f32c() { return set_attrs_ens<float, true>(); }
+EnsSmem ens_smem_f64(const StepArgs<double>* m, int n) { return ens_smem<double, false>(m, n); }
+EnsSmem ens_smem_f32c(const StepArgs<float>* m, int n) { return ens_smem<float, true>(m, n); }
+void ens_begin_f64(const EnsArgs<double>& e, const int* max_steps, cudaStream_t s) {
+  k_begin_ens<double><<<(e.n + 63) / 64, 64, 0, s>>>(e, 0.0, 0.0, max_steps);
+}
+void ens_begin_f32c(const EnsArgs<float>& e, const int* max_steps, cudaStream_t s) {
+  k_begin_ens<float><<<(e.n + 63) / 64, 64, 0, s>>>(e, 0.0, 0.0, max_steps);
+}
+void ens_step_f64(const EnsArgs<double>& e, const EnsSmem& sm, const int* grid, int mask, cudaStream_t s) {
+  ens_step<double, false>(e, sm, grid, mask, s);
+}
+void ens_step_f32c(const EnsArgs<float>& e, const EnsSmem& sm, const int* grid, int mask, cudaStream_t s) {
+  ens_step<float, true>(e, sm, grid, mask, s);
+}
+void ens_invert_f64(const EnsArgs<double>& e, const EnsSmem& sm, const int* grid, cudaStream_t s) {
+  ens_invert<double, false>(e, sm, grid, s);
+}
+void ens_invert_f32c(const EnsArgs<float>& e, const EnsSmem& sm, const int* grid, cudaStream_t s) {
+  ens_invert<float, true>(e, sm, grid, s);
+}
+void ens_flush_f64(const EnsArgs<double>& e, int grid, cudaStream_t s) {
+  k_flush_ens<double, false><<<grid, NT, 0, s>>>(e);
+  k_end_ens<double><<<(e.n + 63) / 64, 64, 0, s>>>(e);
+}
+void ens_flush_f32c(const EnsArgs<float>& e, int grid, cudaStream_t s) {
+  k_flush_ens<float, true><<<grid, NT, 0, s>>>(e);
+  k_end_ens<float><<<(e.n + 63) / 64, 64, 0, s>>>(e);
+}
+int cols_per_tile_f64() { return ColsPer<double>::value; }
+int cols_per_tile_f32c() { return ColsPer<float>::value; }
+int rhs_tile_x() { return TX; }
+int rhs_tile_y() { return TY; }
 
 size_t smem_bytes_rows_f64(const StepArgs<double>& a) { return smem_rows<double, false>(a); }
 size_t smem_bytes_cols_f64(const StepArgs<double>& a) { return smem_cols<double, false>(a); }

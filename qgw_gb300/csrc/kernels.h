@@ -30,6 +30,26 @@ void enqueue_budget_f64(const StepArgs<double>& a, const double* wts, double* pa
 void enqueue_budget_f32c(const StepArgs<float>& a, const double* wts, double* part, int nblk, double scale,
                          double* out, cudaStream_t s);
 
+// ensembles (one persistent launch per stage over all members)
+struct EnsSmem { size_t bytes[4]; };
+cudaError_t ens_prepare_f64();
+cudaError_t ens_prepare_f32c();
+EnsSmem ens_smem_f64(const StepArgs<double>* host_members, int n);
+EnsSmem ens_smem_f32c(const StepArgs<float>* host_members, int n);
+void ens_begin_f64(const EnsArgs<double>& e, const int* max_steps, cudaStream_t s);
+void ens_begin_f32c(const EnsArgs<float>& e, const int* max_steps, cudaStream_t s);
+// mask: bit k launches kernel k (0 rows forward, 1 columns, 2 rows inverse, 3 RHS)
+void ens_step_f64(const EnsArgs<double>& e, const EnsSmem& sm, const int* grid, int mask, cudaStream_t s);
+void ens_step_f32c(const EnsArgs<float>& e, const EnsSmem& sm, const int* grid, int mask, cudaStream_t s);
+void ens_invert_f64(const EnsArgs<double>& e, const EnsSmem& sm, const int* grid, cudaStream_t s);
+void ens_invert_f32c(const EnsArgs<float>& e, const EnsSmem& sm, const int* grid, cudaStream_t s);
+void ens_flush_f64(const EnsArgs<double>& e, int grid, cudaStream_t s);
+void ens_flush_f32c(const EnsArgs<float>& e, int grid, cudaStream_t s);
+int cols_per_tile_f64();
+int cols_per_tile_f32c();
+int rhs_tile_x();
+int rhs_tile_y();
+
 size_t smem_bytes_rows_f64(const StepArgs<double>& a);
 size_t smem_bytes_cols_f64(const StepArgs<double>& a);
 size_t smem_bytes_rhs_f64(const StepArgs<double>& a);

@@ -38,7 +38,7 @@ struct DevState {
   int stop_reason;                 // 0 nsteps, 1 t_out, 2 tend, 3 non-finite
   int nonfinite;
   int step_index;                  // RHS evaluations so far (slab rotation)
-  int pad_;
+  int max_steps;                   // > 0: stop after this many steps in the call
 };
 
 // Everything a step kernel needs, passed by value.
@@ -93,6 +93,16 @@ template <typename T> struct StepArgs {
   int CT;                          // (unused by the kernels; kept for layout)
   int vec_cols;                    // rows are 16-byte aligned: 16-byte column loads
   int low_k64;                     // compensated: FP64 divide for mode 0, j,k < low_k64
+};
+
+// A batch of runs advanced by one launch per stage (see kernels.cu).
+template <typename T> struct EnsArgs {
+  const StepArgs<T>* members;  // device array, n entries
+  const int* start_rows;       // n+1 prefix sums of per-member work items (rows, ny)
+  const int* start_cols;       // column tiles x modes
+  const int* start_rhs;        // RHS tiles x layers
+  const int* total;            // [4]: items of K1, K2, K3, K4
+  int n;
 };
 
 }  // namespace qgw
