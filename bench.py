@@ -49,6 +49,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32c", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=0, help="0: same as --steps")
+    ap.add_argument("--ensemble-steps", type=int, default=40, help="0: skip the ensemble measurement")
+    ap.add_argument("--ensemble-members", type=int, default=64)
     return ap.parse_args()
 
 
@@ -337,6 +339,10 @@ def run_ours(args, rank, world, local_rank):
                               "step_frac": step_bytes / hbm_peak},
                  "error_vs_fp64": errs, "dtype": "f32 (q as f32 hi+lo)"}
 
+    ensemble = None
+    if args.ensemble_steps > 0:
+        ensemble = run_ensemble(args, capi, configs, torch, barrier, max_over_ranks, world)
+
     if rank != 0:
         return None
     cpu = None
@@ -356,9 +362,55 @@ def run_ours(args, rank, world, local_rank):
         "roofline": roofline, "roofline_fp64": roofline_fp64,
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": cl,
         "fp32c": fp32c,
+        "ensemble": ensemble,
         "fp64_tflops_measured": fp64_peak, "fp32_tflops_measured": fp32_peak,
     }
     return out
+
+
+def run_ensemble(args, capi, configs, torch, barrier, max_over_ranks, world):
+    """The batched form: uneven members (grids 128^2..1024^2, 2..10 layers,
+    random wind amplitude, distinct noise seeds), all FP32-compensated, one
+    launch per step stage over all members, replayed as a CUDA graph, grids
+    chosen by the autotuner."""
+    members = configs.ensemble_members(args.ensemble_members)
+    ens = capi.Ensemble([configs.public(p) for p in members], capi.FP32C)
+    q0s = [configs.noise_ic(p, p["_seed"]) for p in members]
+
+    def reset():
+        for i, (p, q0) in enumerate(zip(members, q0s)):
+            ens.set_q(i, q0)
+            ens.fix_dt(i, p["dt"])
+
+    reset()
+    tuned_ms, grids = ens.tune(3)
+    reset()
+    ens.step(3)
+    stream = torch.cuda.ExternalStream(0)
+    lgp = sum(configs.lgp(p) for p in members)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    infos = ens.step(args.ensemble_steps, graph=True)
+    wall = max_over_ranks(time.perf_counter() - t0)
+    assert all(i.steps_taken == args.ensemble_steps for i in infos)
+    # a member alone, for the alone-vs-in-the-mix check (bitwise)
+    k = max(range(len(members)), key=lambda i: configs.lgp(members[i]))
+    psi_mix, q_mix = ens.get(k)
+    ens.close()
+    run = capi.Run(configs.public(members[k]), capi.FP32C)
+    run.set_q(q0s[k])
+    run.fix_dt(members[k]["dt"])
+    run.step(3 + args.ensemble_steps)
+    psi_a, q_a = run.get()
+    run.close()
+    same = bool((psi_a == psi_mix).all() and (q_a == q_mix).all())
+    del stream
+    return {"value": world * lgp * args.ensemble_steps / wall, "unit": "lgp-steps/s", "members": len(members),
+            "lgp_per_step": lgp, "steps": args.ensemble_steps, "ms_per_step": wall / args.ensemble_steps * 1e3,
+            "grids_blocks_per_sm": grids, "tuned_stage_ms": tuned_ms, "graph": True, "dtype": "f32 (q hi+lo)",
+            "largest_member_alone_equals_in_mix": same,
+            "timing": "host wall clock around qgw_ensemble_step (graph replays + flush + state read-back)"}
 
 
 def run_reference(args):
