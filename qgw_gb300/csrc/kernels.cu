@@ -108,6 +108,16 @@ __device__ __forceinline__ void slabs(int si, int& s0, int& s1, int& s2) {
   s2 = (5 - m) % 3;
 }
 
+// The AB3 update q + c0 f0 + c1 f1 + c2 f2 (src/timestep.h:410), with the
+// FMAs written out so that every kernel that applies it rounds the same way.
+template <typename T>
+__device__ __forceinline__ T ab3_plain(T q, T c0, T c1, T c2, T f0, T f1, T f2) {
+  return fmaT(c2, f2, fmaT(c1, f1, fmaT(c0, f0, q)));
+}
+__device__ __forceinline__ float ab3_increment(float c0, float c1, float c2, float f0, float f1, float f2) {
+  return fmaT(c2, f2, fmaT(c1, f1, c0 * f0));
+}
+
 // Compensated add of an increment d to (hi, lo).
 __device__ __forceinline__ void comp_add(float& hi, float& lo, float d) {
   const float s = hi + d;
@@ -155,7 +165,7 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
           float hi = (float)a.q[o];
           if (upd) {
             float lo = (float)a.qlo[o];
-            const float d = (float)c0 * (float)f0[o] + (float)c1 * (float)f1[o] + (float)c2 * (float)f2[o];
+            const float d = ab3_increment((float)c0, (float)c1, (float)c2, (float)f0[o], (float)f1[o], (float)f2[o]);
             comp_add(hi, lo, d);
             a.q[o] = (T)hi;
             a.qlo[o] = (T)lo;
@@ -164,7 +174,7 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
         } else {
           v = a.q[o];
           if (upd) {
-            v = v + c0 * f0[o] + c1 * f1[o] + c2 * f2[o];
+            v = ab3_plain<T>(v, c0, c1, c2, f0[o], f1[o], f2[o]);
             a.q[o] = v;
           }
         }
@@ -766,12 +776,12 @@ __global__ void __launch_bounds__(NT) k_flush(StepArgs<T> a) {
     const size_t o = row * a.pitch + i;
     if (COMP) {
       float hi = (float)a.q[o], lo = (float)a.qlo[o];
-      const float d = (float)c0 * (float)f0[o] + (float)c1 * (float)f1[o] + (float)c2 * (float)f2[o];
+      const float d = ab3_increment((float)c0, (float)c1, (float)c2, (float)f0[o], (float)f1[o], (float)f2[o]);
       comp_add(hi, lo, d);
       a.q[o] = (T)hi;
       a.qlo[o] = (T)lo;
     } else {
-      a.q[o] = a.q[o] + (T)c0 * f0[o] + (T)c1 * f1[o] + (T)c2 * f2[o];
+      a.q[o] = ab3_plain<T>(a.q[o], (T)c0, (T)c1, (T)c2, f0[o], f1[o], f2[o]);
     }
   }
 }
@@ -795,13 +805,14 @@ __global__ void __launch_bounds__(NT) k_flush_ens(EnsArgs<T> e) {
           const size_t o = (size_t)l * sa.lstride + (size_t)j * sa.pitch + i;
           if (COMP) {
             float hi = (float)sa.q[o], lo = (float)sa.qlo[o];
-            const float d = (float)c0 * (float)sa.fab[s0 * fs + o] + (float)c1 * (float)sa.fab[s1 * fs + o] +
-                            (float)c2 * (float)sa.fab[s2 * fs + o];
+            const float d = ab3_increment((float)c0, (float)c1, (float)c2, (float)sa.fab[s0 * fs + o],
+                                          (float)sa.fab[s1 * fs + o], (float)sa.fab[s2 * fs + o]);
             comp_add(hi, lo, d);
             sa.q[o] = (T)hi;
             sa.qlo[o] = (T)lo;
           } else {
-            sa.q[o] = sa.q[o] + (T)c0 * sa.fab[s0 * fs + o] + (T)c1 * sa.fab[s1 * fs + o] + (T)c2 * sa.fab[s2 * fs + o];
+            sa.q[o] = ab3_plain<T>(sa.q[o], (T)c0, (T)c1, (T)c2, sa.fab[s0 * fs + o], sa.fab[s1 * fs + o],
+                                   sa.fab[s2 * fs + o]);
           }
         }
     }
