@@ -18,7 +18,12 @@ LIB = os.path.join(OUT, "libqgw_gpu.so")
 DRIVER = os.path.join(OUT, "qg_gpu")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"] + ARCH
+# -fmad=false: no implicit multiply-add contraction.  Every FMA of the hot
+# loops is explicit (fmaT), so an expression rounds the same way in every
+# kernel it is inlined into (a run gives bitwise the same result alone and in
+# an ensemble), and the scalar dt/AB3 formulas round like the reference's.
+NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-O2",
+           "--expt-relaxed-constexpr"] + ARCH
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall"]
 
 CU_SOURCES = ["kernels.cu", "api.cu", "ensemble.cu", "probe.cu", "noalloc.cu"]
