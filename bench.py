@@ -51,6 +51,10 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=0, help="0: same as --steps")
     ap.add_argument("--ensemble-steps", type=int, default=40, help="0: skip the ensemble measurement")
     ap.add_argument("--ensemble-members", type=int, default=64)
+    ap.add_argument("--serve-requests", type=int, default=64, help="0: skip the serving measurement")
+    ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrivals per second")
+    ap.add_argument("--serve-step-scale", type=int, default=50,
+                    help="request step counts are U[500, 5000] divided by this factor")
     return ap.parse_args()
 
 
@@ -343,6 +347,10 @@ def run_ours(args, rank, world, local_rank):
     if args.ensemble_steps > 0:
         ensemble = run_ensemble(args, capi, configs, torch, barrier, max_over_ranks, world)
 
+    serving = None
+    if args.serve_requests > 0:
+        serving = run_serving(args, capi, configs)
+
     if rank != 0:
         return None
     cpu = None
@@ -363,6 +371,7 @@ def run_ours(args, rank, world, local_rank):
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": cl,
         "fp32c": fp32c,
         "ensemble": ensemble,
+        "serving": serving,
         "fp64_tflops_measured": fp64_peak, "fp32_tflops_measured": fp32_peak,
     }
     return out
@@ -411,6 +420,59 @@ def run_ensemble(args, capi, configs, torch, barrier, max_over_ranks, world):
             "grids_blocks_per_sm": grids, "tuned_stage_ms": tuned_ms, "graph": True, "dtype": "f32 (q hi+lo)",
             "largest_member_alone_equals_in_mix": same,
             "timing": "host wall clock around qgw_ensemble_step (graph replays + flush + state read-back)"}
+
+
+def run_serving(args, capi, configs):
+    """The serving form: Poisson arrivals of runs with grids from 256^2 to
+    2048^2, 2..20 layers, FP64 or FP32-compensated at 50/50, random wind
+    amplitude and noise seed; admission by HBM footprint, continuous
+    batching, latency from submission to result."""
+    import numpy as np
+    import threading
+    rng = np.random.Generator(np.random.PCG64(5000))
+    reqs = []
+    t = 0.0
+    for k in range(args.serve_requests):
+        t += rng.exponential(1.0 / args.serve_rate)
+        NX = int(rng.choice([256, 512, 1024, 2048]))
+        nl = int(rng.integers(2, 21))
+        tau = float(rng.uniform(0.04, 0.12))
+        prec = int(rng.integers(0, 2))
+        steps = int(rng.integers(500, 5001)) // max(1, args.serve_step_scale)
+        p = configs.basin_params(NX, nl, tau_nm2=tau, dt=600.0, n_hyper=4, nu_hyper=1e9)
+        reqs.append((t, p, prec, max(1, steps), 6000 + k))
+    pool = capi.Pool(budget_bytes=0, steps_per_tick=16)
+    ids = [None] * len(reqs)
+    t0 = time.perf_counter()
+
+    def submitter():
+        for k, (ta, p, prec, steps, seed) in enumerate(reqs):
+            q0 = configs.noise_ic(p, seed)
+            dt = ta - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            ids[k] = pool.submit(p, q0, prec, steps)
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    th.join()
+    lat, work = [], 0.0
+    for k, rid in enumerate(ids):
+        st = pool.poll(rid, wait_ms=600000)
+        assert st == 0, st
+        _, _, _, l3 = pool.fetch(rid)
+        lat.append(l3[2])
+        work += configs.lgp(reqs[k][1]) * reqs[k][3]
+    makespan = time.perf_counter() - t0
+    stats = pool.stats()
+    pool.close()
+    lat = np.array(lat)
+    return {"requests": len(reqs), "arrival_rate_per_s": args.serve_rate,
+            "steps": f"U[500, 5000] / {args.serve_step_scale}", "grids": "{256,512,1024,2048}^2",
+            "layers": "U{2..20}", "precision": "FP64 / FP32c 50/50",
+            "throughput": work / makespan, "unit": "lgp-steps/s", "makespan_s": makespan,
+            "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+            "max_resident": stats["max_resident"], "ticks": stats["ticks"]}
 
 
 def run_reference(args):

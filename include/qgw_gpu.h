@@ -247,6 +247,31 @@ int qgw_ensemble_step(qgw_ensemble* ens, int nsteps, const int* max_steps, int u
 int qgw_ensemble_tune(qgw_ensemble* ens, int trial_steps, float* best_ms);
 int qgw_ensemble_grids(qgw_ensemble* ens, int* blocks_per_sm);
 
+/* ---- serving: continuous batching on one GPU -----------------------------
+ * Any thread submits requests (params, initial q in the reference layout,
+ * precision, step count); a worker thread admits them in arrival order
+ * while their device footprint fits the HBM budget (0: 80% of free memory),
+ * keeps admitted runs resident, advances all resident runs by up to
+ * steps_per_tick steps per tick (FP64 and FP32c batches on two streams), and
+ * retires finished runs, freeing their memory for the next admission.  A
+ * request whose footprint exceeds the budget finishes with
+ * QGW_ERR_ADMISSION.  Results are bitwise those of the same run alone.
+ * No reference counterpart: the reference runs one configuration per
+ * process. */
+typedef struct qgw_pool qgw_pool;
+int qgw_pool_create(size_t hbm_budget_bytes, int steps_per_tick, qgw_pool** out);
+int qgw_pool_submit(qgw_pool* pool, const qgw_params* p, const double* q0, int precision, int nsteps,
+                    long long* id);
+/* QGW_OK when request id has finished (its own status in *status), else
+ * QGW_ERR_NOT_READY; blocks up to wait_ms. */
+int qgw_pool_poll(qgw_pool* pool, long long id, int wait_ms, int* status);
+/* Copy out and forget a finished request; latency[3] = seconds queued,
+ * seconds resident, seconds from submit to result. */
+int qgw_pool_fetch(qgw_pool* pool, long long id, double* psi, double* q, qgw_time* tm, double* latency);
+/* stats[6]: completed, admitted, ticks, max resident, lgp-steps, bytes in use */
+int qgw_pool_stats(qgw_pool* pool, double* stats);
+void qgw_pool_destroy(qgw_pool* pool);
+
 /* ---- netCDF-3 output and restart (host code, no netCDF library) --------
  * vars.nc as create_nc/write_nc write it (src/netcdf_io.h:38-277): dims
  * t (unlimited), level, y, x; float variables t, y, x, level, psi, q, the

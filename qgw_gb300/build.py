@@ -24,10 +24,14 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # an ensemble), and the scalar dt/AB3 formulas round like the reference's.
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-O2",
            "--expt-relaxed-constexpr"] + ARCH
-CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall"]
+CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unknown-pragmas", "-pthread"]
+
+
+def cuda_include() -> str:
+    return os.path.join(os.path.dirname(os.path.dirname(nvcc())), "include")
 
 CU_SOURCES = ["kernels.cu", "api.cu", "ensemble.cu", "probe.cu", "noalloc.cu"]
-CXX_SOURCES = ["host.cpp", "ncio.cpp"]
+CXX_SOURCES = ["host.cpp", "ncio.cpp", "serve.cpp"]
 
 
 def nvcc() -> str:
@@ -67,7 +71,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_v: bool = False) -> 
         jobs.append((s, [nv] + flags + ["-c", os.path.join(SRC, s), "-o", o], o))
     for s in cxx:
         o = os.path.join(objdir, s + ".o")
-        jobs.append((s, ["g++"] + CXXFLAGS + ["-c", os.path.join(SRC, s), "-o", o], o))
+        jobs.append((s, ["g++"] + CXXFLAGS + ["-I", cuda_include(), "-c", os.path.join(SRC, s), "-o", o], o))
 
     def run(job):
         name, cmd, _ = job

@@ -46,6 +46,8 @@ EXPORTS = [
     "qgw_ensemble_create", "qgw_ensemble_destroy", "qgw_ensemble_size", "qgw_ensemble_member",
     "qgw_ensemble_set_q", "qgw_ensemble_set_time", "qgw_ensemble_get", "qgw_ensemble_step",
     "qgw_ensemble_tune", "qgw_ensemble_grids",
+    "qgw_pool_create", "qgw_pool_submit", "qgw_pool_poll", "qgw_pool_fetch", "qgw_pool_stats",
+    "qgw_pool_destroy",
 ]
 
 
@@ -107,6 +109,14 @@ def load(path: str = LIB_PATH):
     lib.qgw_ensemble_step.argtypes = [V, I, P(I), I, P(QgwStepInfo)]
     lib.qgw_ensemble_tune.argtypes = [V, I, P(ctypes.c_float)]
     lib.qgw_ensemble_grids.argtypes = [V, P(I)]
+    LL = ctypes.c_longlong
+    lib.qgw_pool_create.argtypes = [ctypes.c_size_t, I, P(V)]
+    lib.qgw_pool_submit.argtypes = [V, pp, D, I, I, P(LL)]
+    lib.qgw_pool_poll.argtypes = [V, LL, I, P(I)]
+    lib.qgw_pool_fetch.argtypes = [V, LL, D, D, P(QgwTime), D]
+    lib.qgw_pool_stats.argtypes = [V, D]
+    lib.qgw_pool_destroy.argtypes = [V]
+    lib.qgw_pool_destroy.restype = None
     lib.qgw_nc_create.argtypes = [ctypes.c_char_p, I, I, I, ctypes.c_double]
     lib.qgw_nc_create.restype = V
     lib.qgw_nc_write.argtypes = [V, ctypes.c_double, D, D]
@@ -225,6 +235,61 @@ class Ensemble:
         g = (ctypes.c_int * 4)()
         _check(self.lib.qgw_ensemble_grids(self.h, g), "qgw_ensemble_grids")
         return list(ms), list(g)
+
+
+class Pool:
+    """Continuous-batching serving pool (worker thread in the library)."""
+
+    def __init__(self, budget_bytes: int = 0, steps_per_tick: int = 32):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        _check(self.lib.qgw_pool_create(int(budget_bytes), int(steps_per_tick), ctypes.byref(h)), "qgw_pool_create")
+        self.h = h
+        self.shapes = {}
+
+    def submit(self, params, q0: np.ndarray, precision: int, nsteps: int) -> int:
+        s = to_struct(params)
+        q0 = np.ascontiguousarray(q0, dtype=np.float64)
+        rid = ctypes.c_longlong()
+        _check(self.lib.qgw_pool_submit(self.h, ctypes.byref(s), _dp(q0), int(precision), int(nsteps),
+                                        ctypes.byref(rid)), "qgw_pool_submit")
+        self.shapes[rid.value] = halo_shape(params)
+        return rid.value
+
+    def poll(self, rid: int, wait_ms: int = 0):
+        """None while running, else the request's status."""
+        st = ctypes.c_int()
+        rc = self.lib.qgw_pool_poll(self.h, ctypes.c_longlong(rid), int(wait_ms), ctypes.byref(st))
+        if rc == -11:
+            return None
+        _check(rc, "qgw_pool_poll")
+        return st.value
+
+    def fetch(self, rid: int):
+        shape = self.shapes.pop(rid)
+        psi, q = np.empty(shape), np.empty(shape)
+        tm = QgwTime()
+        lat = np.zeros(3)
+        _check(self.lib.qgw_pool_fetch(self.h, ctypes.c_longlong(rid), _dp(psi), _dp(q), ctypes.byref(tm),
+                                       _dp(lat)), "qgw_pool_fetch")
+        return psi, q, {"t": tm.t, "dt": tm.dt}, lat
+
+    def stats(self):
+        s = np.zeros(6)
+        _check(self.lib.qgw_pool_stats(self.h, _dp(s)), "qgw_pool_stats")
+        keys = ["completed", "admitted", "ticks", "max_resident", "lgp_steps", "bytes_in_use"]
+        return dict(zip(keys, s.tolist()))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.qgw_pool_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class NcWriter:

@@ -17,25 +17,10 @@
 #include "kernels.h"
 #include "qgw_device.cuh"
 #include "run.h"
+#include "ensemble_core.h"
 
 struct qgw_ensemble {
-  int precision = 0;
-  int nsm = 0;
-  cudaStream_t stream = nullptr;
-  std::vector<qgw_run*> members;
-  // device member table and work lists
-  void* d_members = nullptr;
-  int* d_lists = nullptr;  // start_rows | start_cols | start_rhs | total[4]
-  int* d_maxsteps = nullptr;
-  qgw::EnsArgs<double> e64{};
-  qgw::EnsArgs<float> e32{};
-  qgw::EnsSmem sm{};
-  int total[4] = {0, 0, 0, 0};
-  int bps[4] = {2, 2, 2, 2};  // persistent blocks per SM, per stage (tuned)
-  int grid[4] = {0, 0, 0, 0};
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  std::vector<qgw::DevState> h_states;
+  qgw::EnsembleCore core;  // owns its members
 };
 
 namespace {
@@ -51,19 +36,19 @@ int cuda_fail(cudaError_t e) {
     if (e_ != cudaSuccess) return cuda_fail(e_); \
   } while (0)
 
-void drop_graph(qgw_ensemble* e) {
+void drop_graph(qgw::EnsembleCore* e) {
   if (e->exec) cudaGraphExecDestroy(e->exec);
   if (e->graph) cudaGraphDestroy(e->graph);
   e->exec = nullptr;
   e->graph = nullptr;
 }
 
-void set_grids(qgw_ensemble* e) {
+void set_grids(qgw::EnsembleCore* e) {
   for (int s = 0; s < 4; ++s) e->grid[s] = std::max(1, std::min(e->total[s], e->nsm * e->bps[s]));
 }
 
 // member table, per-stage work lists and shared-memory sizes
-int build_tables(qgw_ensemble* e) {
+int build_tables(qgw::EnsembleCore* e) {
   const int n = (int)e->members.size();
   const int ct = e->precision == QGW_FP64 ? qgw::cols_per_tile_f64() : qgw::cols_per_tile_f32c();
   const int tx = qgw::rhs_tile_x(), ty = qgw::rhs_tile_y();
@@ -83,6 +68,8 @@ int build_tables(qgw_ensemble* e) {
   tot[2] = rows[n];
   tot[3] = rhs[n];
   for (int s = 0; s < 4; ++s) e->total[s] = tot[s];
+  qgw::ens_core_free_tables(e);
+  if (n == 0) return QGW_OK;
   CK(cudaMalloc(&e->d_lists, sizeof(int) * lists.size()));
   CK(cudaMemcpyAsync(e->d_lists, lists.data(), sizeof(int) * lists.size(), cudaMemcpyHostToDevice, e->stream));
   CK(cudaMalloc(&e->d_maxsteps, sizeof(int) * n));
@@ -108,12 +95,12 @@ int build_tables(qgw_ensemble* e) {
   return QGW_OK;
 }
 
-void launch_step(qgw_ensemble* e, int mask) {
+void launch_step(qgw::EnsembleCore* e, int mask) {
   if (e->precision == QGW_FP64) qgw::ens_step_f64(e->e64, e->sm, e->grid, mask, e->stream);
   else qgw::ens_step_f32c(e->e32, e->sm, e->grid, mask, e->stream);
 }
 
-int ensure_graph(qgw_ensemble* e) {
+int ensure_graph(qgw::EnsembleCore* e) {
   if (e->exec) return QGW_OK;
   CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
   launch_step(e, 15);
@@ -124,7 +111,7 @@ int ensure_graph(qgw_ensemble* e) {
   return QGW_OK;
 }
 
-int read_states(qgw_ensemble* e) {
+int read_states(qgw::EnsembleCore* e) {
   const int n = (int)e->members.size();
   e->h_states.resize(n);
   for (int i = 0; i < n; ++i)
@@ -141,11 +128,12 @@ extern "C" {
 int qgw_ensemble_create(int n, const qgw_params* params, int precision, qgw_ensemble** out) {
   if (!params || !out || n < 1) return QGW_ERR_PARAM;
   *out = nullptr;
-  qgw_ensemble* e = new qgw_ensemble();
+  qgw_ensemble* ens = new qgw_ensemble();
+  qgw::EnsembleCore* e = &ens->core;
   e->precision = precision;
   int dev = 0, rc = QGW_OK;
   auto fail = [&](int code) {
-    qgw_ensemble_destroy(e);
+    qgw_ensemble_destroy(ens);
     return code;
   };
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(QGW_ERR_CUDA);
@@ -156,44 +144,60 @@ int qgw_ensemble_create(int n, const qgw_params* params, int precision, qgw_ense
     if ((rc = qgw_create(&params[i], nullptr, nullptr, nullptr, nullptr, precision, &r))) return fail(rc);
     e->members.push_back(r);
   }
-  const cudaError_t pe = precision == QGW_FP64 ? qgw::ens_prepare_f64() : qgw::ens_prepare_f32c();
-  if (pe != cudaSuccess) return fail(cuda_fail(pe));
-  if ((rc = build_tables(e))) return fail(rc);
-  *out = e;
+  if ((rc = qgw::ens_core_build(e))) return fail(rc);
+  *out = ens;
   return QGW_OK;
 }
 
-void qgw_ensemble_destroy(qgw_ensemble* e) {
-  if (!e) return;
+void qgw_ensemble_destroy(qgw_ensemble* ens) {
+  if (!ens) return;
+  qgw::EnsembleCore* e = &ens->core;
   if (e->stream) cudaStreamSynchronize(e->stream);
-  drop_graph(e);
+  qgw::ens_core_free_tables(e);
   for (qgw_run* r : e->members) qgw_destroy(r);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete ens;
+}
+
+int qgw_ensemble_size(qgw_ensemble* ens) { return ens ? (int)ens->core.members.size() : 0; }
+
+qgw_run* qgw_ensemble_member(qgw_ensemble* ens, int i) {
+  if (!ens || i < 0 || i >= (int)ens->core.members.size()) return nullptr;
+  cudaStreamSynchronize(ens->core.stream);
+  return ens->core.members[i];
+}
+
+}  // extern "C"
+
+namespace qgw {
+
+void ens_core_free_tables(EnsembleCore* e) {
+  drop_graph(e);
   if (e->d_members) cudaFree(e->d_members);
   if (e->d_lists) cudaFree(e->d_lists);
   if (e->d_maxsteps) cudaFree(e->d_maxsteps);
-  if (e->stream) cudaStreamDestroy(e->stream);
-  delete e;
+  e->d_members = nullptr;
+  e->d_lists = nullptr;
+  e->d_maxsteps = nullptr;
 }
 
-int qgw_ensemble_size(qgw_ensemble* e) { return e ? (int)e->members.size() : 0; }
-
-qgw_run* qgw_ensemble_member(qgw_ensemble* e, int i) {
-  if (!e || i < 0 || i >= (int)e->members.size()) return nullptr;
-  cudaStreamSynchronize(e->stream);
-  return e->members[i];
+int ens_core_build(EnsembleCore* e) {
+  const cudaError_t pe = e->precision == QGW_FP64 ? ens_prepare_f64() : ens_prepare_f32c();
+  if (pe != cudaSuccess) return cuda_fail(pe);
+  return build_tables(e);
 }
 
-int qgw_ensemble_step(qgw_ensemble* e, int nsteps, const int* max_steps, int use_graph, qgw_step_info* infos) {
-  if (!e || nsteps < 0) return QGW_ERR_PARAM;
+int ens_core_step(EnsembleCore* e, int nsteps, const int* max_steps, bool use_graph) {
   const int n = (int)e->members.size();
+  if (n == 0) return QGW_OK;
   for (qgw_run* r : e->members)
     if (!r->has_q) return QGW_ERR_STATE;
   for (qgw_run* r : e->members) CK(cudaStreamSynchronize(r->stream));
   std::vector<int> ms(n, 0);
   if (max_steps) std::memcpy(ms.data(), max_steps, sizeof(int) * n);
   CK(cudaMemcpyAsync(e->d_maxsteps, ms.data(), sizeof(int) * n, cudaMemcpyHostToDevice, e->stream));
-  if (e->precision == QGW_FP64) qgw::ens_begin_f64(e->e64, e->d_maxsteps, e->stream);
-  else qgw::ens_begin_f32c(e->e32, e->d_maxsteps, e->stream);
+  if (e->precision == QGW_FP64) ens_begin_f64(e->e64, e->d_maxsteps, e->stream);
+  else ens_begin_f32c(e->e32, e->d_maxsteps, e->stream);
   int rc;
   if (use_graph && (rc = ensure_graph(e))) return rc;
   const int chunk = 256;
@@ -207,15 +211,30 @@ int qgw_ensemble_step(qgw_ensemble* e, int nsteps, const int* max_steps, int use
     if (done < nsteps) {
       if ((rc = read_states(e))) return rc;
       bool any = false;
-      for (const auto& s : e->h_states) any = any || s.active;
+      for (const auto& st : e->h_states) any = any || st.active;
       if (!any) break;
     }
   }
   const int fgrid = std::max(1, std::min(e->total[0], e->nsm * 4));
-  if (e->precision == QGW_FP64) qgw::ens_flush_f64(e->e64, fgrid, e->stream);
-  else qgw::ens_flush_f32c(e->e32, fgrid, e->stream);
+  if (e->precision == QGW_FP64) ens_flush_f64(e->e64, fgrid, e->stream);
+  else ens_flush_f32c(e->e32, fgrid, e->stream);
   CK(cudaGetLastError());
-  if ((rc = read_states(e))) return rc;
+  return QGW_OK;
+}
+
+int ens_core_finish(EnsembleCore* e) { return read_states(e); }
+
+}  // namespace qgw
+
+extern "C" {
+
+int qgw_ensemble_step(qgw_ensemble* ens, int nsteps, const int* max_steps, int use_graph, qgw_step_info* infos) {
+  if (!ens || nsteps < 0) return QGW_ERR_PARAM;
+  qgw::EnsembleCore* e = &ens->core;
+  const int n = (int)e->members.size();
+  int rc = qgw::ens_core_step(e, nsteps, max_steps, use_graph != 0);
+  if (rc) return rc;
+  if ((rc = qgw::ens_core_finish(e))) return rc;
   bool bad = false;
   for (int i = 0; i < n; ++i) {
     const qgw::DevState& s = e->h_states[i];
@@ -240,8 +259,9 @@ int qgw_ensemble_step(qgw_ensemble* e, int nsteps, const int* max_steps, int use
 // scalars and AB3 history, so call it before the time loop (it re-applies
 // qgw_set_q's reset of the history).  best_ms[4] (optional) receives the
 // per-stage times of the chosen grids.
-int qgw_ensemble_tune(qgw_ensemble* e, int trial_steps, float* best_ms) {
-  if (!e || trial_steps < 1) return QGW_ERR_PARAM;
+int qgw_ensemble_tune(qgw_ensemble* ens, int trial_steps, float* best_ms) {
+  if (!ens || trial_steps < 1) return QGW_ERR_PARAM;
+  qgw::EnsembleCore* e = &ens->core;
   for (qgw_run* r : e->members)
     if (!r->has_q) return QGW_ERR_STATE;
   const int n = (int)e->members.size();
@@ -289,25 +309,29 @@ int qgw_ensemble_tune(qgw_ensemble* e, int trial_steps, float* best_ms) {
   return QGW_OK;
 }
 
-int qgw_ensemble_set_q(qgw_ensemble* e, int i, const double* q) {
+int qgw_ensemble_set_q(qgw_ensemble* ens, int i, const double* q) {
+  qgw::EnsembleCore* e = ens ? &ens->core : nullptr;
   if (!e || i < 0 || i >= (int)e->members.size()) return QGW_ERR_PARAM;
   CK(cudaStreamSynchronize(e->stream));
   return qgw_set_q(e->members[i], q);
 }
 
-int qgw_ensemble_set_time(qgw_ensemble* e, int i, const qgw_time* tm) {
+int qgw_ensemble_set_time(qgw_ensemble* ens, int i, const qgw_time* tm) {
+  qgw::EnsembleCore* e = ens ? &ens->core : nullptr;
   if (!e || i < 0 || i >= (int)e->members.size()) return QGW_ERR_PARAM;
   CK(cudaStreamSynchronize(e->stream));
   return qgw_set_time(e->members[i], tm);
 }
 
-int qgw_ensemble_get(qgw_ensemble* e, int i, double* psi, double* q) {
+int qgw_ensemble_get(qgw_ensemble* ens, int i, double* psi, double* q) {
+  qgw::EnsembleCore* e = ens ? &ens->core : nullptr;
   if (!e || i < 0 || i >= (int)e->members.size()) return QGW_ERR_PARAM;
   CK(cudaStreamSynchronize(e->stream));
   return qgw_get(e->members[i], psi, q);
 }
 
-int qgw_ensemble_grids(qgw_ensemble* e, int* bps4) {
+int qgw_ensemble_grids(qgw_ensemble* ens, int* bps4) {
+  qgw::EnsembleCore* e = ens ? &ens->core : nullptr;
   if (!e || !bps4) return QGW_ERR_PARAM;
   for (int s = 0; s < 4; ++s) bps4[s] = e->bps[s];
   return QGW_OK;

@@ -1,0 +1,76 @@
+"""Serving pool: continuous batching with HBM-footprint admission.  Each
+result must be bitwise the result of the same run alone, whatever else was
+resident while it ran."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from qgw_gb300 import configs as C
+
+pytestmark = pytest.mark.gpu
+
+
+def alone(capi, p, prec, q0, n):
+    r = capi.Run(p, prec)
+    r.set_q(q0)
+    r.fix_dt(p["dt"])
+    r.step(n)
+    out = r.get()
+    r.close()
+    return out
+
+
+def test_pool_results_equal_alone(qgwlib):
+    reqs = [(C.cfg1(64), 0, 23), (C.cfg2(128, 5), 1, 40), (dict(C.cfg1(64), NY=32), 1, 7),
+            (C.cfg2(64, 10), 0, 31), (C.basin_params(32, 2, dt=900.0), 1, 50), (C.cfg1(128), 0, 12)]
+    pool = qgwlib.Pool(budget_bytes=0, steps_per_tick=8)
+    ids = []
+    for k, (p, prec, n) in enumerate(reqs):
+        ids.append(pool.submit(p, C.noise_ic(p, 900 + k), prec, n))
+        time.sleep(0.01 * k)  # arrivals while others run
+    for rid in ids:
+        assert pool.poll(rid, wait_ms=60000) == 0
+    st = pool.stats()
+    assert st["completed"] == len(reqs) and st["max_resident"] >= 2
+    for k, ((p, prec, n), rid) in enumerate(zip(reqs, ids)):
+        psi, q, tm, lat = pool.fetch(rid)
+        psi_a, q_a = alone(qgwlib, p, prec, C.noise_ic(p, 900 + k), n)
+        assert np.array_equal(q, q_a) and np.array_equal(psi, psi_a), k
+        assert tm["t"] == pytest.approx(n * p["dt"])
+        assert lat[2] >= lat[1] >= 0
+    pool.close()
+
+
+def test_pool_admission_by_footprint(qgwlib):
+    small = C.cfg1(64)
+    fp = qgwlib.footprint(small, 0)
+    pool = qgwlib.Pool(budget_bytes=int(fp * 1.5), steps_per_tick=4)  # one resident at a time
+    ids = [pool.submit(small, C.noise_ic(small, k), 0, 10) for k in range(3)]
+    big = C.cfg2(256, 10)
+    too_big = pool.submit(big, C.noise_ic(big, 1), 0, 5)
+    for rid in ids:
+        assert pool.poll(rid, wait_ms=60000) == 0
+    assert pool.poll(too_big, wait_ms=60000) == -9  # QGW_ERR_ADMISSION
+    assert pool.stats()["max_resident"] == 1
+    pool.close()
+
+
+def test_pool_concurrent_submitters(qgwlib):
+    pool = qgwlib.Pool(steps_per_tick=16)
+    out = {}
+
+    def client(k):
+        p = C.basin_params(64, 3, dt=1200.0)
+        rid = pool.submit(p, C.noise_ic(p, 100 + k), k % 2, 20 + k)
+        assert pool.poll(rid, wait_ms=60000) == 0
+        out[k] = pool.fetch(rid)
+
+    th = [threading.Thread(target=client, args=(k,)) for k in range(8)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert len(out) == 8
+    pool.close()
