@@ -60,15 +60,18 @@ int upload(qgw_run* r, T** out, const std::vector<double>& host) {
 
 // choose the modes per row block and the columns per column block so that
 // each block's two work buffers stay within the shared-memory budget
-// QGW_ROW_SMEM_KB (optional) overrides the 96 KiB budget: a tuning knob
-size_t row_budget() {
+// Shared-memory budget of the row kernels' work buffers.  Measured at
+// 1024^2 x 10 on GB300: 64 KiB (3 blocks/SM) is fastest for FP64 and 40 KiB
+// (4-5 blocks/SM) for FP32; QGW_ROW_SMEM_KB overrides it (tuning knob).
+size_t row_budget(size_t elem) {
   const char* e = std::getenv("QGW_ROW_SMEM_KB");
   const long v = e ? std::atol(e) : 0;
-  return (v >= 16 && v <= 220) ? (size_t)v * 1024 : (size_t)96 * 1024;
+  if (v >= 16 && v <= 220) return (size_t)v * 1024;
+  return elem == 8 ? (size_t)64 * 1024 : (size_t)40 * 1024;
 }
 
 void choose_groups(int nl, int Mx, int My, size_t elem, int* G1, int* CT) {
-  const size_t budget = row_budget();
+  const size_t budget = row_budget(elem);
   int g = (int)(budget / (2 * (size_t)qgw::padded_len(Mx) * elem));
   if (g < 1) g = 1;
   if (g > 16) g = 16;
@@ -196,7 +199,7 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
     a.zeta_mode = 1;
     if ((rc = dalloc(r, &a.spec2, field))) return rc;
     if ((rc = dalloc(r, &a.zeta, field))) return rc;
-    const size_t budget = row_budget();
+    const size_t budget = row_budget(sizeof(T));
     int g3 = (int)(budget / (4 * (size_t)qgw::padded_len(r->nx + 1) * sizeof(T)));
     g3 = g3 < 1 ? 1 : (g3 > 8 ? 8 : g3);
     const int ng = (r->nl + g3 - 1) / g3;
