@@ -203,12 +203,13 @@ def read_measured_peaks():
 
 
 def read_traffic(precision):
-    """Per-launch DRAM traffic of the dominant kernel from the committed ncu
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu
     summary (profiles/traffic.json), if present."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
-            return json.load(f).get("fp64" if precision == 0 else "fp32c")
+            d = json.load(f).get("fp64" if precision == 0 else "fp32c")
+        return d.get("bytes") if d else None
     except (OSError, ValueError):
         return None
 
