@@ -61,14 +61,13 @@ int upload(qgw_run* r, T** out, const std::vector<double>& host) {
 // choose the modes per row block and the columns per column block so that
 // each block's two work buffers stay within the shared-memory budget
 // Shared-memory budget of the row kernels' work buffers.  Measured at
-// 1024^2 x 10 on GB300: 64 KiB (3 blocks/SM) is fastest for FP64; the FP32
-// warp-form kernels hold mode rows plus 8 work rows (74 KiB: 8 mode rows);
-// QGW_ROW_SMEM_KB overrides it (tuning knob).
+// 1024^2 x 10 on GB300: 64 KiB (3 blocks/SM) is fastest for FP64 and 40 KiB
+// (4-5 blocks/SM) for FP32; QGW_ROW_SMEM_KB overrides it (tuning knob).
 size_t row_budget(size_t elem) {
   const char* e = std::getenv("QGW_ROW_SMEM_KB");
   const long v = e ? std::atol(e) : 0;
   if (v >= 16 && v <= 220) return (size_t)v * 1024;
-  return elem == 8 ? (size_t)64 * 1024 : (size_t)74 * 1024;
+  return elem == 8 ? (size_t)64 * 1024 : (size_t)40 * 1024;
 }
 
 void choose_groups(int nl, int Mx, int My, size_t elem, int* G1, int* CT) {
@@ -182,14 +181,6 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   a.has_topo = 0;
   a.has_wind = p.tau0 != 0;
   choose_groups(r->nl, r->nx + 1, r->ny + 1, sizeof(T), &a.G1, &a.CT);
-  if (sizeof(T) == 4) {
-    // warp-form row kernels: G mode rows plus one work row per warp (8)
-    const int rows = (int)(row_budget(sizeof(T)) / ((size_t)qgw::padded_len(r->nx + 1) * sizeof(T)));
-    int g = rows - 8;
-    g = g < 1 ? 1 : (g > 16 ? 16 : g);
-    const int ng = (r->nl + g - 1) / g;
-    a.G1 = (r->nl + ng - 1) / ng;
-  }
   a.low_k64 = 8;
   // 16-byte column vectors: rows 16-byte aligned and a whole number of
   // 32-byte column tiles per row, so a tile never crosses into the next row
@@ -209,7 +200,7 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
     if ((rc = dalloc(r, &a.spec2, field))) return rc;
     if ((rc = dalloc(r, &a.zeta, field))) return rc;
     const size_t budget = row_budget(sizeof(T));
-    int g3 = ((int)(budget / ((size_t)qgw::padded_len(r->nx + 1) * sizeof(T))) - 8) / 2;
+    int g3 = (int)(budget / (4 * (size_t)qgw::padded_len(r->nx + 1) * sizeof(T)));
     g3 = g3 < 1 ? 1 : (g3 > 8 ? 8 : g3);
     const int ng = (r->nl + g3 - 1) / g3;
     a.G3 = (r->nl + ng - 1) / ng;

@@ -358,230 +358,6 @@ __device__ __forceinline__ void body_rows_inv(const StepArgs<T>& a, int step_mod
   }
 }
 
-
-// ------------------------------------------------------ warp-level DST
-// One row per warp: the same work items as dst_block, separated by
-// __syncwarp only, so the warps of a block never wait for each other.  The
-// result is always returned in A (copied back from B when the pass count
-// leaves it there).
-constexpr int NW = NT / 32;  // warps per block
-
-template <typename T>
-__device__ void warp_dst(T* A, T* B, const DstGeom& g, const DstTables<T>& tb) {
-  const int lane = threadIdx.x & 31;
-  const int H = g.H;
-  for (int j = lane + 1; j <= H; j += 32) dst_pre_item<T>(A, B, j, g, tb.pre);
-  __syncwarp();
-  T* src = B;
-  T* dst = A;
-  int Ns = 1;
-  for (int p = 0; p < g.npass; ++p) {
-    const int R = g.radix[p], nb = H / R;
-    for (int b = lane; b < nb; b += 32) stockham_dispatch<T>(R, (const C2<T>*)src, (C2<T>*)dst, b, Ns, H, tb.tw);
-    __syncwarp();
-    Ns *= R;
-    T* t = src; src = dst; dst = t;
-  }
-  for (int k = lane; k < (H >> 1); k += 32) {
-    dst_split_item<T>((const C2<T>*)src, dst, k, g, tb.spl);
-    if (k == 0) dst_split_item<T>((const C2<T>*)src, dst, H >> 1, g, tb.spl);
-  }
-  __syncwarp();
-  T tot = T(0);
-  if (lane < g.nchunk) tot = dst_scan_chunk<T>(dst, lane, g);
-  T incl = tot;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const T u = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += u;
-  }
-  T ex = __shfl_up_sync(0xffffffffu, incl, 1);
-  if (lane > 0 && lane < g.nchunk) dst_scan_fix<T>(dst, lane, ex, g);
-  __syncwarp();
-  if (dst != A) {
-    const int n = padded_len(g.M);
-    for (int i = lane; i < n; i += 32) A[i] = dst[i];
-    __syncwarp();
-  }
-}
-
-// K1, warp form (FP32): one block per row, the projection by the whole
-// block, then one mode row per warp.
-template <typename T, bool COMP>
-__device__ __forceinline__ void body_rows_fwd_w(const StepArgs<T>& a, int step_mode, int j, unsigned char* smem_raw) {
-  DevState* st = a.state;
-  if (step_mode && !st->active) return;
-  const int ld = padded_len(a.gx.M);
-  T* A = (T*)smem_raw;
-  T* Wk = A + (size_t)a.G1 * ld;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const bool ab3 = step_mode && st->pending;
-  int s0 = 0, s1 = 0, s2 = 0;
-  slabs(st->step_index, s0, s1, s2);
-  const T c0 = (T)st->c0, c1 = (T)st->c1, c2 = (T)st->c2;
-  const size_t fs = (size_t)a.nl * a.lstride;
-  const T* f0 = a.fab + s0 * fs;
-  const T* f1 = a.fab + s1 * fs;
-  const T* f2 = a.fab + s2 * fs;
-  const T* cl = a.cl2m;
-  for (int m0 = 0; m0 < a.nl; m0 += a.G1) {
-    const int G = min(a.G1, a.nl - m0);
-    const bool upd = ab3 && m0 == 0;
-    for (int i = threadIdx.x; i < a.nx; i += NT) {
-      const int pi = pr(i);
-      for (int gg = 0; gg < G; ++gg) A[gg * ld + pi] = T(0);
-      for (int l = 0; l < a.nl; ++l) {
-        const size_t o = (size_t)l * a.lstride + (size_t)j * a.pitch + i;
-        float hi = (float)a.q[o];
-        if (COMP && upd) {
-          float lo = (float)a.qlo[o];
-          const float d = ab3_increment((float)c0, (float)c1, (float)c2, (float)f0[o], (float)f1[o], (float)f2[o]);
-          comp_add(hi, lo, d);
-          a.q[o] = (T)hi;
-          a.qlo[o] = (T)lo;
-        }
-        const T v = (T)hi;
-        const T* crow = cl + (size_t)m0 * a.nl + l;
-        for (int gg = 0; gg < G; ++gg) A[gg * ld + pi] = fmaT(__ldg(crow + gg * a.nl), v, A[gg * ld + pi]);
-      }
-    }
-    __syncthreads();
-    for (int r = warp; r < G; r += NW) {
-      warp_dst<T>(A + r * ld, Wk + warp * ld, a.gx, a.tx);
-      T* dstrow = a.spec + (size_t)(m0 + r) * a.lstride + (size_t)j * a.pitch;
-      for (int i = lane; i < a.nx; i += 32) dstrow[i] = A[r * ld + pr(i)];
-      __syncwarp();
-    }
-    __syncthreads();
-  }
-}
-
-// K3, warp form (FP32): mode rows (and spectral zeta rows) inverse-
-// transformed one per warp, then back-projected by the whole block.
-template <typename T, bool COMP>
-__device__ __forceinline__ void body_rows_inv_w(const StepArgs<T>& a, int step_mode, int j, unsigned char* smem_raw) {
-  DevState* st = a.state;
-  if (step_mode && !st->active) return;
-  const int ld = padded_len(a.gx.M);
-  const bool zm = COMP && a.zeta_mode;
-  const int Gb = zm ? a.G3 : a.G1;
-  T* A = (T*)smem_raw;
-  T* Wk = A + (size_t)(zm ? 2 * Gb : Gb) * ld;
-  const int warp = threadIdx.x >> 5;
-  const T* cm = a.cm2l;
-  for (int m0 = 0; m0 < a.nl; m0 += Gb) {
-    const int G = min(Gb, a.nl - m0);
-    for (int gg = 0; gg < G; ++gg) {
-      const T* srow = a.spec + (size_t)(m0 + gg) * a.lstride + (size_t)j * a.pitch;
-      for (int i = threadIdx.x; i < a.nx; i += NT) A[gg * ld + pr(i)] = srow[i];
-      if (zm) {
-        const T* zrow = a.spec2 + (size_t)(m0 + gg) * a.lstride + (size_t)j * a.pitch;
-        for (int i = threadIdx.x; i < a.nx; i += NT) A[(G + gg) * ld + pr(i)] = zrow[i];
-      }
-    }
-    __syncthreads();
-    const int nrows = zm ? 2 * G : G;
-    for (int r = warp; r < nrows; r += NW) warp_dst<T>(A + r * ld, Wk + warp * ld, a.gx, a.tx);
-    __syncthreads();
-    for (int i = threadIdx.x; i < a.nx; i += NT) {
-      const int pi = pr(i);
-      for (int l = 0; l < a.nl; ++l) {
-        const size_t o = (size_t)l * a.lstride + (size_t)j * a.pitch + i;
-        const T* crow = cm + (size_t)l * a.nl + m0;
-        T acc = (m0 == 0) ? T(0) : a.psi[o];
-        for (int gg = 0; gg < G; ++gg) acc = fmaT(__ldg(crow + gg), A[gg * ld + pi], acc);
-        a.psi[o] = acc;
-        if (zm) {
-          T zc = (m0 == 0) ? T(0) : a.zeta[o];
-          for (int gg = 0; gg < G; ++gg) zc = fmaT(__ldg(crow + gg), A[(G + gg) * ld + pi], zc);
-          a.zeta[o] = zc;
-        }
-      }
-    }
-    __syncthreads();
-  }
-}
-
-// K2, warp form (FP32): CT columns per block, one column per warp, the
-// transposed loads and stores done by the whole block.
-template <typename T, bool COMP>
-__device__ __forceinline__ void body_cols_w(const StepArgs<T>& a, int step_mode, int bx, int m, unsigned char* smem_raw) {
-  constexpr int CT = ColsPer<T>::value;
-  DevState* st = a.state;
-  if (step_mode && !st->active) return;
-  const int k0 = bx * CT;
-  const int CTb = min(CT, a.nx - k0);
-  const int ld = padded_len(a.gy.M);
-  const bool zm = COMP && a.zeta_mode;
-  const int nbuf = zm ? 3 : 2;
-  T* base = (T*)smem_raw;  // column c: rows base + c*nbuf*ld (A), +ld (B), +2ld (C)
-  T* S = a.spec + (size_t)m * a.lstride;
-  const int ny = a.ny;
-  const bool vec = a.vec_cols != 0;
-  T v[CT];
-  for (int jj = threadIdx.x; jj < ny; jj += NT) {
-    const T* src = S + (size_t)jj * a.pitch + k0;
-    if (vec) load_cols<T, CT>(src, v);
-    else
-      for (int c = 0; c < CT; ++c) v[c] = c < CTb ? src[c] : T(0);
-    const int pj = pr(jj);
-#pragma unroll
-    for (int c = 0; c < CT; ++c) base[(size_t)c * nbuf * ld + pj] = v[c];
-  }
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (warp < CT) {
-    const int c = warp;
-    T* Ac = base + (size_t)c * nbuf * ld;
-    T* Bc = Ac + ld;
-    T* Cc = Bc + ld;
-    warp_dst<T>(Ac, Bc, a.gy, a.ty);
-    const int k = min(k0 + c, a.nx - 1);
-    const double iRd2 = a.iRd2[m];
-    const float ird2f = (float)iRd2, normf = (float)a.norm, lx2f = (float)a.lx2, ly2f = (float)a.ly2;
-    const float lsq = a.Lsqf[k], sx = zm ? a.sx2f[k] : 0.f;
-    for (int jj = lane; jj < ny; jj += 32) {
-      const int pj = pr(jj);
-      float x;
-      if (m == 0 && jj < a.low_k64 && k < a.low_k64) {
-        // barotropic mode, lowest wavenumbers: divide in FP64
-        const double fact = -(a.Lsq[k] + a.Ksq[jj] + iRd2);
-        x = (float)((double)Ac[pj] / fact / a.norm);
-      } else {
-        const float fact = -((lsq + a.Ksqf[jj]) + ird2f);
-        x = (float)Ac[pj] / (fact * normf);
-      }
-      Ac[pj] = (T)x;
-      if (zm) Cc[pj] = (T)(fmaT(lx2f, sx, ly2f * a.sy2f[jj]) * x);
-    }
-    __syncwarp();
-    warp_dst<T>(Ac, Bc, a.gy, a.ty);
-    if (zm) warp_dst<T>(Cc, Bc, a.gy, a.ty);
-  }
-  __syncthreads();
-  for (int jj = threadIdx.x; jj < ny; jj += NT) {
-    const int pj = pr(jj);
-#pragma unroll
-    for (int c = 0; c < CT; ++c) v[c] = c < CTb ? base[(size_t)c * nbuf * ld + pj] : T(0);
-    T* dst = S + (size_t)jj * a.pitch + k0;
-    if (vec) store_cols<T, CT>(dst, v);
-    else
-      for (int c = 0; c < CTb; ++c) dst[c] = v[c];
-  }
-  if (zm) {
-    T* S2 = a.spec2 + (size_t)m * a.lstride;
-    for (int jj = threadIdx.x; jj < ny; jj += NT) {
-      const int pj = pr(jj);
-#pragma unroll
-      for (int c = 0; c < CT; ++c) v[c] = c < CTb ? base[(size_t)c * nbuf * ld + 2 * ld + pj] : T(0);
-      T* dst = S2 + (size_t)jj * a.pitch + k0;
-      if (vec) store_cols<T, CT>(dst, v);
-      else
-        for (int c = 0; c < CTb; ++c) dst[c] = v[c];
-    }
-  }
-}
-
 // ------------------------------------------------------------------ K4
 __device__ __forceinline__ unsigned long long absbits(double v) {
   return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL;
@@ -855,22 +631,19 @@ template <typename T, bool COMP>
 __global__ void __launch_bounds__(NT) k_rows_fwd(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
-  if constexpr (COMP) body_rows_fwd_w<T, COMP>(a, step_mode, blockIdx.x, smem_raw);
-  else body_rows_fwd<T, COMP>(a, step_mode, blockIdx.x, smem_raw, tot);
+  body_rows_fwd<T, COMP>(a, step_mode, blockIdx.x, smem_raw, tot);
 }
 template <typename T, bool COMP>
 __global__ void __launch_bounds__(NT) k_cols(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
-  if constexpr (COMP) body_cols_w<T, COMP>(a, step_mode, blockIdx.x, blockIdx.y, smem_raw);
-  else body_cols<T, COMP>(a, step_mode, blockIdx.x, blockIdx.y, smem_raw, tot);
+  body_cols<T, COMP>(a, step_mode, blockIdx.x, blockIdx.y, smem_raw, tot);
 }
 template <typename T, bool COMP>
 __global__ void __launch_bounds__(NT) k_rows_inv(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
-  if constexpr (COMP) body_rows_inv_w<T, COMP>(a, step_mode, blockIdx.x, smem_raw);
-  else body_rows_inv<T, COMP>(a, step_mode, blockIdx.x, smem_raw, tot);
+  body_rows_inv<T, COMP>(a, step_mode, blockIdx.x, smem_raw, tot);
 }
 template <typename T, bool COMP, int R>
 __global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
@@ -914,8 +687,7 @@ __global__ void __launch_bounds__(NT) k_rows_fwd_ens(EnsArgs<T> e, int step_mode
   __shared__ StepArgs<T> sa;
   for (int item = blockIdx.x; item < e.total[0]; item += gridDim.x) {
     const int local = ens_item(e, e.start_rows, item, &sa);
-    if constexpr (COMP) body_rows_fwd_w<T, COMP>(sa, step_mode, local, smem_raw);
-    else body_rows_fwd<T, COMP>(sa, step_mode, local, smem_raw, tot);
+    body_rows_fwd<T, COMP>(sa, step_mode, local, smem_raw, tot);
     __syncthreads();
   }
 }
@@ -928,8 +700,7 @@ __global__ void __launch_bounds__(NT) k_cols_ens(EnsArgs<T> e, int step_mode) {
   for (int item = blockIdx.x; item < e.total[1]; item += gridDim.x) {
     const int local = ens_item(e, e.start_cols, item, &sa);
     const int ntx = (sa.nx + CT - 1) / CT;
-    if constexpr (COMP) body_cols_w<T, COMP>(sa, step_mode, local % ntx, local / ntx, smem_raw);
-    else body_cols<T, COMP>(sa, step_mode, local % ntx, local / ntx, smem_raw, tot);
+    body_cols<T, COMP>(sa, step_mode, local % ntx, local / ntx, smem_raw, tot);
     __syncthreads();
   }
 }
@@ -940,8 +711,7 @@ __global__ void __launch_bounds__(NT) k_rows_inv_ens(EnsArgs<T> e, int step_mode
   __shared__ StepArgs<T> sa;
   for (int item = blockIdx.x; item < e.total[2]; item += gridDim.x) {
     const int local = ens_item(e, e.start_rows, item, &sa);
-    if constexpr (COMP) body_rows_inv_w<T, COMP>(sa, step_mode, local, smem_raw);
-    else body_rows_inv<T, COMP>(sa, step_mode, local, smem_raw, tot);
+    body_rows_inv<T, COMP>(sa, step_mode, local, smem_raw, tot);
     __syncthreads();
   }
 }
@@ -1108,18 +878,14 @@ __global__ void k_budget_final(const double* part, int nblk, double scale, doubl
 
 // ------------------------------------------------------------- launchers
 template <typename T, bool COMP>
-static size_t smem_rows(const StepArgs<T>& a) {
-  if (COMP) return (size_t)(a.G1 + NW) * padded_len(a.gx.M) * sizeof(T);  // warp form
-  return (size_t)2 * a.G1 * padded_len(a.gx.M) * sizeof(T);
-}
+static size_t smem_rows(const StepArgs<T>& a) { return (size_t)2 * a.G1 * padded_len(a.gx.M) * sizeof(T); }
 template <typename T, bool COMP>
 static size_t smem_cols(const StepArgs<T>& a) {
   return (size_t)((COMP && a.zeta_mode) ? 3 : 2) * ColsPer<T>::value * padded_len(a.gy.M) * sizeof(T);
 }
 template <typename T, bool COMP>
 static size_t smem_rows_inv(const StepArgs<T>& a) {
-  if (COMP) return (size_t)((a.zeta_mode ? 2 * a.G3 : a.G1) + NW) * padded_len(a.gx.M) * sizeof(T);
-  return smem_rows<T, COMP>(a);
+  return (COMP && a.zeta_mode) ? (size_t)4 * a.G3 * padded_len(a.gx.M) * sizeof(T) : smem_rows<T, COMP>(a);
 }
 template <typename T>
 static size_t smem_rhs_r(int r) {
