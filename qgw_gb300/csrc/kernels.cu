@@ -30,6 +30,7 @@ namespace qgw {
 
 constexpr int NT = 256;          // threads per block in every step kernel
 constexpr int GMAX = 16;         // max rows of one batched DST in a block
+constexpr int NLMAX = 32;        // max layers on the GPU path
 constexpr int TX = 32, TY = 16;  // RHS tile (interior points)
 constexpr double TEPS = 1e-9;    // src/timestep.h:288
 constexpr double HUGEV = 1e30;   // src/qg.c:43
@@ -129,15 +130,83 @@ __device__ __forceinline__ void comp_add(float& hi, float& lo, float d) {
   hi = h2;
 }
 
+// ------------------------------------------------------- mode projections
+// The nl x G coefficients of one mode group are staged in shared memory as
+// cst[l * GMAX + gg] (zero for gg >= G), so one vector load serves a row of
+// the group and the group loops have a compile-time width GB >= G.  A padded
+// slot multiplies a zero value by a zero coefficient, which leaves every
+// accumulator unchanged.
+template <int GB, typename T>
+__device__ __forceinline__ void ld_coefs(const T* __restrict__ c, T* r) {
+  if constexpr (sizeof(T) == 4 && GB >= 4) {
+#pragma unroll
+    for (int v = 0; v < GB / 4; ++v) {
+      const float4 x = reinterpret_cast<const float4*>(c)[v];
+      r[4 * v] = x.x; r[4 * v + 1] = x.y; r[4 * v + 2] = x.z; r[4 * v + 3] = x.w;
+    }
+  } else if constexpr (sizeof(T) == 8 && GB >= 2) {
+#pragma unroll
+    for (int v = 0; v < GB / 2; ++v) {
+      const double2 x = reinterpret_cast<const double2*>(c)[v];
+      r[2 * v] = x.x; r[2 * v + 1] = x.y;
+    }
+  } else {
+#pragma unroll
+    for (int g = 0; g < GB; ++g) r[g] = c[g];
+  }
+}
+
+// smallest compile-time group width that holds G rows
+__device__ __forceinline__ int group_width(int G) { return G <= 1 ? 1 : G <= 2 ? 2 : G <= 4 ? 4 : G <= 8 ? 8 : 16; }
+
 // ------------------------------------------------------------------ K1
 // One block per row j.  Mode groups are processed in turn by the same block:
 // the AB3 update is applied (and q written) while forming the first group,
 // and later groups re-read the updated q written by the same thread, so no
-// block ever reads a q value another block may be updating.  The projection
-// accumulates in shared memory (one FMA per layer and mode).
+// block ever reads a q value another block may be updating.  Each thread
+// accumulates the G modes of its points in registers, layer by layer.
+template <typename T, bool COMP, int GB>
+__device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool upd, T c0, T c1, T c2, const T* f0,
+                                            const T* f1, const T* f2, int G, T* A, int ld, const T* cst) {
+  for (int i = threadIdx.x; i < a.nx; i += NT) {
+    T acc[GB];
+#pragma unroll
+    for (int g = 0; g < GB; ++g) acc[g] = T(0);
+    size_t o = (size_t)j * a.pitch + i;
+    for (int l = 0; l < a.nl; ++l, o += a.lstride) {
+      T v;
+      if (COMP) {
+        float hi = (float)a.q[o];
+        if (upd) {
+          float lo = (float)a.qlo[o];
+          const float d = ab3_increment((float)c0, (float)c1, (float)c2, (float)f0[o], (float)f1[o], (float)f2[o]);
+          comp_add(hi, lo, d);
+          a.q[o] = (T)hi;
+          a.qlo[o] = (T)lo;
+        }
+        v = (T)hi;
+      } else {
+        v = a.q[o];
+        if (upd) {
+          v = ab3_plain<T>(v, c0, c1, c2, f0[o], f1[o], f2[o]);
+          a.q[o] = v;
+        }
+      }
+      T c[GB];
+      ld_coefs<GB, T>(cst + l * GMAX, c);
+#pragma unroll
+      for (int g = 0; g < GB; ++g) acc[g] = fmaT(c[g], v, acc[g]);
+    }
+    const int pi = pr(i);
+#pragma unroll
+    for (int g = 0; g < GB; ++g)
+      if (g < G) A[g * ld + pi] = acc[g];
+  }
+}
+
 template <typename T, bool COMP>
 __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mode, int j, unsigned char* smem_raw,
-                                              T* tot) {
+                                              T* tot, T* cst) {
   DevState* st = a.state;
   if (step_mode && !st->active) return;
   const int ld = padded_len(a.gx.M);
@@ -151,36 +220,22 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
   const T* f0 = a.fab + s0 * fs;
   const T* f1 = a.fab + s1 * fs;
   const T* f2 = a.fab + s2 * fs;
-  const T* cl = a.cl2m;
+  const int tid = threadIdx.x;
+  const int GB = group_width(a.G1);
   for (int m0 = 0; m0 < a.nl; m0 += a.G1) {
     const int G = min(a.G1, a.nl - m0);
     const bool upd = ab3 && m0 == 0;
-    for (int i = threadIdx.x; i < a.nx; i += NT) {
-      const int pi = pr(i);
-      for (int gg = 0; gg < G; ++gg) A[gg * ld + pi] = T(0);
-      for (int l = 0; l < a.nl; ++l) {
-        const size_t o = (size_t)l * a.lstride + (size_t)j * a.pitch + i;
-        T v;
-        if (COMP) {
-          float hi = (float)a.q[o];
-          if (upd) {
-            float lo = (float)a.qlo[o];
-            const float d = ab3_increment((float)c0, (float)c1, (float)c2, (float)f0[o], (float)f1[o], (float)f2[o]);
-            comp_add(hi, lo, d);
-            a.q[o] = (T)hi;
-            a.qlo[o] = (T)lo;
-          }
-          v = (T)hi;
-        } else {
-          v = a.q[o];
-          if (upd) {
-            v = ab3_plain<T>(v, c0, c1, c2, f0[o], f1[o], f2[o]);
-            a.q[o] = v;
-          }
-        }
-        const T* crow = cl + (size_t)m0 * a.nl + l;
-        for (int gg = 0; gg < G; ++gg) A[gg * ld + pi] = fmaT(__ldg(crow + gg * a.nl), v, A[gg * ld + pi]);
-      }
+    for (int w = tid; w < a.nl * GMAX; w += NT) {
+      const int l = w / GMAX, g = w - l * GMAX;
+      cst[w] = g < G ? a.cl2m[(size_t)(m0 + g) * a.nl + l] : T(0);
+    }
+    __syncthreads();
+    switch (GB) {
+      case 1: project_fwd<T, COMP, 1>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst); break;
+      case 2: project_fwd<T, COMP, 2>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst); break;
+      case 4: project_fwd<T, COMP, 4>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst); break;
+      case 8: project_fwd<T, COMP, 8>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst); break;
+      default: project_fwd<T, COMP, 16>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst); break;
     }
     __syncthreads();
     T* O = dst_block<T>(A, B, G, ld, a.gx, a.tx, tot);
@@ -315,10 +370,41 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
 // ------------------------------------------------------------------ K3
 // One block per row j; mode groups in turn.  In zeta mode each group also
 // inverse-transforms the spectral zeta rows (rows G..2G-1 of the batch) and
-// back-projects them into zeta.
+// back-projects them into zeta.  Each thread holds the G transformed values
+// of its point in registers and adds their contribution to every layer;
+// groups after the first accumulate onto the partial sums in psi (zeta).
+template <typename T, bool ZM, int GB>
+__device__ __forceinline__ void project_inv(const StepArgs<T>& a, int j, int m0, int G, const T* O, int ld,
+                                            const T* cst) {
+  for (int i = threadIdx.x; i < a.nx; i += NT) {
+    const int pi = pr(i);
+    T u[GB], z[ZM ? GB : 1];
+#pragma unroll
+    for (int g = 0; g < GB; ++g) {
+      u[g] = g < G ? O[g * ld + pi] : T(0);
+      if (ZM) z[g] = g < G ? O[(G + g) * ld + pi] : T(0);
+    }
+    size_t o = (size_t)j * a.pitch + i;
+    for (int l = 0; l < a.nl; ++l, o += a.lstride) {
+      T c[GB];
+      ld_coefs<GB, T>(cst + l * GMAX, c);
+      T acc = (m0 == 0) ? T(0) : a.psi[o];
+#pragma unroll
+      for (int g = 0; g < GB; ++g) acc = fmaT(c[g], u[g], acc);
+      a.psi[o] = acc;
+      if (ZM) {
+        T zc = (m0 == 0) ? T(0) : a.zeta[o];
+#pragma unroll
+        for (int g = 0; g < GB; ++g) zc = fmaT(c[g], z[g], zc);
+        a.zeta[o] = zc;
+      }
+    }
+  }
+}
+
 template <typename T, bool COMP>
 __device__ __forceinline__ void body_rows_inv(const StepArgs<T>& a, int step_mode, int j, unsigned char* smem_raw,
-                                              T* tot) {
+                                              T* tot, T* cst) {
   DevState* st = a.state;
   if (step_mode && !st->active) return;
   const int ld = padded_len(a.gx.M);
@@ -326,7 +412,7 @@ __device__ __forceinline__ void body_rows_inv(const StepArgs<T>& a, int step_mod
   const int Gb = zm ? a.G3 : a.G1;
   T* A = (T*)smem_raw;
   T* B = A + (size_t)(zm ? 2 * Gb : Gb) * ld;
-  const T* cm = a.cm2l;
+  const int GB = group_width(Gb);
   for (int m0 = 0; m0 < a.nl; m0 += Gb) {
     const int G = min(Gb, a.nl - m0);
     for (int gg = 0; gg < G; ++gg) {
@@ -337,21 +423,26 @@ __device__ __forceinline__ void body_rows_inv(const StepArgs<T>& a, int step_mod
         for (int i = threadIdx.x; i < a.nx; i += NT) A[(G + gg) * ld + pr(i)] = zrow[i];
       }
     }
+    for (int w = threadIdx.x; w < a.nl * GMAX; w += NT) {
+      const int l = w / GMAX, g = w - l * GMAX;
+      cst[w] = g < G ? a.cm2l[(size_t)l * a.nl + m0 + g] : T(0);
+    }
     __syncthreads();
     T* O = dst_block<T>(A, B, zm ? 2 * G : G, ld, a.gx, a.tx, tot);
-    for (int i = threadIdx.x; i < a.nx; i += NT) {
-      const int pi = pr(i);
-      for (int l = 0; l < a.nl; ++l) {
-        const size_t o = (size_t)l * a.lstride + (size_t)j * a.pitch + i;
-        const T* crow = cm + (size_t)l * a.nl + m0;
-        T acc = (m0 == 0) ? T(0) : a.psi[o];
-        for (int gg = 0; gg < G; ++gg) acc = fmaT(__ldg(crow + gg), O[gg * ld + pi], acc);
-        a.psi[o] = acc;
-        if (zm) {
-          T zc = (m0 == 0) ? T(0) : a.zeta[o];
-          for (int gg = 0; gg < G; ++gg) zc = fmaT(__ldg(crow + gg), O[(G + gg) * ld + pi], zc);
-          a.zeta[o] = zc;
-        }
+    if (zm) {
+      switch (GB) {
+        case 1: project_inv<T, true, 1>(a, j, m0, G, O, ld, cst); break;
+        case 2: project_inv<T, true, 2>(a, j, m0, G, O, ld, cst); break;
+        case 4: project_inv<T, true, 4>(a, j, m0, G, O, ld, cst); break;
+        default: project_inv<T, true, 8>(a, j, m0, G, O, ld, cst); break;
+      }
+    } else {
+      switch (GB) {
+        case 1: project_inv<T, false, 1>(a, j, m0, G, O, ld, cst); break;
+        case 2: project_inv<T, false, 2>(a, j, m0, G, O, ld, cst); break;
+        case 4: project_inv<T, false, 4>(a, j, m0, G, O, ld, cst); break;
+        case 8: project_inv<T, false, 8>(a, j, m0, G, O, ld, cst); break;
+        default: project_inv<T, false, 16>(a, j, m0, G, O, ld, cst); break;
       }
     }
     __syncthreads();
@@ -631,7 +722,8 @@ template <typename T, bool COMP>
 __global__ void __launch_bounds__(NT) k_rows_fwd(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
-  body_rows_fwd<T, COMP>(a, step_mode, blockIdx.x, smem_raw, tot);
+  __shared__ __align__(16) T cst[NLMAX * GMAX];
+  body_rows_fwd<T, COMP>(a, step_mode, blockIdx.x, smem_raw, tot, cst);
 }
 template <typename T, bool COMP>
 __global__ void __launch_bounds__(NT) k_cols(StepArgs<T> a, int step_mode) {
@@ -643,7 +735,8 @@ template <typename T, bool COMP>
 __global__ void __launch_bounds__(NT) k_rows_inv(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
-  body_rows_inv<T, COMP>(a, step_mode, blockIdx.x, smem_raw, tot);
+  __shared__ __align__(16) T cst[NLMAX * GMAX];
+  body_rows_inv<T, COMP>(a, step_mode, blockIdx.x, smem_raw, tot, cst);
 }
 template <typename T, bool COMP, int R>
 __global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
@@ -684,10 +777,11 @@ template <typename T, bool COMP>
 __global__ void __launch_bounds__(NT) k_rows_fwd_ens(EnsArgs<T> e, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
+  __shared__ __align__(16) T cst[NLMAX * GMAX];
   __shared__ StepArgs<T> sa;
   for (int item = blockIdx.x; item < e.total[0]; item += gridDim.x) {
     const int local = ens_item(e, e.start_rows, item, &sa);
-    body_rows_fwd<T, COMP>(sa, step_mode, local, smem_raw, tot);
+    body_rows_fwd<T, COMP>(sa, step_mode, local, smem_raw, tot, cst);
     __syncthreads();
   }
 }
@@ -708,10 +802,11 @@ template <typename T, bool COMP>
 __global__ void __launch_bounds__(NT) k_rows_inv_ens(EnsArgs<T> e, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
+  __shared__ __align__(16) T cst[NLMAX * GMAX];
   __shared__ StepArgs<T> sa;
   for (int item = blockIdx.x; item < e.total[2]; item += gridDim.x) {
     const int local = ens_item(e, e.start_rows, item, &sa);
-    body_rows_inv<T, COMP>(sa, step_mode, local, smem_raw, tot);
+    body_rows_inv<T, COMP>(sa, step_mode, local, smem_raw, tot, cst);
     __syncthreads();
   }
 }
@@ -909,7 +1004,7 @@ static cudaError_t set_attrs(const StepArgs<T>& a) {
   if (e != cudaSuccess) return e;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return e;
-  const size_t static_tot = sizeof(T) * GMAX * 32 + 64;
+  const size_t static_tot = sizeof(T) * (GMAX * 32 + NLMAX * GMAX) + 64;
   if (smem_rows<T, COMP>(a) + static_tot > (size_t)optin || smem_cols<T, COMP>(a) + static_tot > (size_t)optin ||
       smem_rows_inv<T, COMP>(a) + static_tot > (size_t)optin || rhs_halo(a) > RHS_RMAX ||
       smem_rhs<T>(a) + 1024 > (size_t)optin)
@@ -1027,7 +1122,7 @@ static cudaError_t set_attrs_ens() {
   if (e != cudaSuccess) return e;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return e;
-  const int lim = optin - (int)(sizeof(T) * GMAX * 32 + sizeof(StepArgs<T>) + 128);
+  const int lim = optin - (int)(sizeof(T) * (GMAX * 32 + NLMAX * GMAX) + sizeof(StepArgs<T>) + 128);
   if ((e = cudaFuncSetAttribute(k_rows_fwd_ens<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
     return e;
   if ((e = cudaFuncSetAttribute(k_rows_inv_ens<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
