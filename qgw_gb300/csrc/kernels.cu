@@ -130,6 +130,18 @@ __device__ __forceinline__ void comp_add(float& hi, float& lo, float d) {
   hi = h2;
 }
 
+// Asynchronous global -> shared element copies (no register staging), so the
+// independent tile loads of a block are all in flight at once.
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T* smem_dst, const T* gsrc) {
+  const unsigned int d = (unsigned int)__cvta_generic_to_shared(smem_dst);
+  if constexpr (sizeof(T) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(gsrc) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // ------------------------------------------------------- mode projections
 // The nl x G coefficients of one mode group are staged in shared memory as
 // cst[l * GMAX + gg] (zero for gg >= G), so one vector load serves a row of
@@ -520,12 +532,13 @@ __device__ void scalar_update(DevState* st, double Delta, double cfl) {
 }
 
 // RHS tile of TX x TY points of one layer; block (32, 8); R = halo radius
-// of psi (the number of hyperviscosity sweeps, at least 1).
-template <typename T, bool COMP, int R>
-__device__ __forceinline__ void body_rhs(const StepArgs<T>& a, int bx, int by, int k, unsigned int total,
-                                         unsigned char* smem_raw) {
-  DevState* st = a.state;
-  if (!st->active) return;
+// of psi (the number of hyperviscosity sweeps, at least 1).  EDGE: the tile
+// plus its halo touches a wall, so loads are bounds-checked and ghost values
+// follow adjust_bc; interior tiles (the vast majority) skip all of that.
+// Returns this thread's CFL maximum |dpsi| as bits in the arithmetic width.
+template <typename T, bool COMP, int R, bool EDGE>
+__device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArgs<T>& a, int i0, int j0, int k,
+                                                                    int step_index, unsigned char* smem_raw) {
   constexpr int W = TX + 2 * R, HH = TY + 2 * R;
   constexpr int QW = TX + 2, QH = TY + 2;
   T* ps = (T*)smem_raw;       // HH x W, psi with halo R
@@ -536,11 +549,8 @@ __device__ __forceinline__ void body_rhs(const StepArgs<T>& a, int bx, int by, i
   T* dyq = dyp + QW * TY;
   T* dxp = dyq + QW * TY;     // QH x TX
   T* dxq = dxp + TX * QH;
-  __shared__ unsigned long long wmax[NT / 32];
-  __shared__ int is_last;
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const int i0 = bx * TX, j0 = by * TY;
-  const int nx = a.nx, ny = a.ny;
+  const int nx = a.nx, ny = a.ny, pitch = a.pitch;
   const T* psiL = a.psi + (size_t)k * a.lstride;
   const T* qL = a.q + (size_t)k * a.lstride;
   const bool zm = COMP && a.zeta_mode;
@@ -553,27 +563,53 @@ __device__ __forceinline__ void body_rhs(const StepArgs<T>& a, int bx, int by, i
 #define PS(x, y) ps[((y) + R) * W + (x) + R]
 #define QS(x, y) qs[((y) + 1) * QW + (x) + 1]
   const int tid = tx + ty * 32;
-  for (int w = tid; w < HH * W; w += NT) {
-    const int y = w / W, x = w - y * W;
-    const int gi = i0 + x - R, gj = j0 + y - R;
-    T v = T(0);
-    if (gi >= 0 && gi < nx && gj >= 0 && gj < ny) v = psiL[(size_t)gj * a.pitch + gi];
-    ps[w] = v;
+  if (EDGE) {
+    for (int w = tid; w < HH * W; w += NT) {
+      const int y = w / W, x = w - y * W;
+      const int gi = i0 + x - R, gj = j0 + y - R;
+      T v = T(0);
+      if (gi >= 0 && gi < nx && gj >= 0 && gj < ny) v = psiL[(size_t)gj * pitch + gi];
+      ps[w] = v;
+    }
+  } else {
+    // interior tile: psi, q and (zeta mode) the raw zeta of the first
+    // sweep's region are independent, so all three copies go out together
+    const T* src = psiL + (size_t)(j0 - R) * pitch + (i0 - R);
+    for (int w = tid; w < HH * W; w += NT) {
+      const int y = w / W, x = w - y * W;
+      cp_async_elem(ps + w, src + y * pitch + x);
+    }
+    const T* qsrc = qL + (size_t)(j0 - 1) * pitch + (i0 - 1);
+    for (int w = tid; w < QH * QW; w += NT) {
+      const int y = w / QW, x = w - y * QW;
+      cp_async_elem(qs + w, qsrc + y * pitch + x);
+    }
+    if (zm && a.nsweep >= 1) {
+      constexpr int W1 = W - 2, H1 = HH - 2;
+      const T* zsrc = zetaL + (size_t)(j0 + 1 - R) * pitch + (i0 + 1 - R);
+      for (int w = tid; w < W1 * H1; w += NT) {
+        const int yr = w / W1, xr = w - yr * W1;
+        cp_async_elem(L0 + (yr + 1) * W + xr + 1, zsrc + yr * pitch + xr);
+      }
+    }
+    cp_async_wait_all();
   }
   __syncthreads();
   // q with one ghost point: adjust_bc(q, 1, psi), src/domain.h:308-348
-  for (int w = tid; w < QH * QW; w += NT) {
-    const int y = w / QW, x = w - y * QW;
-    const int xx = x - 1, yy = y - 1;
-    const int gi = i0 + xx, gj = j0 + yy;
-    const bool inx = gi >= 0 && gi < nx, iny = gj >= 0 && gj < ny;
-    T v = T(0);
-    if (inx && iny) v = qL[(size_t)gj * a.pitch + gi];
-    else if (iny && gi == -1) v = cbc * PS(xx + 1, yy);
-    else if (iny && gi == nx) v = cbc * PS(xx - 1, yy);
-    else if (inx && gj == -1) v = cbc * PS(xx, yy + 1);
-    else if (inx && gj == ny) v = cbc * PS(xx, yy - 1);
-    qs[w] = v;
+  if (EDGE) {
+    for (int w = tid; w < QH * QW; w += NT) {
+      const int y = w / QW, x = w - y * QW;
+      const int xx = x - 1, yy = y - 1;
+      const int gi = i0 + xx, gj = j0 + yy;
+      const bool inx = gi >= 0 && gi < nx, iny = gj >= 0 && gj < ny;
+      T v = T(0);
+      if (inx && iny) v = qL[(size_t)gj * pitch + gi];
+      else if (iny && gi == -1) v = cbc * PS(xx + 1, yy);
+      else if (iny && gi == nx) v = cbc * PS(xx - 1, yy);
+      else if (inx && gj == -1) v = cbc * PS(xx, yy + 1);
+      else if (inx && gj == ny) v = cbc * PS(xx, yy - 1);
+      qs[w] = v;
+    }
   }
   // hyperviscosity chain (calc_diff, src/dynamics.h:13-44) on the tile with
   // a shrinking halo; sweeps are unscaled (no 1/Delta^2), the scale is in
@@ -586,28 +622,44 @@ __device__ __forceinline__ void body_rhs(const StepArgs<T>& a, int bx, int by, i
   for (int s = 1; s <= R; ++s) {
     if (s <= a.nsweep) {
       __syncthreads();
-      const T ghs = (T)a.gh[s];
       const int Ws = W - 2 * s, Hs = HH - 2 * s;
-      for (int w = tid; w < Ws * Hs; w += NT) {
-        const int yr = w / Ws, xr = w - yr * Ws;
-        const int x = xr + s, y = yr + s;
-        const int xx = x - R, yy = y - R;
-        const int gi = i0 + xx, gj = j0 + yy;
-        const bool inx = gi >= 0 && gi < nx, iny = gj >= 0 && gj < ny;
-        const int o = y * W + x;
-        T v = T(0);
-        if (inx && iny) {
-          if (s == 1 && zm) {
-            v = d2 * zetaL[(size_t)gj * a.pitch + gi];
-          } else {
-            const T sum = (Lp[o + 1] + Lp[o - 1]) + (Lp[o + W] + Lp[o - W]);
-            v = fmaT(T(-4), Lp[o], sum);
-          }
-        } else if (iny && gi == -1) v = ghs * PS(xx + 1, yy);
-        else if (iny && gi == nx) v = ghs * PS(xx - 1, yy);
-        else if (inx && gj == -1) v = ghs * PS(xx, yy + 1);
-        else if (inx && gj == ny) v = ghs * PS(xx, yy - 1);
-        Lc[o] = v;
+      if (EDGE) {
+        const T ghs = (T)a.gh[s];
+        for (int w = tid; w < Ws * Hs; w += NT) {
+          const int yr = w / Ws, xr = w - yr * Ws;
+          const int x = xr + s, y = yr + s;
+          const int xx = x - R, yy = y - R;
+          const int gi = i0 + xx, gj = j0 + yy;
+          const bool inx = gi >= 0 && gi < nx, iny = gj >= 0 && gj < ny;
+          const int o = y * W + x;
+          T v = T(0);
+          if (inx && iny) {
+            if (s == 1 && zm) {
+              v = d2 * zetaL[(size_t)gj * pitch + gi];
+            } else {
+              const T sum = (Lp[o + 1] + Lp[o - 1]) + (Lp[o + W] + Lp[o - W]);
+              v = fmaT(T(-4), Lp[o], sum);
+            }
+          } else if (iny && gi == -1) v = ghs * PS(xx + 1, yy);
+          else if (iny && gi == nx) v = ghs * PS(xx - 1, yy);
+          else if (inx && gj == -1) v = ghs * PS(xx, yy + 1);
+          else if (inx && gj == ny) v = ghs * PS(xx, yy - 1);
+          Lc[o] = v;
+        }
+      } else if (s == 1 && zm) {
+        // the raw zeta is already in place (L0 == Lc): scale it
+        for (int w = tid; w < Ws * Hs; w += NT) {
+          const int yr = w / Ws, xr = w - yr * Ws;
+          const int o = (yr + s) * W + xr + s;
+          Lc[o] = d2 * Lc[o];
+        }
+      } else {
+        for (int w = tid; w < Ws * Hs; w += NT) {
+          const int yr = w / Ws, xr = w - yr * Ws;
+          const int o = (yr + s) * W + xr + s;
+          const T sum = (Lp[o + 1] + Lp[o - 1]) + (Lp[o + W] + Lp[o - W]);
+          Lc[o] = fmaT(T(-4), Lp[o], sum);
+        }
       }
       Lp = Lc;
       Lc = (Lc == L0) ? L1 : L0;
@@ -632,14 +684,14 @@ __device__ __forceinline__ void body_rhs(const StepArgs<T>& a, int bx, int by, i
 #define DX(arr, x, y) arr[((y) + 1) * TX + (x)]
   const size_t fs = (size_t)a.nl * a.lstride;
   int s0, s1, s2;
-  slabs(st->step_index + 1, s0, s1, s2);
+  slabs(step_index + 1, s0, s1, s2);
   T* fout = a.fab + s0 * fs + (size_t)k * a.lstride;
   const bool bottom = (k == a.nl - 1);
   decltype(absbits_native(T(0))) mymax_n = 0;
   const int x = tx;
   for (int y = ty; y < TY; y += 8) {
     const int gi = i0 + x, gj = j0 + y;
-    if (gi >= nx || gj >= ny) continue;
+    if (EDGE && (gi >= nx || gj >= ny)) continue;
     // Arakawa Jacobian J(psi, q) (jacobian_lev, src/domain.h:17-27) with the
     // centred differences shared: 2 products + 8 fused terms
     T J = DX(dxp, x, y) * DY(dyq, x, y);
@@ -663,7 +715,7 @@ __device__ __forceinline__ void body_rhs(const StepArgs<T>& a, int bx, int by, i
     if (k == 0 && a.has_wind) f += a.wind[gj];
     if (bottom) {
       if (a.has_drag) {
-        const T lp = zm ? d2 * zetaL[(size_t)gj * a.pitch + gi]
+        const T lp = zm ? d2 * zetaL[(size_t)gj * pitch + gi]
                         : fmaT(T(-4), PS(x, y), (PS(x + 1, y) + PS(x - 1, y)) + (PS(x, y + 1) + PS(x, y - 1)));
         f = fmaT(drag, lp, f);
       }
@@ -683,7 +735,7 @@ __device__ __forceinline__ void body_rhs(const StepArgs<T>& a, int bx, int by, i
         f = fmaT(topo_c, jt, f);
       }
     }
-    fout[(size_t)gj * a.pitch + gi] = f;
+    fout[(size_t)gj * pitch + gi] = f;
     // CFL (adjust_timestep, src/timestep.h:346-359): one-sided differences
     const T du = PS(x + 1, y) - PS(x, y);
     const T dv = PS(x, y + 1) - PS(x, y);
@@ -691,11 +743,28 @@ __device__ __forceinline__ void body_rhs(const StepArgs<T>& a, int bx, int by, i
     const auto bm = bu > bv ? bu : bv;
     mymax_n = bm > mymax_n ? bm : mymax_n;
   }
-  unsigned long long mymax = widen_absbits<T>(mymax_n);
 #undef DY
 #undef DX
 #undef PS
 #undef QS
+  return mymax_n;
+}
+
+template <typename T, bool COMP, int R>
+__device__ __forceinline__ void body_rhs(const StepArgs<T>& a, int bx, int by, int k, unsigned int total,
+                                         unsigned char* smem_raw) {
+  DevState* st = a.state;
+  if (!st->active) return;
+  __shared__ unsigned long long wmax[NT / 32];
+  __shared__ int is_last;
+  const int i0 = bx * TX, j0 = by * TY;
+  const bool edge = i0 < R || j0 < R || i0 + TX + R > a.nx || j0 + TY + R > a.ny;
+  const int si = st->step_index;
+  const unsigned long long mymax_w =
+      widen_absbits<T>(edge ? rhs_tile<T, COMP, R, true>(a, i0, j0, k, si, smem_raw)
+                            : rhs_tile<T, COMP, R, false>(a, i0, j0, k, si, smem_raw));
+  unsigned long long mymax = mymax_w;
+  const int tid = threadIdx.x + threadIdx.y * 32;
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long u = __shfl_xor_sync(0xffffffffu, mymax, o);
     mymax = u > mymax ? u : mymax;
@@ -739,7 +808,7 @@ __global__ void __launch_bounds__(NT) k_rows_inv(StepArgs<T> a, int step_mode) {
   body_rows_inv<T, COMP>(a, step_mode, blockIdx.x, smem_raw, tot, cst);
 }
 template <typename T, bool COMP, int R>
-__global__ void __launch_bounds__(NT) k_rhs(StepArgs<T> a) {
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 1) k_rhs(StepArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   body_rhs<T, COMP, R>(a, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x * gridDim.y * gridDim.z, smem_raw);
 }
