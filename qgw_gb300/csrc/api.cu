@@ -63,24 +63,28 @@ int upload(qgw_run* r, T** out, const std::vector<double>& host) {
 // Shared-memory budget of the row kernels' work buffers.  Measured at
 // 1024^2 x 10 on GB300: 64 KiB (3 blocks/SM) is fastest for FP64 and 40 KiB
 // (4-5 blocks/SM) for FP32; QGW_ROW_SMEM_KB overrides it (tuning knob).
-size_t row_budget(size_t elem) {
-  const char* e = std::getenv("QGW_ROW_SMEM_KB");
+// Shared-memory budget of the work buffers of the row kernels: which = 1 for
+// the forward rows kernel (K1), 3 for the inverse rows kernel (K3).  The
+// defaults come from measured sweeps at 1024^2 x 10 on GB300; the
+// environment variables QGW_ROW_SMEM_KB (K1) and QGW_INV_SMEM_KB (K3)
+// override them.
+size_t row_budget(size_t elem, int which) {
+  const char* e = std::getenv(which == 3 ? "QGW_INV_SMEM_KB" : "QGW_ROW_SMEM_KB");
   const long v = e ? std::atol(e) : 0;
   if (v >= 16 && v <= 220) return (size_t)v * 1024;
-  return elem == 8 ? (size_t)64 * 1024 : (size_t)40 * 1024;
+  if (elem == 8) return (size_t)48 * 1024;
+  return (size_t)(which == 3 ? 96 : 56) * 1024;
 }
 
-void choose_groups(int nl, int Mx, int My, size_t elem, int* G1, int* CT) {
-  const size_t budget = row_budget(elem);
-  int g = (int)(budget / (2 * (size_t)qgw::padded_len(Mx) * elem));
+// Modes per block of a row kernel: as many as the budget holds (each mode
+// takes rows_per_mode rows in each of the two DST work buffers), then
+// balanced over the resulting number of groups.
+int mode_group(int nl, int M, size_t elem, size_t budget, int rows_per_mode, int gmax) {
+  int g = (int)(budget / (2 * (size_t)rows_per_mode * qgw::padded_len(M) * elem));
   if (g < 1) g = 1;
-  if (g > 16) g = 16;
+  if (g > gmax) g = gmax;
   const int ngroups = (nl + g - 1) / g;
-  *G1 = (nl + ngroups - 1) / ngroups;
-  int ct = (int)(budget / (2 * (size_t)My * elem));
-  if (ct < 1) ct = 1;
-  if (ct > 16) ct = 16;
-  *CT = ct;
+  return (nl + ngroups - 1) / ngroups;
 }
 
 template <typename T>
@@ -180,7 +184,9 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   a.topo_fac = p.f0 / dhb;
   a.has_topo = 0;
   a.has_wind = p.tau0 != 0;
-  choose_groups(r->nl, r->nx + 1, r->ny + 1, sizeof(T), &a.G1, &a.CT);
+  a.G1 = mode_group(r->nl, r->nx + 1, sizeof(T), row_budget(sizeof(T), 1), 1, 16);
+  a.G3 = mode_group(r->nl, r->nx + 1, sizeof(T), row_budget(sizeof(T), 3), 1, 16);
+  a.CT = 0;
   a.low_k64 = 8;
   // 16-byte column vectors: rows 16-byte aligned and a whole number of
   // 32-byte column tiles per row, so a tile never crosses into the next row
@@ -191,7 +197,6 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   // by stencils lose ~(k_max/k_min)^2 of relative accuracy at grid scale.
   // The discrete Laplacian zeta is therefore formed spectrally (exact
   // symbol) and feeds the hyperviscosity chain and the bottom drag.
-  a.G3 = a.G1;
   a.zeta_mode = 0;
   a.spec2 = nullptr;
   a.zeta = nullptr;
@@ -199,13 +204,8 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
     a.zeta_mode = 1;
     if ((rc = dalloc(r, &a.spec2, field))) return rc;
     if ((rc = dalloc(r, &a.zeta, field))) return rc;
-    const size_t budget = row_budget(sizeof(T));
-    int g3 = (int)(budget / (4 * (size_t)qgw::padded_len(r->nx + 1) * sizeof(T)));
-    g3 = g3 < 1 ? 1 : (g3 > 8 ? 8 : g3);
-    const int ng = (r->nl + g3 - 1) / g3;
-    a.G3 = (r->nl + ng - 1) / ng;
-    int ct = (int)(budget / (3 * (size_t)(r->ny + 1) * sizeof(T)));
-    a.CT = ct < 1 ? 1 : (ct > 16 ? 16 : ct);
+    // K3 transforms psi and zeta rows of each mode: two rows per mode
+    a.G3 = mode_group(r->nl, r->nx + 1, sizeof(T), row_budget(sizeof(T), 3), 2, 8);
     std::vector<double> sx(r->nx), sy(r->ny);
     for (int k = 0; k < r->nx; ++k) { const double s = std::sin(M_PI * (k + 1) / (2.0 * (r->nx + 1))); sx[k] = s * s; }
     for (int j = 0; j < r->ny; ++j) { const double s = std::sin(M_PI * (j + 1) / (2.0 * (r->ny + 1))); sy[j] = s * s; }

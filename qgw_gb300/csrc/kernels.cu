@@ -23,6 +23,7 @@
 
 #include <algorithm>
 
+#include "dst_fixed.cuh"
 #include "kernels.h"
 #include "qgw_device.cuh"
 
@@ -43,8 +44,8 @@ template <typename T> struct ColsPer { static constexpr int value = sizeof(T) ==
 // the whole block; B is the second work buffer.  Returns the buffer that
 // holds the output.
 template <typename T>
-__device__ T* dst_block(T* A, T* B, int nrows, int ld, const DstGeom& g, const DstTables<T>& tb,
-                        T* tot) {
+__device__ __forceinline__ T* dst_block_generic(T* A, T* B, int nrows, int ld, const DstGeom& g,
+                                                const DstTables<T>& tb, T* tot) {
   const int tid = threadIdx.x + threadIdx.y * blockDim.x, nth = blockDim.x * blockDim.y;
   const int H = g.H, lgH = __ffs(H) - 1;
   for (int w = tid; w < (nrows << lgH); w += nth) {
@@ -100,6 +101,21 @@ __device__ T* dst_block(T* A, T* B, int nrows, int ld, const DstGeom& g, const D
   }
   __syncthreads();
   return dst;
+}
+
+// Block DST of any supported length: lengths M = 128..2048 use the
+// compile-time specialisations of dst_fixed.cuh, others the generic loops.
+template <typename T>
+__device__ __forceinline__ T* dst_block(T* A, T* B, int nrows, int ld, const DstGeom& g, const DstTables<T>& tb,
+                                        T* tot) {
+  switch (g.H) {
+    case 64: return dst_block_fixed<T, 6>(A, B, nrows, ld, tb);
+    case 128: return dst_block_fixed<T, 7>(A, B, nrows, ld, tb);
+    case 256: return dst_block_fixed<T, 8>(A, B, nrows, ld, tb);
+    case 512: return dst_block_fixed<T, 9>(A, B, nrows, ld, tb);
+    case 1024: return dst_block_fixed<T, 10>(A, B, nrows, ld, tb);
+    default: return dst_block_generic<T>(A, B, nrows, ld, g, tb, tot);
+  }
 }
 
 __device__ __forceinline__ void slabs(int si, int& s0, int& s1, int& s2) {
@@ -421,7 +437,7 @@ __device__ __forceinline__ void body_rows_inv(const StepArgs<T>& a, int step_mod
   if (step_mode && !st->active) return;
   const int ld = padded_len(a.gx.M);
   const bool zm = COMP && a.zeta_mode;
-  const int Gb = zm ? a.G3 : a.G1;
+  const int Gb = a.G3;
   T* A = (T*)smem_raw;
   T* B = A + (size_t)(zm ? 2 * Gb : Gb) * ld;
   const int GB = group_width(Gb);
@@ -855,7 +871,7 @@ __global__ void __launch_bounds__(NT) k_rows_fwd_ens(EnsArgs<T> e, int step_mode
   }
 }
 template <typename T, bool COMP>
-__global__ void __launch_bounds__(NT) k_cols_ens(EnsArgs<T> e, int step_mode) {
+__global__ void __launch_bounds__(NT, 2) k_cols_ens(EnsArgs<T> e, int step_mode) {
   constexpr int CT = ColsPer<T>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
@@ -1049,7 +1065,7 @@ static size_t smem_cols(const StepArgs<T>& a) {
 }
 template <typename T, bool COMP>
 static size_t smem_rows_inv(const StepArgs<T>& a) {
-  return (COMP && a.zeta_mode) ? (size_t)4 * a.G3 * padded_len(a.gx.M) * sizeof(T) : smem_rows<T, COMP>(a);
+  return (size_t)((COMP && a.zeta_mode) ? 4 : 2) * a.G3 * padded_len(a.gx.M) * sizeof(T);
 }
 template <typename T>
 static size_t smem_rhs_r(int r) {

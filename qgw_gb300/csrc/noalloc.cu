@@ -156,6 +156,7 @@ extern "C" int qgw_invert_pv_noalloc(const qgw_params* p, const double* cl2m, co
     qgw::StepArgs<double> probe{};
     probe.nl = 1;
     probe.G1 = 1;
+    probe.G3 = 1;
     probe.CT = 1;
     probe.gx.M = probe.gy.M = 4;
     if (qgw::prepare_f64(probe) != cudaSuccess) return QGW_ERR_CUDA;
@@ -228,6 +229,7 @@ extern "C" int qgw_invert_pv_noalloc(const qgw_params* p, const double* cl2m, co
   g = g < 1 ? 1 : (g > 16 ? 16 : g);
   const int ngroups = (nl + g - 1) / g;
   a.G1 = (nl + ngroups - 1) / ngroups;
+  a.G3 = a.G1;
   int ct = (int)(budget / (2 * (size_t)(ny + 1) * sizeof(double)));
   a.CT = ct < 1 ? 1 : (ct > 16 ? 16 : ct);
   qgw::enqueue_invert_f64(a, s);
