@@ -63,26 +63,36 @@ int upload(qgw_run* r, T** out, const std::vector<double>& host) {
 // Shared-memory budget of the row kernels' work buffers.  Measured at
 // 1024^2 x 10 on GB300: 64 KiB (3 blocks/SM) is fastest for FP64 and 40 KiB
 // (4-5 blocks/SM) for FP32; QGW_ROW_SMEM_KB overrides it (tuning knob).
-// Shared-memory budget of the work buffers of the row kernels: which = 1 for
-// the forward rows kernel (K1), 3 for the inverse rows kernel (K3).  The
-// defaults come from measured sweeps at 1024^2 x 10 on GB300; the
-// environment variables QGW_ROW_SMEM_KB (K1) and QGW_INV_SMEM_KB (K3)
-// override them.
-size_t row_budget(size_t elem, int which) {
-  const char* e = std::getenv(which == 3 ? "QGW_INV_SMEM_KB" : "QGW_ROW_SMEM_KB");
+// Shared-memory budget of the work buffers of the forward rows kernel (K1):
+// 48 KiB (FP64) / 56 KiB (FP32), which keeps four blocks per SM; measured
+// at 1024^2 and 2048^2 x 10 on GB300.  QGW_ROW_SMEM_KB overrides it.
+size_t row_budget(size_t elem) {
+  const char* e = std::getenv("QGW_ROW_SMEM_KB");
   const long v = e ? std::atol(e) : 0;
   if (v >= 16 && v <= 220) return (size_t)v * 1024;
-  if (elem == 8) return (size_t)48 * 1024;
-  return (size_t)(which == 3 ? 96 : 56) * 1024;
+  return (size_t)(elem == 8 ? 48 : 56) * 1024;
 }
 
-// Modes per block of a row kernel: as many as the budget holds (each mode
-// takes rows_per_mode rows in each of the two DST work buffers), then
-// balanced over the resulting number of groups.
-int mode_group(int nl, int M, size_t elem, size_t budget, int rows_per_mode, int gmax) {
+// Layers per block of the inverse rows kernel (K3): the measured optimum is
+// a fixed group size rather than a byte budget (each group re-reads the
+// row's spectral data, while larger groups cost occupancy): 3 layers with
+// the zeta rows, 2 without, within 110 KiB of work buffers.
+// QGW_INV_GROUP overrides the size.
+int inv_group(int zeta) {
+  const char* e = std::getenv("QGW_INV_GROUP");
+  const int v = e ? std::atoi(e) : 0;
+  if (v >= 1 && v <= 16) return v;
+  return zeta ? 3 : 2;
+}
+
+// Modes (layers) per block of a row kernel: as many as the budget holds (each
+// takes rows_per_mode rows in each of the two DST work buffers), at most
+// gmax and at most want, then balanced over the resulting number of groups.
+int mode_group(int nl, int M, size_t elem, size_t budget, int rows_per_mode, int gmax, int want) {
   int g = (int)(budget / (2 * (size_t)rows_per_mode * qgw::padded_len(M) * elem));
-  if (g < 1) g = 1;
+  if (g > want) g = want;
   if (g > gmax) g = gmax;
+  if (g < 1) g = 1;
   const int ngroups = (nl + g - 1) / g;
   return (nl + ngroups - 1) / ngroups;
 }
@@ -184,13 +194,13 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   a.topo_fac = p.f0 / dhb;
   a.has_topo = 0;
   a.has_wind = p.tau0 != 0;
-  a.G1 = mode_group(r->nl, r->nx + 1, sizeof(T), row_budget(sizeof(T), 1), 1, 16);
-  a.G3 = mode_group(r->nl, r->nx + 1, sizeof(T), row_budget(sizeof(T), 3), 1, 16);
+  a.G1 = mode_group(r->nl, r->nx + 1, sizeof(T), row_budget(sizeof(T)), 1, 16, 16);
+  a.G3 = mode_group(r->nl, r->nx + 1, sizeof(T), 110 * 1024, 1, 16, inv_group(0));
   a.CT = 0;
   a.low_k64 = 8;
   // 16-byte column vectors: rows 16-byte aligned and a whole number of
-  // 32-byte column tiles per row, so a tile never crosses into the next row
-  const int ct = (int)(32 / sizeof(T));
+  // column tiles per row, so a tile never crosses into the next row
+  const int ct = sizeof(T) == 8 ? qgw::cols_per_tile_f64() : qgw::cols_per_tile_f32c();
   a.vec_cols = ((size_t)r->pitch * sizeof(T)) % 16 == 0 && r->pitch % ct == 0;
   // compensated path: psi's FP32 round-off is white in wavenumber while psi
   // itself is dominated by the largest scales, so Laplacians of psi taken
@@ -205,7 +215,7 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
     if ((rc = dalloc(r, &a.spec2, field))) return rc;
     if ((rc = dalloc(r, &a.zeta, field))) return rc;
     // K3 transforms psi and zeta rows of each mode: two rows per mode
-    a.G3 = mode_group(r->nl, r->nx + 1, sizeof(T), row_budget(sizeof(T), 3), 2, 8);
+    a.G3 = mode_group(r->nl, r->nx + 1, sizeof(T), 110 * 1024, 2, 8, inv_group(1));
     std::vector<double> sx(r->nx), sy(r->ny);
     for (int k = 0; k < r->nx; ++k) { const double s = std::sin(M_PI * (k + 1) / (2.0 * (r->nx + 1))); sx[k] = s * s; }
     for (int j = 0; j < r->ny; ++j) { const double s = std::sin(M_PI * (j + 1) / (2.0 * (r->ny + 1))); sy[j] = s * s; }

@@ -36,8 +36,10 @@ constexpr int TX = 32, TY = 16;  // RHS tile (interior points)
 constexpr double TEPS = 1e-9;    // src/timestep.h:288
 constexpr double HUGEV = 1e30;   // src/qg.c:43
 
-// columns per block of the column kernel: 32 bytes, two 16-byte vectors
-template <typename T> struct ColsPer { static constexpr int value = sizeof(T) == 8 ? 4 : 8; };
+// columns per block of the column kernel (one or two 16-byte vectors per row):
+// four, so that the three work buffers of the compensated path leave room
+// for four blocks per SM
+template <typename T> struct ColsPer { static constexpr int value = 4; };
 
 // --------------------------------------------------------------- DST block
 // Batched DST-I of nrows rows (row r at A + r*ld, padded input format) by
@@ -281,23 +283,29 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
 // that each column is a contiguous padded row.
 template <typename T, int CT>
 __device__ __forceinline__ void load_cols(const T* __restrict__ src, T* v) {
+  constexpr int NV = CT * (int)sizeof(T) / 16, PV = 16 / (int)sizeof(T);
+  static_assert(NV >= 1 && CT * sizeof(T) == 16 * NV, "whole 16-byte vectors");
   const uint4* p = reinterpret_cast<const uint4*>(src);
-  uint4 u0 = p[0], u1 = p[1];
-  const T* a0 = reinterpret_cast<const T*>(&u0);
-  const T* a1 = reinterpret_cast<const T*>(&u1);
 #pragma unroll
-  for (int c = 0; c < CT / 2; ++c) { v[c] = a0[c]; v[CT / 2 + c] = a1[c]; }
+  for (int n = 0; n < NV; ++n) {
+    const uint4 u = p[n];
+    const T* a = reinterpret_cast<const T*>(&u);
+#pragma unroll
+    for (int c = 0; c < PV; ++c) v[n * PV + c] = a[c];
+  }
 }
 template <typename T, int CT>
 __device__ __forceinline__ void store_cols(T* __restrict__ dst, const T* v) {
-  uint4 u0, u1;
-  T* a0 = reinterpret_cast<T*>(&u0);
-  T* a1 = reinterpret_cast<T*>(&u1);
-#pragma unroll
-  for (int c = 0; c < CT / 2; ++c) { a0[c] = v[c]; a1[c] = v[CT / 2 + c]; }
+  constexpr int NV = CT * (int)sizeof(T) / 16, PV = 16 / (int)sizeof(T);
   uint4* p = reinterpret_cast<uint4*>(dst);
-  p[0] = u0;
-  p[1] = u1;
+#pragma unroll
+  for (int n = 0; n < NV; ++n) {
+    uint4 u;
+    T* a = reinterpret_cast<T*>(&u);
+#pragma unroll
+    for (int c = 0; c < PV; ++c) a[c] = v[n * PV + c];
+    p[n] = u;
+  }
 }
 
 template <typename T, bool COMP>
@@ -396,37 +404,42 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
 }
 
 // ------------------------------------------------------------------ K3
-// One block per row j; mode groups in turn.  In zeta mode each group also
-// inverse-transforms the spectral zeta rows (rows G..2G-1 of the batch) and
-// back-projects them into zeta.  Each thread holds the G transformed values
-// of its point in registers and adds their contribution to every layer;
-// groups after the first accumulate onto the partial sums in psi (zeta).
+// One block per row j; LAYER groups in turn.  The mode -> layer projection
+// is linear and acts point by point, so it commutes with the x-DST: each
+// group first forms the spectral rows of its layers, sum_m cm2l[l][m] *
+// spec_m (and of zeta from spec2 in zeta mode), then inverse-transforms them
+// and writes psi_l (zeta_l) once.  The spectral rows of row j are re-read by
+// each group (from cache); nothing is accumulated in global memory.
 template <typename T, bool ZM, int GB>
-__device__ __forceinline__ void project_inv(const StepArgs<T>& a, int j, int m0, int G, const T* O, int ld,
-                                            const T* cst) {
+__device__ __forceinline__ void project_spec(const StepArgs<T>& a, int j, int G, T* A, int ld, const T* cst) {
   for (int i = threadIdx.x; i < a.nx; i += NT) {
-    const int pi = pr(i);
-    T u[GB], z[ZM ? GB : 1];
+    T acc[GB], zacc[ZM ? GB : 1];
 #pragma unroll
     for (int g = 0; g < GB; ++g) {
-      u[g] = g < G ? O[g * ld + pi] : T(0);
-      if (ZM) z[g] = g < G ? O[(G + g) * ld + pi] : T(0);
+      acc[g] = T(0);
+      if (ZM) zacc[g] = T(0);
     }
     size_t o = (size_t)j * a.pitch + i;
-    for (int l = 0; l < a.nl; ++l, o += a.lstride) {
+#pragma unroll 2
+    for (int m = 0; m < a.nl; ++m, o += a.lstride) {
       T c[GB];
-      ld_coefs<GB, T>(cst + l * GMAX, c);
-      T acc = (m0 == 0) ? T(0) : a.psi[o];
+      ld_coefs<GB, T>(cst + m * GMAX, c);
+      const T v = a.spec[o];
 #pragma unroll
-      for (int g = 0; g < GB; ++g) acc = fmaT(c[g], u[g], acc);
-      a.psi[o] = acc;
+      for (int g = 0; g < GB; ++g) acc[g] = fmaT(c[g], v, acc[g]);
       if (ZM) {
-        T zc = (m0 == 0) ? T(0) : a.zeta[o];
+        const T z = a.spec2[o];
 #pragma unroll
-        for (int g = 0; g < GB; ++g) zc = fmaT(c[g], z[g], zc);
-        a.zeta[o] = zc;
+        for (int g = 0; g < GB; ++g) zacc[g] = fmaT(c[g], z, zacc[g]);
       }
     }
+    const int pi = pr(i);
+#pragma unroll
+    for (int g = 0; g < GB; ++g)
+      if (g < G) {
+        A[g * ld + pi] = acc[g];
+        if (ZM) A[(G + g) * ld + pi] = zacc[g];
+      }
   }
 }
 
@@ -441,36 +454,37 @@ __device__ __forceinline__ void body_rows_inv(const StepArgs<T>& a, int step_mod
   T* A = (T*)smem_raw;
   T* B = A + (size_t)(zm ? 2 * Gb : Gb) * ld;
   const int GB = group_width(Gb);
-  for (int m0 = 0; m0 < a.nl; m0 += Gb) {
-    const int G = min(Gb, a.nl - m0);
-    for (int gg = 0; gg < G; ++gg) {
-      const T* srow = a.spec + (size_t)(m0 + gg) * a.lstride + (size_t)j * a.pitch;
-      for (int i = threadIdx.x; i < a.nx; i += NT) A[gg * ld + pr(i)] = srow[i];
-      if (zm) {
-        const T* zrow = a.spec2 + (size_t)(m0 + gg) * a.lstride + (size_t)j * a.pitch;
-        for (int i = threadIdx.x; i < a.nx; i += NT) A[(G + gg) * ld + pr(i)] = zrow[i];
-      }
-    }
+  for (int l0 = 0; l0 < a.nl; l0 += Gb) {
+    const int G = min(Gb, a.nl - l0);
     for (int w = threadIdx.x; w < a.nl * GMAX; w += NT) {
-      const int l = w / GMAX, g = w - l * GMAX;
-      cst[w] = g < G ? a.cm2l[(size_t)l * a.nl + m0 + g] : T(0);
+      const int m = w / GMAX, g = w - m * GMAX;
+      cst[w] = g < G ? a.cm2l[(size_t)(l0 + g) * a.nl + m] : T(0);
     }
     __syncthreads();
-    T* O = dst_block<T>(A, B, zm ? 2 * G : G, ld, a.gx, a.tx, tot);
     if (zm) {
       switch (GB) {
-        case 1: project_inv<T, true, 1>(a, j, m0, G, O, ld, cst); break;
-        case 2: project_inv<T, true, 2>(a, j, m0, G, O, ld, cst); break;
-        case 4: project_inv<T, true, 4>(a, j, m0, G, O, ld, cst); break;
-        default: project_inv<T, true, 8>(a, j, m0, G, O, ld, cst); break;
+        case 1: project_spec<T, true, 1>(a, j, G, A, ld, cst); break;
+        case 2: project_spec<T, true, 2>(a, j, G, A, ld, cst); break;
+        case 4: project_spec<T, true, 4>(a, j, G, A, ld, cst); break;
+        default: project_spec<T, true, 8>(a, j, G, A, ld, cst); break;
       }
     } else {
       switch (GB) {
-        case 1: project_inv<T, false, 1>(a, j, m0, G, O, ld, cst); break;
-        case 2: project_inv<T, false, 2>(a, j, m0, G, O, ld, cst); break;
-        case 4: project_inv<T, false, 4>(a, j, m0, G, O, ld, cst); break;
-        case 8: project_inv<T, false, 8>(a, j, m0, G, O, ld, cst); break;
-        default: project_inv<T, false, 16>(a, j, m0, G, O, ld, cst); break;
+        case 1: project_spec<T, false, 1>(a, j, G, A, ld, cst); break;
+        case 2: project_spec<T, false, 2>(a, j, G, A, ld, cst); break;
+        case 4: project_spec<T, false, 4>(a, j, G, A, ld, cst); break;
+        case 8: project_spec<T, false, 8>(a, j, G, A, ld, cst); break;
+        default: project_spec<T, false, 16>(a, j, G, A, ld, cst); break;
+      }
+    }
+    __syncthreads();
+    T* O = dst_block<T>(A, B, zm ? 2 * G : G, ld, a.gx, a.tx, tot);
+    for (int g = 0; g < G; ++g) {
+      T* prow = a.psi + (size_t)(l0 + g) * a.lstride + (size_t)j * a.pitch;
+      for (int i = threadIdx.x; i < a.nx; i += NT) prow[i] = O[g * ld + pr(i)];
+      if (zm) {
+        T* zrow = a.zeta + (size_t)(l0 + g) * a.lstride + (size_t)j * a.pitch;
+        for (int i = threadIdx.x; i < a.nx; i += NT) zrow[i] = O[(G + g) * ld + pr(i)];
       }
     }
     __syncthreads();
@@ -804,7 +818,7 @@ __device__ __forceinline__ void body_rhs(const StepArgs<T>& a, int bx, int by, i
 
 // ------------------------------------------------- single-run wrappers
 template <typename T, bool COMP>
-__global__ void __launch_bounds__(NT) k_rows_fwd(StepArgs<T> a, int step_mode) {
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 3) k_rows_fwd(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
   __shared__ __align__(16) T cst[NLMAX * GMAX];
@@ -817,7 +831,7 @@ __global__ void __launch_bounds__(NT) k_cols(StepArgs<T> a, int step_mode) {
   body_cols<T, COMP>(a, step_mode, blockIdx.x, blockIdx.y, smem_raw, tot);
 }
 template <typename T, bool COMP>
-__global__ void __launch_bounds__(NT) k_rows_inv(StepArgs<T> a, int step_mode) {
+__global__ void __launch_bounds__(NT, 3) k_rows_inv(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
   __shared__ __align__(16) T cst[NLMAX * GMAX];
