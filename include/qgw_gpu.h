@@ -230,9 +230,9 @@ int qgw_probe_fp_rates(double* fp64_tflops, double* fp32_tflops);
  * (max_steps[i] > 0 caps member i), each stage as one persistent launch
  * over all members' work items, the four launches of a step captured once
  * as a CUDA graph (use_graph != 0) and replayed.  A member's result is
- * bitwise the same alone and in any ensemble.  qgw_ensemble_tune times each
- * stage for several persistent grid sizes and keeps the fastest; the trial
- * launches advance the state, so set q afterwards.  No reference
+ * bitwise the same alone and in any ensemble.  qgw_ensemble_tune chooses
+ * each stage's persistent grid size in turn, timing whole steps for every
+ * candidate; the trial steps advance the state, so set q afterwards.  No reference
  * counterpart: the reference runs one configuration per process. */
 typedef struct qgw_ensemble qgw_ensemble;
 int qgw_ensemble_create(int nmembers, const qgw_params* params, int precision, qgw_ensemble** out);

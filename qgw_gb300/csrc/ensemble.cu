@@ -43,8 +43,27 @@ void drop_graph(qgw::EnsembleCore* e) {
   e->graph = nullptr;
 }
 
+int stage_occupancy(const qgw::EnsembleCore* e, int stage, size_t smem) {
+  return e->precision == QGW_FP64 ? qgw::ens_blocks_per_sm_f64(stage, smem) : qgw::ens_blocks_per_sm_f32c(stage, smem);
+}
+
+// persistent grid of each stage: bps blocks per SM, never more than can be
+// resident at once (blocks beyond that would wait for a second wave); bps 0
+// gives one block per work item
+int stage_grid(const qgw::EnsembleCore* e, int total, int bps, int occ) {
+  if (total <= 0) return 0;
+  if (bps <= 0) return total;
+  return std::max(1, std::min(total, e->nsm * std::min(bps, occ)));
+}
+
 void set_grids(qgw::EnsembleCore* e) {
-  for (int s = 0; s < 4; ++s) e->grid[s] = std::max(1, std::min(e->total[s], e->nsm * e->bps[s]));
+  for (int s = 0; s < 3; ++s)
+    e->grid[s] = std::max(1, stage_grid(e, e->total[s], e->bps[s], stage_occupancy(e, s, e->sm.bytes[s])));
+  e->grid[3] = 0;
+  for (int r = 1; r <= 4; ++r) {
+    e->rhs_grid[r] = stage_grid(e, e->rhs_total[r], e->bps[3], stage_occupancy(e, 3 + r, e->sm.rhs_bytes[r]));
+    e->grid[3] += e->rhs_grid[r];
+  }
 }
 
 // member table, per-stage work lists and shared-memory sizes
@@ -52,43 +71,54 @@ int build_tables(qgw::EnsembleCore* e) {
   const int n = (int)e->members.size();
   const int ct = e->precision == QGW_FP64 ? qgw::cols_per_tile_f64() : qgw::cols_per_tile_f32c();
   const int tx = qgw::rhs_tile_x(), ty = qgw::rhs_tile_y();
-  std::vector<int> lists(3 * (n + 1) + 4, 0);
+  const size_t L = (size_t)n + 1;
+  std::vector<int> lists(3 * L + 4 + 4 * (L + 4), 0);
   int* rows = lists.data();
-  int* cols = rows + (n + 1);
-  int* rhs = cols + (n + 1);
+  int* cols = rows + L;
+  int* rhs = cols + L;
+  int* tot = rhs + L;
+  int* rr[5] = {nullptr, tot + 4, tot + 4 + (L + 4), tot + 4 + 2 * (L + 4), tot + 4 + 3 * (L + 4)};
   for (int i = 0; i < n; ++i) {
     const qgw_run* r = e->members[i];
+    const int R = e->precision == QGW_FP64 ? qgw::rhs_halo_of_f64(r->a64) : qgw::rhs_halo_of_f32c(r->a32);
+    const int tiles = ((r->nx + tx - 1) / tx) * ((r->ny + ty - 1) / ty) * r->nl;
     rows[i + 1] = rows[i] + r->ny;
     cols[i + 1] = cols[i] + ((r->nx + ct - 1) / ct) * r->nl;
-    rhs[i + 1] = rhs[i] + ((r->nx + tx - 1) / tx) * ((r->ny + ty - 1) / ty) * r->nl;
+    rhs[i + 1] = rhs[i] + tiles;
+    for (int h = 1; h <= 4; ++h) rr[h][i + 1] = rr[h][i] + (h == R ? tiles : 0);
   }
-  int* tot = rhs + (n + 1);
   tot[0] = rows[n];
   tot[1] = cols[n];
   tot[2] = rows[n];
   tot[3] = rhs[n];
   for (int s = 0; s < 4; ++s) e->total[s] = tot[s];
+  for (int h = 1; h <= 4; ++h) {
+    rr[h][L + 3] = rr[h][n];  // total[3] of the radius-h list
+    e->rhs_total[h] = rr[h][n];
+  }
   qgw::ens_core_free_tables(e);
   if (n == 0) return QGW_OK;
   CK(cudaMalloc(&e->d_lists, sizeof(int) * lists.size()));
   CK(cudaMemcpyAsync(e->d_lists, lists.data(), sizeof(int) * lists.size(), cudaMemcpyHostToDevice, e->stream));
   CK(cudaMalloc(&e->d_maxsteps, sizeof(int) * n));
+  const int* d = e->d_lists;
+  const int* drr[5] = {nullptr, d + (rr[1] - rows), d + (rr[2] - rows), d + (rr[3] - rows), d + (rr[4] - rows)};
   if (e->precision == QGW_FP64) {
     std::vector<qgw::StepArgs<double>> h(n);
     for (int i = 0; i < n; ++i) h[i] = e->members[i]->a64;
     CK(cudaMalloc(&e->d_members, sizeof(h[0]) * n));
     CK(cudaMemcpyAsync(e->d_members, h.data(), sizeof(h[0]) * n, cudaMemcpyHostToDevice, e->stream));
     e->sm = qgw::ens_smem_f64(h.data(), n);
-    e->e64 = {(const qgw::StepArgs<double>*)e->d_members, e->d_lists, e->d_lists + (n + 1),
-              e->d_lists + 2 * (n + 1), e->d_lists + 3 * (n + 1), n};
+    e->e64 = {(const qgw::StepArgs<double>*)e->d_members, d, d + L, d + 2 * L, d + 3 * L, n};
+    for (int r = 1; r <= 4; ++r) e->r64[r] = {e->e64.members, d, d + L, drr[r], drr[r] + L, n};
   } else {
     std::vector<qgw::StepArgs<float>> h(n);
     for (int i = 0; i < n; ++i) h[i] = e->members[i]->a32;
     CK(cudaMalloc(&e->d_members, sizeof(h[0]) * n));
     CK(cudaMemcpyAsync(e->d_members, h.data(), sizeof(h[0]) * n, cudaMemcpyHostToDevice, e->stream));
     e->sm = qgw::ens_smem_f32c(h.data(), n);
-    e->e32 = {(const qgw::StepArgs<float>*)e->d_members, e->d_lists, e->d_lists + (n + 1),
-              e->d_lists + 2 * (n + 1), e->d_lists + 3 * (n + 1), n};
+    e->e32 = {(const qgw::StepArgs<float>*)e->d_members, d, d + L, d + 2 * L, d + 3 * L, n};
+    for (int r = 1; r <= 4; ++r) e->r32[r] = {e->e32.members, d, d + L, drr[r], drr[r] + L, n};
   }
   set_grids(e);
   CK(cudaStreamSynchronize(e->stream));
@@ -96,8 +126,8 @@ int build_tables(qgw::EnsembleCore* e) {
 }
 
 void launch_step(qgw::EnsembleCore* e, int mask) {
-  if (e->precision == QGW_FP64) qgw::ens_step_f64(e->e64, e->sm, e->grid, mask, e->stream);
-  else qgw::ens_step_f32c(e->e32, e->sm, e->grid, mask, e->stream);
+  if (e->precision == QGW_FP64) qgw::ens_step_f64(e->e64, e->r64, e->sm, e->grid, e->rhs_grid, mask, e->stream);
+  else qgw::ens_step_f32c(e->e32, e->r32, e->sm, e->grid, e->rhs_grid, mask, e->stream);
 }
 
 int ensure_graph(qgw::EnsembleCore* e) {
@@ -253,12 +283,13 @@ int qgw_ensemble_step(qgw_ensemble* ens, int nsteps, const int* max_steps, int u
   return bad ? QGW_ERR_NAN : QGW_OK;
 }
 
-// Autotuner: for each stage, time `trial_steps` launches of that stage
-// alone for every candidate persistent grid (blocks per SM), keep the
-// fastest.  Runs on the current state and then restores the members' time
-// scalars and AB3 history, so call it before the time loop (it re-applies
-// qgw_set_q's reset of the history).  best_ms[4] (optional) receives the
-// per-stage times of the chosen grids.
+// Autotuner: coordinate descent over the persistent grid of each stage
+// (blocks per SM from a candidate list), each candidate timed over
+// `trial_steps` whole steps, so that every stage is measured in the context
+// of the others (caches, the member states the step leaves behind).  Runs
+// on the current state and then restores the members' time scalars; the
+// trial steps advance q, so callers re-set q before the time loop.
+// best_ms[4] (optional) receives the step time after each stage's choice.
 int qgw_ensemble_tune(qgw_ensemble* ens, int trial_steps, float* best_ms) {
   if (!ens || trial_steps < 1) return QGW_ERR_PARAM;
   qgw::EnsembleCore* e = &ens->core;
@@ -269,7 +300,7 @@ int qgw_ensemble_tune(qgw_ensemble* ens, int trial_steps, float* best_ms) {
   for (int i = 0; i < n; ++i) qgw_get_time(e->members[i], &saved[i]);
   std::vector<int> ms(n, 0);
   CK(cudaMemcpyAsync(e->d_maxsteps, ms.data(), sizeof(int) * n, cudaMemcpyHostToDevice, e->stream));
-  const int cands[] = {1, 2, 3, 4, 6, 8};
+  const int cands[] = {0, 1, 2, 3, 4, 5, 6, 8};  // 0: one block per work item
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
@@ -277,14 +308,20 @@ int qgw_ensemble_tune(qgw_ensemble* ens, int trial_steps, float* best_ms) {
   for (int s = 0; s < 4; ++s) {
     float best = 1e30f;
     int best_b = e->bps[s];
+    int occ = 1;
+    if (s < 3) occ = stage_occupancy(e, s, e->sm.bytes[s]);
+    else
+      for (int r = 1; r <= 4; ++r)
+        if (e->rhs_total[r] > 0) occ = std::max(occ, stage_occupancy(e, 3 + r, e->sm.rhs_bytes[r]));
     for (int b : cands) {
+      if (b > occ) break;  // same grid as the resident maximum
       e->bps[s] = b;
       set_grids(e);
       if (e->precision == QGW_FP64) qgw::ens_begin_f64(e->e64, e->d_maxsteps, e->stream);
       else qgw::ens_begin_f32c(e->e32, e->d_maxsteps, e->stream);
-      launch_step(e, 1 << s);  // warm-up
+      launch_step(e, 15);  // warm-up
       CK(cudaEventRecord(e0, e->stream));
-      for (int t = 0; t < trial_steps; ++t) launch_step(e, 1 << s);
+      for (int t = 0; t < trial_steps; ++t) launch_step(e, 15);
       CK(cudaEventRecord(e1, e->stream));
       CK(cudaEventSynchronize(e1));
       float msr = 0;
@@ -298,10 +335,11 @@ int qgw_ensemble_tune(qgw_ensemble* ens, int trial_steps, float* best_ms) {
   set_grids(e);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  // apply the last pending AB3 update of the trial steps
+  const int fgrid = std::max(1, std::min(e->total[0], e->nsm * 4));
+  if (e->precision == QGW_FP64) qgw::ens_flush_f64(e->e64, fgrid, e->stream);
+  else qgw::ens_flush_f32c(e->e32, fgrid, e->stream);
   CK(cudaGetLastError());
-  // the trial launches advanced the state: restore time scalars and clear
-  // the history; q itself was only touched by AB3 updates of zero history
-  // when nothing was pending, so callers re-set q before the time loop
   for (int i = 0; i < n; ++i) {
     qgw_run* r = e->members[i];
     qgw_set_time(r, &saved[i]);

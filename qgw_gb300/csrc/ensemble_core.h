@@ -18,14 +18,22 @@ struct EnsembleCore {
   cudaStream_t stream = nullptr;
   std::vector<qgw_run*> members;  // not owned by the core
   void* d_members = nullptr;      // device member table
-  int* d_lists = nullptr;         // start_rows | start_cols | start_rhs | total[4]
+  // start_rows | start_cols | start_rhs | total[4], then per halo radius
+  // R = 1..4: start_rhs of the members with radius R | total[4]
+  int* d_lists = nullptr;
   int* d_maxsteps = nullptr;
   EnsArgs<double> e64{};
   EnsArgs<float> e32{};
+  EnsArgs<double> r64[5]{};       // RHS stage per halo radius R (index 1..4)
+  EnsArgs<float> r32[5]{};
   EnsSmem sm{};
   int total[4] = {0, 0, 0, 0};
-  int bps[4] = {2, 2, 2, 2};      // persistent blocks per SM, per stage (tuned)
+  int rhs_total[5] = {0, 0, 0, 0, 0};
+  // persistent blocks per SM, per stage (tuned; capped by residency);
+  // 0: one block per work item
+  int bps[4] = {8, 8, 8, 8};
   int grid[4] = {0, 0, 0, 0};
+  int rhs_grid[5] = {0, 0, 0, 0, 0};
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<DevState> h_states;

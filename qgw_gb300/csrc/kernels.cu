@@ -851,79 +851,106 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 1) k_rhs(StepArgs<T> 
 // scalars, own CFL counter), so a member's result does not depend on which
 // other members share the launch.
 template <typename T>
-__device__ __forceinline__ int ens_item(const EnsArgs<T>& e, const int* start, int item, StepArgs<T>* sa) {
-  __shared__ int s_mi;
-  if (threadIdx.x == 0 && threadIdx.y == 0) {
-    int lo = 0, hi = e.n - 1;
-    while (lo < hi) {  // last member whose start <= item
-      const int mid = (lo + hi + 1) >> 1;
-      if (start[mid] <= item) lo = mid;
-      else hi = mid - 1;
+__device__ __forceinline__ int ens_item(const EnsArgs<T>& e, const int* start, int item, StepArgs<T>* sa,
+                                        int* cur) {
+  __shared__ int s_mi, s_start;
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+  if (tid == 0) {
+    // a block's items increase, so its member index never decreases: scan
+    // forward from the member it holds (binary search for the first item)
+    int lo;
+    if (*cur >= 0) {
+      lo = *cur;
+      while (lo + 1 < e.n && start[lo + 1] <= item) ++lo;
+    } else {
+      lo = 0;
+      int hi = e.n - 1;
+      while (lo < hi) {  // last member whose start <= item
+        const int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= item) lo = mid;
+        else hi = mid - 1;
+      }
     }
     s_mi = lo;
+    s_start = start[lo];
   }
   __syncthreads();
   const int mi = s_mi;
-  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
-  const int* srcw = reinterpret_cast<const int*>(e.members + mi);
-  int* dstw = reinterpret_cast<int*>(sa);
-  for (int w = tid; w < (int)(sizeof(StepArgs<T>) / 4); w += blockDim.x * blockDim.y) dstw[w] = srcw[w];
+  if (mi != *cur) {
+    // the block moves to another member: copy its arguments (block-uniform)
+    const int* srcw = reinterpret_cast<const int*>(e.members + mi);
+    int* dstw = reinterpret_cast<int*>(sa);
+    for (int w = tid; w < (int)(sizeof(StepArgs<T>) / 4); w += blockDim.x * blockDim.y) dstw[w] = srcw[w];
+    __syncthreads();
+    if (tid == 0) *cur = mi;
+  }
+  return item - s_start;
+}
+
+// the member whose arguments a block holds: none yet
+__device__ __forceinline__ void ens_init_cur(int* cur) {
+  if (threadIdx.x == 0 && threadIdx.y == 0) *cur = -1;
   __syncthreads();
-  return item - start[mi];
 }
 
 template <typename T, bool COMP>
-__global__ void __launch_bounds__(NT) k_rows_fwd_ens(EnsArgs<T> e, int step_mode) {
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 2) k_rows_fwd_ens(EnsArgs<T> e, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
   __shared__ __align__(16) T cst[NLMAX * GMAX];
   __shared__ StepArgs<T> sa;
+  __shared__ int cur;
+  ens_init_cur(&cur);
   for (int item = blockIdx.x; item < e.total[0]; item += gridDim.x) {
-    const int local = ens_item(e, e.start_rows, item, &sa);
+    const int local = ens_item(e, e.start_rows, item, &sa, &cur);
     body_rows_fwd<T, COMP>(sa, step_mode, local, smem_raw, tot, cst);
     __syncthreads();
   }
 }
 template <typename T, bool COMP>
-__global__ void __launch_bounds__(NT, 2) k_cols_ens(EnsArgs<T> e, int step_mode) {
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 2) k_cols_ens(EnsArgs<T> e, int step_mode) {
   constexpr int CT = ColsPer<T>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
   __shared__ StepArgs<T> sa;
+  __shared__ int cur;
+  ens_init_cur(&cur);
   for (int item = blockIdx.x; item < e.total[1]; item += gridDim.x) {
-    const int local = ens_item(e, e.start_cols, item, &sa);
+    const int local = ens_item(e, e.start_cols, item, &sa, &cur);
     const int ntx = (sa.nx + CT - 1) / CT;
     body_cols<T, COMP>(sa, step_mode, local % ntx, local / ntx, smem_raw, tot);
     __syncthreads();
   }
 }
 template <typename T, bool COMP>
-__global__ void __launch_bounds__(NT) k_rows_inv_ens(EnsArgs<T> e, int step_mode) {
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 2) k_rows_inv_ens(EnsArgs<T> e, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
   __shared__ __align__(16) T cst[NLMAX * GMAX];
   __shared__ StepArgs<T> sa;
+  __shared__ int cur;
+  ens_init_cur(&cur);
   for (int item = blockIdx.x; item < e.total[2]; item += gridDim.x) {
-    const int local = ens_item(e, e.start_rows, item, &sa);
+    const int local = ens_item(e, e.start_rows, item, &sa, &cur);
     body_rows_inv<T, COMP>(sa, step_mode, local, smem_raw, tot, cst);
     __syncthreads();
   }
 }
-template <typename T, bool COMP>
-__global__ void __launch_bounds__(NT) k_rhs_ens(EnsArgs<T> e) {
+// RHS stage of an ensemble: one launch per halo radius R over the members
+// with that radius (the work list of the launch gives the others no items),
+// so each launch runs the same specialised body as a single run.
+template <typename T, bool COMP, int R>
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 3) k_rhs_ens(EnsArgs<T> e) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ StepArgs<T> sa;
+  __shared__ int cur;
+  ens_init_cur(&cur);
   for (int item = blockIdx.x; item < e.total[3]; item += gridDim.x) {
-    const int local = ens_item(e, e.start_rhs, item, &sa);
+    const int local = ens_item(e, e.start_rhs, item, &sa, &cur);
     const int ntx = (sa.nx + TX - 1) / TX, nty = (sa.ny + TY - 1) / TY;
     const int bx = local % ntx, rest = local / ntx, by = rest % nty, bz = rest / nty;
     const unsigned int total = (unsigned int)(ntx * nty * sa.nl);
-    switch (sa.nsweep > 0 ? sa.nsweep : 1) {
-      case 1: body_rhs<T, COMP, 1>(sa, bx, by, bz, total, smem_raw); break;
-      case 2: body_rhs<T, COMP, 2>(sa, bx, by, bz, total, smem_raw); break;
-      case 3: body_rhs<T, COMP, 3>(sa, bx, by, bz, total, smem_raw); break;
-      default: body_rhs<T, COMP, 4>(sa, bx, by, bz, total, smem_raw); break;
-    }
+    body_rhs<T, COMP, R>(sa, bx, by, bz, total, smem_raw);
     __syncthreads();
   }
 }
@@ -986,8 +1013,10 @@ __global__ void k_end(DevState* st) { st->pending = 0; }
 template <typename T, bool COMP>
 __global__ void __launch_bounds__(NT) k_flush_ens(EnsArgs<T> e) {
   __shared__ StepArgs<T> sa;
+  __shared__ int cur;
+  ens_init_cur(&cur);
   for (int item = blockIdx.x; item < e.total[0]; item += gridDim.x) {
-    const int j = ens_item(e, e.start_rows, item, &sa);
+    const int j = ens_item(e, e.start_rows, item, &sa, &cur);
     const DevState* st = sa.state;
     if (st->pending) {
       int s0, s1, s2;
@@ -1227,8 +1256,11 @@ static cudaError_t set_attrs_ens() {
   if ((e = cudaFuncSetAttribute(k_rows_inv_ens<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
     return e;
   if ((e = cudaFuncSetAttribute(k_cols_ens<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
-  return cudaFuncSetAttribute(k_rhs_ens<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              optin - (int)(sizeof(StepArgs<T>) + 1024));
+  const int rl = optin - (int)(sizeof(StepArgs<T>) + 1024);
+  if ((e = cudaFuncSetAttribute(k_rhs_ens<T, COMP, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, rl))) return e;
+  if ((e = cudaFuncSetAttribute(k_rhs_ens<T, COMP, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, rl))) return e;
+  if ((e = cudaFuncSetAttribute(k_rhs_ens<T, COMP, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, rl))) return e;
+  return cudaFuncSetAttribute(k_rhs_ens<T, COMP, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, rl);
 }
 
 template <typename T, bool COMP>
@@ -1240,16 +1272,24 @@ static EnsSmem ens_smem(const StepArgs<T>* host_members, int n) {
     s.bytes[1] = std::max(s.bytes[1], smem_cols<T, COMP>(a));
     s.bytes[2] = std::max(s.bytes[2], smem_rows_inv<T, COMP>(a));
     s.bytes[3] = std::max(s.bytes[3], smem_rhs<T>(a));
+    s.rhs_bytes[rhs_halo(a)] = smem_rhs<T>(a);
   }
   return s;
 }
 
 template <typename T, bool COMP>
-static void ens_step(const EnsArgs<T>& e, const EnsSmem& sm, const int* grid, int which_mask, cudaStream_t s) {
+static void ens_step(const EnsArgs<T>& e, const EnsArgs<T>* er, const EnsSmem& sm, const int* grid, const int* rgrid,
+                     int which_mask, cudaStream_t s) {
   if (which_mask & 1) k_rows_fwd_ens<T, COMP><<<grid[0], NT, sm.bytes[0], s>>>(e, 1);
   if (which_mask & 2) k_cols_ens<T, COMP><<<grid[1], NT, sm.bytes[1], s>>>(e, 1);
   if (which_mask & 4) k_rows_inv_ens<T, COMP><<<grid[2], NT, sm.bytes[2], s>>>(e, 1);
-  if (which_mask & 8) k_rhs_ens<T, COMP><<<grid[3], dim3(32, 8), sm.bytes[3], s>>>(e);
+  if (which_mask & 8) {
+    const dim3 blk(32, 8);
+    if (rgrid[1] > 0) k_rhs_ens<T, COMP, 1><<<rgrid[1], blk, sm.rhs_bytes[1], s>>>(er[1]);
+    if (rgrid[2] > 0) k_rhs_ens<T, COMP, 2><<<rgrid[2], blk, sm.rhs_bytes[2], s>>>(er[2]);
+    if (rgrid[3] > 0) k_rhs_ens<T, COMP, 3><<<rgrid[3], blk, sm.rhs_bytes[3], s>>>(er[3]);
+    if (rgrid[4] > 0) k_rhs_ens<T, COMP, 4><<<rgrid[4], blk, sm.rhs_bytes[4], s>>>(er[4]);
+  }
 }
 template <typename T, bool COMP>
 static void ens_invert(const EnsArgs<T>& e, const EnsSmem& sm, const int* grid, cudaStream_t s) {
@@ -1257,6 +1297,25 @@ static void ens_invert(const EnsArgs<T>& e, const EnsSmem& sm, const int* grid, 
   k_cols_ens<T, COMP><<<grid[1], NT, sm.bytes[1], s>>>(e, 0);
   k_rows_inv_ens<T, COMP><<<grid[2], NT, sm.bytes[2], s>>>(e, 0);
 }
+
+template <typename T, bool COMP>
+static int ens_occupancy(int stage, size_t smem) {
+  int b = 0;
+  cudaError_t e = cudaSuccess;
+  if (stage == 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_rows_fwd_ens<T, COMP>, NT, smem);
+  if (stage == 1) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_cols_ens<T, COMP>, NT, smem);
+  if (stage == 2) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_rows_inv_ens<T, COMP>, NT, smem);
+  // stage 3 + R: the RHS kernel of halo radius R
+  if (stage == 4) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_rhs_ens<T, COMP, 1>, NT, smem);
+  if (stage == 5) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_rhs_ens<T, COMP, 2>, NT, smem);
+  if (stage == 6) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_rhs_ens<T, COMP, 3>, NT, smem);
+  if (stage == 7) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_rhs_ens<T, COMP, 4>, NT, smem);
+  return e == cudaSuccess && b > 0 ? b : 1;
+}
+int ens_blocks_per_sm_f64(int stage, size_t smem) { return ens_occupancy<double, false>(stage, smem); }
+int ens_blocks_per_sm_f32c(int stage, size_t smem) { return ens_occupancy<float, true>(stage, smem); }
+int rhs_halo_of_f64(const StepArgs<double>& a) { return rhs_halo(a); }
+int rhs_halo_of_f32c(const StepArgs<float>& a) { return rhs_halo(a); }
 
 cudaError_t ens_prepare_f64() { return set_attrs_ens<double, false>(); }
 cudaError_t ens_prepare_f32c() { return set_attrs_ens<float, true>(); }
@@ -1268,11 +1327,13 @@ void ens_begin_f64(const EnsArgs<double>& e, const int* max_steps, cudaStream_t 
 void ens_begin_f32c(const EnsArgs<float>& e, const int* max_steps, cudaStream_t s) {
   k_begin_ens<float><<<(e.n + 63) / 64, 64, 0, s>>>(e, 0.0, 0.0, max_steps);
 }
-void ens_step_f64(const EnsArgs<double>& e, const EnsSmem& sm, const int* grid, int mask, cudaStream_t s) {
-  ens_step<double, false>(e, sm, grid, mask, s);
+void ens_step_f64(const EnsArgs<double>& e, const EnsArgs<double>* er, const EnsSmem& sm, const int* grid,
+                  const int* rgrid, int mask, cudaStream_t s) {
+  ens_step<double, false>(e, er, sm, grid, rgrid, mask, s);
 }
-void ens_step_f32c(const EnsArgs<float>& e, const EnsSmem& sm, const int* grid, int mask, cudaStream_t s) {
-  ens_step<float, true>(e, sm, grid, mask, s);
+void ens_step_f32c(const EnsArgs<float>& e, const EnsArgs<float>* er, const EnsSmem& sm, const int* grid,
+                   const int* rgrid, int mask, cudaStream_t s) {
+  ens_step<float, true>(e, er, sm, grid, rgrid, mask, s);
 }
 void ens_invert_f64(const EnsArgs<double>& e, const EnsSmem& sm, const int* grid, cudaStream_t s) {
   ens_invert<double, false>(e, sm, grid, s);

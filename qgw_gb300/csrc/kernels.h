@@ -31,20 +31,33 @@ void enqueue_budget_f32c(const StepArgs<float>& a, const double* wts, double* pa
                          double* out, cudaStream_t s);
 
 // ensembles (one persistent launch per stage over all members)
-struct EnsSmem { size_t bytes[4]; };
+// dynamic shared memory per stage; the RHS stage per halo radius R (rhs_bytes[R], 0: no member)
+struct EnsSmem { size_t bytes[4]; size_t rhs_bytes[5]; };
 cudaError_t ens_prepare_f64();
 cudaError_t ens_prepare_f32c();
 EnsSmem ens_smem_f64(const StepArgs<double>* host_members, int n);
 EnsSmem ens_smem_f32c(const StepArgs<float>* host_members, int n);
 void ens_begin_f64(const EnsArgs<double>& e, const int* max_steps, cudaStream_t s);
 void ens_begin_f32c(const EnsArgs<float>& e, const int* max_steps, cudaStream_t s);
-// mask: bit k launches kernel k (0 rows forward, 1 columns, 2 rows inverse, 3 RHS)
-void ens_step_f64(const EnsArgs<double>& e, const EnsSmem& sm, const int* grid, int mask, cudaStream_t s);
-void ens_step_f32c(const EnsArgs<float>& e, const EnsSmem& sm, const int* grid, int mask, cudaStream_t s);
+// mask: bit k launches kernel k (0 rows forward, 1 columns, 2 rows inverse,
+// 3 RHS); the RHS stage is one launch per halo radius R with er[R] (whose
+// work list holds only the members of that radius) and grid rgrid[R] (0: none)
+void ens_step_f64(const EnsArgs<double>& e, const EnsArgs<double>* er, const EnsSmem& sm, const int* grid,
+                  const int* rgrid, int mask, cudaStream_t s);
+void ens_step_f32c(const EnsArgs<float>& e, const EnsArgs<float>* er, const EnsSmem& sm, const int* grid,
+                   const int* rgrid, int mask, cudaStream_t s);
 void ens_invert_f64(const EnsArgs<double>& e, const EnsSmem& sm, const int* grid, cudaStream_t s);
 void ens_invert_f32c(const EnsArgs<float>& e, const EnsSmem& sm, const int* grid, cudaStream_t s);
 void ens_flush_f64(const EnsArgs<double>& e, int grid, cudaStream_t s);
 void ens_flush_f32c(const EnsArgs<float>& e, int grid, cudaStream_t s);
+// resident blocks per SM of an ensemble stage kernel with `smem` bytes of
+// dynamic shared memory (stage 0 rows forward, 1 columns, 2 rows inverse,
+// 3 + R the RHS kernel of halo radius R = 1..4)
+int ens_blocks_per_sm_f64(int stage, size_t smem);
+int ens_blocks_per_sm_f32c(int stage, size_t smem);
+// halo radius R of a run's RHS kernel (the number of hyperviscosity sweeps, at least 1)
+int rhs_halo_of_f64(const StepArgs<double>& a);
+int rhs_halo_of_f32c(const StepArgs<float>& a);
 int cols_per_tile_f64();
 int cols_per_tile_f32c();
 int rhs_tile_x();
