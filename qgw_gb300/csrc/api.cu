@@ -232,6 +232,24 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
     a.lx2 = -4.0 / (r->Delta * r->Delta);
     a.ly2 = a.lx2;
   }
+  // FP32 copies of the constants of the compensated kernels (one rounding
+  // of the same double expressions the FP64 kernels use)
+  std::memset(a.fc, 0, sizeof(a.fc));
+  a.fc[qgw::FC_D2] = (float)(r->Delta * r->Delta);
+  a.fc[qgw::FC_CBC] = (float)a.cbc;
+  a.fc[qgw::FC_MINV12] = (float)(-a.inv12d2);
+  a.fc[qgw::FC_B2D] = (float)a.b2d;
+  a.fc[qgw::FC_NUD2] = (float)a.nu_d2;
+  a.fc[qgw::FC_NUH] = (float)a.nuh_scaled;
+  a.fc[qgw::FC_DRAG] = (float)a.drag_d2;
+  a.fc[qgw::FC_TOPOC] = (float)(-(a.inv12d2 * a.topo_fac));
+  for (int g = 1; g <= 4; ++g) a.fc[qgw::FC_GH1 + g - 1] = (float)a.gh[g];
+  a.fc[qgw::FC_NORM] = (float)r->norm;
+  a.fc[qgw::FC_LX2] = (float)a.lx2;
+  a.fc[qgw::FC_LY2] = (float)a.ly2;
+  float* fi;
+  if ((rc = upload<float>(r, &fi, r->iRd2))) return rc;
+  a.iRd2f = fi;
   return QGW_OK;
 }
 

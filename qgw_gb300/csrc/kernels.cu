@@ -148,6 +148,12 @@ __device__ __forceinline__ void comp_add(float& hi, float& lo, float d) {
   hi = h2;
 }
 
+// a run constant in the arithmetic type: the double itself, or its FP32 copy
+// made on the host (no conversion on the device)
+template <typename T> __device__ __forceinline__ T pick(double d, float f);
+template <> __device__ __forceinline__ double pick<double>(double d, float) { return d; }
+template <> __device__ __forceinline__ float pick<float>(double, float f) { return f; }
+
 // Asynchronous global -> shared element copies (no register staging), so the
 // independent tile loads of a block are all in flight at once.
 template <typename T>
@@ -339,7 +345,8 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
   T* O = dst_block<T>(A, B, CT, ld, a.gy, a.ty, tot);
   const double iRd2 = a.iRd2[m];
   const bool zm = COMP && a.zeta_mode;
-  const float ird2f = (float)iRd2, normf = (float)a.norm, lx2f = (float)a.lx2, ly2f = (float)a.ly2;
+  const float ird2f = COMP ? a.iRd2f[m] : 0.f;
+  const float normf = a.fc[FC_NORM], lx2f = a.fc[FC_LX2], ly2f = a.fc[FC_LY2];
   for (int jj = threadIdx.x; jj < ny; jj += NT) {
     const int pj = pr(jj);
     if (!COMP) {
@@ -586,10 +593,11 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
   const bool zm = COMP && a.zeta_mode;
   const T* zetaL = zm ? a.zeta + (size_t)k * a.lstride : nullptr;
   // every double parameter converted once (conversions run on the FP64 pipe)
-  const T d2 = (T)(a.Delta * a.Delta);
-  const T cbc = (T)a.cbc;
-  const T m_inv12 = (T)(-a.inv12d2), b2d = (T)a.b2d, nu_d2 = (T)a.nu_d2, nuh = (T)a.nuh_scaled;
-  const T drag = (T)a.drag_d2, topo_c = -(T)(a.inv12d2 * a.topo_fac);
+  const T d2 = pick<T>(a.Delta * a.Delta, a.fc[FC_D2]);
+  const T cbc = pick<T>(a.cbc, a.fc[FC_CBC]);
+  const T m_inv12 = pick<T>(-a.inv12d2, a.fc[FC_MINV12]), b2d = pick<T>(a.b2d, a.fc[FC_B2D]);
+  const T nu_d2 = pick<T>(a.nu_d2, a.fc[FC_NUD2]), nuh = pick<T>(a.nuh_scaled, a.fc[FC_NUH]);
+  const T drag = pick<T>(a.drag_d2, a.fc[FC_DRAG]), topo_c = pick<T>(-(a.inv12d2 * a.topo_fac), a.fc[FC_TOPOC]);
 #define PS(x, y) ps[((y) + R) * W + (x) + R]
 #define QS(x, y) qs[((y) + 1) * QW + (x) + 1]
   const int tid = tx + ty * 32;
@@ -654,7 +662,7 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
       __syncthreads();
       const int Ws = W - 2 * s, Hs = HH - 2 * s;
       if (EDGE) {
-        const T ghs = (T)a.gh[s];
+        const T ghs = pick<T>(a.gh[s], a.fc[FC_GH1 + s - 1]);
         for (int w = tid; w < Ws * Hs; w += NT) {
           const int yr = w / Ws, xr = w - yr * Ws;
           const int x = xr + s, y = yr + s;

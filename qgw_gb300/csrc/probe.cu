@@ -6,12 +6,17 @@
 #include "../../include/qgw_gpu.h"
 
 namespace {
+// explicit fused multiply-adds: the library is compiled without implicit
+// contraction (-fmad=false), which would otherwise split them in two
+__device__ __forceinline__ double fma_t(double x, double a, double b) { return __fma_rn(x, a, b); }
+__device__ __forceinline__ float fma_t(float x, float a, float b) { return __fmaf_rn(x, a, b); }
+
 template <typename T>
 __global__ void k_fma_chains(T* out, int iters, T a, T b) {
   T x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
   for (int i = 0; i < iters; ++i) {
-    x0 = x0 * a + b; x1 = x1 * a + b; x2 = x2 * a + b; x3 = x3 * a + b;
-    x4 = x4 * a + b; x5 = x5 * a + b; x6 = x6 * a + b; x7 = x7 * a + b;
+    x0 = fma_t(x0, a, b); x1 = fma_t(x1, a, b); x2 = fma_t(x2, a, b); x3 = fma_t(x3, a, b);
+    x4 = fma_t(x4, a, b); x5 = fma_t(x5, a, b); x6 = fma_t(x6, a, b); x7 = fma_t(x7, a, b);
   }
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }

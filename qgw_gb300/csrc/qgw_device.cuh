@@ -90,9 +90,30 @@ template <typename T> struct StepArgs {
   const float* Ksqf;
   const float* sx2f;
   const float* sy2f;
+  // FP32 copies of the RHS and Helmholtz constants (compensated path), made
+  // on the host: a double -> float conversion runs on the FP64 pipe
+  float fc[16];
+  const float* iRd2f;
   int CT;                          // (unused by the kernels; kept for layout)
   int vec_cols;                    // rows are 16-byte aligned: 16-byte column loads
   int low_k64;                     // compensated: FP64 divide for mode 0, j,k < low_k64
+};
+
+// indices into StepArgs::fc
+enum FcIndex {
+  FC_D2 = 0,      // Delta^2
+  FC_CBC,         // cbc
+  FC_MINV12,      // -inv12d2
+  FC_B2D,         // b2d
+  FC_NUD2,        // nu_d2
+  FC_NUH,         // nuh_scaled
+  FC_DRAG,        // drag_d2
+  FC_TOPOC,       // -(inv12d2 * topo_fac)
+  FC_GH1,         // gh[1..4]
+  FC_NORM = FC_GH1 + 4,
+  FC_LX2,
+  FC_LY2,
+  FC_COUNT
 };
 
 // A batch of runs advanced by one launch per stage (see kernels.cu).
