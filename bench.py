@@ -156,14 +156,19 @@ class Clocks:
 
 # --------------------------------------------------------------- roofline
 def bytes_per_lgp(precision):
-    """Algorithmic HBM bytes per layer-gridpoint of each step kernel:
-    rows forward reads q, f0, f1, f2 and writes q and the spectral field;
-    columns read/write the spectral field (+ the FP64 Helmholtz table);
-    rows inverse read the spectral field and write psi; the RHS reads psi and
-    q and writes f0."""
+    """Algorithmic HBM bytes per layer-gridpoint of each step kernel.
+    Plain FP64: rows forward read q, f0, f1, f2 and write q and the spectral
+    field (48); columns read/write the spectral field and read the Helmholtz
+    table (24); rows inverse read the spectral field and write psi (16); the
+    RHS reads psi and q and writes f0 (24).  Compensated FP32 with the
+    spectral zeta: rows forward read q hi/lo, f0, f1, f2 and write q hi/lo
+    and the spectral field (32); columns read the spectral field and write it
+    and the spectral zeta (12); rows inverse read both spectral fields and
+    write psi and zeta (16); the RHS reads psi, q hi and zeta and writes f0
+    (16)."""
     if precision == 0:
         return [48.0, 24.0, 16.0, 24.0]
-    return [32.0, 8.0, 8.0, 12.0]
+    return [32.0, 12.0, 16.0, 16.0]
 
 
 def fp64_ops_per_lgp(nl, M, nsweep):
@@ -215,7 +220,7 @@ def read_traffic(precision):
 
 
 KERNEL_NAMES = ["rows_fwd (AB3 + projection + x-DST)", "cols (y-DST, Helmholtz, inverse y-DST)",
-                "rows_inv (inverse x-DST + back-projection)", "rhs (Jacobian, viscosity, forcing, CFL)"]
+                "rows_inv (spectral projection + inverse x-DST)", "rhs (Jacobian, viscosity, forcing, CFL)"]
 
 
 # -------------------------------------------------------------------- ours
