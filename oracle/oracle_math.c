@@ -46,6 +46,106 @@ void om_dst1_direct(int n, int howmany, double* data, int stride, int dist) {
   free(s);
 }
 
+/* ------------------------------------------------------ 2-D real DFT pair */
+
+/* cos and sin of 2 pi m / N, m = 0..N-1, from the exactly reduced sine
+ * table: sin(2 pi m / N) = sin(pi (2m) / N) and, for even N,
+ * cos(2 pi m / N) = sin(pi (2m + N/2) / N); odd N falls back to libm. */
+static void trig_table_any(int N, double* c, double* s) {
+  if (N % 2 == 0) {
+    double* t = sin_table(N);  /* sin(pi m' / N), m' < 2N */
+    for (int m = 0; m < N; ++m) {
+      s[m] = t[(2 * (long)m) % (2 * N)];
+      c[m] = t[(2 * (long)m + N / 2) % (2 * N)];
+    }
+    free(t);
+    return;
+  }
+  for (int m = 0; m < N; ++m) {
+    c[m] = cos(2.0 * OM_PI * (double)m / (double)N);
+    s[m] = sin(2.0 * OM_PI * (double)m / (double)N);
+  }
+}
+
+/* complex DFT of length n along a strided sequence (sign -1 forward, +1
+ * backward), unnormalised, in place through a scratch copy */
+static void cdft_strided(int n, double* re, double* im, int dist, int sign, const double* c, const double* s,
+                         double* tr, double* ti) {
+  for (int k = 0; k < n; ++k) {
+    double ar = 0.0, ai = 0.0;
+    for (int j = 0; j < n; ++j) {
+      const long m = ((long)j * k) % n;
+      const double xr = re[(size_t)j * dist], xi = im[(size_t)j * dist];
+      const double wr = c[m], wi = sign * s[m];
+      ar += xr * wr - xi * wi;
+      ai += xr * wi + xi * wr;
+    }
+    tr[k] = ar;
+    ti[k] = ai;
+  }
+  for (int k = 0; k < n; ++k) {
+    re[(size_t)k * dist] = tr[k];
+    im[(size_t)k * dist] = ti[k];
+  }
+}
+
+void om_dft_r2c_2d(int n0, int n1, double* data) {
+  const int h = n1 / 2 + 1, ld = 2 * h;
+  double *c1 = malloc(sizeof(double) * n1), *s1 = malloc(sizeof(double) * n1);
+  double *c0 = malloc(sizeof(double) * n0), *s0 = malloc(sizeof(double) * n0);
+  trig_table_any(n1, c1, s1);
+  trig_table_any(n0, c0, s0);
+  double* row = malloc(sizeof(double) * (size_t)n1);
+  double *tr = malloc(sizeof(double) * (size_t)(n0 > n1 ? n0 : n1)), *ti = malloc(sizeof(double) * (size_t)(n0 > n1 ? n0 : n1));
+  /* rows: real -> half spectrum */
+  for (int r = 0; r < n0; ++r) {
+    double* d = data + (size_t)r * ld;
+    memcpy(row, d, sizeof(double) * (size_t)n1);
+    for (int k = 0; k < h; ++k) {
+      double ar = 0.0, ai = 0.0;
+      for (int j = 0; j < n1; ++j) {
+        const long m = ((long)j * k) % n1;
+        ar += row[j] * c1[m];
+        ai -= row[j] * s1[m];
+      }
+      d[2 * k] = ar;
+      d[2 * k + 1] = ai;
+    }
+  }
+  /* columns: complex forward DFT of length n0 */
+  for (int k = 0; k < h; ++k) cdft_strided(n0, data + 2 * k, data + 2 * k + 1, ld, -1, c0, s0, tr, ti);
+  free(c1); free(s1); free(c0); free(s0); free(row); free(tr); free(ti);
+}
+
+void om_dft_c2r_2d(int n0, int n1, double* data) {
+  const int h = n1 / 2 + 1, ld = 2 * h;
+  double *c1 = malloc(sizeof(double) * n1), *s1 = malloc(sizeof(double) * n1);
+  double *c0 = malloc(sizeof(double) * n0), *s0 = malloc(sizeof(double) * n0);
+  trig_table_any(n1, c1, s1);
+  trig_table_any(n0, c0, s0);
+  double *tr = malloc(sizeof(double) * (size_t)(n0 > n1 ? n0 : n1)), *ti = malloc(sizeof(double) * (size_t)(n0 > n1 ? n0 : n1));
+  double* spec = malloc(sizeof(double) * (size_t)ld);
+  /* columns: complex backward DFT of length n0 */
+  for (int k = 0; k < h; ++k) cdft_strided(n0, data + 2 * k, data + 2 * k + 1, ld, +1, c0, s0, tr, ti);
+  /* rows: half spectrum -> real, x_j = sum_k Y_k e^{+2 pi i jk/n1} over the
+   * Hermitian completion Y_{n1-k} = conj(Y_k); the k = 0 and (even n1)
+   * k = n1/2 terms contribute their real parts only */
+  for (int r = 0; r < n0; ++r) {
+    double* d = data + (size_t)r * ld;
+    memcpy(spec, d, sizeof(double) * (size_t)ld);
+    for (int j = 0; j < n1; ++j) {
+      double acc = spec[0];
+      for (int k = 1; k < h; ++k) {
+        const long m = ((long)j * k) % n1;
+        const double term = spec[2 * k] * c1[m] - spec[2 * k + 1] * s1[m];
+        acc += (n1 % 2 == 0 && k == n1 / 2) ? term : 2.0 * term;
+      }
+      d[j] = acc;
+    }
+  }
+  free(c1); free(s1); free(c0); free(s0); free(tr); free(ti); free(spec);
+}
+
 /* ------------------------------------------------------- radix-2 complex FFT */
 
 typedef struct {

@@ -30,6 +30,20 @@ void om_dst1(int n, int howmany, double* data, int stride, int dist);
 /* 2-D DST-I of a row-major (n0 rows, n1 columns) array in place. */
 void om_dst2(int n0, int n1, double* data, int fast);
 
+/* 2-D real DFT pair with FFTW's conventions (fftw_plan_dft_r2c_2d /
+ * fftw_plan_dft_c2r_2d, in place, the layout the reference's periodic
+ * inversion uses, src/elliptic.h:32-47,103-118): data holds n0 rows of
+ * 2*(n1/2+1) doubles; r2c reads n1 reals per row and writes n1/2+1 complex
+ * values per row,
+ *     Y[k0][k1] = sum_{j0,j1} x[j0][j1] exp(-2 pi i (j0 k0/n0 + j1 k1/n1));
+ * c2r is the unnormalised inverse (c2r(r2c(x)) = n0 n1 x) for Hermitian
+ * input: after the backward transform along the first dimension, the
+ * k1 = 0 and k1 = n1/2 entries of each row enter by their real parts.
+ * Direct O(n^2) sums per dimension with exactly reduced twiddle tables
+ * (accurate to a few ulp). */
+void om_dft_r2c_2d(int n0, int n1, double* data);
+void om_dft_c2r_2d(int n0, int n1, double* data);
+
 /* Eigen-decomposition of a row-major n x n matrix a that is tridiagonal
  * with a[i][i+1]*a[i+1][i] > 0 (or both zero).  Outputs as LAPACK dgeev with
  * row-major storage: eigenvalues w (unsorted), right eigenvectors in the

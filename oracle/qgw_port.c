@@ -209,15 +209,25 @@ port_run* port_create(const qgw_params* pin, int fast_dst) {
   r->nyp2 = r->ny + 2;
   r->X = calloc(r->nxp2, sizeof(double));
   r->Y = calloc(r->nyp2, sizeof(double));
-  r->K = calloc(r->nyp2, sizeof(double));
+  r->K = calloc(r->nyp2 > r->nxp2 ? r->nyp2 : r->nxp2, sizeof(double));
   r->L = calloc(r->nxp2, sizeof(double));
-  for (int i = 0; i < r->nxp2; ++i) r->X[i] = i * r->Delta;
-  for (int j = 0; j < r->nyp2; ++j) r->Y[j] = j * r->Delta;
-  for (int j = 1; j < r->ny + 1; ++j) r->K[j] = PORT_PI * j / p->Lx;
-  for (int i = 1; i < r->nx + 1; ++i) r->L[i] = PORT_PI * i / p->Lx;
-  /* init_elliptic, src/elliptic.h:102-147 (bounded) */
-  r->norm = 4.0 * (r->nx + 1) * (r->ny + 1);
-  r->wrk = calloc((size_t)r->nx * r->ny, sizeof(double));
+  const int periodic = p->bc_fac == -1;
+  /* periodic: the zero of X and Y is at the second grid point (:144-148) */
+  const int off = periodic ? -1 : 0;
+  for (int i = 0; i < r->nxp2; ++i) r->X[i] = (i + off) * r->Delta;
+  for (int j = 0; j < r->nyp2; ++j) r->Y[j] = (j + off) * r->Delta;
+  if (periodic) {
+    /* src/domain.h:163-168 (serial: K0 = 0, Nk = NXp2/2) */
+    for (int j = 0; j < r->nx; ++j) r->L[j] = 2 * PORT_PI / p->Lx * (((j + r->nx / 2) % r->nx) - r->nx / 2);
+    for (int i = 0; i < (r->nx + 2) / 2; ++i) r->K[i] = 2 * PORT_PI * i / p->Lx;
+  } else {
+    for (int j = 1; j < r->ny + 1; ++j) r->K[j] = PORT_PI * j / p->Lx;
+    for (int i = 1; i < r->nx + 1; ++i) r->L[i] = PORT_PI * i / p->Lx;
+  }
+  /* init_elliptic, src/elliptic.h:102-147: periodic rows of Nx+2 doubles
+   * (the in-place r2c layout), bounded rows of Nx */
+  r->norm = periodic ? (double)p->NX * p->NY : 4.0 * (r->nx + 1) * (r->ny + 1);
+  r->wrk = calloc((size_t)(r->nx + 2) * r->ny, sizeof(double));
   r->cl2m = calloc((size_t)r->nl * r->nl, sizeof(double));
   r->cm2l = calloc((size_t)r->nl * r->nl, sizeof(double));
   r->iRd2 = calloc(r->nl, sizeof(double));
@@ -258,8 +268,23 @@ void port_destroy(port_run* r) {
 
 /* ---------------------------------------------------- boundary values */
 
+/* adjust_bc, periodic branch, src/domain.h:225-256: South, North, West,
+ * East copies in that order (the corners end up periodic). */
+static void port_adjust_bc_periodic(port_run* r, double* f) {
+  for (int k = 0; k < r->nl; ++k) {
+    for (int i = 0; i < r->nxp2; ++i) f[IDX(r, i, 0, k)] = f[IDX(r, i, r->ny, k)];
+    for (int i = 0; i < r->nxp2; ++i) f[IDX(r, i, r->ny + 1, k)] = f[IDX(r, i, 1, k)];
+    for (int j = 0; j < r->nyp2; ++j) f[IDX(r, 0, j, k)] = f[IDX(r, r->nx, j, k)];
+    for (int j = 0; j < r->nyp2; ++j) f[IDX(r, r->nx + 1, j, k)] = f[IDX(r, 1, j, k)];
+  }
+}
+
 /* adjust_bc, bounded branch, src/domain.h:308-348. */
 static void port_adjust_bc(port_run* r, double* f, int field_type) {
+  if (r->p.bc_fac == -1) {
+    port_adjust_bc_periodic(r, f);
+    return;
+  }
   const double psi_bc = 0.0, c = 2 * r->p.bc_fac / sq(r->Delta);
   const double* psi = r->psi;
   for (int k = 0; k < r->nl; ++k) {
@@ -284,10 +309,50 @@ static void port_adjust_bc(port_run* r, double* f, int field_type) {
 
 /* ------------------------------------------------------- PV inversion */
 
+/* invert_pv, src/elliptic.h:76-155, periodic branch: rows of Nx+2 doubles
+ * (idx_fft with N_fft = Nxp2, :21), in-place r2c / c2r with the (Nx, Ny)
+ * plan shape of :41-42, the division of :103-117 and the /norm of :131. */
+static void port_invert_periodic(port_run* r) {
+  const int nl = r->nl, nx = r->nx, ny = r->ny, ld = nx + 2, nk = (nx + 2) / 2;
+  double *q = r->q, *psi = r->psi, *w = r->wrk;
+  memset(psi, 0, sizeof(double) * (size_t)r->nxp2 * r->nyp2 * nl);
+  for (int m = 0; m < nl; ++m) {
+    for (int j = 1; j < ny + 1; ++j)
+      for (int i = 1; i < nx + 1; ++i) {
+        double acc = 0;
+        for (int l = 0; l < nl; ++l) acc += r->cl2m[m * nl + l] * q[IDX(r, i, j, l)];
+        w[(size_t)(j - 1) * ld + (i - 1)] = acc;
+      }
+    om_dft_r2c_2d(nx, ny, w);
+    for (int j = 0; j < nx; ++j)
+      for (int i = 0; i < nk; ++i) {
+        double fact = -(sq(r->L[j]) + sq(r->K[i]) + r->iRd2[m]);
+        if (fact != 0) {
+          w[(size_t)j * ld + 2 * i] = w[(size_t)j * ld + 2 * i] / fact;
+          w[(size_t)j * ld + 2 * i + 1] = w[(size_t)j * ld + 2 * i + 1] / fact;
+        }
+      }
+    w[0] = 0;
+    w[1] = 0;
+    om_dft_c2r_2d(nx, ny, w);
+    for (int j = 1; j < ny + 1; ++j)
+      for (int i = 1; i < nx + 1; ++i) w[(size_t)(j - 1) * ld + (i - 1)] = w[(size_t)(j - 1) * ld + (i - 1)] / r->norm;
+    for (int j = 1; j < ny + 1; ++j)
+      for (int i = 1; i < nx + 1; ++i)
+        for (int l = 0; l < nl; ++l) psi[IDX(r, i, j, l)] += r->cm2l[l * nl + m] * w[(size_t)(j - 1) * ld + (i - 1)];
+  }
+  port_adjust_bc(r, psi, 0);
+  port_adjust_bc(r, q, 1);
+}
+
 /* invert_pv, src/elliptic.h:149-228 (bounded branch). */
 void port_invert(port_run* r) {
   const int nl = r->nl, nx = r->nx, ny = r->ny;
   double *q = r->q, *psi = r->psi, *w = r->wrk;
+  if (r->p.bc_fac == -1) {
+    port_invert_periodic(r);
+    return;
+  }
   memset(psi, 0, sizeof(double) * (size_t)r->nxp2 * r->nyp2 * nl);
   for (int m = 0; m < nl; ++m) {
     for (int j = 1; j < ny + 1; ++j)

@@ -3,8 +3,8 @@
  * reference makes, so that the reference's own src/qg.c can be compiled and
  * run in place as the oracle (test infrastructure only).
  *
- * FFTW: only the closed-basin 2-D RODFT00 plan is implemented
- * (src/elliptic.h:136-139); the periodic r2c/c2r plans return NULL.
+ * FFTW: the closed-basin 2-D RODFT00 plan (src/elliptic.h:136-139) and the
+ * periodic in-place r2c/c2r plans (src/elliptic.h:32-47).
  * The DST uses direct sums with an exactly reduced sine table unless
  * QGW_SHIM_DST=fast, which selects the O(n log n) path of oracle_math.c.
  */
@@ -18,6 +18,7 @@
 
 struct shim_fftw_plan_s {
   int n0, n1;
+  int kind;  /* 0 RODFT00 2-D, 1 r2c 2-D, 2 c2r 2-D */
   double *in, *out;
 };
 
@@ -35,18 +36,27 @@ fftw_plan fftw_plan_r2r_2d(int n0, int n1, double* in, double* out,
   return p;
 }
 
+/* in-place plans only, as the reference makes them */
 fftw_plan fftw_plan_dft_r2c_2d(int n0, int n1, double* in, fftw_complex* out, unsigned flags) {
-  (void)n0; (void)n1; (void)in; (void)out; (void)flags;
-  return NULL;
+  (void)flags;
+  if ((void*)in != (void*)out) return NULL;
+  fftw_plan p = (fftw_plan)calloc(1, sizeof(*p));
+  p->n0 = n0; p->n1 = n1; p->kind = 1; p->in = in; p->out = in;
+  return p;
 }
 
 fftw_plan fftw_plan_dft_c2r_2d(int n0, int n1, fftw_complex* in, double* out, unsigned flags) {
-  (void)n0; (void)n1; (void)in; (void)out; (void)flags;
-  return NULL;
+  (void)flags;
+  if ((void*)in != (void*)out) return NULL;
+  fftw_plan p = (fftw_plan)calloc(1, sizeof(*p));
+  p->n0 = n0; p->n1 = n1; p->kind = 2; p->in = out; p->out = out;
+  return p;
 }
 
 void fftw_execute(const fftw_plan p) {
   if (!p) return;
+  if (p->kind == 1) { om_dft_r2c_2d(p->n0, p->n1, p->out); return; }
+  if (p->kind == 2) { om_dft_c2r_2d(p->n0, p->n1, p->out); return; }
   if (p->in != p->out) memcpy(p->out, p->in, sizeof(double) * (size_t)p->n0 * p->n1);
   om_dst2(p->n0, p->n1, p->out, shim_fast());
 }

@@ -7,7 +7,8 @@ parameter file the reference ships as test/params_03.in (read here from the
 reference tree; the fixture stores the parsed values, not the file).
 
 Run in the container that holds the reference sources:
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # every case
+    python tests/golden/make_golden.py NAME ...   # only these (index merged)
 """
 from __future__ import annotations
 
@@ -69,6 +70,16 @@ def cases():
         p = parse_params_in(ref03)
         p["tend"] = 1e12
         out.append(("ref_params03", p, 30, None, None))
+    # periodic basin (bc_fac = -1): r2c/c2r inversion, periodic ghosts
+    p = C.cfg1(32)
+    p.update(bc_fac=-1.0)
+    out.append(("periodic_nx32", p, 50, 1200.0, None))
+    p = C.cfg2(32, 10)
+    p.update(bc_fac=-1.0)
+    out.append(("periodic_nx32_nl10_hyper", p, 50, 600.0, None))
+    p = C.cfg1(64)
+    p.update(bc_fac=-1.0, h_topo=150.0, w_topo=3e5)
+    out.append(("periodic_topo_nx64", p, 30, 1200.0, None))
     return out
 
 
@@ -76,9 +87,16 @@ def main():
     O.build(ref=True)
     if not O.ref_available():
         raise SystemExit("reference build unavailable")
+    only = set(sys.argv[1:])
+    index_path = os.path.join(HERE, "index.json")
     index = {}
-    for name, params, nsteps, dt, topo in cases():
-        seed = 7000 + len(index)
+    if only and os.path.exists(index_path):
+        with open(index_path) as f:
+            index = json.load(f)
+    for n, (name, params, nsteps, dt, topo) in enumerate(cases()):
+        if only and name not in only:
+            continue
+        seed = 7000 + n
         q0 = C.noise_ic(params, seed)
         r = O.run_ref(params, q0, nsteps, dt_fixed=dt, fast_dst=False)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), q0=q0, psi=r["psi"], q=r["q"],
@@ -86,7 +104,7 @@ def main():
         index[name] = {"params": params, "nsteps": nsteps, "dt_fixed": dt, "seed": seed,
                        "time": r["time"]}
         print(name, r["time"])
-    with open(os.path.join(HERE, "index.json"), "w") as f:
+    with open(index_path, "w") as f:
         json.dump(index, f, indent=1, sort_keys=True)
 
 
