@@ -234,6 +234,68 @@ static const double* sin_get(int M) {
   return NULL;
 }
 
+/* ------------------------------------------------ fast 2-D real DFT pair */
+/* Same transforms as om_dft_r2c_2d / om_dft_c2r_2d for power-of-two sizes,
+ * through the radix-2 complex FFT (rows as complex sequences with zero
+ * imaginary part; the backward transform as conj(FFT(conj))). */
+static int pow2_ok(int n) { return n >= 2 && (n & (n - 1)) == 0; }
+
+static void r2c_2d_fast(int n0, int n1, double* data) {
+  const int h = n1 / 2 + 1, ld = 2 * h;
+  const om_fft_plan* p1 = fft_plan_get(n1);
+  const om_fft_plan* p0 = fft_plan_get(n0);
+  const int nmax = n0 > n1 ? n0 : n1;
+  double *re = malloc(sizeof(double) * (size_t)nmax), *im = malloc(sizeof(double) * (size_t)nmax);
+  for (int r = 0; r < n0; ++r) {
+    double* d = data + (size_t)r * ld;
+    for (int j = 0; j < n1; ++j) { re[j] = d[j]; im[j] = 0.0; }
+    fft_exec(p1, re, im);
+    for (int k = 0; k < h; ++k) { d[2 * k] = re[k]; d[2 * k + 1] = im[k]; }
+  }
+  for (int k = 0; k < h; ++k) {
+    for (int r = 0; r < n0; ++r) { re[r] = data[(size_t)r * ld + 2 * k]; im[r] = data[(size_t)r * ld + 2 * k + 1]; }
+    fft_exec(p0, re, im);
+    for (int r = 0; r < n0; ++r) { data[(size_t)r * ld + 2 * k] = re[r]; data[(size_t)r * ld + 2 * k + 1] = im[r]; }
+  }
+  free(re); free(im);
+}
+
+static void c2r_2d_fast(int n0, int n1, double* data) {
+  const int h = n1 / 2 + 1, ld = 2 * h;
+  const om_fft_plan* p1 = fft_plan_get(n1);
+  const om_fft_plan* p0 = fft_plan_get(n0);
+  const int nmax = n0 > n1 ? n0 : n1;
+  double *re = malloc(sizeof(double) * (size_t)nmax), *im = malloc(sizeof(double) * (size_t)nmax);
+  for (int k = 0; k < h; ++k) {
+    for (int r = 0; r < n0; ++r) { re[r] = data[(size_t)r * ld + 2 * k]; im[r] = -data[(size_t)r * ld + 2 * k + 1]; }
+    fft_exec(p0, re, im);
+    for (int r = 0; r < n0; ++r) { data[(size_t)r * ld + 2 * k] = re[r]; data[(size_t)r * ld + 2 * k + 1] = -im[r]; }
+  }
+  for (int r = 0; r < n0; ++r) {
+    double* d = data + (size_t)r * ld;
+    /* Hermitian completion; k = 0 and k = n1/2 by their real parts */
+    re[0] = d[0]; im[0] = 0.0;
+    for (int k = 1; k < n1 / 2; ++k) {
+      re[k] = d[2 * k]; im[k] = -d[2 * k + 1];
+      re[n1 - k] = d[2 * k]; im[n1 - k] = d[2 * k + 1];
+    }
+    re[n1 / 2] = d[n1]; im[n1 / 2] = 0.0;
+    fft_exec(p1, re, im);
+    for (int j = 0; j < n1; ++j) d[j] = re[j];
+  }
+  free(re); free(im);
+}
+
+void om_dft_r2c_2d_any(int n0, int n1, double* data, int fast) {
+  if (fast && pow2_ok(n0) && pow2_ok(n1)) r2c_2d_fast(n0, n1, data);
+  else om_dft_r2c_2d(n0, n1, data);
+}
+
+void om_dft_c2r_2d_any(int n0, int n1, double* data, int fast) {
+  if (fast && pow2_ok(n0) && pow2_ok(n1)) c2r_2d_fast(n0, n1, data);
+  else om_dft_c2r_2d(n0, n1, data);
+}
+
 /* ------------------------------------------------------------- fast DST-I */
 /*
  * DST-I of length n = M-1 through a real DFT of length M (a published

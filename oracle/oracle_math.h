@@ -43,6 +43,10 @@ void om_dst2(int n0, int n1, double* data, int fast);
  * (accurate to a few ulp). */
 void om_dft_r2c_2d(int n0, int n1, double* data);
 void om_dft_c2r_2d(int n0, int n1, double* data);
+/* The same, through a radix-2 FFT when fast != 0 and both sizes are powers
+ * of two (agrees with the direct sums to round-off). */
+void om_dft_r2c_2d_any(int n0, int n1, double* data, int fast);
+void om_dft_c2r_2d_any(int n0, int n1, double* data, int fast);
 
 /* Eigen-decomposition of a row-major n x n matrix a that is tridiagonal
  * with a[i][i+1]*a[i+1][i] > 0 (or both zero).  Outputs as LAPACK dgeev with

@@ -323,7 +323,7 @@ static void port_invert_periodic(port_run* r) {
         for (int l = 0; l < nl; ++l) acc += r->cl2m[m * nl + l] * q[IDX(r, i, j, l)];
         w[(size_t)(j - 1) * ld + (i - 1)] = acc;
       }
-    om_dft_r2c_2d(nx, ny, w);
+    om_dft_r2c_2d_any(nx, ny, w, r->fast);
     for (int j = 0; j < nx; ++j)
       for (int i = 0; i < nk; ++i) {
         double fact = -(sq(r->L[j]) + sq(r->K[i]) + r->iRd2[m]);
@@ -334,7 +334,7 @@ static void port_invert_periodic(port_run* r) {
       }
     w[0] = 0;
     w[1] = 0;
-    om_dft_c2r_2d(nx, ny, w);
+    om_dft_c2r_2d_any(nx, ny, w, r->fast);
     for (int j = 1; j < ny + 1; ++j)
       for (int i = 1; i < nx + 1; ++i) w[(size_t)(j - 1) * ld + (i - 1)] = w[(size_t)(j - 1) * ld + (i - 1)] / r->norm;
     for (int j = 1; j < ny + 1; ++j)

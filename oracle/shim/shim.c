@@ -55,8 +55,8 @@ fftw_plan fftw_plan_dft_c2r_2d(int n0, int n1, fftw_complex* in, double* out, un
 
 void fftw_execute(const fftw_plan p) {
   if (!p) return;
-  if (p->kind == 1) { om_dft_r2c_2d(p->n0, p->n1, p->out); return; }
-  if (p->kind == 2) { om_dft_c2r_2d(p->n0, p->n1, p->out); return; }
+  if (p->kind == 1) { om_dft_r2c_2d_any(p->n0, p->n1, p->out, shim_fast()); return; }
+  if (p->kind == 2) { om_dft_c2r_2d_any(p->n0, p->n1, p->out, shim_fast()); return; }
   if (p->in != p->out) memcpy(p->out, p->in, sizeof(double) * (size_t)p->n0 * p->n1);
   om_dst2(p->n0, p->n1, p->out, shim_fast());
 }

@@ -105,12 +105,18 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   a.nl = r->nl;
   a.pitch = r->pitch;
   a.lstride = (long long)r->lstride;
-  a.gx = qgw::make_geom(r->nx + 1);
-  a.gy = qgw::make_geom(r->ny + 1);
+  const bool per = p.bc_fac == -1;
+  a.periodic = per ? 1 : 0;
+  // closed basin: DST-I of length n along x and y (M = n + 1); periodic:
+  // real FFT of length NX along x (a complex FFT of NX/2: M = NX) and
+  // complex FFT of length NY along y (M = 2 NY)
+  const int Mx = per ? r->nx : r->nx + 1, My = per ? 2 * r->ny : r->ny + 1;
+  a.gx = qgw::make_geom(Mx);
+  a.gy = qgw::make_geom(My);
   int rc;
-  // DST tables for x and y
+  // transform tables for x and y
   for (int dim = 0; dim < 2; ++dim) {
-    const int M = dim == 0 ? r->nx + 1 : r->ny + 1;
+    const int M = dim == 0 ? Mx : My;
     qgw::DstTablesHost th = qgw::build_dst_tables(M);
     T *tw, *pre, *spl;
     if ((rc = upload<T>(r, &tw, th.tw))) return rc;
@@ -136,9 +142,21 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   if ((rc = dalloc(r, &a.psi, field))) return rc;
   if ((rc = dalloc(r, &a.spec, field))) return rc;
   if ((rc = dalloc(r, &a.fab, 3 * field))) return rc;
-  std::vector<double> Lsq(r->nx), Ksq(r->ny);
-  for (int k = 0; k < r->nx; ++k) { const double L = M_PI * (k + 1) / p.Lx; Lsq[k] = L * L; }
-  for (int j = 0; j < r->ny; ++j) { const double K = M_PI * (j + 1) / p.Lx; Ksq[j] = K * K; }
+  // squared wavenumbers: closed basin L_{k+1}, K_{j+1} (src/domain.h:170-173);
+  // periodic K_k = 2 pi k / Lx along x (k <= NX/2) and L_j = 2 pi f(j) / Lx
+  // along y with the signed frequency f(j) (src/domain.h:163-168), both with
+  // Lx as the reference has them
+  std::vector<double> Lsq(r->nx, 0.0), Ksq(r->ny);
+  if (per) {
+    for (int k = 0; k <= r->nx / 2; ++k) { const double L = 2 * M_PI * k / p.Lx; Lsq[k] = L * L; }
+    for (int j = 0; j < r->ny; ++j) {
+      const double K = 2 * M_PI / p.Lx * (((j + r->ny / 2) % r->ny) - r->ny / 2);
+      Ksq[j] = K * K;
+    }
+  } else {
+    for (int k = 0; k < r->nx; ++k) { const double L = M_PI * (k + 1) / p.Lx; Lsq[k] = L * L; }
+    for (int j = 0; j < r->ny; ++j) { const double K = M_PI * (j + 1) / p.Lx; Ksq[j] = K * K; }
+  }
   double *dL, *dK;
   if ((rc = upload<double>(r, &dL, Lsq))) return rc;
   if ((rc = upload<double>(r, &dK, Ksq))) return rc;
@@ -153,12 +171,16 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   if (r->precision == QGW_FP64) {
     // 1 / (fact * norm), fact = -(sq(L[i]) + sq(K[j]) + iRd2[k]) as in
     // invert_pv, src/elliptic.h:195-200 and the /norm of :207-211
+    // periodic: one factor per complex value k <= NX/2; the mean is removed
+    // (src/elliptic.h:103-117), a zero factor elsewhere is never hit
     std::vector<double> h(field, 0.0);
+    const int nk = per ? r->nx / 2 + 1 : r->nx;
     for (int m = 0; m < r->nl; ++m)
       for (int j = 0; j < r->ny; ++j)
-        for (int k = 0; k < r->nx; ++k) {
+        for (int k = 0; k < nk; ++k) {
           const double fact = -(Lsq[k] + Ksq[j] + r->iRd2[m]);
-          h[(size_t)m * r->lstride + (size_t)j * r->pitch + k] = 1.0 / (fact * r->norm);
+          const bool mean = per && j == 0 && k == 0;
+          h[(size_t)m * r->lstride + (size_t)j * r->pitch + k] = (mean || fact == 0) ? 0.0 : 1.0 / (fact * r->norm);
         }
     double* dh;
     if ((rc = upload<double>(r, &dh, h))) return rc;
@@ -194,8 +216,8 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   a.topo_fac = p.f0 / dhb;
   a.has_topo = 0;
   a.has_wind = p.tau0 != 0;
-  a.G1 = mode_group(r->nl, r->nx + 1, sizeof(T), row_budget(sizeof(T)), 1, 16, 16);
-  a.G3 = mode_group(r->nl, r->nx + 1, sizeof(T), 110 * 1024, 1, 16, inv_group(0));
+  a.G1 = mode_group(r->nl, Mx, sizeof(T), row_budget(sizeof(T)), 1, 16, 16);
+  a.G3 = mode_group(r->nl, Mx, sizeof(T), 110 * 1024, 1, 16, inv_group(0));
   a.CT = 0;
   a.low_k64 = 8;
   // 16-byte column vectors: rows 16-byte aligned and a whole number of
@@ -215,10 +237,17 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
     if ((rc = dalloc(r, &a.spec2, field))) return rc;
     if ((rc = dalloc(r, &a.zeta, field))) return rc;
     // K3 transforms psi and zeta rows of each mode: two rows per mode
-    a.G3 = mode_group(r->nl, r->nx + 1, sizeof(T), 110 * 1024, 2, 8, inv_group(1));
-    std::vector<double> sx(r->nx), sy(r->ny);
-    for (int k = 0; k < r->nx; ++k) { const double s = std::sin(M_PI * (k + 1) / (2.0 * (r->nx + 1))); sx[k] = s * s; }
-    for (int j = 0; j < r->ny; ++j) { const double s = std::sin(M_PI * (j + 1) / (2.0 * (r->ny + 1))); sy[j] = s * s; }
+    a.G3 = mode_group(r->nl, Mx, sizeof(T), 110 * 1024, 2, 8, inv_group(1));
+    // symbol of the 5-point Laplacian: DST-I basis sin^2(pi k / 2(n+1));
+    // periodic Fourier basis sin^2(pi k / N)
+    std::vector<double> sx(r->nx, 0.0), sy(r->ny);
+    if (per) {
+      for (int k = 0; k <= r->nx / 2; ++k) { const double s = std::sin(M_PI * k / r->nx); sx[k] = s * s; }
+      for (int j = 0; j < r->ny; ++j) { const double s = std::sin(M_PI * j / r->ny); sy[j] = s * s; }
+    } else {
+      for (int k = 0; k < r->nx; ++k) { const double s = std::sin(M_PI * (k + 1) / (2.0 * (r->nx + 1))); sx[k] = s * s; }
+      for (int j = 0; j < r->ny; ++j) { const double s = std::sin(M_PI * (j + 1) / (2.0 * (r->ny + 1))); sy[j] = s * s; }
+    }
     double *dsx, *dsy;
     if ((rc = upload<double>(r, &dsx, sx))) return rc;
     if ((rc = upload<double>(r, &dsy, sy))) return rc;
@@ -279,8 +308,9 @@ const char* qgw_strerror(int s) {
 
 int qgw_footprint(const qgw_params* p, int precision, size_t* bytes) {
   if (!p || !bytes) return QGW_ERR_PARAM;
-  const size_t nx = p->NX - (p->bc_fac >= 0 ? 1 : 0), ny = p->NY - (p->bc_fac >= 0 ? 1 : 0);
-  const size_t field = (size_t)p->nl * ny * (nx + 1);
+  const bool per = p->bc_fac == -1;
+  const size_t nx = p->NX - (per ? 0 : 1), ny = p->NY - (per ? 0 : 1);
+  const size_t field = (size_t)p->nl * ny * (nx + (per ? 4 : 1));
   size_t b;
   if (precision == QGW_FP64) b = field * 8 * 7;  // q psi spec f0 f1 f2 hinv
   else b = field * 4 * 9 + field * 8;            // q_hi q_lo psi spec spec2 zeta f0 f1 f2 + FP64 staging
@@ -294,7 +324,12 @@ int qgw_create(const qgw_params* pin, const double* cl2m, const double* cm2l, co
   *out = nullptr;
   if (precision != QGW_FP64 && precision != QGW_FP32C) return QGW_ERR_PARAM;
   const qgw_params& p = *pin;
-  if (p.bc_fac < 0) return QGW_ERR_UNSUPPORTED;            // periodic basin
+  const bool per = p.bc_fac == -1;
+  // negative bc_fac other than the periodic flag has no meaning in the reference
+  if (p.bc_fac < 0 && !per) return QGW_ERR_UNSUPPORTED;
+  // periodic: the reference's r2c layout (src/elliptic.h:21,41) is only
+  // consistent for a square grid; the real FFT needs NX >= 8
+  if (per && (p.NX != p.NY || p.NX < 8)) return QGW_ERR_UNSUPPORTED;
   if (p.k_f != 0 || p.dt_forc_period != 0) return QGW_ERR_UNSUPPORTED;  // stochastic / 4-D forcing
   if (!pow2(p.NX) || !pow2(p.NY) || p.NX > 8192 || p.NY > 8192) return QGW_ERR_UNSUPPORTED;
   if (p.nl < 1 || p.nl > QGW_NL_GPU_MAX) return QGW_ERR_UNSUPPORTED;
@@ -302,14 +337,15 @@ int qgw_create(const qgw_params* pin, const double* cl2m, const double* cm2l, co
   qgw_run* r = new qgw_run();
   r->precision = precision;
   r->p = p;
-  r->nx = p.NX - 1;
-  r->ny = p.NY - 1;
+  r->nx = per ? p.NX : p.NX - 1;
+  r->ny = per ? p.NY : p.NY - 1;
   r->nl = p.nl;
-  r->pitch = r->nx + 1;
+  // periodic rows also hold the NX/2 + 1 complex values of a spectral row
+  r->pitch = per ? r->nx + 4 : r->nx + 1;
   r->lstride = (size_t)r->ny * r->pitch;
   r->Delta = p.Lx / p.NX;
   r->Ly = p.NY * r->Delta;
-  r->norm = 4.0 * (r->nx + 1) * (r->ny + 1);
+  r->norm = per ? (double)p.NX * p.NY : 4.0 * (r->nx + 1) * (r->ny + 1);
   r->cl2m.resize((size_t)r->nl * r->nl);
   r->cm2l.resize((size_t)r->nl * r->nl);
   r->iRd2.resize(r->nl);
@@ -552,7 +588,7 @@ int qgw_get(qgw_run* r, double* psi, double* q) {
   if (!r->has_q) return QGW_ERR_STATE;
   // psi is the inversion of the current q; q alone needs it only for the
   // ghost values of a no-slip or partial-slip wall
-  if (psi || r->p.bc_fac != 0) enqueue_invert(r);
+  if (psi || (r->p.bc_fac != 0 && r->p.bc_fac != -1)) enqueue_invert(r);
   const size_t field = (size_t)r->nl * r->lstride;
   if (psi) {
     const void* src = r->a64.psi;
@@ -580,6 +616,20 @@ int qgw_get(qgw_run* r, double* psi, double* q) {
   // (src/elliptic.h:225-226, src/domain.h:308-348)
   const int nxp2 = r->nx + 2, nyp2 = r->ny + 2;
   const size_t L = (size_t)nxp2 * nyp2;
+  if (r->p.bc_fac == -1) {
+    // periodic copies, South, North, West, East in turn (src/domain.h:225-256)
+    for (double* F : {psi, q}) {
+      if (!F) continue;
+      for (int k = 0; k < r->nl; ++k) {
+        double* f = F + k * L;
+        for (int i = 0; i < nxp2; ++i) f[i] = f[(size_t)r->ny * nxp2 + i];
+        for (int i = 0; i < nxp2; ++i) f[(size_t)(nyp2 - 1) * nxp2 + i] = f[(size_t)nxp2 + i];
+        for (int j = 0; j < nyp2; ++j) f[(size_t)j * nxp2] = f[(size_t)j * nxp2 + r->nx];
+        for (int j = 0; j < nyp2; ++j) f[(size_t)j * nxp2 + nxp2 - 1] = f[(size_t)j * nxp2 + 1];
+      }
+    }
+    return QGW_OK;
+  }
   const double c = 2 * r->p.bc_fac / (r->Delta * r->Delta);
   const double* ps = psi;
   if (q && !psi && c != 0) {

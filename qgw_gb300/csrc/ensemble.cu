@@ -69,7 +69,6 @@ void set_grids(qgw::EnsembleCore* e) {
 // member table, per-stage work lists and shared-memory sizes
 int build_tables(qgw::EnsembleCore* e) {
   const int n = (int)e->members.size();
-  const int ct = e->precision == QGW_FP64 ? qgw::cols_per_tile_f64() : qgw::cols_per_tile_f32c();
   const int tx = qgw::rhs_tile_x(), ty = qgw::rhs_tile_y();
   const size_t L = (size_t)n + 1;
   std::vector<int> lists(3 * L + 4 + 4 * (L + 4), 0);
@@ -83,7 +82,8 @@ int build_tables(qgw::EnsembleCore* e) {
     const int R = e->precision == QGW_FP64 ? qgw::rhs_halo_of_f64(r->a64) : qgw::rhs_halo_of_f32c(r->a32);
     const int tiles = ((r->nx + tx - 1) / tx) * ((r->ny + ty - 1) / ty) * r->nl;
     rows[i + 1] = rows[i] + r->ny;
-    cols[i + 1] = cols[i] + ((r->nx + ct - 1) / ct) * r->nl;
+    const int ctiles = e->precision == QGW_FP64 ? qgw::col_tiles_f64(r->a64) : qgw::col_tiles_f32c(r->a32);
+    cols[i + 1] = cols[i] + ctiles * r->nl;
     rhs[i + 1] = rhs[i] + tiles;
     for (int h = 1; h <= 4; ++h) rr[h][i + 1] = rr[h][i] + (h == R ? tiles : 0);
   }
@@ -126,8 +126,9 @@ int build_tables(qgw::EnsembleCore* e) {
 }
 
 void launch_step(qgw::EnsembleCore* e, int mask) {
-  if (e->precision == QGW_FP64) qgw::ens_step_f64(e->e64, e->r64, e->sm, e->grid, e->rhs_grid, mask, e->stream);
-  else qgw::ens_step_f32c(e->e32, e->r32, e->sm, e->grid, e->rhs_grid, mask, e->stream);
+  if (e->precision == QGW_FP64)
+    qgw::ens_step_f64(e->e64, e->r64, e->sm, e->grid, e->rhs_grid, mask, e->periodic, e->stream);
+  else qgw::ens_step_f32c(e->e32, e->r32, e->sm, e->grid, e->rhs_grid, mask, e->periodic, e->stream);
 }
 
 int ensure_graph(qgw::EnsembleCore* e) {
@@ -169,6 +170,11 @@ int qgw_ensemble_create(int n, const qgw_params* params, int precision, qgw_ense
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(QGW_ERR_CUDA);
   if (cudaDeviceGetAttribute(&e->nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return fail(QGW_ERR_CUDA);
   if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(QGW_ERR_CUDA);
+  // one boundary kind per ensemble: the row and column kernels of a launch
+  // use either the DST-I (closed basin) or the FFT (periodic)
+  e->periodic = params[0].bc_fac == -1;
+  for (int i = 0; i < n; ++i)
+    if ((params[i].bc_fac == -1) != (e->periodic != 0)) return fail(QGW_ERR_UNSUPPORTED);
   for (int i = 0; i < n; ++i) {
     qgw_run* r = nullptr;
     if ((rc = qgw_create(&params[i], nullptr, nullptr, nullptr, nullptr, precision, &r))) return fail(rc);

@@ -14,6 +14,7 @@ namespace qgw {
 
 struct EnsembleCore {
   int precision = 0;
+  int periodic = 0;               // all members doubly periodic (else all bounded)
   int nsm = 0;
   cudaStream_t stream = nullptr;
   std::vector<qgw_run*> members;  // not owned by the core

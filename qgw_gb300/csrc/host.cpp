@@ -288,7 +288,8 @@ extern "C" int qgw_topo(const qgw_params* p, double* topo) {
   auto shelf = [](double x, double d) { return 1 - std::exp(-(x * x) / (2 * (d * d))); };
   for (int j = 0; j < ny + 2; ++j)
     for (int i = 0; i < nx + 2; ++i) {
-      const double X = i * Delta, Y = j * Delta;
+      const int off = p->bc_fac == -1 ? -1 : 0;  // src/domain.h:144-148
+      const double X = (i + off) * Delta, Y = (j + off) * Delta;
       topo[(size_t)j * (nx + 2) + i] =
           p->h_topo * (1 - shelf(X, p->w_topo) * shelf(p->Lx - X, p->w_topo) * shelf(Y, p->w_topo) *
                                shelf(Ly - Y, p->w_topo));
@@ -301,6 +302,7 @@ extern "C" int qgw_topo(const qgw_params* p, double* topo) {
 double qgw_host_wind(const qgw_params* p, int j) {
   const double Delta = p->Lx / p->NX;
   const double Ly = p->NY * Delta;
-  const double Y = j * Delta;
+  // periodic runs put the zero of Y at the second grid point (src/domain.h:144-148)
+  const double Y = (j + (p->bc_fac == -1 ? -1 : 0)) * Delta;
   return (-p->tau0 / p->dh[0] * p->forc_mode * kPi / Ly * std::sin(p->forc_mode * kPi * (Y) / Ly));
 }

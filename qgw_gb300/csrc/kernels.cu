@@ -24,6 +24,7 @@
 #include <algorithm>
 
 #include "dst_fixed.cuh"
+#include "periodic.cuh"
 #include "kernels.h"
 #include "qgw_device.cuh"
 
@@ -240,7 +241,9 @@ __device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool up
   }
 }
 
-template <typename T, bool COMP>
+// PER: doubly periodic basin -- real FFT of the row instead of the DST-I;
+// the spectral row holds X_0..X_H as (re, im) pairs (nx + 2 reals).
+template <typename T, bool COMP, bool PER>
 __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mode, int j, unsigned char* smem_raw,
                                               T* tot, T* cst) {
   DevState* st = a.state;
@@ -274,10 +277,11 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
       default: project_fwd<T, COMP, 16>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst); break;
     }
     __syncthreads();
-    T* O = dst_block<T>(A, B, G, ld, a.gx, a.tx, tot);
+    T* O = PER ? rfft_block<T>(A, B, G, ld, a.gx, a.tx) : dst_block<T>(A, B, G, ld, a.gx, a.tx, tot);
+    const int nout = PER ? a.nx + 2 : a.nx;
     for (int gg = 0; gg < G; ++gg) {
       T* dstrow = a.spec + (size_t)(m0 + gg) * a.lstride + (size_t)j * a.pitch;
-      for (int i = threadIdx.x; i < a.nx; i += NT) dstrow[i] = O[gg * ld + pr(i)];
+      for (int i = threadIdx.x; i < nout; i += NT) dstrow[i] = O[gg * ld + pr(i)];
     }
     __syncthreads();
   }
@@ -410,6 +414,104 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
   }
 }
 
+// ------------------------------------------------------------- K2 periodic
+// Two complex columns k = 2 bx, 2 bx + 1 (one tile of four reals) of one mode
+// per block: complex FFT along y, Helmholtz divide, backward FFT (as the
+// conjugate of the forward FFT of the conjugate), in zeta mode also the
+// spectral 5-point Laplacian of psi.  Columns k > nx/2 are padding.
+template <typename T, bool COMP>
+__device__ __forceinline__ void body_cols_per(const StepArgs<T>& a, int step_mode, int bx, int m, unsigned char* smem_raw) {
+  constexpr int CC = 2;
+  DevState* st = a.state;
+  if (step_mode && !st->active) return;
+  const int H = a.gx.H;  // x: complex columns k = 0..H
+  const int k0 = bx * CC;
+  const int ld = padded_len(a.gy.M);
+  T* A = (T*)smem_raw;
+  T* B = A + (size_t)CC * ld;
+  T* C = B + (size_t)CC * ld;  // zeta mode only
+  T* S = a.spec + (size_t)m * a.lstride;
+  const int ny = a.ny;
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+  for (int jj = tid; jj < ny; jj += NT) {
+    T v[4];
+    load_cols<T, 4>(S + (size_t)jj * a.pitch + 2 * k0, v);
+    const int pj = pc(jj);
+    C2<T>* A0 = (C2<T>*)A;
+    C2<T>* A1 = (C2<T>*)(A + ld);
+    C2<T> z0, z1;
+    z0.x = v[0]; z0.y = v[1]; z1.x = v[2]; z1.y = v[3];
+    A0[pj] = z0;
+    A1[pj] = z1;
+  }
+  __syncthreads();
+  T* O = cfft_block<T>(A, B, CC, ld, a.gy, a.ty.tw);
+  const bool zm = COMP && a.zeta_mode;
+  const double iRd2 = a.iRd2[m];
+  const float ird2f = COMP ? a.iRd2f[m] : 0.f;
+  const float normf = a.fc[FC_NORM], lx2f = a.fc[FC_LX2], ly2f = a.fc[FC_LY2];
+  for (int w = tid; w < CC * ny; w += NT) {
+    const int c = w / ny, jj = w - c * ny;
+    const int k = k0 + c;
+    C2<T>* Oc = (C2<T>*)(O + c * ld);
+    const int pj = pc(jj);
+    C2<T> X = Oc[pj];
+    if (k > H || (k == 0 && jj == 0)) {
+      // padding columns; the mean is removed (src/elliptic.h:114-117)
+      X.x = T(0);
+      X.y = T(0);
+    } else if (!COMP) {
+      const T h = (T)a.hinv[(size_t)m * a.lstride + (size_t)jj * a.pitch + k];
+      X.x = X.x * h;
+      X.y = X.y * h;
+    } else {
+      const int fy = jj <= ny / 2 ? jj : ny - jj;  // |y wavenumber index|
+      if (m == 0 && fy < a.low_k64 && k < a.low_k64) {
+        // barotropic mode, lowest wavenumbers: divide in FP64
+        const double fact = -(a.Lsq[k] + a.Ksq[jj] + iRd2);
+        X.x = (T)((double)X.x / fact / a.norm);
+        X.y = (T)((double)X.y / fact / a.norm);
+      } else {
+        const float fact = -((a.Lsqf[k] + a.Ksqf[jj]) + ird2f);
+        X.x = (T)((float)X.x / (fact * normf));
+        X.y = (T)((float)X.y / (fact * normf));
+      }
+    }
+    if (zm) {
+      const int kk = k > H ? H : k;
+      const float lam = lx2f * a.sx2f[kk] + ly2f * a.sy2f[jj];
+      C2<T> Z;
+      Z.x = (T)(lam * (float)X.x);
+      Z.y = -(T)(lam * (float)X.y);
+      ((C2<T>*)(C + c * ld))[pj] = Z;
+    }
+    X.y = -X.y;  // conjugate: backward FFT = conj(FFT(conj))
+    Oc[pj] = X;
+  }
+  __syncthreads();
+  T* Oth = (O == A) ? B : A;
+  T* O2 = cfft_block<T>(O, Oth, CC, ld, a.gy, a.ty.tw);
+  for (int jj = tid; jj < ny; jj += NT) {
+    const int pj = pc(jj);
+    const C2<T> z0 = ((const C2<T>*)O2)[pj];
+    const C2<T> z1 = ((const C2<T>*)(O2 + ld))[pj];
+    T v[4] = {z0.x, -z0.y, z1.x, -z1.y};
+    store_cols<T, 4>(S + (size_t)jj * a.pitch + 2 * k0, v);
+  }
+  if (zm) {
+    __syncthreads();
+    T* O3 = cfft_block<T>(C, O2 == A ? B : A, CC, ld, a.gy, a.ty.tw);
+    T* S2 = a.spec2 + (size_t)m * a.lstride;
+    for (int jj = tid; jj < ny; jj += NT) {
+      const int pj = pc(jj);
+      const C2<T> z0 = ((const C2<T>*)O3)[pj];
+      const C2<T> z1 = ((const C2<T>*)(O3 + ld))[pj];
+      T v[4] = {z0.x, -z0.y, z1.x, -z1.y};
+      store_cols<T, 4>(S2 + (size_t)jj * a.pitch + 2 * k0, v);
+    }
+  }
+}
+
 // ------------------------------------------------------------------ K3
 // One block per row j; LAYER groups in turn.  The mode -> layer projection
 // is linear and acts point by point, so it commutes with the x-DST: each
@@ -418,8 +520,9 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
 // and writes psi_l (zeta_l) once.  The spectral rows of row j are re-read by
 // each group (from cache); nothing is accumulated in global memory.
 template <typename T, bool ZM, int GB>
-__device__ __forceinline__ void project_spec(const StepArgs<T>& a, int j, int G, T* A, int ld, const T* cst) {
-  for (int i = threadIdx.x; i < a.nx; i += NT) {
+__device__ __forceinline__ void project_spec(const StepArgs<T>& a, int j, int G, T* A, int ld, const T* cst,
+                                             int ncols) {
+  for (int i = threadIdx.x; i < ncols; i += NT) {
     T acc[GB], zacc[ZM ? GB : 1];
 #pragma unroll
     for (int g = 0; g < GB; ++g) {
@@ -450,7 +553,7 @@ __device__ __forceinline__ void project_spec(const StepArgs<T>& a, int j, int G,
   }
 }
 
-template <typename T, bool COMP>
+template <typename T, bool COMP, bool PER>
 __device__ __forceinline__ void body_rows_inv(const StepArgs<T>& a, int step_mode, int j, unsigned char* smem_raw,
                                               T* tot, T* cst) {
   DevState* st = a.state;
@@ -468,30 +571,35 @@ __device__ __forceinline__ void body_rows_inv(const StepArgs<T>& a, int step_mod
       cst[w] = g < G ? a.cm2l[(size_t)(l0 + g) * a.nl + m] : T(0);
     }
     __syncthreads();
+    const int ncols = PER ? a.nx + 2 : a.nx;
     if (zm) {
       switch (GB) {
-        case 1: project_spec<T, true, 1>(a, j, G, A, ld, cst); break;
-        case 2: project_spec<T, true, 2>(a, j, G, A, ld, cst); break;
-        case 4: project_spec<T, true, 4>(a, j, G, A, ld, cst); break;
-        default: project_spec<T, true, 8>(a, j, G, A, ld, cst); break;
+        case 1: project_spec<T, true, 1>(a, j, G, A, ld, cst, ncols); break;
+        case 2: project_spec<T, true, 2>(a, j, G, A, ld, cst, ncols); break;
+        case 4: project_spec<T, true, 4>(a, j, G, A, ld, cst, ncols); break;
+        default: project_spec<T, true, 8>(a, j, G, A, ld, cst, ncols); break;
       }
     } else {
       switch (GB) {
-        case 1: project_spec<T, false, 1>(a, j, G, A, ld, cst); break;
-        case 2: project_spec<T, false, 2>(a, j, G, A, ld, cst); break;
-        case 4: project_spec<T, false, 4>(a, j, G, A, ld, cst); break;
-        case 8: project_spec<T, false, 8>(a, j, G, A, ld, cst); break;
-        default: project_spec<T, false, 16>(a, j, G, A, ld, cst); break;
+        case 1: project_spec<T, false, 1>(a, j, G, A, ld, cst, ncols); break;
+        case 2: project_spec<T, false, 2>(a, j, G, A, ld, cst, ncols); break;
+        case 4: project_spec<T, false, 4>(a, j, G, A, ld, cst, ncols); break;
+        case 8: project_spec<T, false, 8>(a, j, G, A, ld, cst, ncols); break;
+        default: project_spec<T, false, 16>(a, j, G, A, ld, cst, ncols); break;
       }
     }
     __syncthreads();
-    T* O = dst_block<T>(A, B, zm ? 2 * G : G, ld, a.gx, a.tx, tot);
+    const int nrow = zm ? 2 * G : G;
+    T* O = PER ? irfft_block<T>(A, B, nrow, ld, a.gx, a.tx) : dst_block<T>(A, B, nrow, ld, a.gx, a.tx, tot);
+    // periodic: x_{2m+1} is minus the imaginary part of the backward FFT
+    const T odd = PER ? T(-1) : T(1);
     for (int g = 0; g < G; ++g) {
       T* prow = a.psi + (size_t)(l0 + g) * a.lstride + (size_t)j * a.pitch;
-      for (int i = threadIdx.x; i < a.nx; i += NT) prow[i] = O[g * ld + pr(i)];
+      for (int i = threadIdx.x; i < a.nx; i += NT) prow[i] = (i & 1) ? odd * O[g * ld + pr(i)] : O[g * ld + pr(i)];
       if (zm) {
         T* zrow = a.zeta + (size_t)(l0 + g) * a.lstride + (size_t)j * a.pitch;
-        for (int i = threadIdx.x; i < a.nx; i += NT) zrow[i] = O[(G + g) * ld + pr(i)];
+        for (int i = threadIdx.x; i < a.nx; i += NT)
+          zrow[i] = (i & 1) ? odd * O[(G + g) * ld + pr(i)] : O[(G + g) * ld + pr(i)];
       }
     }
     __syncthreads();
@@ -568,6 +676,12 @@ __device__ void scalar_update(DevState* st, double Delta, double cfl) {
   st->done_blocks = 0u;
 }
 
+// index g of a periodic dimension of n points brought into [0, n)
+__device__ __forceinline__ int wrap_index(int g, int n) {
+  const int r = g % n;
+  return r < 0 ? r + n : r;
+}
+
 // RHS tile of TX x TY points of one layer; block (32, 8); R = halo radius
 // of psi (the number of hyperviscosity sweeps, at least 1).  EDGE: the tile
 // plus its halo touches a wall, so loads are bounds-checked and ghost values
@@ -601,7 +715,19 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
 #define PS(x, y) ps[((y) + R) * W + (x) + R]
 #define QS(x, y) qs[((y) + 1) * QW + (x) + 1]
   const int tid = tx + ty * 32;
-  if (EDGE) {
+  const bool per = a.periodic != 0;
+  if (EDGE && per) {
+    // periodic: every halo value is an interior value of the other side
+    // (src/domain.h:225-256); tiles may be wider than the domain
+    for (int w = tid; w < HH * W; w += NT) {
+      const int y = w / W, x = w - y * W;
+      ps[w] = psiL[(size_t)wrap_index(j0 + y - R, ny) * pitch + wrap_index(i0 + x - R, nx)];
+    }
+    for (int w = tid; w < QH * QW; w += NT) {
+      const int y = w / QW, x = w - y * QW;
+      qs[w] = qL[(size_t)wrap_index(j0 + y - 1, ny) * pitch + wrap_index(i0 + x - 1, nx)];
+    }
+  } else if (EDGE) {
     for (int w = tid; w < HH * W; w += NT) {
       const int y = w / W, x = w - y * W;
       const int gi = i0 + x - R, gj = j0 + y - R;
@@ -634,7 +760,7 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
   }
   __syncthreads();
   // q with one ghost point: adjust_bc(q, 1, psi), src/domain.h:308-348
-  if (EDGE) {
+  if (EDGE && !per) {
     for (int w = tid; w < QH * QW; w += NT) {
       const int y = w / QW, x = w - y * QW;
       const int xx = x - 1, yy = y - 1;
@@ -661,7 +787,19 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
     if (s <= a.nsweep) {
       __syncthreads();
       const int Ws = W - 2 * s, Hs = HH - 2 * s;
-      if (EDGE) {
+      if (EDGE && per) {
+        // periodic: no walls, the sweep is the Laplacian everywhere
+        for (int w = tid; w < Ws * Hs; w += NT) {
+          const int yr = w / Ws, xr = w - yr * Ws;
+          const int o = (yr + s) * W + xr + s;
+          if (s == 1 && zm) {
+            Lc[o] = d2 * zetaL[(size_t)wrap_index(j0 + yr + s - R, ny) * pitch + wrap_index(i0 + xr + s - R, nx)];
+          } else {
+            const T sum = (Lp[o + 1] + Lp[o - 1]) + (Lp[o + W] + Lp[o - W]);
+            Lc[o] = fmaT(T(-4), Lp[o], sum);
+          }
+        }
+      } else if (EDGE) {
         const T ghs = pick<T>(a.gh[s], a.fc[FC_GH1 + s - 1]);
         for (int w = tid; w < Ws * Hs; w += NT) {
           const int yr = w / Ws, xr = w - yr * Ws;
@@ -825,25 +963,26 @@ __device__ __forceinline__ void body_rhs(const StepArgs<T>& a, int bx, int by, i
 }
 
 // ------------------------------------------------- single-run wrappers
-template <typename T, bool COMP>
+template <typename T, bool COMP, bool PER>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 3) k_rows_fwd(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
   __shared__ __align__(16) T cst[NLMAX * GMAX];
-  body_rows_fwd<T, COMP>(a, step_mode, blockIdx.x, smem_raw, tot, cst);
+  body_rows_fwd<T, COMP, PER>(a, step_mode, blockIdx.x, smem_raw, tot, cst);
 }
-template <typename T, bool COMP>
+template <typename T, bool COMP, bool PER>
 __global__ void __launch_bounds__(NT) k_cols(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
-  body_cols<T, COMP>(a, step_mode, blockIdx.x, blockIdx.y, smem_raw, tot);
+  if (PER) body_cols_per<T, COMP>(a, step_mode, blockIdx.x, blockIdx.y, smem_raw);
+  else body_cols<T, COMP>(a, step_mode, blockIdx.x, blockIdx.y, smem_raw, tot);
 }
-template <typename T, bool COMP>
+template <typename T, bool COMP, bool PER>
 __global__ void __launch_bounds__(NT, 3) k_rows_inv(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
   __shared__ __align__(16) T cst[NLMAX * GMAX];
-  body_rows_inv<T, COMP>(a, step_mode, blockIdx.x, smem_raw, tot, cst);
+  body_rows_inv<T, COMP, PER>(a, step_mode, blockIdx.x, smem_raw, tot, cst);
 }
 template <typename T, bool COMP, int R>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 1) k_rhs(StepArgs<T> a) {
@@ -901,7 +1040,7 @@ __device__ __forceinline__ void ens_init_cur(int* cur) {
   __syncthreads();
 }
 
-template <typename T, bool COMP>
+template <typename T, bool COMP, bool PER>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 2) k_rows_fwd_ens(EnsArgs<T> e, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
@@ -911,11 +1050,11 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 2) k_rows_fwd_ens(Ens
   ens_init_cur(&cur);
   for (int item = blockIdx.x; item < e.total[0]; item += gridDim.x) {
     const int local = ens_item(e, e.start_rows, item, &sa, &cur);
-    body_rows_fwd<T, COMP>(sa, step_mode, local, smem_raw, tot, cst);
+    body_rows_fwd<T, COMP, PER>(sa, step_mode, local, smem_raw, tot, cst);
     __syncthreads();
   }
 }
-template <typename T, bool COMP>
+template <typename T, bool COMP, bool PER>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 2) k_cols_ens(EnsArgs<T> e, int step_mode) {
   constexpr int CT = ColsPer<T>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -925,12 +1064,13 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 2) k_cols_ens(EnsArgs
   ens_init_cur(&cur);
   for (int item = blockIdx.x; item < e.total[1]; item += gridDim.x) {
     const int local = ens_item(e, e.start_cols, item, &sa, &cur);
-    const int ntx = (sa.nx + CT - 1) / CT;
-    body_cols<T, COMP>(sa, step_mode, local % ntx, local / ntx, smem_raw, tot);
+    const int ntx = PER ? (sa.gx.H + 2) / 2 : (sa.nx + CT - 1) / CT;
+    if (PER) body_cols_per<T, COMP>(sa, step_mode, local % ntx, local / ntx, smem_raw);
+    else body_cols<T, COMP>(sa, step_mode, local % ntx, local / ntx, smem_raw, tot);
     __syncthreads();
   }
 }
-template <typename T, bool COMP>
+template <typename T, bool COMP, bool PER>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 2) k_rows_inv_ens(EnsArgs<T> e, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
@@ -940,7 +1080,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 2) k_rows_inv_ens(Ens
   ens_init_cur(&cur);
   for (int item = blockIdx.x; item < e.total[2]; item += gridDim.x) {
     const int local = ens_item(e, e.start_rows, item, &sa, &cur);
-    body_rows_inv<T, COMP>(sa, step_mode, local, smem_raw, tot, cst);
+    body_rows_inv<T, COMP, PER>(sa, step_mode, local, smem_raw, tot, cst);
     __syncthreads();
   }
 }
@@ -1080,8 +1220,10 @@ __global__ void __launch_bounds__(NT) k_budget_partial(StepArgs<T> a, const doub
     const size_t o = row * a.pitch + i;
     const double p = (double)a.psi[o];
     const double qv = (double)a.q[o] + (a.qlo ? (double)a.qlo[o] : 0.0);
-    const double pe = (i + 1 < a.nx) ? (double)a.psi[o + 1] : 0.0;
-    const double pn = (j + 1 < a.ny) ? (double)a.psi[o + a.pitch] : 0.0;
+    // closed basin: psi = 0 on the walls; periodic: the opposite side
+    const double pe = (i + 1 < a.nx) ? (double)a.psi[o + 1] : (a.periodic ? (double)a.psi[o + 1 - a.nx] : 0.0);
+    const double pn = (j + 1 < a.ny) ? (double)a.psi[o + a.pitch]
+                                     : (a.periodic ? (double)a.psi[o - (size_t)(a.ny - 1) * a.pitch] : 0.0);
     const double u = (pe - p) / a.Delta, v = (pn - p) / a.Delta;
     const double wl = wts[l];
     ke += wl * 0.5 * (u * u + v * v);
@@ -1112,7 +1254,15 @@ template <typename T, bool COMP>
 static size_t smem_rows(const StepArgs<T>& a) { return (size_t)2 * a.G1 * padded_len(a.gx.M) * sizeof(T); }
 template <typename T, bool COMP>
 static size_t smem_cols(const StepArgs<T>& a) {
-  return (size_t)((COMP && a.zeta_mode) ? 3 : 2) * ColsPer<T>::value * padded_len(a.gy.M) * sizeof(T);
+  // periodic: two complex columns of ny values (padded rows of 2 ny reals)
+  const size_t rows = a.periodic ? 2 : ColsPer<T>::value;
+  return (size_t)((COMP && a.zeta_mode) ? 3 : 2) * rows * padded_len(a.gy.M) * sizeof(T);
+}
+// column tiles of one mode: four real columns (DST) or two complex columns
+// k = 0..nx/2 (periodic)
+template <typename T>
+static int col_tiles(const StepArgs<T>& a) {
+  return a.periodic ? (a.gx.H + 2) / 2 : (a.nx + ColsPer<T>::value - 1) / ColsPer<T>::value;
 }
 template <typename T, bool COMP>
 static size_t smem_rows_inv(const StepArgs<T>& a) {
@@ -1146,12 +1296,12 @@ static cudaError_t set_attrs(const StepArgs<T>& a) {
       smem_rhs<T>(a) + 1024 > (size_t)optin)
     return cudaErrorInvalidValue;
   const int lim = optin - (int)static_tot;
-  e = cudaFuncSetAttribute(k_rows_fwd<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_rows_inv<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_cols<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-  if (e != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_rows_fwd<T, COMP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
+  if ((e = cudaFuncSetAttribute(k_rows_inv<T, COMP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
+  if ((e = cudaFuncSetAttribute(k_cols<T, COMP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
+  if ((e = cudaFuncSetAttribute(k_rows_fwd<T, COMP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
+  if ((e = cudaFuncSetAttribute(k_rows_inv<T, COMP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
+  if ((e = cudaFuncSetAttribute(k_cols<T, COMP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
   const int rl = optin - 1024;
   if ((e = cudaFuncSetAttribute(k_rhs<T, COMP, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, rl)) != cudaSuccess)
     return e;
@@ -1164,16 +1314,19 @@ static cudaError_t set_attrs(const StepArgs<T>& a) {
 
 template <typename T, bool COMP>
 static void launch_k1(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
-  k_rows_fwd<T, COMP><<<dim3(a.ny), NT, smem_rows<T, COMP>(a), s>>>(a, step_mode);
+  if (a.periodic) k_rows_fwd<T, COMP, true><<<dim3(a.ny), NT, smem_rows<T, COMP>(a), s>>>(a, step_mode);
+  else k_rows_fwd<T, COMP, false><<<dim3(a.ny), NT, smem_rows<T, COMP>(a), s>>>(a, step_mode);
 }
 template <typename T, bool COMP>
 static void launch_k2(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
-  constexpr int CT = ColsPer<T>::value;
-  k_cols<T, COMP><<<dim3((a.nx + CT - 1) / CT, a.nl), NT, smem_cols<T, COMP>(a), s>>>(a, step_mode);
+  const dim3 grid(col_tiles(a), a.nl);
+  if (a.periodic) k_cols<T, COMP, true><<<grid, NT, smem_cols<T, COMP>(a), s>>>(a, step_mode);
+  else k_cols<T, COMP, false><<<grid, NT, smem_cols<T, COMP>(a), s>>>(a, step_mode);
 }
 template <typename T, bool COMP>
 static void launch_k3(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
-  k_rows_inv<T, COMP><<<dim3(a.ny), NT, smem_rows_inv<T, COMP>(a), s>>>(a, step_mode);
+  if (a.periodic) k_rows_inv<T, COMP, true><<<dim3(a.ny), NT, smem_rows_inv<T, COMP>(a), s>>>(a, step_mode);
+  else k_rows_inv<T, COMP, false><<<dim3(a.ny), NT, smem_rows_inv<T, COMP>(a), s>>>(a, step_mode);
 }
 template <typename T, bool COMP>
 static void launch_rhs(const StepArgs<T>& a, cudaStream_t s) {
@@ -1259,11 +1412,16 @@ static cudaError_t set_attrs_ens() {
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return e;
   const int lim = optin - (int)(sizeof(T) * (GMAX * 32 + NLMAX * GMAX) + sizeof(StepArgs<T>) + 128);
-  if ((e = cudaFuncSetAttribute(k_rows_fwd_ens<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
+  if ((e = cudaFuncSetAttribute(k_rows_fwd_ens<T, COMP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
     return e;
-  if ((e = cudaFuncSetAttribute(k_rows_inv_ens<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
+  if ((e = cudaFuncSetAttribute(k_rows_inv_ens<T, COMP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
     return e;
-  if ((e = cudaFuncSetAttribute(k_cols_ens<T, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
+  if ((e = cudaFuncSetAttribute(k_cols_ens<T, COMP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
+  if ((e = cudaFuncSetAttribute(k_rows_fwd_ens<T, COMP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
+    return e;
+  if ((e = cudaFuncSetAttribute(k_rows_inv_ens<T, COMP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
+    return e;
+  if ((e = cudaFuncSetAttribute(k_cols_ens<T, COMP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
   const int rl = optin - (int)(sizeof(StepArgs<T>) + 1024);
   if ((e = cudaFuncSetAttribute(k_rhs_ens<T, COMP, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, rl))) return e;
   if ((e = cudaFuncSetAttribute(k_rhs_ens<T, COMP, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, rl))) return e;
@@ -1287,10 +1445,16 @@ static EnsSmem ens_smem(const StepArgs<T>* host_members, int n) {
 
 template <typename T, bool COMP>
 static void ens_step(const EnsArgs<T>& e, const EnsArgs<T>* er, const EnsSmem& sm, const int* grid, const int* rgrid,
-                     int which_mask, cudaStream_t s) {
-  if (which_mask & 1) k_rows_fwd_ens<T, COMP><<<grid[0], NT, sm.bytes[0], s>>>(e, 1);
-  if (which_mask & 2) k_cols_ens<T, COMP><<<grid[1], NT, sm.bytes[1], s>>>(e, 1);
-  if (which_mask & 4) k_rows_inv_ens<T, COMP><<<grid[2], NT, sm.bytes[2], s>>>(e, 1);
+                     int which_mask, int periodic, cudaStream_t s) {
+  if (periodic) {
+    if (which_mask & 1) k_rows_fwd_ens<T, COMP, true><<<grid[0], NT, sm.bytes[0], s>>>(e, 1);
+    if (which_mask & 2) k_cols_ens<T, COMP, true><<<grid[1], NT, sm.bytes[1], s>>>(e, 1);
+    if (which_mask & 4) k_rows_inv_ens<T, COMP, true><<<grid[2], NT, sm.bytes[2], s>>>(e, 1);
+  } else {
+    if (which_mask & 1) k_rows_fwd_ens<T, COMP, false><<<grid[0], NT, sm.bytes[0], s>>>(e, 1);
+    if (which_mask & 2) k_cols_ens<T, COMP, false><<<grid[1], NT, sm.bytes[1], s>>>(e, 1);
+    if (which_mask & 4) k_rows_inv_ens<T, COMP, false><<<grid[2], NT, sm.bytes[2], s>>>(e, 1);
+  }
   if (which_mask & 8) {
     const dim3 blk(32, 8);
     if (rgrid[1] > 0) k_rhs_ens<T, COMP, 1><<<rgrid[1], blk, sm.rhs_bytes[1], s>>>(er[1]);
@@ -1300,19 +1464,26 @@ static void ens_step(const EnsArgs<T>& e, const EnsArgs<T>* er, const EnsSmem& s
   }
 }
 template <typename T, bool COMP>
-static void ens_invert(const EnsArgs<T>& e, const EnsSmem& sm, const int* grid, cudaStream_t s) {
-  k_rows_fwd_ens<T, COMP><<<grid[0], NT, sm.bytes[0], s>>>(e, 0);
-  k_cols_ens<T, COMP><<<grid[1], NT, sm.bytes[1], s>>>(e, 0);
-  k_rows_inv_ens<T, COMP><<<grid[2], NT, sm.bytes[2], s>>>(e, 0);
+static void ens_invert(const EnsArgs<T>& e, const EnsSmem& sm, const int* grid, int periodic, cudaStream_t s) {
+  if (periodic) {
+    k_rows_fwd_ens<T, COMP, true><<<grid[0], NT, sm.bytes[0], s>>>(e, 0);
+    k_cols_ens<T, COMP, true><<<grid[1], NT, sm.bytes[1], s>>>(e, 0);
+    k_rows_inv_ens<T, COMP, true><<<grid[2], NT, sm.bytes[2], s>>>(e, 0);
+    return;
+  }
+  k_rows_fwd_ens<T, COMP, false><<<grid[0], NT, sm.bytes[0], s>>>(e, 0);
+  k_cols_ens<T, COMP, false><<<grid[1], NT, sm.bytes[1], s>>>(e, 0);
+  k_rows_inv_ens<T, COMP, false><<<grid[2], NT, sm.bytes[2], s>>>(e, 0);
 }
 
 template <typename T, bool COMP>
 static int ens_occupancy(int stage, size_t smem) {
   int b = 0;
   cudaError_t e = cudaSuccess;
-  if (stage == 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_rows_fwd_ens<T, COMP>, NT, smem);
-  if (stage == 1) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_cols_ens<T, COMP>, NT, smem);
-  if (stage == 2) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_rows_inv_ens<T, COMP>, NT, smem);
+  // the periodic variants have the same register and shared-memory needs
+  if (stage == 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_rows_fwd_ens<T, COMP, false>, NT, smem);
+  if (stage == 1) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_cols_ens<T, COMP, false>, NT, smem);
+  if (stage == 2) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_rows_inv_ens<T, COMP, false>, NT, smem);
   // stage 3 + R: the RHS kernel of halo radius R
   if (stage == 4) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_rhs_ens<T, COMP, 1>, NT, smem);
   if (stage == 5) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_rhs_ens<T, COMP, 2>, NT, smem);
@@ -1323,6 +1494,8 @@ static int ens_occupancy(int stage, size_t smem) {
 int ens_blocks_per_sm_f64(int stage, size_t smem) { return ens_occupancy<double, false>(stage, smem); }
 int ens_blocks_per_sm_f32c(int stage, size_t smem) { return ens_occupancy<float, true>(stage, smem); }
 int rhs_halo_of_f64(const StepArgs<double>& a) { return rhs_halo(a); }
+int col_tiles_f64(const StepArgs<double>& a) { return col_tiles(a); }
+int col_tiles_f32c(const StepArgs<float>& a) { return col_tiles(a); }
 int rhs_halo_of_f32c(const StepArgs<float>& a) { return rhs_halo(a); }
 
 cudaError_t ens_prepare_f64() { return set_attrs_ens<double, false>(); }
@@ -1336,18 +1509,18 @@ void ens_begin_f32c(const EnsArgs<float>& e, const int* max_steps, cudaStream_t 
   k_begin_ens<float><<<(e.n + 63) / 64, 64, 0, s>>>(e, 0.0, 0.0, max_steps);
 }
 void ens_step_f64(const EnsArgs<double>& e, const EnsArgs<double>* er, const EnsSmem& sm, const int* grid,
-                  const int* rgrid, int mask, cudaStream_t s) {
-  ens_step<double, false>(e, er, sm, grid, rgrid, mask, s);
+                  const int* rgrid, int mask, int periodic, cudaStream_t s) {
+  ens_step<double, false>(e, er, sm, grid, rgrid, mask, periodic, s);
 }
 void ens_step_f32c(const EnsArgs<float>& e, const EnsArgs<float>* er, const EnsSmem& sm, const int* grid,
-                   const int* rgrid, int mask, cudaStream_t s) {
-  ens_step<float, true>(e, er, sm, grid, rgrid, mask, s);
+                   const int* rgrid, int mask, int periodic, cudaStream_t s) {
+  ens_step<float, true>(e, er, sm, grid, rgrid, mask, periodic, s);
 }
-void ens_invert_f64(const EnsArgs<double>& e, const EnsSmem& sm, const int* grid, cudaStream_t s) {
-  ens_invert<double, false>(e, sm, grid, s);
+void ens_invert_f64(const EnsArgs<double>& e, const EnsSmem& sm, const int* grid, int periodic, cudaStream_t s) {
+  ens_invert<double, false>(e, sm, grid, periodic, s);
 }
-void ens_invert_f32c(const EnsArgs<float>& e, const EnsSmem& sm, const int* grid, cudaStream_t s) {
-  ens_invert<float, true>(e, sm, grid, s);
+void ens_invert_f32c(const EnsArgs<float>& e, const EnsSmem& sm, const int* grid, int periodic, cudaStream_t s) {
+  ens_invert<float, true>(e, sm, grid, periodic, s);
 }
 void ens_flush_f64(const EnsArgs<double>& e, int grid, cudaStream_t s) {
   k_flush_ens<double, false><<<grid, NT, 0, s>>>(e);

@@ -42,12 +42,14 @@ void ens_begin_f32c(const EnsArgs<float>& e, const int* max_steps, cudaStream_t 
 // mask: bit k launches kernel k (0 rows forward, 1 columns, 2 rows inverse,
 // 3 RHS); the RHS stage is one launch per halo radius R with er[R] (whose
 // work list holds only the members of that radius) and grid rgrid[R] (0: none)
+// periodic != 0: every member is a doubly periodic basin (the row and column
+// kernels use the real / complex FFT instead of the DST-I)
 void ens_step_f64(const EnsArgs<double>& e, const EnsArgs<double>* er, const EnsSmem& sm, const int* grid,
-                  const int* rgrid, int mask, cudaStream_t s);
+                  const int* rgrid, int mask, int periodic, cudaStream_t s);
 void ens_step_f32c(const EnsArgs<float>& e, const EnsArgs<float>* er, const EnsSmem& sm, const int* grid,
-                   const int* rgrid, int mask, cudaStream_t s);
-void ens_invert_f64(const EnsArgs<double>& e, const EnsSmem& sm, const int* grid, cudaStream_t s);
-void ens_invert_f32c(const EnsArgs<float>& e, const EnsSmem& sm, const int* grid, cudaStream_t s);
+                   const int* rgrid, int mask, int periodic, cudaStream_t s);
+void ens_invert_f64(const EnsArgs<double>& e, const EnsSmem& sm, const int* grid, int periodic, cudaStream_t s);
+void ens_invert_f32c(const EnsArgs<float>& e, const EnsSmem& sm, const int* grid, int periodic, cudaStream_t s);
 void ens_flush_f64(const EnsArgs<double>& e, int grid, cudaStream_t s);
 void ens_flush_f32c(const EnsArgs<float>& e, int grid, cudaStream_t s);
 // resident blocks per SM of an ensemble stage kernel with `smem` bytes of
@@ -57,6 +59,9 @@ int ens_blocks_per_sm_f64(int stage, size_t smem);
 int ens_blocks_per_sm_f32c(int stage, size_t smem);
 // halo radius R of a run's RHS kernel (the number of hyperviscosity sweeps, at least 1)
 int rhs_halo_of_f64(const StepArgs<double>& a);
+// column-kernel work items (tiles) per mode of a run
+int col_tiles_f64(const StepArgs<double>& a);
+int col_tiles_f32c(const StepArgs<float>& a);
 int rhs_halo_of_f32c(const StepArgs<float>& a);
 int cols_per_tile_f64();
 int cols_per_tile_f32c();

@@ -13,6 +13,8 @@
 //   fab    3 slabs of the AB3 history (f0/f1/f2 rotate by step index)
 //   hinv   FP64 path only: 1 / (-(L^2 + K^2 + iRd2_m) * norm) per (m, j, k)
 //   topo   (ny+2) x (nx+2) reference layout (only when non-zero)
+// The doubly periodic basin keeps the same layout with nx = NX, ny = NY and
+// pitch = NX + 4 (room for the NX/2 + 1 complex values of a spectral row).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -97,6 +99,11 @@ template <typename T> struct StepArgs {
   int CT;                          // (unused by the kernels; kept for layout)
   int vec_cols;                    // rows are 16-byte aligned: 16-byte column loads
   int low_k64;                     // compensated: FP64 divide for mode 0, j,k < low_k64
+  // doubly periodic basin (bc_fac = -1): nx = NX, ny = NY interior points,
+  // pitch = NX + 4; gx has M = NX (real FFT of length NX as a complex FFT
+  // of NX/2), gy has M = 2 NY (complex FFT of length NY); spectral rows hold
+  // X_0..X_{NX/2} as (re, im) pairs; ghost values wrap around
+  int periodic;
 };
 
 // indices into StepArgs::fc

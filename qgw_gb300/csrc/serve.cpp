@@ -66,7 +66,8 @@ struct qgw_pool {
   long long next_id = 1;
   bool stop = false;
   std::thread worker;
-  qgw::EnsembleCore batch[2];  // [0] FP64, [1] FP32c
+  // batch b: precision b % 2 (0 FP64, 1 FP32c), boundary b / 2 (0 closed, 1 periodic)
+  qgw::EnsembleCore batch[4];
   // statistics
   long long completed = 0, admitted = 0, ticks = 0;
   double lgp_steps = 0;
@@ -76,9 +77,11 @@ struct qgw_pool {
 namespace {
 
 size_t lgp_of(const qgw_params& p) {
-  const size_t nx = p.NX - 1, ny = p.NY - 1;
-  return nx * ny * (size_t)p.nl;
+  const size_t cut = p.bc_fac == -1 ? 0 : 1;  // a closed basin has NX-1 interior points
+  return (p.NX - cut) * (p.NY - cut) * (size_t)p.nl;
 }
+
+int batch_of(const qgw_params& p, int precision) { return (precision == QGW_FP64 ? 0 : 1) + (p.bc_fac == -1 ? 2 : 0); }
 
 int admit_one(qgw_pool* pl, const std::shared_ptr<Request>& r) {
   qgw_run* run = nullptr;
@@ -97,17 +100,18 @@ int admit_one(qgw_pool* pl, const std::shared_ptr<Request>& r) {
 }
 
 void rebuild(qgw_pool* pl) {
-  for (int b = 0; b < 2; ++b) {
+  for (int b = 0; b < 4; ++b) {
     qgw::EnsembleCore& e = pl->batch[b];
     e.members.clear();
     for (auto& r : pl->resident)
-      if ((r->precision == QGW_FP64) == (b == 0)) e.members.push_back(r->run);
+      if (batch_of(r->p, r->precision) == b) e.members.push_back(r->run);
     qgw::ens_core_build(&e);
   }
 }
 
 void retire(qgw_pool* pl, const std::shared_ptr<Request>& r, int status) {
-  const size_t n3 = (size_t)r->p.nl * (r->p.NY + 1) * (r->p.NX + 1);
+  const size_t ring = r->p.bc_fac == -1 ? 2 : 1;  // interior + ghost ring
+  const size_t n3 = (size_t)r->p.nl * (r->p.NY + ring) * (r->p.NX + ring);
   if (status == QGW_OK) {
     r->psi.resize(n3);
     r->q.resize(n3);
@@ -126,10 +130,11 @@ void retire(qgw_pool* pl, const std::shared_ptr<Request>& r, int status) {
 
 void worker_loop(qgw_pool* pl) {
   cudaSetDevice(pl->device);
-  for (int b = 0; b < 2; ++b) {
+  for (int b = 0; b < 4; ++b) {
     cudaStreamCreateWithFlags(&pl->batch[b].stream, cudaStreamNonBlocking);
     cudaDeviceGetAttribute(&pl->batch[b].nsm, cudaDevAttrMultiProcessorCount, pl->device);
-    pl->batch[b].precision = b == 0 ? QGW_FP64 : QGW_FP32C;
+    pl->batch[b].precision = b % 2 == 0 ? QGW_FP64 : QGW_FP32C;
+    pl->batch[b].periodic = b / 2;
   }
   for (;;) {
     // admission, in arrival order, by footprint
@@ -174,9 +179,9 @@ void worker_loop(qgw_pool* pl) {
     if (changed) rebuild(pl);
     if (pl->resident.empty()) continue;
     pl->max_resident = std::max(pl->max_resident, (int)pl->resident.size());
-    // one tick: both batches enqueued before either is waited on
-    std::vector<int> caps[2];
-    for (int b = 0; b < 2; ++b) {
+    // one tick: every batch enqueued (own stream) before any is waited on
+    std::vector<int> caps[4];
+    for (int b = 0; b < 4; ++b) {
       qgw::EnsembleCore& e = pl->batch[b];
       if (e.members.empty()) continue;
       for (qgw_run* run : e.members)
@@ -185,7 +190,7 @@ void worker_loop(qgw_pool* pl) {
       qgw::ens_core_step(&e, pl->steps_per_tick, caps[b].data(), false);
     }
     std::vector<std::shared_ptr<Request>> finished;
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < 4; ++b) {
       qgw::EnsembleCore& e = pl->batch[b];
       if (e.members.empty()) continue;
       qgw::ens_core_finish(&e);
@@ -208,7 +213,7 @@ void worker_loop(qgw_pool* pl) {
       rebuild(pl);
     }
   }
-  for (int b = 0; b < 2; ++b) {
+  for (int b = 0; b < 4; ++b) {
     qgw::ens_core_free_tables(&pl->batch[b]);
     if (pl->batch[b].stream) cudaStreamDestroy(pl->batch[b].stream);
   }
@@ -244,7 +249,8 @@ int qgw_pool_submit(qgw_pool* pl, const qgw_params* p, const double* q0, int pre
   r->p = *p;
   r->precision = precision;
   r->nsteps = nsteps;
-  const size_t n3 = (size_t)p->nl * (p->NY + 1) * (p->NX + 1);
+  const size_t ring = p->bc_fac == -1 ? 2 : 1;  // interior + ghost ring
+  const size_t n3 = (size_t)p->nl * (p->NY + ring) * (p->NX + ring);
   r->q0.assign(q0, q0 + n3);
   int rc = qgw_footprint(p, precision, &r->footprint);
   if (rc) return rc;
