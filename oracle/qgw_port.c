@@ -28,10 +28,16 @@ struct port_run {
   double *wrk, *cl2m, *cm2l, *iRd2, *K, *L, *X, *Y;
   double t, dt, dt0, dt1, DT_max, t_out;
   int fast;
+  /* stochastic ring forcing (src/forcing.h:11-30,67-201) */
+  double kf;               /* k_f / (2 pi) */
+  int NF, NKf, NP, Np;     /* transform size, half size, ring points */
+  int *ind_i, *ind_j;
+  double *forc, *forc_f, *forc_p;
 };
 
 #define IDX(r, i, j, k) ((size_t)(k) * (r)->nxp2 * (r)->nyp2 + (size_t)(j) * (r)->nxp2 + (size_t)(i))
 static double sq(double x) { return x * x; }
+static void port_init_forcing(port_run* r);
 
 /* ------------------------------------------------------------- params */
 
@@ -254,11 +260,84 @@ port_run* port_create(const qgw_params* pin, int fast_dst) {
   r->dt1 = r->dt;
   r->t = 0;
   r->t_out = 0;
+  port_init_forcing(r);
+  srand(1); /* the sequence a fresh reference process draws from */
   return r;
+}
+
+/* init_stoch_forc, src/forcing.h:67-168 (serial): the thin ring of
+ * wavenumbers |k| ~ k_f (in cycles per unit length, dk = 1/Lx) of the
+ * N_F x (N_F/2+1) half spectrum, N_F = NX (the unreduced grid size). */
+static void port_init_forcing(port_run* r) {
+  const qgw_params* p = &r->p;
+  if (p->k_f == 0) return;
+  r->kf = p->k_f / (2 * PORT_PI);
+  /* N_F = NX (periodic) or NXp1, which after init_domain's NX -= 1 is the
+   * unreduced NX as well (src/forcing.h:78-82) */
+  r->NF = p->NX;
+  r->NKf = r->NF / 2 + 1;
+  r->forc = calloc((size_t)r->nxp2 * r->nyp2, sizeof(double));
+  r->forc_f = calloc((size_t)2 * r->NKf * r->NF, sizeof(double));
+  r->forc_p = calloc((size_t)r->NF * r->NF, sizeof(double));
+  const double dk = 1. / p->Lx;
+  const int N_ind = (int)(4 * PORT_PI * r->kf / dk);
+  r->ind_i = calloc(N_ind > 0 ? N_ind : 1, sizeof(int));
+  r->ind_j = calloc(N_ind > 0 ? N_ind : 1, sizeof(int));
+  r->NP = 0;
+  r->Np = 0;
+  for (int j = 0; j < r->NF; j++)
+    for (int i = 0; i < r->NKf; i++) {
+      double l = (((j + r->NF / 2) % r->NF) - r->NF / 2) * dk;
+      double k = (i)*dk;
+      double dist_k = fabs(k - sqrt(sq(r->kf) - sq(l)));
+      double a = fabs(l - sqrt(sq(r->kf) - sq(k))), b = fabs(l + sqrt(sq(r->kf) - sq(k)));
+      double dist_l = (a < b) ? a : b; /* the min macro of src/qg.c:40 */
+      if (dist_k < dk / 2 || dist_l < dk / 2) {
+        r->NP += 1;
+        if (r->Np < N_ind) {
+          r->ind_i[r->Np] = i;
+          r->ind_j[r->Np] = j;
+        }
+        r->Np += 1;
+      }
+    }
+}
+
+/* calc_forc, src/forcing.h:170-201, with normal_noise / noise of :62-63;
+ * rand() is the C library's (seeded at port_create, like a fresh reference
+ * process).  C leaves the order of the two rand() calls of normal_noise
+ * unspecified; the reference compiled in place (gcc) makes the logarithm's
+ * first, which the golden fixtures pin (bit-identical results). */
+static void port_calc_forc(port_run* r) {
+  if (r->NP <= 1) return;
+  memset(r->forc_f, 0, sizeof(double) * 2 * (size_t)r->NKf * r->NF);
+  for (int ii = 0; ii < r->Np; ii++) {
+    const int i = r->ind_i[ii], j = r->ind_j[ii];
+    const double envelope = sqrt((double)8 / ((r->NP - 1) * 2)) * PORT_PI * r->kf;
+    const double rl = (double)rand(); /* log argument */
+    const double rc = (double)rand(); /* cos argument */
+    const double nn = sqrt(-2. * log((rl + 1.) / ((double)(RAND_MAX) + 2.))) * cos(2 * PORT_PI * rc / (double)RAND_MAX);
+    const double magnitude = r->p.sigma_f * nn;
+    const double phase = ((double)rand() / RAND_MAX) * 2 * PORT_PI;
+    r->forc_f[2 * ((size_t)j * r->NKf + i)] = envelope * magnitude * cos(phase);
+    r->forc_f[2 * ((size_t)j * r->NKf + i) + 1] = envelope * magnitude * sin(phase);
+  }
+  /* out-of-place c2r of the N_F x N_F plan */
+  const size_t ld = 2 * (size_t)r->NKf;
+  double* t = malloc(sizeof(double) * ld * r->NF);
+  memcpy(t, r->forc_f, sizeof(double) * ld * r->NF);
+  om_dft_c2r_2d_any(r->NF, r->NF, t, r->fast);
+  for (int j = 0; j < r->NF; j++)
+    for (int i = 0; i < r->NF; i++) r->forc_p[(size_t)j * r->NF + i] = t[(size_t)j * ld + i];
+  free(t);
+  for (int j = 0; j < r->NF; j++)
+    for (int i = 0; i < r->NF; i++)
+      if (i + 1 < r->nxp2 && j + 1 < r->nyp2) r->forc[IDX(r, i + 1, j + 1, 0)] = r->forc_p[(size_t)j * r->NF + i];
 }
 
 void port_destroy(port_run* r) {
   if (!r) return;
+  free(r->ind_i); free(r->ind_j); free(r->forc); free(r->forc_f); free(r->forc_p);
   free(r->X); free(r->Y); free(r->K); free(r->L); free(r->wrk);
   free(r->cl2m); free(r->cm2l); free(r->iRd2);
   free(r->psi); free(r->q); free(r->diff); free(r->lapn); free(r->topo);
@@ -478,8 +557,8 @@ static double port_adjust_timestep(port_run* r) {
   return dt;
 }
 
-/* timestep, src/timestep.h:386-439 (forcing add-ons off: k_f = 0 and
- * dt_forc_period = 0). */
+/* timestep, src/timestep.h:386-439 (with the stochastic forcing; the 4-D
+ * forcing add-on is off: dt_forc_period = 0). */
 void port_timestep(port_run* r) {
   double* swap = r->fab[2];
   r->fab[2] = r->fab[1];
@@ -500,6 +579,11 @@ void port_timestep(port_run* r) {
         const size_t s = IDX(r, i, j, k);
         r->q[s] = r->q[s] + c0 * f0[s] + c1 * f1[s] + c2 * f2[s];
       }
+  if (r->p.k_f != 0) { /* src/timestep.h:415-421 */
+    port_calc_forc(r);
+    for (int j = 1; j < r->ny + 1; ++j)
+      for (int i = 1; i < r->nx + 1; ++i) r->q[IDX(r, i, j, 0)] += r->forc[IDX(r, i, j, 0)] * sqrt(dt);
+  }
   r->t = r->t + dt;
 }
 

@@ -3,8 +3,9 @@
  * reference makes, so that the reference's own src/qg.c can be compiled and
  * run in place as the oracle (test infrastructure only).
  *
- * FFTW: the closed-basin 2-D RODFT00 plan (src/elliptic.h:136-139) and the
- * periodic in-place r2c/c2r plans (src/elliptic.h:32-47).
+ * FFTW: the closed-basin 2-D RODFT00 plan (src/elliptic.h:136-139), the
+ * periodic in-place r2c/c2r plans (src/elliptic.h:32-47) and the
+ * out-of-place c2r of the stochastic forcing (src/forcing.h:124).
  * The DST uses direct sums with an exactly reduced sine table unless
  * QGW_SHIM_DST=fast, which selects the O(n log n) path of oracle_math.c.
  */
@@ -18,7 +19,7 @@
 
 struct shim_fftw_plan_s {
   int n0, n1;
-  int kind;  /* 0 RODFT00 2-D, 1 r2c 2-D, 2 c2r 2-D */
+  int kind;  /* 0 RODFT00 2-D, 1 r2c 2-D in place, 2 c2r 2-D in place, 3 c2r 2-D out of place */
   double *in, *out;
 };
 
@@ -47,9 +48,9 @@ fftw_plan fftw_plan_dft_r2c_2d(int n0, int n1, double* in, fftw_complex* out, un
 
 fftw_plan fftw_plan_dft_c2r_2d(int n0, int n1, fftw_complex* in, double* out, unsigned flags) {
   (void)flags;
-  if ((void*)in != (void*)out) return NULL;
   fftw_plan p = (fftw_plan)calloc(1, sizeof(*p));
-  p->n0 = n0; p->n1 = n1; p->kind = 2; p->in = out; p->out = out;
+  p->n0 = n0; p->n1 = n1; p->in = (double*)in; p->out = out;
+  p->kind = ((void*)in == (void*)out) ? 2 : 3;
   return p;
 }
 
@@ -57,6 +58,17 @@ void fftw_execute(const fftw_plan p) {
   if (!p) return;
   if (p->kind == 1) { om_dft_r2c_2d_any(p->n0, p->n1, p->out, shim_fast()); return; }
   if (p->kind == 2) { om_dft_c2r_2d_any(p->n0, p->n1, p->out, shim_fast()); return; }
+  if (p->kind == 3) {
+    /* input n0 x (n1/2+1) complex, output n0 x n1 reals: run in place on a
+     * copy with the padded row layout, then pack the rows */
+    const size_t ld = 2 * (size_t)(p->n1 / 2 + 1);
+    double* t = (double*)malloc(sizeof(double) * ld * (size_t)p->n0);
+    memcpy(t, p->in, sizeof(double) * ld * (size_t)p->n0);
+    om_dft_c2r_2d_any(p->n0, p->n1, t, shim_fast());
+    for (int r = 0; r < p->n0; ++r) memcpy(p->out + (size_t)r * p->n1, t + (size_t)r * ld, sizeof(double) * (size_t)p->n1);
+    free(t);
+    return;
+  }
   if (p->in != p->out) memcpy(p->out, p->in, sizeof(double) * (size_t)p->n0 * p->n1);
   om_dst2(p->n0, p->n1, p->out, shim_fast());
 }

@@ -80,7 +80,21 @@ def cases():
     p = C.cfg1(64)
     p.update(bc_fac=-1.0, h_topo=150.0, w_topo=3e5)
     out.append(("periodic_topo_nx64", p, 30, 1200.0, None))
+    # stochastic ring forcing (src/forcing.h:67-201), the reference's own
+    # test configurations scaled down (test/params_05.in periodic,
+    # test/params_02.in closed): rand() from a fresh process
+    p = stochastic_params(32, -1.0)
+    out.append(("stochastic_periodic_nx32", p, 30, 5e-4, None))
+    p = stochastic_params(64, 0.0)
+    p.update(k_f=30.0)
+    out.append(("stochastic_closed_nx64", p, 20, 5e-4, None))
     return out
+
+
+def stochastic_params(NX, bc_fac):
+    return dict(NX=NX, NY=NX, nl=1, Lx=1.0, f0=2.0, beta=0.0, tau0=0.0, forc_mode=4.0, k_f=20.0,
+                sigma_f=3.0, bc_fac=bc_fac, dh=[1.0], N2=[0.0], nu=0.01, hEkb=0.0, tend=1e12,
+                dt_out=0.01, cfl=0.2, n_hyper=0, nu_hyper=0.0)
 
 
 def main():

@@ -148,6 +148,18 @@ def test_device_dst_blocks_on_host(dstcore, M):
     assert np.linalg.norm(yf - ref) <= 1e-5 * np.linalg.norm(ref)
 
 
+@pytest.mark.parametrize("seed", [1, 7, 12345, 0])
+def test_forcing_generator_is_the_c_library_rand(tmp_path, seed):
+    """The stochastic forcing's generator restates the C library's rand()
+    (the reference's noise source, src/forcing.h:62-63)."""
+    so = str(tmp_path / "grand.so")
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-o", so,
+                           os.path.join(ROOT, "tests", "cpu", "glibc_rand_check.cpp")])
+    lib = ctypes.CDLL(so)
+    lib.glibc_rand_mismatches.argtypes = [ctypes.c_uint, ctypes.c_int]
+    assert lib.glibc_rand_mismatches(seed, 200000) == 0
+
+
 def test_footprint_grows_with_size(qgwlib):
     small = qgwlib.footprint(C.cfg1(256), qgwlib.FP64)
     big = qgwlib.footprint(C.cfg2(1024), qgwlib.FP64)
