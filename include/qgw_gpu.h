@@ -165,6 +165,15 @@ int qgw_put_q(qgw_run* run, const double* q);
 int qgw_get_time(qgw_run* run, qgw_time* out);
 int qgw_set_time(qgw_run* run, const qgw_time* in);
 
+/* Stochastic ring forcing (k_f != 0, src/forcing.h:67-201): the noise is
+ * the C library's rand() sequence, which the reference draws unseeded, so a
+ * run starts from seed 1 like a fresh reference process and continues it
+ * across qgw_step calls.  qgw_set_forcing_seed restarts the sequence as
+ * srand(seed) would (independent realisations for ensembles).  No reference
+ * counterpart (the reference never seeds).  QGW_ERR_STATE when the run has
+ * no forcing. */
+int qgw_set_forcing_seed(qgw_run* run, unsigned int seed);
+
 /* Advance up to nsteps reference time steps (timestep(), src/timestep.h:386).
  * t_out is the next output time used by the dt snapping of
  * adjust_timestep (src/timestep.h:369-381); pass 0 for none.  Mirrors the

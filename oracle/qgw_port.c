@@ -280,9 +280,12 @@ static void port_init_forcing(port_run* r) {
   r->forc_f = calloc((size_t)2 * r->NKf * r->NF, sizeof(double));
   r->forc_p = calloc((size_t)r->NF * r->NF, sizeof(double));
   const double dk = 1. / p->Lx;
-  const int N_ind = (int)(4 * PORT_PI * r->kf / dk);
-  r->ind_i = calloc(N_ind > 0 ? N_ind : 1, sizeof(int));
-  r->ind_j = calloc(N_ind > 0 ? N_ind : 1, sizeof(int));
+  /* room for every entry of the half spectrum (the reference sizes these
+   * 4 pi k_f / dk, src/forcing.h:131-133, which the ring never exceeds in
+   * the configurations tested) */
+  const int N_ind = r->NF * r->NKf;
+  r->ind_i = calloc(N_ind, sizeof(int));
+  r->ind_j = calloc(N_ind, sizeof(int));
   r->NP = 0;
   r->Np = 0;
   for (int j = 0; j < r->NF; j++)

@@ -40,6 +40,7 @@ STATUS = {
 EXPORTS = [
     "qgw_params_default", "qgw_params_read", "qgw_eigmode", "qgw_check_timestep", "qgw_topo",
     "qgw_create", "qgw_destroy", "qgw_set_q", "qgw_set_q_device", "qgw_put_q", "qgw_get_time", "qgw_set_time",
+    "qgw_set_forcing_seed",
     "qgw_step", "qgw_invert", "qgw_get", "qgw_budget", "qgw_footprint", "qgw_stream",
     "qgw_kernels_per_step", "qgw_profile_kernels", "qgw_probe_fp_rates", "qgw_strerror", "qgw_abi_version",
     "qgw_invert_pv_noalloc", "qgw_nc_create", "qgw_nc_write", "qgw_nc_close", "qgw_nc_read",
@@ -92,6 +93,7 @@ def load(path: str = LIB_PATH):
     lib.qgw_stream.argtypes = [V]
     lib.qgw_stream.restype = V
     lib.qgw_kernels_per_step.argtypes = [V]
+    lib.qgw_set_forcing_seed.argtypes = [V, ctypes.c_uint]
     lib.qgw_profile_kernels.argtypes = [V, I, P(ctypes.c_float)]
     lib.qgw_probe_fp_rates.argtypes = [D, D]
     lib.qgw_strerror.argtypes = [I]
@@ -379,6 +381,10 @@ class Run:
         tm = QgwTime(t, dt, dt if dt0 is None else dt0, dt if dt1 is None else dt1,
                      dt if DT_max is None else DT_max)
         _check(self.lib.qgw_set_time(self.h, ctypes.byref(tm)), "qgw_set_time")
+
+    def set_forcing_seed(self, seed: int):
+        """Restart the stochastic forcing's noise sequence as srand(seed)."""
+        _check(self.lib.qgw_set_forcing_seed(self.h, int(seed)), "qgw_set_forcing_seed")
 
     def fix_dt(self, dt: float):
         self.set_time(0.0, dt, dt, dt, dt)

@@ -261,6 +261,48 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
     a.lx2 = -4.0 / (r->Delta * r->Delta);
     a.ly2 = a.lx2;
   }
+  // stochastic ring forcing (src/forcing.h:67-201); the reference forces
+  // only when the ring has more than one point (:172)
+  std::memset(&a.fr, 0, sizeof(a.fr));
+  {
+    std::vector<int> ij;
+    const int NP = qgw_host_forcing_ring(&p, &ij);
+    if (NP > 1) {
+      qgw::ForcArgs<T>& f = a.fr;
+      f.on = 1;
+      f.nring = NP;
+      f.NF = p.NX;
+      f.fpitch = p.NX + 4;
+      f.gx = qgw::make_geom(f.NF);
+      f.gy = qgw::make_geom(2 * f.NF);
+      for (int dim = 0; dim < 2; ++dim) {
+        qgw::DstTablesHost th = qgw::build_dst_tables(dim == 0 ? f.NF : 2 * f.NF);
+        T *tw, *pre, *spl;
+        if ((rc = upload<T>(r, &tw, th.tw))) return rc;
+        if ((rc = upload<T>(r, &pre, th.pre))) return rc;
+        if ((rc = upload<T>(r, &spl, th.spl))) return rc;
+        qgw::DstTables<T>& t = dim == 0 ? f.tx : f.ty;
+        t.tw = (const qgw::C2<T>*)tw;
+        t.pre = (const qgw::C2<T>*)pre;
+        t.spl = (const qgw::C2<T>*)spl;
+      }
+      int* dring;
+      if ((rc = dalloc(r, &dring, ij.size()))) return rc;
+      CK(cudaMemcpyAsync(dring, ij.data(), sizeof(int) * ij.size(), cudaMemcpyHostToDevice, r->stream));
+      f.ring = dring;
+      const double kf = p.k_f / (2 * M_PI);
+      f.env = std::sqrt((double)8 / ((NP - 1) * 2)) * M_PI * kf;
+      f.sigma = p.sigma_f;
+      qgw::GlibcRand g;
+      qgw::glibc_rand_seed(&g, 1);  // rand() of a fresh process
+      if ((rc = dalloc(r, &f.rng, 1))) return rc;
+      CK(cudaMemcpyAsync(f.rng, &g, sizeof(g), cudaMemcpyHostToDevice, r->stream));
+      if ((rc = dalloc(r, &f.spec, (size_t)f.NF * f.fpitch))) return rc;
+      if ((rc = dalloc(r, &f.spec2, (size_t)f.NF * f.fpitch))) return rc;
+      if ((rc = dalloc(r, &f.field, (size_t)r->ny * r->pitch))) return rc;
+      CK(cudaStreamSynchronize(r->stream));
+    }
+  }
   // FP32 copies of the constants of the compensated kernels (one rounding
   // of the same double expressions the FP64 kernels use)
   std::memset(a.fc, 0, sizeof(a.fc));
@@ -314,6 +356,7 @@ int qgw_footprint(const qgw_params* p, int precision, size_t* bytes) {
   size_t b;
   if (precision == QGW_FP64) b = field * 8 * 7;  // q psi spec f0 f1 f2 hinv
   else b = field * 4 * 9 + field * 8;            // q_hi q_lo psi spec spec2 zeta f0 f1 f2 + FP64 staging
+  if (p->k_f != 0) b += (size_t)3 * p->NX * (p->NX + 4) * (precision == QGW_FP64 ? 8 : 4);  // forcing
   *bytes = b + (size_t)(nx + ny) * 64 + (1 << 20);
   return QGW_OK;
 }
@@ -330,7 +373,7 @@ int qgw_create(const qgw_params* pin, const double* cl2m, const double* cm2l, co
   // periodic: the reference's r2c layout (src/elliptic.h:21,41) is only
   // consistent for a square grid; the real FFT needs NX >= 8
   if (per && (p.NX != p.NY || p.NX < 8)) return QGW_ERR_UNSUPPORTED;
-  if (p.k_f != 0 || p.dt_forc_period != 0) return QGW_ERR_UNSUPPORTED;  // stochastic / 4-D forcing
+  if (p.dt_forc_period != 0) return QGW_ERR_UNSUPPORTED;  // 4-D forcing from input files
   if (!pow2(p.NX) || !pow2(p.NY) || p.NX > 8192 || p.NY > 8192) return QGW_ERR_UNSUPPORTED;
   if (p.nl < 1 || p.nl > QGW_NL_GPU_MAX) return QGW_ERR_UNSUPPORTED;
   if (!(p.Lx > 0) || !(p.cfl > 0)) return QGW_ERR_PARAM;
@@ -467,6 +510,7 @@ static int reset_history(qgw_run* r) {
   CK(cudaMemsetAsync(&d->done_blocks, 0, sizeof(unsigned int), r->stream));
   CK(cudaMemsetAsync(&d->pending, 0, sizeof(int), r->stream));
   CK(cudaMemsetAsync(&d->step_index, 0, sizeof(int), r->stream));
+  CK(cudaMemsetAsync(&d->forc_step, 0, sizeof(int), r->stream));
   CK(cudaMemsetAsync(&d->nonfinite, 0, sizeof(int), r->stream));
   return QGW_OK;
 }
@@ -518,6 +562,17 @@ int qgw_get_time(qgw_run* r, qgw_time* out) {
   out->dt0 = r->h_state->dt0;
   out->dt1 = r->h_state->dt1;
   out->DT_max = r->h_state->DT_max;
+  return QGW_OK;
+}
+
+int qgw_set_forcing_seed(qgw_run* r, unsigned int seed) {
+  if (!r) return QGW_ERR_PARAM;
+  qgw::GlibcRand* rng = r->precision == QGW_FP64 ? r->a64.fr.rng : r->a32.fr.rng;
+  if (!rng) return QGW_ERR_STATE;
+  qgw::GlibcRand g;
+  qgw::glibc_rand_seed(&g, seed);
+  CK(cudaMemcpyAsync(rng, &g, sizeof(g), cudaMemcpyHostToDevice, r->stream));
+  CK(cudaStreamSynchronize(r->stream));
   return QGW_OK;
 }
 

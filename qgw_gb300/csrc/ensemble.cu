@@ -129,6 +129,15 @@ void launch_step(qgw::EnsembleCore* e, int mask) {
   if (e->precision == QGW_FP64)
     qgw::ens_step_f64(e->e64, e->r64, e->sm, e->grid, e->rhs_grid, mask, e->periodic, e->stream);
   else qgw::ens_step_f32c(e->e32, e->r32, e->sm, e->grid, e->rhs_grid, mask, e->periodic, e->stream);
+  // stochastic forcing: its own small launches per forced member, after the RHS
+  if (mask & 8)
+    for (qgw_run* r : e->members) {
+      if (e->precision == QGW_FP64) {
+        if (r->a64.fr.on) qgw::enqueue_forcing_f64(r->a64, e->stream);
+      } else if (r->a32.fr.on) {
+        qgw::enqueue_forcing_f32c(r->a32, e->stream);
+      }
+    }
 }
 
 int ensure_graph(qgw::EnsembleCore* e) {

@@ -299,6 +299,29 @@ extern "C" int qgw_topo(const qgw_params* p, double* topo) {
 
 // forcing_q (src/domain.h:33) on interior row j (1-based), written with the
 // reference's operator order.
+int qgw_host_forcing_ring(const qgw_params* p, std::vector<int>* ij) {
+  if (p->k_f == 0) return 0;
+  const double kf = p->k_f / (2 * kPi);  // k_f /= 2*pi (src/forcing.h:72)
+  const int NF = p->NX;                   // N_F = NX, or NXp1 of the reduced NX
+  const int NK = NF / 2 + 1;
+  const double dk = 1. / p->Lx;
+  int NP = 0;
+  for (int j = 0; j < NF; j++)
+    for (int i = 0; i < NK; i++) {
+      const double l = (((j + NF / 2) % NF) - NF / 2) * dk;
+      const double k = (i)*dk;
+      const double dist_k = std::fabs(k - std::sqrt(kf * kf - l * l));
+      const double a = std::fabs(l - std::sqrt(kf * kf - k * k)), b = std::fabs(l + std::sqrt(kf * kf - k * k));
+      const double dist_l = (a < b) ? a : b;  // the min macro of src/qg.c:40
+      if (dist_k < dk / 2 || dist_l < dk / 2) {
+        ++NP;
+        ij->push_back(i);
+        ij->push_back(j);
+      }
+    }
+  return NP;
+}
+
 double qgw_host_wind(const qgw_params* p, int j) {
   const double Delta = p->Lx / p->NX;
   const double Ly = p->NY * Delta;

@@ -202,9 +202,12 @@ __device__ __forceinline__ int group_width(int G) { return G <= 1 ? 1 : G <= 2 ?
 // and later groups re-read the updated q written by the same thread, so no
 // block ever reads a q value another block may be updating.  Each thread
 // accumulates the G modes of its points in registers, layer by layer.
+// frow (optional): the stochastic forcing of row j, added to layer 0 as
+// frow * sqdt after the AB3 update (src/timestep.h:415-421)
 template <typename T, bool COMP, int GB>
 __device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool upd, T c0, T c1, T c2, const T* f0,
-                                            const T* f1, const T* f2, int G, T* A, int ld, const T* cst) {
+                                            const T* f1, const T* f2, int G, T* A, int ld, const T* cst,
+                                            const T* frow, T sqdt) {
   for (int i = threadIdx.x; i < a.nx; i += NT) {
     T acc[GB];
 #pragma unroll
@@ -218,6 +221,7 @@ __device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool up
           float lo = (float)a.qlo[o];
           const float d = ab3_increment((float)c0, (float)c1, (float)c2, (float)f0[o], (float)f1[o], (float)f2[o]);
           comp_add(hi, lo, d);
+          if (frow && l == 0) comp_add(hi, lo, (float)frow[i] * (float)sqdt);
           a.q[o] = (T)hi;
           a.qlo[o] = (T)lo;
         }
@@ -226,6 +230,7 @@ __device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool up
         v = a.q[o];
         if (upd) {
           v = ab3_plain<T>(v, c0, c1, c2, f0[o], f1[o], f2[o]);
+          if (frow && l == 0) v = v + frow[i] * sqdt;
           a.q[o] = v;
         }
       }
@@ -261,6 +266,8 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
   const T* f2 = a.fab + s2 * fs;
   const int tid = threadIdx.x;
   const int GB = group_width(a.G1);
+  const T* frow = (ab3 && a.fr.on) ? a.fr.field + (size_t)j * a.pitch : nullptr;
+  const T sqdt = frow ? (T)sqrt(st->dt) : T(0);
   for (int m0 = 0; m0 < a.nl; m0 += a.G1) {
     const int G = min(a.G1, a.nl - m0);
     const bool upd = ab3 && m0 == 0;
@@ -270,11 +277,11 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
     }
     __syncthreads();
     switch (GB) {
-      case 1: project_fwd<T, COMP, 1>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst); break;
-      case 2: project_fwd<T, COMP, 2>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst); break;
-      case 4: project_fwd<T, COMP, 4>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst); break;
-      case 8: project_fwd<T, COMP, 8>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst); break;
-      default: project_fwd<T, COMP, 16>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst); break;
+      case 1: project_fwd<T, COMP, 1>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt); break;
+      case 2: project_fwd<T, COMP, 2>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt); break;
+      case 4: project_fwd<T, COMP, 4>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt); break;
+      case 8: project_fwd<T, COMP, 8>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt); break;
+      default: project_fwd<T, COMP, 16>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt); break;
     }
     __syncthreads();
     T* O = PER ? rfft_block<T>(A, B, G, ld, a.gx, a.tx) : dst_block<T>(A, B, G, ld, a.gx, a.tx, tot);
@@ -1134,6 +1141,7 @@ __global__ void __launch_bounds__(NT) k_flush(StepArgs<T> a) {
   int s0, s1, s2;
   slabs(st->step_index, s0, s1, s2);
   const double c0 = st->c0, c1 = st->c1, c2 = st->c2;
+  const double sqdt = sqrt(st->dt);
   const size_t fs = (size_t)a.nl * a.lstride;
   const T* f0 = a.fab + s0 * fs;
   const T* f1 = a.fab + s1 * fs;
@@ -1143,14 +1151,19 @@ __global__ void __launch_bounds__(NT) k_flush(StepArgs<T> a) {
     const size_t row = w / a.nx;
     const int i = (int)(w - row * a.nx);
     const size_t o = row * a.pitch + i;
+    // layer 0 also takes the stochastic forcing (src/timestep.h:415-421)
+    const T* fo = (a.fr.on && row < (size_t)a.ny) ? a.fr.field + o : nullptr;
     if (COMP) {
       float hi = (float)a.q[o], lo = (float)a.qlo[o];
       const float d = ab3_increment((float)c0, (float)c1, (float)c2, (float)f0[o], (float)f1[o], (float)f2[o]);
       comp_add(hi, lo, d);
+      if (fo) comp_add(hi, lo, (float)*fo * (float)sqdt);
       a.q[o] = (T)hi;
       a.qlo[o] = (T)lo;
     } else {
-      a.q[o] = ab3_plain<T>(a.q[o], (T)c0, (T)c1, (T)c2, f0[o], f1[o], f2[o]);
+      T v = ab3_plain<T>(a.q[o], (T)c0, (T)c1, (T)c2, f0[o], f1[o], f2[o]);
+      if (fo) v = v + *fo * (T)sqdt;
+      a.q[o] = v;
     }
   }
 }
@@ -1170,25 +1183,132 @@ __global__ void __launch_bounds__(NT) k_flush_ens(EnsArgs<T> e) {
       int s0, s1, s2;
       slabs(st->step_index, s0, s1, s2);
       const double c0 = st->c0, c1 = st->c1, c2 = st->c2;
+      const double sqdt = sqrt(st->dt);
       const size_t fs = (size_t)sa.nl * sa.lstride;
       for (int l = 0; l < sa.nl; ++l)
         for (int i = threadIdx.x; i < sa.nx; i += NT) {
           const size_t o = (size_t)l * sa.lstride + (size_t)j * sa.pitch + i;
+          const T* fo = (sa.fr.on && l == 0) ? sa.fr.field + o : nullptr;
           if (COMP) {
             float hi = (float)sa.q[o], lo = (float)sa.qlo[o];
             const float d = ab3_increment((float)c0, (float)c1, (float)c2, (float)sa.fab[s0 * fs + o],
                                           (float)sa.fab[s1 * fs + o], (float)sa.fab[s2 * fs + o]);
             comp_add(hi, lo, d);
+            if (fo) comp_add(hi, lo, (float)*fo * (float)sqdt);
             sa.q[o] = (T)hi;
             sa.qlo[o] = (T)lo;
           } else {
-            sa.q[o] = ab3_plain<T>(sa.q[o], (T)c0, (T)c1, (T)c2, sa.fab[s0 * fs + o], sa.fab[s1 * fs + o],
-                                   sa.fab[s2 * fs + o]);
+            T v = ab3_plain<T>(sa.q[o], (T)c0, (T)c1, (T)c2, sa.fab[s0 * fs + o], sa.fab[s1 * fs + o],
+                               sa.fab[s2 * fs + o]);
+            if (fo) v = v + *fo * (T)sqdt;
+            sa.q[o] = v;
           }
         }
     }
     __syncthreads();
   }
+}
+
+// --------------------------------------------------- stochastic forcing
+// F1: new ring amplitudes after each completed step (calc_forc,
+// src/forcing.h:170-190): three draws per ring point from the C-library
+// sequence in the order the reference consumes them (the logarithm's,
+// the cosine's, the phase's), made by one thread chunk by chunk; the
+// transcendental functions run on all threads.
+constexpr double QGW_PI = 3.14159265358979323846;
+constexpr int FORC_CHUNK = 1024;
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_forc_modes(StepArgs<T> a) {
+  DevState* st = a.state;
+  const ForcArgs<T>& f = a.fr;
+  __shared__ uint32_t rv[3 * FORC_CHUNK];
+  __shared__ GlibcRand g;
+  __shared__ int go;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    go = st->forc_step != st->step_index;  // one field per completed step
+    if (go) g = *f.rng;
+  }
+  __syncthreads();
+  if (!go) return;
+  for (int c0 = 0; c0 < f.nring; c0 += FORC_CHUNK) {
+    const int nc = min(FORC_CHUNK, f.nring - c0);
+    if (tid == 0)
+      for (int k = 0; k < 3 * nc; ++k) rv[k] = glibc_rand_next(&g);
+    __syncthreads();
+    for (int k = tid; k < nc; k += NT) {
+      const int ii = c0 + k;
+      const int i = f.ring[2 * ii], j = f.ring[2 * ii + 1];
+      const double rl = (double)rv[3 * k], rc = (double)rv[3 * k + 1], rp = (double)rv[3 * k + 2];
+      const double nn = sqrt(-2. * log((rl + 1.) / (GLIBC_RAND_MAX + 2.))) * cos(2 * QGW_PI * rc / GLIBC_RAND_MAX);
+      const double em = f.env * (f.sigma * nn);
+      const double ph = rp / GLIBC_RAND_MAX * 2 * QGW_PI;
+      T* d = f.spec + (size_t)j * f.fpitch + 2 * i;
+      d[0] = (T)(em * cos(ph));
+      d[1] = (T)(em * sin(ph));
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    *f.rng = g;
+    st->forc_step = st->step_index;
+  }
+}
+
+// F2: backward complex FFT along j of two complex columns i per block
+// (the first dimension of the NF x NF c2r, unnormalised).
+template <typename T>
+__global__ void __launch_bounds__(NT) k_forc_cols(StepArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const ForcArgs<T>& f = a.fr;
+  const int ld = padded_len(f.gy.M);
+  T* A = (T*)smem_raw;
+  T* B = A + 2 * ld;
+  const int c4 = 4 * blockIdx.x;
+  for (int j = threadIdx.x; j < f.NF; j += NT) {
+    T v[4];
+    load_cols<T, 4>(f.spec + (size_t)j * f.fpitch + c4, v);
+    C2<T> z0, z1;
+    z0.x = v[0]; z0.y = -v[1]; z1.x = v[2]; z1.y = -v[3];
+    ((C2<T>*)A)[pc(j)] = z0;
+    ((C2<T>*)(A + ld))[pc(j)] = z1;
+  }
+  __syncthreads();
+  T* O = cfft_block<T>(A, B, 2, ld, f.gy, f.ty.tw);
+  for (int j = threadIdx.x; j < f.NF; j += NT) {
+    const C2<T> z0 = ((const C2<T>*)O)[pc(j)];
+    const C2<T> z1 = ((const C2<T>*)(O + ld))[pc(j)];
+    T v[4] = {z0.x, -z0.y, z1.x, -z1.y};
+    store_cols<T, 4>(f.spec2 + (size_t)j * f.fpitch + c4, v);
+  }
+}
+
+// F3: c2r along i of row j, written as the forcing of the run's interior
+// row j (forc[i+1][j+1] = forc_p[j][i], src/forcing.h:196-200).
+template <typename T>
+__global__ void __launch_bounds__(NT) k_forc_rows(StepArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const ForcArgs<T>& f = a.fr;
+  const int j = blockIdx.x;
+  const int ld = padded_len(f.gx.M);
+  T* A = (T*)smem_raw;
+  T* B = A + ld;
+  const T* src = f.spec2 + (size_t)j * f.fpitch;
+  for (int i = threadIdx.x; i < f.NF + 2; i += NT) A[pr(i)] = src[i];
+  __syncthreads();
+  T* O = irfft_block<T>(A, B, 1, ld, f.gx, f.tx);
+  T* dst = f.field + (size_t)j * a.pitch;
+  for (int i = threadIdx.x; i < a.nx; i += NT) dst[i] = (i & 1) ? -O[pr(i)] : O[pr(i)];
+}
+
+template <typename T>
+static void launch_forcing(const StepArgs<T>& a, cudaStream_t s) {
+  const ForcArgs<T>& f = a.fr;
+  if (!f.on) return;
+  k_forc_modes<T><<<1, NT, 0, s>>>(a);
+  k_forc_cols<T><<<(f.NF / 2 + 2) / 2, NT, (size_t)4 * padded_len(f.gy.M) * sizeof(T), s>>>(a);
+  k_forc_rows<T><<<a.ny, NT, (size_t)2 * padded_len(f.gx.M) * sizeof(T), s>>>(a);
 }
 
 // FP32c <-> FP64 conversions for the boundary copies
@@ -1302,6 +1422,8 @@ static cudaError_t set_attrs(const StepArgs<T>& a) {
   if ((e = cudaFuncSetAttribute(k_rows_fwd<T, COMP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
   if ((e = cudaFuncSetAttribute(k_rows_inv<T, COMP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
   if ((e = cudaFuncSetAttribute(k_cols<T, COMP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
+  if ((e = cudaFuncSetAttribute(k_forc_cols<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
+  if ((e = cudaFuncSetAttribute(k_forc_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
   const int rl = optin - 1024;
   if ((e = cudaFuncSetAttribute(k_rhs<T, COMP, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, rl)) != cudaSuccess)
     return e;
@@ -1373,11 +1495,15 @@ void enqueue_begin(DevState* st, double t_out, double tend, cudaStream_t s) { k_
 void enqueue_step_f64(const StepArgs<double>& a, cudaStream_t s) {
   launch_invert<double, false>(a, 1, s);
   launch_rhs<double, false>(a, s);
+  launch_forcing<double>(a, s);
 }
 void enqueue_step_f32c(const StepArgs<float>& a, cudaStream_t s) {
   launch_invert<float, true>(a, 1, s);
   launch_rhs<float, true>(a, s);
+  launch_forcing<float>(a, s);
 }
+void enqueue_forcing_f64(const StepArgs<double>& a, cudaStream_t s) { launch_forcing<double>(a, s); }
+void enqueue_forcing_f32c(const StepArgs<float>& a, cudaStream_t s) { launch_forcing<float>(a, s); }
 void enqueue_invert_f64(const StepArgs<double>& a, cudaStream_t s) { launch_invert<double, false>(a, 0, s); }
 void enqueue_invert_f32c(const StepArgs<float>& a, cudaStream_t s) { launch_invert<float, true>(a, 0, s); }
 void enqueue_flush_f64(const StepArgs<double>& a, cudaStream_t s) { launch_flush<double, false>(a, s); }

@@ -16,6 +16,9 @@ void enqueue_step_f64(const StepArgs<double>& a, cudaStream_t s);
 void enqueue_step_f32c(const StepArgs<float>& a, cudaStream_t s);
 void enqueue_invert_f64(const StepArgs<double>& a, cudaStream_t s);
 void enqueue_invert_f32c(const StepArgs<float>& a, cudaStream_t s);
+// the stochastic forcing kernels of one step (ensembles launch them per member)
+void enqueue_forcing_f64(const StepArgs<double>& a, cudaStream_t s);
+void enqueue_forcing_f32c(const StepArgs<float>& a, cudaStream_t s);
 void enqueue_flush_f64(const StepArgs<double>& a, cudaStream_t s);
 void enqueue_flush_f32c(const StepArgs<float>& a, cudaStream_t s);
 // which: 0 rows forward, 1 columns, 2 rows inverse, 3 RHS (step mode)

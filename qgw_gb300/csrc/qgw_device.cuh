@@ -21,6 +21,7 @@
 #include <stdint.h>
 
 #include "dst_core.h"
+#include "glibc_rand.h"
 
 namespace qgw {
 
@@ -41,6 +42,27 @@ struct DevState {
   int nonfinite;
   int step_index;                  // RHS evaluations so far (slab rotation)
   int max_steps;                   // > 0: stop after this many steps in the call
+  int forc_step;                   // step_index of the current stochastic forcing field
+};
+
+// Stochastic thin-ring forcing (src/forcing.h:67-201): each step a new
+// field of random complex amplitudes on the ring of the NF x (NF/2+1) half
+// spectrum, transformed by a 2-D c2r of size NF x NF (NF = NX), added to
+// layer 0 as forc * sqrt(dt) after the AB3 update (src/timestep.h:415-421).
+template <typename T> struct ForcArgs {
+  int on;                          // k_f != 0 and more than one ring point
+  int nring;                       // ring points (i, j)
+  int NF;                          // transform size
+  int fpitch;                      // row pitch (reals) of the spectral buffers
+  DstGeom gx, gy;                  // real FFT of NF along i; complex FFT of NF along j
+  DstTables<T> tx, ty;
+  const int* ring;                 // 2 * nring: i, j
+  double env;                      // sqrt(8 / ((N_P - 1) 2)) pi k_f / (2 pi)
+  double sigma;                    // sigma_f
+  GlibcRand* rng;                  // the C-library generator's state
+  T* spec;                         // NF x fpitch: ring amplitudes (zero elsewhere)
+  T* spec2;                        // NF x fpitch: after the transform along j
+  T* field;                        // [ny][pitch] of the run: the forcing of layer 0
 };
 
 // Everything a step kernel needs, passed by value.
@@ -99,6 +121,7 @@ template <typename T> struct StepArgs {
   int CT;                          // (unused by the kernels; kept for layout)
   int vec_cols;                    // rows are 16-byte aligned: 16-byte column loads
   int low_k64;                     // compensated: FP64 divide for mode 0, j,k < low_k64
+  ForcArgs<T> fr;                  // stochastic forcing (fr.on = 0: none)
   // doubly periodic basin (bc_fac = -1): nx = NX, ny = NY interior points,
   // pitch = NX + 4; gx has M = NX (real FFT of length NX as a complex FFT
   // of NX/2), gy has M = 2 NY (complex FFT of length NY); spectral rows hold

@@ -183,7 +183,8 @@ def test_step_stops_at_t_out_and_tend(qgwlib):
 
 
 def test_unsupported_configs_fail_loudly(qgwlib):
-    for bad in (dict(C.cfg1(64), NX=100), dict(C.cfg1(64), bc_fac=-0.5), dict(C.cfg1(64), k_f=3.0)):
+    for bad in (dict(C.cfg1(64), NX=100), dict(C.cfg1(64), bc_fac=-0.5),
+                dict(C.cfg1(64), dt_forc=1.0, dt_forc_period=10.0)):
         with pytest.raises(qgwlib.QgwError) as e:
             qgwlib.Run(bad)
         assert e.value.status == -6

@@ -23,13 +23,19 @@ def alone(capi, p, prec, q0, n):
 
 
 def test_pool_results_equal_alone(qgwlib):
-    reqs = [(C.cfg1(64), 0, 23), (C.cfg2(128, 5), 1, 40), (dict(C.cfg1(64), NY=32), 1, 7),
-            (C.cfg2(64, 10), 0, 31), (C.basin_params(32, 2, dt=900.0), 1, 50), (C.cfg1(128), 0, 12)]
+    # the first request is long, so the later ones arrive while it runs; the
+    # last two are a periodic basin and a stochastically forced periodic
+    # basin (batched apart from the closed basins)
+    forced = dict(NX=32, NY=32, nl=1, Lx=1.0, f0=2.0, beta=0.0, tau0=0.0, k_f=20.0, sigma_f=3.0,
+                  bc_fac=-1.0, dh=[1.0], N2=[0.0], nu=0.01, hEkb=0.0, tend=1e12, cfl=0.2, dt=2e-4)
+    reqs = [(C.cfg1(64), 0, 3000), (C.cfg2(128, 5), 1, 40), (dict(C.cfg1(64), NY=32), 1, 7),
+            (C.cfg2(64, 10), 0, 31), (C.basin_params(32, 2, dt=900.0), 1, 50), (C.cfg1(128), 0, 12),
+            (dict(C.cfg1(64), bc_fac=-1.0), 0, 17), (forced, 0, 25)]
     pool = qgwlib.Pool(budget_bytes=0, steps_per_tick=8)
     ids = []
     for k, (p, prec, n) in enumerate(reqs):
         ids.append(pool.submit(p, C.noise_ic(p, 900 + k), prec, n))
-        time.sleep(0.01 * k)  # arrivals while others run
+        time.sleep(0.002)  # arrivals while the first runs
     for rid in ids:
         assert pool.poll(rid, wait_ms=60000) == 0
     st = pool.stats()
