@@ -70,6 +70,7 @@ def _port_lib():
         lib.port_invert.argtypes = [vp]
         lib.port_timestep.argtypes = [vp]
         lib.port_run_steps.argtypes = [vp, ip, ip]
+        lib.port_set_forcing_records.argtypes = [vp, dp, ip]
         lib.port_run_steps.restype = ip
         lib.port_dst1.argtypes = [ip, ip, dp, ip]
         lib.port_params_read.argtypes = [ctypes.POINTER(QgwParams), ctypes.c_char_p]
@@ -115,6 +116,12 @@ class Port:
         topo = np.ascontiguousarray(topo, dtype=np.float64)
         self.lib.port_set_topo(self.h, _dp(topo))
 
+    def set_forcing_records(self, rec: np.ndarray):
+        """The 4-D forcing's records, (nrec,) + the reference layout."""
+        rec = np.ascontiguousarray(rec, dtype=np.float64)
+        assert rec.shape[1:] == self.shape
+        self.lib.port_set_forcing_records(self.h, _dp(rec), rec.shape[0])
+
     def get(self):
         psi, q = np.empty(self.shape), np.empty(self.shape)
         self.lib.port_get(self.h, _dp(psi), _dp(q))
@@ -149,9 +156,45 @@ class Port:
         return self.lib.port_run_steps(self.h, int(n), int(snap))
 
 
-def run_port(params, q0, nsteps, dt_fixed=None, topo=None, fast_dst=True):
-    """Port counterpart of ``run_ref``: returns psi, q after ``nsteps``."""
+def forcing_file_shape(params, nrec):
+    """Shape of the q_forcing_3d records read_nc expects in input_vars.nc
+    (src/netcdf_io.h:286-382): the full grid with walls, or the interior of
+    a periodic basin."""
+    nl, nyp2, nxp2 = halo_shape(params)
+    ibc = 1 if float(params.get("bc_fac", 0.0)) == -1 else 0
+    return (nrec, nl, nyp2 - 2 * ibc, nxp2 - 2 * ibc)
+
+
+def forcing_records_layout(params, frec_file: np.ndarray) -> np.ndarray:
+    """File records -> the reference layout read_nc fills (doubles)."""
+    nl, nyp2, nxp2 = halo_shape(params)
+    out = np.zeros((frec_file.shape[0], nl, nyp2, nxp2))
+    if float(params.get("bc_fac", 0.0)) == -1:
+        out[:, :, 1:-1, 1:-1] = frec_file
+    else:
+        out[:] = frec_file
+    return out
+
+
+def write_forcing_file(path, params, frec_file: np.ndarray):
+    """input_vars.nc with q_forcing_3d(time, level, y, x), float."""
+    from scipy.io import netcdf_file
+    f = netcdf_file(path, "w", version=2)
+    f.createDimension("time", None)
+    f.createDimension("level", frec_file.shape[1])
+    f.createDimension("y", frec_file.shape[2])
+    f.createDimension("x", frec_file.shape[3])
+    v = f.createVariable("q_forcing_3d", "f4", ("time", "level", "y", "x"))
+    v[:] = frec_file.astype(np.float32)
+    f.close()
+
+
+def run_port(params, q0, nsteps, dt_fixed=None, topo=None, fast_dst=True, forcing_records=None):
+    """Port counterpart of ``run_ref``: returns psi, q after ``nsteps``.
+    ``forcing_records``: the 4-D forcing's records in the file layout."""
     p = Port(params, fast_dst)
+    if forcing_records is not None:
+        p.set_forcing_records(forcing_records_layout(params, forcing_records))
     if topo is not None:
         p.set_topo(topo)
     p.set_q(q0)
@@ -170,7 +213,8 @@ def run_port(params, q0, nsteps, dt_fixed=None, topo=None, fast_dst=True):
 
 
 def run_ref(params, q0: Optional[np.ndarray], nsteps: int, dt_fixed: Optional[float] = None,
-            mode: str = "step", topo: Optional[np.ndarray] = None, fast_dst: bool = False):
+            mode: str = "step", topo: Optional[np.ndarray] = None, fast_dst: bool = False,
+            forcing_records: Optional[np.ndarray] = None):
     """Run the reference's own step code (compiled in place) and return its
     outputs.  ``params`` may carry the extra ``dt`` key; it is written to the
     params file but the reference ignores it."""
@@ -190,6 +234,8 @@ def run_ref(params, q0: Optional[np.ndarray], nsteps: int, dt_fixed: Optional[fl
             tf = os.path.join(d, "topo.bin")
             np.ascontiguousarray(topo, dtype=np.float64).tofile(tf)
             args.append(tf)
+        if forcing_records is not None:  # read by the reference itself (src/forcing.h:270-271)
+            write_forcing_file(os.path.join(d, "input_vars.nc"), params, forcing_records)
         env = dict(os.environ)
         env["QGW_SHIM_DST"] = "fast" if fast_dst else "direct"
         subprocess.run(args, check=True, cwd=d, env=env, stdout=subprocess.DEVNULL)

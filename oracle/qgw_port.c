@@ -33,6 +33,10 @@ struct port_run {
   int NF, NKf, NP, Np;     /* transform size, half size, ring points */
   int *ind_i, *ind_j;
   double *forc, *forc_f, *forc_p;
+  /* 4-D forcing records (src/forcing.h:33-43,226-288): n_rec fields of the
+   * reference layout, as read_nc loads them from input_vars.nc */
+  int nrec;
+  double* frec;
 };
 
 #define IDX(r, i, j, k) ((size_t)(k) * (r)->nxp2 * (r)->nyp2 + (size_t)(j) * (r)->nxp2 + (size_t)(i))
@@ -340,7 +344,7 @@ static void port_calc_forc(port_run* r) {
 
 void port_destroy(port_run* r) {
   if (!r) return;
-  free(r->ind_i); free(r->ind_j); free(r->forc); free(r->forc_f); free(r->forc_p);
+  free(r->ind_i); free(r->ind_j); free(r->forc); free(r->forc_f); free(r->forc_p); free(r->frec);
   free(r->X); free(r->Y); free(r->K); free(r->L); free(r->wrk);
   free(r->cl2m); free(r->cm2l); free(r->iRd2);
   free(r->psi); free(r->q); free(r->diff); free(r->lapn); free(r->topo);
@@ -560,8 +564,8 @@ static double port_adjust_timestep(port_run* r) {
   return dt;
 }
 
-/* timestep, src/timestep.h:386-439 (with the stochastic forcing; the 4-D
- * forcing add-on is off: dt_forc_period = 0). */
+/* timestep, src/timestep.h:386-439, with the stochastic and 4-D forcing
+ * add-ons. */
 void port_timestep(port_run* r) {
   double* swap = r->fab[2];
   r->fab[2] = r->fab[1];
@@ -587,6 +591,24 @@ void port_timestep(port_run* r) {
     for (int j = 1; j < r->ny + 1; ++j)
       for (int i = 1; i < r->nx + 1; ++i) r->q[IDX(r, i, j, 0)] += r->forc[IDX(r, i, j, 0)] * sqrt(dt);
   }
+  if (r->p.dt_forc_period != 0 && r->nrec > 0) { /* src/timestep.h:423-433 */
+    /* calc_4d_forcing, src/forcing.h:259-287: linear interpolation in t
+     * (the time before this step's increment) between records irec1, irec2 */
+    const int n_rec = (int)floor(r->p.dt_forc_period / r->p.dt_forc);
+    const int irec1 = ((int)floor(r->t / r->p.dt_forc)) % n_rec;
+    const int irec2 = (irec1 + 1) % n_rec;
+    const double w2 = r->t / r->p.dt_forc - (int)floor(r->t / r->p.dt_forc);
+    const double w1 = 1 - w2;
+    const size_t n3 = (size_t)r->nxp2 * r->nyp2 * r->nl;
+    const double *t1 = r->frec + (size_t)irec1 * n3, *t2 = r->frec + (size_t)irec2 * n3;
+    for (int k = 0; k < r->nl; ++k)
+      for (int j = 1; j < r->ny + 1; ++j)
+        for (int i = 1; i < r->nx + 1; ++i) {
+          const size_t s = IDX(r, i, j, k);
+          const double qf = w1 * t1[s] + w2 * t2[s];
+          r->q[s] += qf * dt;
+        }
+  }
   r->t = r->t + dt;
 }
 
@@ -606,6 +628,14 @@ void port_sizes(const port_run* r, int* nx, int* ny, int* nl) { *nx = r->nx; *ny
 
 void port_set_q(port_run* r, const double* q) {
   memcpy(r->q, q, sizeof(double) * (size_t)r->nxp2 * r->nyp2 * r->nl);
+}
+
+void port_set_forcing_records(port_run* r, const double* rec, int nrec) {
+  const size_t n3 = (size_t)r->nxp2 * r->nyp2 * r->nl;
+  free(r->frec);
+  r->frec = (double*)malloc(sizeof(double) * n3 * (nrec > 0 ? nrec : 1));
+  memcpy(r->frec, rec, sizeof(double) * n3 * nrec);
+  r->nrec = nrec;
 }
 
 void port_set_topo(port_run* r, const double* topo) {

@@ -26,6 +26,8 @@ void port_destroy(port_run* r);
 
 void port_sizes(const port_run* r, int* nx, int* ny, int* nl);
 void port_set_q(port_run* r, const double* q);
+/* the 4-D forcing's records: nrec fields in the reference layout */
+void port_set_forcing_records(port_run* r, const double* rec, int nrec);
 void port_set_topo(port_run* r, const double* topo);
 void port_get(const port_run* r, double* psi, double* q);
 void port_get_modes(const port_run* r, double* cl2m, double* cm2l, double* iRd2);

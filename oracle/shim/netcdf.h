@@ -1,8 +1,9 @@
 /*
  * netcdf.h (oracle shim) -- declares the netCDF C calls the reference makes
- * (src/netcdf_io.h:38-382).  In the oracle every call returns an error, so
- * the reference's output and restart code prints its error and returns
- * (src/netcdf_io.h:16); test infrastructure only.
+ * (src/netcdf_io.h:38-382).  In the oracle the writers return an error, so
+ * the reference's output code prints its error and returns
+ * (src/netcdf_io.h:16), and the readers read classic-format files (shim.c);
+ * test infrastructure only.
  */
 #ifndef QGW_SHIM_NETCDF_H
 #define QGW_SHIM_NETCDF_H

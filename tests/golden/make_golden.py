@@ -88,6 +88,14 @@ def cases():
     p = stochastic_params(64, 0.0)
     p.update(k_f=30.0)
     out.append(("stochastic_closed_nx64", p, 20, 5e-4, None))
+    # 4-D forcing from input_vars.nc (src/forcing.h:226-288): 3 records of
+    # q_forcing_3d, period 3 dt_forc, the run crossing record boundaries
+    for name, bc, nx in (("forcing4d_closed_nx32", 0.0, 32), ("forcing4d_periodic_nx32", -1.0, 32)):
+        p = C.cfg1(nx)
+        p.update(bc_fac=bc, dt_forc=7200.0, dt_forc_period=3 * 7200.0)
+        rng = np.random.Generator(np.random.PCG64(8100 + int(nx) + int(bc)))
+        frec = (rng.normal(0.0, 1e-11, size=O.forcing_file_shape(p, 3))).astype(np.float32)
+        out.append((name, p, 40, 1200.0, None, frec))
     return out
 
 
@@ -107,14 +115,17 @@ def main():
     if only and os.path.exists(index_path):
         with open(index_path) as f:
             index = json.load(f)
-    for n, (name, params, nsteps, dt, topo) in enumerate(cases()):
+    for n, case in enumerate(cases()):
+        name, params, nsteps, dt, topo = case[:5]
+        frec = case[5] if len(case) > 5 else None
         if only and name not in only:
             continue
         seed = 7000 + n
         q0 = C.noise_ic(params, seed)
-        r = O.run_ref(params, q0, nsteps, dt_fixed=dt, fast_dst=False)
+        r = O.run_ref(params, q0, nsteps, dt_fixed=dt, fast_dst=False, forcing_records=frec)
+        extra = {} if frec is None else {"frec": frec}
         np.savez_compressed(os.path.join(HERE, name + ".npz"), q0=q0, psi=r["psi"], q=r["q"],
-                            cl2m=r["modes"][0], cm2l=r["modes"][1], iRd2=r["modes"][2])
+                            cl2m=r["modes"][0], cm2l=r["modes"][1], iRd2=r["modes"][2], **extra)
         index[name] = {"params": params, "nsteps": nsteps, "dt_fixed": dt, "seed": seed,
                        "time": r["time"]}
         print(name, r["time"])

@@ -74,14 +74,17 @@ def test_ab3_constant_dt_coefficients():
 def test_port_matches_reference_golden(oracle_mod, name):
     meta, d = G.load(name)
     p = meta["params"]
-    r = oracle_mod.run_port(p, d["q0"], meta["nsteps"], dt_fixed=meta["dt_fixed"], fast_dst=False)
+    frec = d.get("frec")
+    r = oracle_mod.run_port(p, d["q0"], meta["nsteps"], dt_fixed=meta["dt_fixed"], fast_dst=False,
+                            forcing_records=frec)
     # same DST algorithm as the golden run: bit-identical
     assert np.array_equal(r["q"], d["q"])
     assert np.array_equal(r["psi"], d["psi"])
     for k in ("t", "dt", "dt0", "dt1"):
         assert r["time"][k] == meta["time"][k]
     # the fast DST differs only by round-off
-    r2 = oracle_mod.run_port(p, d["q0"], meta["nsteps"], dt_fixed=meta["dt_fixed"], fast_dst=True)
+    r2 = oracle_mod.run_port(p, d["q0"], meta["nsteps"], dt_fixed=meta["dt_fixed"], fast_dst=True,
+                             forcing_records=frec)
     assert oracle_mod.rel_l2(r2["q"], d["q"]) < 1e-13
     assert oracle_mod.rel_l2(r2["psi"], d["psi"]) < 1e-13
 
