@@ -174,6 +174,17 @@ int qgw_set_time(qgw_run* run, const qgw_time* in);
  * no forcing. */
 int qgw_set_forcing_seed(qgw_run* run, unsigned int seed);
 
+/* 4-D forcing (dt_forc_period != 0, src/forcing.h:226-288): the
+ * n_rec = dt_forc_period / dt_forc records of q_forcing_3d that the
+ * reference reads from input_vars.nc (read_nc, src/netcdf_io.h:286-382),
+ * given here in the reference layout (n_rec, nl, ny+2, nx+2) as read_nc
+ * fills them; they stay resident on the device.  Each step adds
+ * (w1 rec[i1] + w2 rec[i2]) * dt to every layer, the weights linear in the
+ * time before the step (calc_4d_forcing).  nrec must be at least n_rec
+ * (the first n_rec are used).  A run configured with 4-D forcing refuses
+ * to step (QGW_ERR_STATE) until its records are set. */
+int qgw_set_forcing_records(qgw_run* run, const double* records, int nrec);
+
 /* Advance up to nsteps reference time steps (timestep(), src/timestep.h:386).
  * t_out is the next output time used by the dt snapping of
  * adjust_timestep (src/timestep.h:369-381); pass 0 for none.  Mirrors the
@@ -255,6 +266,8 @@ int qgw_ensemble_step(qgw_ensemble* ens, int nsteps, const int* max_steps, int u
                       qgw_step_info* infos);
 int qgw_ensemble_tune(qgw_ensemble* ens, int trial_steps, float* best_ms);
 int qgw_ensemble_grids(qgw_ensemble* ens, int* blocks_per_sm);
+/* qgw_set_forcing_records for member i (the member table is rebuilt). */
+int qgw_ensemble_set_forcing_records(qgw_ensemble* ens, int i, const double* records, int nrec);
 
 /* ---- serving: continuous batching on one GPU -----------------------------
  * Any thread submits requests (params, initial q in the reference layout,

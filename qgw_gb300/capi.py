@@ -40,7 +40,7 @@ STATUS = {
 EXPORTS = [
     "qgw_params_default", "qgw_params_read", "qgw_eigmode", "qgw_check_timestep", "qgw_topo",
     "qgw_create", "qgw_destroy", "qgw_set_q", "qgw_set_q_device", "qgw_put_q", "qgw_get_time", "qgw_set_time",
-    "qgw_set_forcing_seed",
+    "qgw_set_forcing_seed", "qgw_set_forcing_records", "qgw_ensemble_set_forcing_records",
     "qgw_step", "qgw_invert", "qgw_get", "qgw_budget", "qgw_footprint", "qgw_stream",
     "qgw_kernels_per_step", "qgw_profile_kernels", "qgw_probe_fp_rates", "qgw_strerror", "qgw_abi_version",
     "qgw_invert_pv_noalloc", "qgw_nc_create", "qgw_nc_write", "qgw_nc_close", "qgw_nc_read",
@@ -93,6 +93,8 @@ def load(path: str = LIB_PATH):
     lib.qgw_stream.argtypes = [V]
     lib.qgw_stream.restype = V
     lib.qgw_kernels_per_step.argtypes = [V]
+    lib.qgw_set_forcing_records.argtypes = [V, D, I]
+    lib.qgw_ensemble_set_forcing_records.argtypes = [V, I, D, I]
     lib.qgw_set_forcing_seed.argtypes = [V, ctypes.c_uint]
     lib.qgw_profile_kernels.argtypes = [V, I, P(ctypes.c_float)]
     lib.qgw_probe_fp_rates.argtypes = [D, D]
@@ -230,6 +232,12 @@ class Ensemble:
         psi, q = np.empty(self.shapes[i]), np.empty(self.shapes[i])
         _check(self.lib.qgw_ensemble_get(self.h, int(i), _dp(psi), _dp(q)), "qgw_ensemble_get")
         return psi, q
+
+    def set_forcing_records(self, i: int, rec: np.ndarray):
+        """The 4-D forcing's records of member i, (nrec,) + the reference layout."""
+        rec = np.ascontiguousarray(rec, dtype=np.float64)
+        _check(self.lib.qgw_ensemble_set_forcing_records(self.h, int(i), _dp(rec), rec.shape[0]),
+               "qgw_ensemble_set_forcing_records")
 
     def tune(self, trial_steps: int = 3):
         ms = (ctypes.c_float * 4)()
@@ -381,6 +389,11 @@ class Run:
         tm = QgwTime(t, dt, dt if dt0 is None else dt0, dt if dt1 is None else dt1,
                      dt if DT_max is None else DT_max)
         _check(self.lib.qgw_set_time(self.h, ctypes.byref(tm)), "qgw_set_time")
+
+    def set_forcing_records(self, rec: np.ndarray):
+        """The 4-D forcing's records, (nrec,) + the reference layout."""
+        rec = np.ascontiguousarray(rec, dtype=np.float64)
+        _check(self.lib.qgw_set_forcing_records(self.h, _dp(rec), rec.shape[0]), "qgw_set_forcing_records")
 
     def set_forcing_seed(self, seed: int):
         """Restart the stochastic forcing's noise sequence as srand(seed)."""

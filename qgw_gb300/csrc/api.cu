@@ -373,7 +373,12 @@ int qgw_create(const qgw_params* pin, const double* cl2m, const double* cm2l, co
   // periodic: the reference's r2c layout (src/elliptic.h:21,41) is only
   // consistent for a square grid; the real FFT needs NX >= 8
   if (per && (p.NX != p.NY || p.NX < 8)) return QGW_ERR_UNSUPPORTED;
-  if (p.dt_forc_period != 0) return QGW_ERR_UNSUPPORTED;  // 4-D forcing from input files
+  if (p.dt_forc_period != 0) {
+    // init_4d_forcing's checks (src/forcing.h:236-250), as errors
+    if (p.dt_forc == 0) return QGW_ERR_PARAM;
+    const int n_rec = (int)std::floor(p.dt_forc_period / p.dt_forc);
+    if (n_rec < 1 || n_rec * p.dt_forc != p.dt_forc_period) return QGW_ERR_PARAM;
+  }
   if (!pow2(p.NX) || !pow2(p.NY) || p.NX > 8192 || p.NY > 8192) return QGW_ERR_UNSUPPORTED;
   if (p.nl < 1 || p.nl > QGW_NL_GPU_MAX) return QGW_ERR_UNSUPPORTED;
   if (!(p.Lx > 0) || !(p.cfl > 0)) return QGW_ERR_PARAM;
@@ -565,6 +570,43 @@ int qgw_get_time(qgw_run* r, qgw_time* out) {
   return QGW_OK;
 }
 
+}  // extern "C"
+
+template <typename T>
+static int set_records(qgw_run* r, StepArgs<T>& a, const double* rec, int n_rec) {
+  const size_t rs = (size_t)r->nl * r->lstride;
+  const int nxp2 = r->nx + 2, nyp2 = r->ny + 2;
+  std::vector<T> h(rs * n_rec, T(0));
+  for (int n = 0; n < n_rec; ++n)
+    for (int l = 0; l < r->nl; ++l)
+      for (int j = 0; j < r->ny; ++j)
+        for (int i = 0; i < r->nx; ++i)
+          h[n * rs + (size_t)l * r->lstride + (size_t)j * r->pitch + i] =
+              (T)rec[(((size_t)n * r->nl + l) * nyp2 + (j + 1)) * nxp2 + (i + 1)];
+  if (!a.frec) {
+    T* d;
+    int rc = dalloc(r, &d, h.size());
+    if (rc) return rc;
+    a.frec = d;
+  }
+  CK(cudaMemcpyAsync((void*)a.frec, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, r->stream));
+  CK(cudaStreamSynchronize(r->stream));
+  a.nrec = n_rec;
+  a.dt_forc = r->p.dt_forc;
+  return QGW_OK;
+}
+
+extern "C" {
+
+int qgw_set_forcing_records(qgw_run* r, const double* rec, int nrec) {
+  if (!r || !rec) return QGW_ERR_PARAM;
+  if (r->p.dt_forc_period == 0) return QGW_ERR_STATE;
+  const int n_rec = (int)std::floor(r->p.dt_forc_period / r->p.dt_forc);
+  if (nrec < n_rec) return QGW_ERR_PARAM;
+  return r->precision == QGW_FP64 ? set_records<double>(r, r->a64, rec, n_rec)
+                                  : set_records<float>(r, r->a32, rec, n_rec);
+}
+
 int qgw_set_forcing_seed(qgw_run* r, unsigned int seed) {
   if (!r) return QGW_ERR_PARAM;
   qgw::GlibcRand* rng = r->precision == QGW_FP64 ? r->a64.fr.rng : r->a32.fr.rng;
@@ -592,6 +634,8 @@ static void enqueue_invert(qgw_run* r) {
 int qgw_step(qgw_run* r, int nsteps, double t_out, double tend, qgw_step_info* info) {
   if (!r) return QGW_ERR_PARAM;
   if (!r->has_q) return QGW_ERR_STATE;
+  if (r->p.dt_forc_period != 0 && (r->precision == QGW_FP64 ? r->a64.nrec : r->a32.nrec) == 0)
+    return QGW_ERR_STATE;  // 4-D forcing records not set
   if (nsteps < 0) return QGW_ERR_PARAM;
   qgw::enqueue_begin(r->d_state, t_out, tend, r->stream);
   const int chunk = 256;

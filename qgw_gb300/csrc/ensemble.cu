@@ -235,8 +235,11 @@ int ens_core_build(EnsembleCore* e) {
 int ens_core_step(EnsembleCore* e, int nsteps, const int* max_steps, bool use_graph) {
   const int n = (int)e->members.size();
   if (n == 0) return QGW_OK;
-  for (qgw_run* r : e->members)
+  for (qgw_run* r : e->members) {
     if (!r->has_q) return QGW_ERR_STATE;
+    if (r->p.dt_forc_period != 0 && (r->precision == QGW_FP64 ? r->a64.nrec : r->a32.nrec) == 0)
+      return QGW_ERR_STATE;  // 4-D forcing records not set
+  }
   for (qgw_run* r : e->members) CK(cudaStreamSynchronize(r->stream));
   std::vector<int> ms(n, 0);
   if (max_steps) std::memcpy(ms.data(), max_steps, sizeof(int) * n);
@@ -381,6 +384,14 @@ int qgw_ensemble_get(qgw_ensemble* ens, int i, double* psi, double* q) {
   if (!e || i < 0 || i >= (int)e->members.size()) return QGW_ERR_PARAM;
   CK(cudaStreamSynchronize(e->stream));
   return qgw_get(e->members[i], psi, q);
+}
+
+int qgw_ensemble_set_forcing_records(qgw_ensemble* ens, int i, const double* rec, int nrec) {
+  qgw::EnsembleCore* e = ens ? &ens->core : nullptr;
+  if (!e || i < 0 || i >= (int)e->members.size()) return QGW_ERR_PARAM;
+  CK(cudaStreamSynchronize(e->stream));
+  const int rc = qgw_set_forcing_records(e->members[i], rec, nrec);
+  return rc ? rc : qgw::ens_core_build(e);  // the member table holds the record pointers
 }
 
 int qgw_ensemble_grids(qgw_ensemble* ens, int* bps4) {

@@ -167,6 +167,28 @@ __device__ __forceinline__ void cp_async_elem(T* smem_dst, const T* gsrc) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// Records and weights of the 4-D forcing at time t (calc_4d_forcing,
+// src/forcing.h:259-287): q_forc = w1 rec[i1] + w2 rec[i2].
+struct Forc4D {
+  int i1, i2;
+  double w1, w2;
+};
+__device__ __forceinline__ Forc4D forc4d_at(double t, double dt_forc, int nrec) {
+  Forc4D r;
+  const double fl = floor(t / dt_forc);
+  r.i1 = ((int)fl) % nrec;
+  r.i2 = (r.i1 + 1) % nrec;
+  r.w2 = t / dt_forc - (int)fl;
+  r.w1 = 1 - r.w2;
+  return r;
+}
+// q + q_forc * dt for one point (the reference's order: the weighted sum,
+// then the product with dt, then the add)
+template <typename T>
+__device__ __forceinline__ T forc4d_term(const T* rec1, const T* rec2, size_t o, T w1, T w2, T dt) {
+  return (w1 * rec1[o] + w2 * rec2[o]) * dt;
+}
+
 // ------------------------------------------------------- mode projections
 // The nl x G coefficients of one mode group are staged in shared memory as
 // cst[l * GMAX + gg] (zero for gg >= G), so one vector load serves a row of
@@ -207,7 +229,8 @@ __device__ __forceinline__ int group_width(int G) { return G <= 1 ? 1 : G <= 2 ?
 template <typename T, bool COMP, int GB>
 __device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool upd, T c0, T c1, T c2, const T* f0,
                                             const T* f1, const T* f2, int G, T* A, int ld, const T* cst,
-                                            const T* frow, T sqdt) {
+                                            const T* frow, T sqdt, const T* r1, const T* r2, T w1, T w2,
+                                            T dtf) {
   for (int i = threadIdx.x; i < a.nx; i += NT) {
     T acc[GB];
 #pragma unroll
@@ -222,6 +245,7 @@ __device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool up
           const float d = ab3_increment((float)c0, (float)c1, (float)c2, (float)f0[o], (float)f1[o], (float)f2[o]);
           comp_add(hi, lo, d);
           if (frow && l == 0) comp_add(hi, lo, (float)frow[i] * (float)sqdt);
+          if (r1) comp_add(hi, lo, (float)forc4d_term<T>(r1, r2, o, w1, w2, dtf));
           a.q[o] = (T)hi;
           a.qlo[o] = (T)lo;
         }
@@ -231,6 +255,7 @@ __device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool up
         if (upd) {
           v = ab3_plain<T>(v, c0, c1, c2, f0[o], f1[o], f2[o]);
           if (frow && l == 0) v = v + frow[i] * sqdt;
+          if (r1) v = v + forc4d_term<T>(r1, r2, o, w1, w2, dtf);
           a.q[o] = v;
         }
       }
@@ -268,6 +293,18 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
   const int GB = group_width(a.G1);
   const T* frow = (ab3 && a.fr.on) ? a.fr.field + (size_t)j * a.pitch : nullptr;
   const T sqdt = frow ? (T)sqrt(st->dt) : T(0);
+  const T* r1 = nullptr;
+  const T* r2 = nullptr;
+  T w1 = T(0), w2 = T(0), dtf = T(0);
+  if (ab3 && a.nrec > 0) {
+    const Forc4D fw = forc4d_at(st->t_prev, a.dt_forc, a.nrec);
+    const size_t rs = (size_t)a.nl * a.lstride;
+    r1 = a.frec + fw.i1 * rs;
+    r2 = a.frec + fw.i2 * rs;
+    w1 = (T)fw.w1;
+    w2 = (T)fw.w2;
+    dtf = (T)st->dt;
+  }
   for (int m0 = 0; m0 < a.nl; m0 += a.G1) {
     const int G = min(a.G1, a.nl - m0);
     const bool upd = ab3 && m0 == 0;
@@ -277,11 +314,16 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
     }
     __syncthreads();
     switch (GB) {
-      case 1: project_fwd<T, COMP, 1>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt); break;
-      case 2: project_fwd<T, COMP, 2>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt); break;
-      case 4: project_fwd<T, COMP, 4>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt); break;
-      case 8: project_fwd<T, COMP, 8>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt); break;
-      default: project_fwd<T, COMP, 16>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt); break;
+      case 1: project_fwd<T, COMP, 1>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt, r1, r2, w1, w2,
+                                     dtf); break;
+      case 2: project_fwd<T, COMP, 2>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt, r1, r2, w1, w2,
+                                     dtf); break;
+      case 4: project_fwd<T, COMP, 4>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt, r1, r2, w1, w2,
+                                     dtf); break;
+      case 8: project_fwd<T, COMP, 8>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt, r1, r2, w1, w2,
+                                     dtf); break;
+      default: project_fwd<T, COMP, 16>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt, r1, r2, w1, w2,
+                                     dtf); break;
     }
     __syncthreads();
     T* O = PER ? rfft_block<T>(A, B, G, ld, a.gx, a.tx) : dst_block<T>(A, B, G, ld, a.gx, a.tx, tot);
@@ -666,6 +708,7 @@ __device__ void scalar_update(DevState* st, double Delta, double cfl) {
   st->c2 = dt * dt * (dt / 3 + dt0 / 2) / (dt1 * (dt0 + dt1));
   st->pending = 1;
   const double tn = t + dt;
+  st->t_prev = t;
   st->t = tn;
   st->step_index += 1;
   st->steps_taken += 1;
@@ -1147,6 +1190,16 @@ __global__ void __launch_bounds__(NT) k_flush(StepArgs<T> a) {
   const T* f1 = a.fab + s1 * fs;
   const T* f2 = a.fab + s2 * fs;
   const size_t n = (size_t)a.nl * a.ny * a.nx;
+  const T* r1 = nullptr;
+  const T* r2 = nullptr;
+  T w1 = T(0), w2 = T(0);
+  if (a.nrec > 0) {
+    const Forc4D fw = forc4d_at(st->t_prev, a.dt_forc, a.nrec);
+    r1 = a.frec + fw.i1 * fs;
+    r2 = a.frec + fw.i2 * fs;
+    w1 = (T)fw.w1;
+    w2 = (T)fw.w2;
+  }
   for (size_t w = blockIdx.x * (size_t)NT + threadIdx.x; w < n; w += (size_t)gridDim.x * NT) {
     const size_t row = w / a.nx;
     const int i = (int)(w - row * a.nx);
@@ -1158,11 +1211,13 @@ __global__ void __launch_bounds__(NT) k_flush(StepArgs<T> a) {
       const float d = ab3_increment((float)c0, (float)c1, (float)c2, (float)f0[o], (float)f1[o], (float)f2[o]);
       comp_add(hi, lo, d);
       if (fo) comp_add(hi, lo, (float)*fo * (float)sqdt);
+      if (r1) comp_add(hi, lo, (float)forc4d_term<T>(r1, r2, o, w1, w2, (T)st->dt));
       a.q[o] = (T)hi;
       a.qlo[o] = (T)lo;
     } else {
       T v = ab3_plain<T>(a.q[o], (T)c0, (T)c1, (T)c2, f0[o], f1[o], f2[o]);
       if (fo) v = v + *fo * (T)sqdt;
+      if (r1) v = v + forc4d_term<T>(r1, r2, o, w1, w2, (T)st->dt);
       a.q[o] = v;
     }
   }
@@ -1185,6 +1240,16 @@ __global__ void __launch_bounds__(NT) k_flush_ens(EnsArgs<T> e) {
       const double c0 = st->c0, c1 = st->c1, c2 = st->c2;
       const double sqdt = sqrt(st->dt);
       const size_t fs = (size_t)sa.nl * sa.lstride;
+      const T* r1 = nullptr;
+      const T* r2 = nullptr;
+      T w1 = T(0), w2 = T(0);
+      if (sa.nrec > 0) {
+        const Forc4D fw = forc4d_at(st->t_prev, sa.dt_forc, sa.nrec);
+        r1 = sa.frec + fw.i1 * fs;
+        r2 = sa.frec + fw.i2 * fs;
+        w1 = (T)fw.w1;
+        w2 = (T)fw.w2;
+      }
       for (int l = 0; l < sa.nl; ++l)
         for (int i = threadIdx.x; i < sa.nx; i += NT) {
           const size_t o = (size_t)l * sa.lstride + (size_t)j * sa.pitch + i;
@@ -1195,12 +1260,14 @@ __global__ void __launch_bounds__(NT) k_flush_ens(EnsArgs<T> e) {
                                           (float)sa.fab[s1 * fs + o], (float)sa.fab[s2 * fs + o]);
             comp_add(hi, lo, d);
             if (fo) comp_add(hi, lo, (float)*fo * (float)sqdt);
+            if (r1) comp_add(hi, lo, (float)forc4d_term<T>(r1, r2, o, w1, w2, (T)st->dt));
             sa.q[o] = (T)hi;
             sa.qlo[o] = (T)lo;
           } else {
             T v = ab3_plain<T>(sa.q[o], (T)c0, (T)c1, (T)c2, sa.fab[s0 * fs + o], sa.fab[s1 * fs + o],
                                sa.fab[s2 * fs + o]);
             if (fo) v = v + *fo * (T)sqdt;
+            if (r1) v = v + forc4d_term<T>(r1, r2, o, w1, w2, (T)st->dt);
             sa.q[o] = v;
           }
         }

@@ -43,6 +43,7 @@ struct DevState {
   int step_index;                  // RHS evaluations so far (slab rotation)
   int max_steps;                   // > 0: stop after this many steps in the call
   int forc_step;                   // step_index of the current stochastic forcing field
+  double t_prev;                   // t before the last step's increment (4-D forcing time)
 };
 
 // Stochastic thin-ring forcing (src/forcing.h:67-201): each step a new
@@ -122,6 +123,12 @@ template <typename T> struct StepArgs {
   int vec_cols;                    // rows are 16-byte aligned: 16-byte column loads
   int low_k64;                     // compensated: FP64 divide for mode 0, j,k < low_k64
   ForcArgs<T> fr;                  // stochastic forcing (fr.on = 0: none)
+  // 4-D forcing (src/forcing.h:226-288): nrec records [nrec][nl][ny][pitch],
+  // interpolated linearly in time with period nrec * dt_forc, added to every
+  // layer as q_forc * dt after the AB3 update (src/timestep.h:423-433)
+  const T* frec;
+  int nrec;                        // 0: no 4-D forcing
+  double dt_forc;
   // doubly periodic basin (bc_fac = -1): nx = NX, ny = NY interior points,
   // pitch = NX + 4; gx has M = NX (real FFT of length NX as a complex FFT
   // of NX/2), gy has M = 2 NY (complex FFT of length NY); spectral rows hold

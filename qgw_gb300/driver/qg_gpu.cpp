@@ -13,6 +13,7 @@
 #include <sys/stat.h>
 #include <sys/types.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -77,8 +78,27 @@ int main(int argc, char** argv) {
   if (dir.empty()) return 1;
   backup_config(file_param, dir);
 
-  const int nx = p.NX - 1, ny = p.NY - 1, nl = p.nl;
+  // interior points: NX - 1 in a closed basin (src/domain.h:71-74), NX when
+  // periodic; files hold the full grid with walls, or the periodic interior
+  // (ibc = 1, src/netcdf_io.h:41-47,295-301)
+  const bool per = p.bc_fac == -1;
+  const int nx = per ? p.NX : p.NX - 1, ny = per ? p.NY : p.NY - 1, nl = p.nl;
+  const int ibc = per ? 1 : 0, nxo = nx + 2 - 2 * ibc, nyo = ny + 2 - 2 * ibc;
   const size_t n2 = (size_t)(nx + 2) * (ny + 2), n3 = n2 * nl;
+  const size_t n2o = (size_t)nxo * nyo, n3o = n2o * nl;
+  // file layout <-> reference layout, nk fields
+  auto to_ref = [&](const std::vector<double>& f, std::vector<double>& full, int nk) {
+    for (int k = 0; k < nk; ++k)
+      for (int j = ibc; j < ny + 2 - ibc; ++j)
+        for (int i = ibc; i < nx + 2 - ibc; ++i)
+          full[(size_t)k * n2 + (size_t)j * (nx + 2) + i] = f[(size_t)k * n2o + (size_t)(j - ibc) * nxo + (i - ibc)];
+  };
+  auto to_file = [&](const std::vector<double>& full, std::vector<double>& f, int nk) {
+    for (int k = 0; k < nk; ++k)
+      for (int j = ibc; j < ny + 2 - ibc; ++j)
+        for (int i = ibc; i < nx + 2 - ibc; ++i)
+          f[(size_t)k * n2o + (size_t)(j - ibc) * nxo + (i - ibc)] = full[(size_t)k * n2 + (size_t)j * (nx + 2) + i];
+  };
   std::vector<double> cl2m((size_t)nl * nl), cm2l((size_t)nl * nl), iRd2(nl);
   if ((rc = qgw_eigmode(&p, cl2m.data(), cm2l.data(), iRd2.data()))) {
     std::printf("vertical modes: %s\n", qgw_strerror(rc));
@@ -89,12 +109,20 @@ int main(int argc, char** argv) {
     std::printf("iRd2: %g , def radius: %g\n", iRd2[k], iRd2[k] > 0 ? std::sqrt(1 / iRd2[k]) : 0.0);
 
   // restart (src/qg.c:160-164): q and topo from record 0 of restart.nc
-  std::vector<double> q(n3, 0.0), psi(n3, 0.0), topo;
+  std::vector<double> q(n3, 0.0), psi(n3, 0.0), topo, fbuf(n3o);
   if (file_exists("restart.nc")) {
-    if (qgw_nc_read("restart.nc", "q", 0, q.data(), (long)n3) > 0) std::printf("Reading variable  q!\n");
-    topo.resize(n2);
-    if (qgw_nc_read("restart.nc", "topo", 0, topo.data(), (long)n2) > 0) std::printf("Reading variable  topo!\n");
-    else topo.clear();
+    if (qgw_nc_read("restart.nc", "q", 0, fbuf.data(), (long)n3o) > 0) {
+      std::printf("Reading variable  q!\n");
+      to_ref(fbuf, q, nl);
+    }
+    topo.assign(n2, 0.0);
+    std::vector<double> tb(n2o);
+    if (qgw_nc_read("restart.nc", "topo", 0, tb.data(), (long)n2o) > 0) {
+      std::printf("Reading variable  topo!\n");
+      to_ref(tb, topo, 1);
+    } else {
+      topo.clear();
+    }
   }
   qgw_run* run = nullptr;
   rc = qgw_create(&p, cl2m.data(), cm2l.data(), iRd2.data(), topo.empty() ? nullptr : topo.data(), precision, &run);
@@ -103,11 +131,34 @@ int main(int argc, char** argv) {
     return 1;
   }
   qgw_set_q(run, q.data());
+  // 4-D forcing: the n_rec records of q_forcing_3d in input_vars.nc
+  // (init_4d_forcing / calc_4d_forcing, src/forcing.h:226-288), all
+  // resident on the device; a missing file leaves zero records, as the
+  // reference's read_nc prints its error and returns
+  if (p.dt_forc_period != 0) {
+    std::printf("Init 4d forcing. \n");
+    const int n_rec = (int)std::floor(p.dt_forc_period / p.dt_forc);
+    std::vector<double> rec((size_t)n_rec * n3, 0.0), one(n3);
+    for (int r = 0; r < n_rec; ++r) {
+      if (qgw_nc_read("input_vars.nc", "q_forcing_3d", r, fbuf.data(), (long)n3o) <= 0) {
+        std::printf("input_vars.nc: record %d of q_forcing_3d not read\n", r);
+        continue;
+      }
+      std::fill(one.begin(), one.end(), 0.0);
+      to_ref(fbuf, one, nl);
+      std::copy(one.begin(), one.end(), rec.begin() + (size_t)r * n3);
+    }
+    if ((rc = qgw_set_forcing_records(run, rec.data(), n_rec))) {
+      std::printf("qgw_set_forcing_records: %s\n", qgw_strerror(rc));
+      return 1;
+    }
+  }
   qgw_time tm;
   qgw_get_time(run, &tm);
   std::printf("Maximum time step: DT_MAX = %g \nInitial time step: dt = %g \n", tm.DT_max, tm.dt);
 
-  qgw_nc* nc = qgw_nc_create((dir + "vars.nc").c_str(), nl, ny + 2, nx + 2, p.Lx / p.NX);
+  qgw_nc* nc = qgw_nc_create((dir + "vars.nc").c_str(), nl, nyo, nxo, p.Lx / p.NX);
+  std::vector<double> psio(n3o), qo(n3o);
   if (!nc) {
     std::printf("cannot create %svars.nc\n", dir.c_str());
     return 1;
@@ -121,7 +172,9 @@ int main(int argc, char** argv) {
       t_out += p.dt_out;
       qgw_get(run, psi.data(), q.data());
       std::printf("Write output, t = %e \n", t);
-      qgw_nc_write(nc, t, psi.data(), q.data());
+      to_file(psi, psio, nl);
+      to_file(q, qo, nl);
+      qgw_nc_write(nc, t, psio.data(), qo.data());
     }
     qgw_step_info info;
     rc = qgw_step(run, 1 << 30, t_out, p.tend, &info);

@@ -21,8 +21,22 @@ def rel(a, b):
     return np.linalg.norm(a - b) / nb if nb > 0 else np.linalg.norm(a - b)
 
 
-def gpu_run(capi, params, q0, nsteps, dt_fixed, precision=0, topo=None, snap=False):
+def records_layout(params, frec_file):
+    """The 4-D forcing's file records (input_vars.nc layout) in the
+    reference layout read_nc fills (src/netcdf_io.h:360-370)."""
+    nl, nyp2, nxp2 = C.halo_shape(params)
+    out = np.zeros((frec_file.shape[0], nl, nyp2, nxp2))
+    if float(params.get("bc_fac", 0.0)) == -1:
+        out[:, :, 1:-1, 1:-1] = frec_file
+    else:
+        out[:] = frec_file
+    return out
+
+
+def gpu_run(capi, params, q0, nsteps, dt_fixed, precision=0, topo=None, snap=False, frec=None):
     r = capi.Run(params, precision, topo=topo)
+    if frec is not None:
+        r.set_forcing_records(records_layout(params, frec))
     r.set_q(q0)
     if dt_fixed:
         r.fix_dt(dt_fixed)
@@ -51,7 +65,7 @@ def gpu_run(capi, params, q0, nsteps, dt_fixed, precision=0, topo=None, snap=Fal
 def test_fp64_matches_reference_golden(qgwlib, name):
     meta, d = G.load(name)
     p = meta["params"]
-    psi, q, tm = gpu_run(qgwlib, p, d["q0"], meta["nsteps"], meta["dt_fixed"])
+    psi, q, tm = gpu_run(qgwlib, p, d["q0"], meta["nsteps"], meta["dt_fixed"], frec=d.get("frec"))
     assert rel(q, d["q"]) <= TOL64, rel(q, d["q"])
     assert rel(psi, d["psi"]) <= TOL64, rel(psi, d["psi"])
     assert tm["t"] == pytest.approx(meta["time"]["t"], rel=1e-14)
@@ -183,8 +197,8 @@ def test_step_stops_at_t_out_and_tend(qgwlib):
 
 
 def test_unsupported_configs_fail_loudly(qgwlib):
-    for bad in (dict(C.cfg1(64), NX=100), dict(C.cfg1(64), bc_fac=-0.5),
-                dict(C.cfg1(64), dt_forc=1.0, dt_forc_period=10.0)):
+    deep = dict(C.cfg2(64, 33))  # more layers than the GPU kernels hold (32)
+    for bad in (dict(C.cfg1(64), NX=100), dict(C.cfg1(64), bc_fac=-0.5), deep):
         with pytest.raises(qgwlib.QgwError) as e:
             qgwlib.Run(bad)
         assert e.value.status == -6
