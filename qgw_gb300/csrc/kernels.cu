@@ -226,7 +226,9 @@ __device__ __forceinline__ int group_width(int G) { return G <= 1 ? 1 : G <= 2 ?
 // accumulates the G modes of its points in registers, layer by layer.
 // frow (optional): the stochastic forcing of row j, added to layer 0 as
 // frow * sqdt after the AB3 update (src/timestep.h:415-421)
-template <typename T, bool COMP, int GB>
+// FORCED: the stochastic or 4-D forcing is on (a separate instantiation, so
+// that the unforced loop carries none of it)
+template <typename T, bool COMP, int GB, bool FORCED>
 __device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool upd, T c0, T c1, T c2, const T* f0,
                                             const T* f1, const T* f2, int G, T* A, int ld, const T* cst,
                                             const T* frow, T sqdt, const T* r1, const T* r2, T w1, T w2,
@@ -244,8 +246,10 @@ __device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool up
           float lo = (float)a.qlo[o];
           const float d = ab3_increment((float)c0, (float)c1, (float)c2, (float)f0[o], (float)f1[o], (float)f2[o]);
           comp_add(hi, lo, d);
-          if (frow && l == 0) comp_add(hi, lo, (float)frow[i] * (float)sqdt);
-          if (r1) comp_add(hi, lo, (float)forc4d_term<T>(r1, r2, o, w1, w2, dtf));
+          if (FORCED) {
+            if (frow && l == 0) comp_add(hi, lo, (float)frow[i] * (float)sqdt);
+            if (r1) comp_add(hi, lo, (float)forc4d_term<T>(r1, r2, o, w1, w2, dtf));
+          }
           a.q[o] = (T)hi;
           a.qlo[o] = (T)lo;
         }
@@ -254,8 +258,10 @@ __device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool up
         v = a.q[o];
         if (upd) {
           v = ab3_plain<T>(v, c0, c1, c2, f0[o], f1[o], f2[o]);
-          if (frow && l == 0) v = v + frow[i] * sqdt;
-          if (r1) v = v + forc4d_term<T>(r1, r2, o, w1, w2, dtf);
+          if (FORCED) {
+            if (frow && l == 0) v = v + frow[i] * sqdt;
+            if (r1) v = v + forc4d_term<T>(r1, r2, o, w1, w2, dtf);
+          }
           a.q[o] = v;
         }
       }
@@ -313,18 +319,27 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
       cst[w] = g < G ? a.cl2m[(size_t)(m0 + g) * a.nl + l] : T(0);
     }
     __syncthreads();
-    switch (GB) {
-      case 1: project_fwd<T, COMP, 1>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt, r1, r2, w1, w2,
-                                     dtf); break;
-      case 2: project_fwd<T, COMP, 2>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt, r1, r2, w1, w2,
-                                     dtf); break;
-      case 4: project_fwd<T, COMP, 4>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt, r1, r2, w1, w2,
-                                     dtf); break;
-      case 8: project_fwd<T, COMP, 8>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt, r1, r2, w1, w2,
-                                     dtf); break;
-      default: project_fwd<T, COMP, 16>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt, r1, r2, w1, w2,
-                                     dtf); break;
+    const bool forced = upd && (frow || r1);
+#define QGW_PF(GBV, F) project_fwd<T, COMP, GBV, F>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt, r1, \
+                                                  r2, w1, w2, dtf)
+    if (forced) {
+      switch (GB) {
+        case 1: QGW_PF(1, true); break;
+        case 2: QGW_PF(2, true); break;
+        case 4: QGW_PF(4, true); break;
+        case 8: QGW_PF(8, true); break;
+        default: QGW_PF(16, true); break;
+      }
+    } else {
+      switch (GB) {
+        case 1: QGW_PF(1, false); break;
+        case 2: QGW_PF(2, false); break;
+        case 4: QGW_PF(4, false); break;
+        case 8: QGW_PF(8, false); break;
+        default: QGW_PF(16, false); break;
+      }
     }
+#undef QGW_PF
     __syncthreads();
     T* O = PER ? rfft_block<T>(A, B, G, ld, a.gx, a.tx) : dst_block<T>(A, B, G, ld, a.gx, a.tx, tot);
     const int nout = PER ? a.nx + 2 : a.nx;
