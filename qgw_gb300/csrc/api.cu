@@ -355,7 +355,8 @@ int qgw_footprint(const qgw_params* p, int precision, size_t* bytes) {
   const size_t field = (size_t)p->nl * ny * (nx + (per ? 4 : 1));
   size_t b;
   if (precision == QGW_FP64) b = field * 8 * 7;  // q psi spec f0 f1 f2 hinv
-  else b = field * 4 * 9 + field * 8;            // q_hi q_lo psi spec spec2 zeta f0 f1 f2 + FP64 staging
+  else b = field * 4 * 9;                        // q_hi q_lo psi spec spec2 zeta f0 f1 f2
+  b += (size_t)p->nl * (ny + 2) * (nx + 2) * 8;  // reference-layout staging for host copies
   if (p->k_f != 0) b += (size_t)3 * p->NX * (p->NX + 4) * (precision == QGW_FP64 ? 8 : 4);  // forcing
   *bytes = b + (size_t)(nx + ny) * 64 + (1 << 20);
   return QGW_OK;
@@ -418,7 +419,10 @@ int qgw_create(const qgw_params* pin, const double* cl2m, const double* cm2l, co
     if ((rc = setup_args<double>(r, r->a64))) return fail(rc);
   } else {
     if ((rc = setup_args<float>(r, r->a32))) return fail(rc);
-    if ((rc = dalloc(r, &r->d_stage, (size_t)r->nl * r->lstride))) return fail(rc);
+  }
+  {
+    const size_t nfull = (size_t)r->nl * (r->ny + 2) * (r->nx + 2);
+    if ((rc = dalloc(r, &r->d_full, nfull))) return fail(rc);
   }
   // topography: explicit array, or the analytic shelf when h_topo != 0
   std::vector<double> th;
@@ -479,31 +483,6 @@ void qgw_destroy(qgw_run* r) {
 void* qgw_stream(qgw_run* r) { return r ? (void*)r->stream : nullptr; }
 int qgw_kernels_per_step(qgw_run* r) { return r ? 4 : 0; }
 
-static cudaMemcpy3DParms copy_params(qgw_run* r, const void* src, bool src_ref, void* dst, bool dst_ref,
-                                     size_t elem) {
-  // reference layout: (nl, ny+2, nx+2), interior at (1, 1); device layout:
-  // (nl, ny, pitch), interior at (0, 0)
-  cudaMemcpy3DParms c{};
-  const size_t rw = (size_t)(r->nx + 2) * elem, dw = (size_t)r->pitch * elem;
-  if (src_ref) {
-    c.srcPtr = make_cudaPitchedPtr((void*)src, rw, r->nx + 2, r->ny + 2);
-    c.srcPos = make_cudaPos(elem, 1, 0);
-  } else {
-    c.srcPtr = make_cudaPitchedPtr((void*)src, dw, r->pitch, r->ny);
-    c.srcPos = make_cudaPos(0, 0, 0);
-  }
-  if (dst_ref) {
-    c.dstPtr = make_cudaPitchedPtr(dst, rw, r->nx + 2, r->ny + 2);
-    c.dstPos = make_cudaPos(elem, 1, 0);
-  } else {
-    c.dstPtr = make_cudaPitchedPtr(dst, dw, r->pitch, r->ny);
-    c.dstPos = make_cudaPos(0, 0, 0);
-  }
-  c.extent = make_cudaExtent((size_t)r->nx * elem, r->ny, r->nl);
-  c.kind = cudaMemcpyDefault;
-  return c;
-}
-
 static int reset_history(qgw_run* r) {
   const size_t field = (size_t)r->nl * r->lstride;
   void* fab = r->precision == QGW_FP64 ? (void*)r->a64.fab : (void*)r->a32.fab;
@@ -520,19 +499,27 @@ static int reset_history(qgw_run* r) {
   return QGW_OK;
 }
 
+// q in the reference layout -> the run layout: one contiguous copy into the
+// staging buffer (or the caller's device array directly), then a kernel
+static int load_q(qgw_run* r, const double* q, bool device_src) {
+  const double* full = q;
+  if (!device_src) {
+    const size_t nfull = (size_t)r->nl * (r->ny + 2) * (r->nx + 2);
+    CK(cudaMemcpyAsync(r->d_full, q, sizeof(double) * nfull, cudaMemcpyHostToDevice, r->stream));
+    full = r->d_full;
+  }
+  if (r->precision == QGW_FP64)
+    qgw::enqueue_unpack_f64(full, r->a64.q, r->nx, r->ny, r->nl, r->pitch, r->stream);
+  else
+    qgw::enqueue_unpack_split(full, r->a32.q, r->a32.qlo, r->nx, r->ny, r->nl, r->pitch, r->stream);
+  return QGW_OK;
+}
+
 static int set_q_impl(qgw_run* r, const double* q, bool device_src) {
   if (!r || !q) return QGW_ERR_PARAM;
-  (void)device_src;
-  if (r->precision == QGW_FP64) {
-    cudaMemcpy3DParms c = copy_params(r, q, true, r->a64.q, false, sizeof(double));
-    CK(cudaMemcpy3DAsync(&c, r->stream));
-  } else {
-    cudaMemcpy3DParms c = copy_params(r, q, true, r->d_stage, false, sizeof(double));
-    CK(cudaMemcpy3DAsync(&c, r->stream));
-    qgw::enqueue_split_f64(r->d_stage, r->a32.q, r->a32.qlo, (size_t)r->nl * r->lstride, r->stream);
-  }
-  int rc = reset_history(r);
+  int rc = load_q(r, q, device_src);
   if (rc) return rc;
+  if ((rc = reset_history(r))) return rc;
   CK(cudaStreamSynchronize(r->stream));
   CK(cudaGetLastError());
   r->has_q = true;
@@ -545,14 +532,8 @@ int qgw_set_q_device(qgw_run* r, const double* q) { return set_q_impl(r, q, true
 int qgw_put_q(qgw_run* r, const double* q) {
   if (!r || !q) return QGW_ERR_PARAM;
   if (!r->has_q) return QGW_ERR_STATE;
-  if (r->precision == QGW_FP64) {
-    cudaMemcpy3DParms c = copy_params(r, q, true, r->a64.q, false, sizeof(double));
-    CK(cudaMemcpy3DAsync(&c, r->stream));
-  } else {
-    cudaMemcpy3DParms c = copy_params(r, q, true, r->d_stage, false, sizeof(double));
-    CK(cudaMemcpy3DAsync(&c, r->stream));
-    qgw::enqueue_split_f64(r->d_stage, r->a32.q, r->a32.qlo, (size_t)r->nl * r->lstride, r->stream);
-  }
+  int rc = load_q(r, q, false);
+  if (rc) return rc;
   CK(cudaStreamSynchronize(r->stream));
   CK(cudaGetLastError());
   return QGW_OK;
@@ -688,29 +669,23 @@ int qgw_get(qgw_run* r, double* psi, double* q) {
   // psi is the inversion of the current q; q alone needs it only for the
   // ghost values of a no-slip or partial-slip wall
   if (psi || (r->p.bc_fac != 0 && r->p.bc_fac != -1)) enqueue_invert(r);
-  const size_t field = (size_t)r->nl * r->lstride;
-  if (psi) {
-    const void* src = r->a64.psi;
-    if (r->precision != QGW_FP64) {
-      qgw::enqueue_join_f64(r->a32.psi, nullptr, r->d_stage, field, r->stream);
-      src = r->d_stage;
-    }
-    cudaMemcpy3DParms c = copy_params(r, src, false, psi, true, sizeof(double));
-    CK(cudaMemcpy3DAsync(&c, r->stream));
-  }
-  std::vector<double> psi_tmp;
-  if (q) {
-    const void* src = r->a64.q;
-    if (r->precision != QGW_FP64) {
-      CK(cudaStreamSynchronize(r->stream));
-      qgw::enqueue_join_f64(r->a32.q, r->a32.qlo, r->d_stage, field, r->stream);
-      src = r->d_stage;
-    }
-    cudaMemcpy3DParms c = copy_params(r, src, false, q, true, sizeof(double));
-    CK(cudaMemcpy3DAsync(&c, r->stream));
-  }
+  const size_t nfull = (size_t)r->nl * (r->ny + 2) * (r->nx + 2);
+  // one field out through the staging buffer: pack (interior), contiguous copy
+  auto fetch = [&](bool want_psi, double* host) -> int {
+    if (r->precision == QGW_FP64)
+      qgw::enqueue_pack_f64(want_psi ? r->a64.psi : r->a64.q, r->d_full, r->nx, r->ny, r->nl, r->pitch, r->stream);
+    else
+      qgw::enqueue_pack_join(want_psi ? r->a32.psi : r->a32.q, want_psi ? nullptr : r->a32.qlo, r->d_full, r->nx,
+                             r->ny, r->nl, r->pitch, r->stream);
+    CK(cudaMemcpyAsync(host, r->d_full, sizeof(double) * nfull, cudaMemcpyDeviceToHost, r->stream));
+    CK(cudaStreamSynchronize(r->stream));
+    return QGW_OK;
+  };
+  int rc;
+  if (psi && (rc = fetch(true, psi))) return rc;
+  if (q && (rc = fetch(false, q))) return rc;
   CK(cudaGetLastError());
-  CK(cudaStreamSynchronize(r->stream));
+  std::vector<double> psi_tmp;
   // ghost rings as adjust_bc leaves them after invert_pv
   // (src/elliptic.h:225-226, src/domain.h:308-348)
   const int nxp2 = r->nx + 2, nyp2 = r->ny + 2;
@@ -733,11 +708,7 @@ int qgw_get(qgw_run* r, double* psi, double* q) {
   const double* ps = psi;
   if (q && !psi && c != 0) {
     psi_tmp.resize(L * r->nl);
-    cudaMemcpy3DParms cp = copy_params(r, r->precision == QGW_FP64 ? (const void*)r->a64.psi : (const void*)r->d_stage,
-                                       false, psi_tmp.data(), true, sizeof(double));
-    if (r->precision != QGW_FP64) qgw::enqueue_join_f64(r->a32.psi, nullptr, r->d_stage, field, r->stream);
-    CK(cudaMemcpy3DAsync(&cp, r->stream));
-    CK(cudaStreamSynchronize(r->stream));
+    if ((rc = fetch(true, psi_tmp.data()))) return rc;
     ps = psi_tmp.data();
   }
   for (int k = 0; k < r->nl; ++k) {

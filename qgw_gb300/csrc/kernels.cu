@@ -1393,6 +1393,41 @@ static void launch_forcing(const StepArgs<T>& a, cudaStream_t s) {
   k_forc_rows<T><<<a.ny, NT, (size_t)2 * padded_len(f.gx.M) * sizeof(T), s>>>(a);
 }
 
+// Boundary copies: the reference layout (nl, ny+2, nx+2) in one contiguous
+// device buffer <-> the interior-only run layout; a host array then crosses
+// the link in one contiguous copy instead of one row per DMA segment.
+template <typename T, bool SPLIT>
+__global__ void __launch_bounds__(256) k_unpack(const double* __restrict__ full, T* __restrict__ dst,
+                                                T* __restrict__ lo, int nx, int ny, int nl, int pitch) {
+  const size_t n = (size_t)nl * ny * nx;
+  for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < n; w += (size_t)gridDim.x * blockDim.x) {
+    const size_t row = w / nx;
+    const int i = (int)(w - row * nx);
+    const int l = (int)(row / ny), j = (int)(row - (size_t)l * ny);
+    const double v = full[((size_t)l * (ny + 2) + (j + 1)) * (nx + 2) + (i + 1)];
+    const size_t o = row * pitch + i;
+    if (SPLIT) {
+      const float h = (float)v;
+      dst[o] = (T)h;
+      lo[o] = (T)(float)(v - (double)h);
+    } else {
+      dst[o] = (T)v;
+    }
+  }
+}
+template <typename T>
+__global__ void __launch_bounds__(256) k_pack(const T* __restrict__ src, const T* __restrict__ lo,
+                                              double* __restrict__ full, int nx, int ny, int nl, int pitch) {
+  const size_t n = (size_t)nl * ny * nx;
+  for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < n; w += (size_t)gridDim.x * blockDim.x) {
+    const size_t row = w / nx;
+    const int i = (int)(w - row * nx);
+    const int l = (int)(row / ny), j = (int)(row - (size_t)l * ny);
+    const size_t o = row * pitch + i;
+    full[((size_t)l * (ny + 2) + (j + 1)) * (nx + 2) + (i + 1)] = (double)src[o] + (lo ? (double)lo[o] : 0.0);
+  }
+}
+
 // FP32c <-> FP64 conversions for the boundary copies
 __global__ void k_split_f64(const double* src, float* hi, float* lo, size_t n) {
   for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < n; w += (size_t)gridDim.x * blockDim.x) {
@@ -1592,6 +1627,21 @@ void enqueue_flush_f64(const StepArgs<double>& a, cudaStream_t s) { launch_flush
 void enqueue_flush_f32c(const StepArgs<float>& a, cudaStream_t s) { launch_flush<float, true>(a, s); }
 void enqueue_step_kernel_f64(const StepArgs<double>& a, int which, cudaStream_t s) { launch_one<double, false>(a, which, s); }
 void enqueue_step_kernel_f32c(const StepArgs<float>& a, int which, cudaStream_t s) { launch_one<float, true>(a, which, s); }
+
+void enqueue_unpack_f64(const double* full, double* q, int nx, int ny, int nl, int pitch, cudaStream_t s) {
+  k_unpack<double, false><<<152 * 8, 256, 0, s>>>(full, q, nullptr, nx, ny, nl, pitch);
+}
+void enqueue_unpack_split(const double* full, float* hi, float* lo, int nx, int ny, int nl, int pitch,
+                          cudaStream_t s) {
+  k_unpack<float, true><<<152 * 8, 256, 0, s>>>(full, hi, lo, nx, ny, nl, pitch);
+}
+void enqueue_pack_f64(const double* src, double* full, int nx, int ny, int nl, int pitch, cudaStream_t s) {
+  k_pack<double><<<152 * 8, 256, 0, s>>>(src, nullptr, full, nx, ny, nl, pitch);
+}
+void enqueue_pack_join(const float* hi, const float* lo, double* full, int nx, int ny, int nl, int pitch,
+                       cudaStream_t s) {
+  k_pack<float><<<152 * 8, 256, 0, s>>>(hi, lo, full, nx, ny, nl, pitch);
+}
 
 void enqueue_split_f64(const double* src, float* hi, float* lo, size_t n, cudaStream_t s) {
   k_split_f64<<<1024, 256, 0, s>>>(src, hi, lo, n);

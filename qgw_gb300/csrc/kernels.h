@@ -25,6 +25,13 @@ void enqueue_flush_f32c(const StepArgs<float>& a, cudaStream_t s);
 void enqueue_step_kernel_f64(const StepArgs<double>& a, int which, cudaStream_t s);
 void enqueue_step_kernel_f32c(const StepArgs<float>& a, int which, cudaStream_t s);
 
+// reference layout (nl, ny+2, nx+2), contiguous on the device <-> run layout
+void enqueue_unpack_f64(const double* full, double* q, int nx, int ny, int nl, int pitch, cudaStream_t s);
+void enqueue_unpack_split(const double* full, float* hi, float* lo, int nx, int ny, int nl, int pitch,
+                          cudaStream_t s);
+void enqueue_pack_f64(const double* src, double* full, int nx, int ny, int nl, int pitch, cudaStream_t s);
+void enqueue_pack_join(const float* hi, const float* lo, double* full, int nx, int ny, int nl, int pitch,
+                       cudaStream_t s);
 void enqueue_split_f64(const double* src, float* hi, float* lo, size_t n, cudaStream_t s);
 void enqueue_join_f64(const float* hi, const float* lo, double* dst, size_t n, cudaStream_t s);
 

@@ -19,7 +19,7 @@ struct qgw_run {
   std::vector<void*> allocs;
   qgw::DevState* d_state = nullptr;
   qgw::DevState* h_state = nullptr;  // pinned
-  double* d_stage = nullptr;    // FP64 staging field (compensated path)
+  double* d_full = nullptr;        // (nl, ny+2, nx+2) reference-layout staging for host copies
   double* d_wts = nullptr;
   double* d_part = nullptr;
   double* d_bout = nullptr;
