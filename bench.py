@@ -224,6 +224,30 @@ KERNEL_NAMES = ["rows_fwd (AB3 + projection + x-DST)", "cols (y-DST, Helmholtz, 
 
 
 # -------------------------------------------------------------------- ours
+def rank_ops(world, device):
+    """Replica coordination: a barrier and the maximum of a value over ranks
+    (each rank runs its own whole run; no data-path collective)."""
+    import torch
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    return barrier, max_over_ranks
+
+
+def whole_job_rate(lgp_per_rank, steps, seconds_max, world):
+    """lgp-steps/s of all replicas together, timed by the slowest rank."""
+    return world * lgp_per_rank * steps / seconds_max
+
+
 def run_ours(args, rank, world, local_rank):
     import numpy as np
     import torch
@@ -235,16 +259,7 @@ def run_ours(args, rank, world, local_rank):
     lgp = lgp_of(p)
     q0 = configs.noise_ic(p, 2000)
 
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-
-    def max_over_ranks(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+    barrier, max_over_ranks = rank_ops(world, "cuda")
 
     def timed(precision, K, W, clocks=None):
         run = capi.Run(p, precision)
@@ -273,7 +288,7 @@ def run_ours(args, rank, world, local_rank):
     K, W = args.steps, args.warmup
     clocks = Clocks(local_rank)
     run64, ms64, kms64, cl = timed(0, K, W, clocks)
-    value = world * lgp * K / (ms64 / 1e3)
+    value = whole_job_rate(lgp, K, ms64 / 1e3, world)
 
     hbm_peak, peak_kind = read_measured_peaks()
     fp64_peak, fp32_peak = capi.probe_fp_rates()
