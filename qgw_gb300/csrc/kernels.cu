@@ -907,22 +907,6 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
     }
   }
   __syncthreads();
-  // centred differences shared between neighbouring Jacobian evaluations
-  for (int w = tid; w < TY * QW; w += NT) {
-    const int y = w / QW, x = w - y * QW;
-    const int xx = x - 1;
-    dyp[w] = PS(xx, y + 1) - PS(xx, y - 1);
-    dyq[w] = QS(xx, y + 1) - QS(xx, y - 1);
-  }
-  for (int w = tid; w < QH * TX; w += NT) {
-    const int y = w / TX, x = w - y * TX;
-    const int yy = y - 1;
-    dxp[w] = PS(x + 1, yy) - PS(x - 1, yy);
-    dxq[w] = QS(x + 1, yy) - QS(x - 1, yy);
-  }
-  __syncthreads();
-#define DY(arr, x, y) arr[(y) * QW + (x) + 1]
-#define DX(arr, x, y) arr[((y) + 1) * TX + (x)]
   const size_t fs = (size_t)a.nl * a.lstride;
   int s0, s1, s2;
   slabs(step_index + 1, s0, s1, s2);
@@ -930,23 +914,13 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
   const bool bottom = (k == a.nl - 1);
   decltype(absbits_native(T(0))) mymax_n = 0;
   const int x = tx;
-  for (int y = ty; y < TY; y += 8) {
+  // the rest of the RHS at one point (src/dynamics.h:55-69) given its
+  // Jacobian J and the centred differences dxp = psi_E - psi_W,
+  // dyp = psi_N - psi_S; then the CFL maximum
+  auto finish = [&](int y, T J, T dxp, T dyp) {
     const int gi = i0 + x, gj = j0 + y;
-    if (EDGE && (gi >= nx || gj >= ny)) continue;
-    // Arakawa Jacobian J(psi, q) (jacobian_lev, src/domain.h:17-27) with the
-    // centred differences shared: 2 products + 8 fused terms
-    T J = DX(dxp, x, y) * DY(dyq, x, y);
-    J = fmaT(-DY(dyp, x, y), DX(dxq, x, y), J);
-    J = fmaT(PS(x + 1, y), DY(dyq, x + 1, y), J);
-    J = fmaT(-PS(x - 1, y), DY(dyq, x - 1, y), J);
-    J = fmaT(-PS(x, y + 1), DX(dxq, x, y + 1), J);
-    J = fmaT(PS(x, y - 1), DX(dxq, x, y - 1), J);
-    J = fmaT(QS(x, y + 1), DX(dxp, x, y + 1), J);
-    J = fmaT(-QS(x, y - 1), DX(dxp, x, y - 1), J);
-    J = fmaT(-QS(x + 1, y), DY(dyp, x + 1, y), J);
-    J = fmaT(QS(x - 1, y), DY(dyp, x - 1, y), J);
     // rhs, src/dynamics.h:55-58: -J - beta psi_x + nu lap q + nu_h lap^n psi
-    T f = fmaT(m_inv12, J, -(b2d * DX(dxp, x, y)));
+    T f = fmaT(m_inv12, J, -(b2d * dxp));
     if (a.has_nu) {
       const T lq = fmaT(T(-4), QS(x, y), (QS(x + 1, y) + QS(x - 1, y)) + (QS(x, y + 1) + QS(x, y - 1)));
       f = fmaT(nu_d2, lq, f);
@@ -965,7 +939,7 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
         const int tp = nx + 2;
         const double* tb = a.topo + (size_t)(gj + 1) * tp + (gi + 1);
 #define TP(dx, dy) ((T)tb[(dy) * tp + (dx)])
-        const T jt = (DX(dxp, x, y) * (TP(0, 1) - TP(0, -1)) - DY(dyp, x, y) * (TP(1, 0) - TP(-1, 0))
+        const T jt = (dxp * (TP(0, 1) - TP(0, -1)) - dyp * (TP(1, 0) - TP(-1, 0))
                       + PS(x + 1, y) * (TP(1, 1) - TP(1, -1)) - PS(x - 1, y) * (TP(-1, 1) - TP(-1, -1))
                       - PS(x, y + 1) * (TP(1, 1) - TP(-1, 1)) + PS(x, y - 1) * (TP(1, -1) - TP(-1, -1))
                       + TP(0, 1) * (PS(x + 1, y + 1) - PS(x - 1, y + 1))
@@ -983,6 +957,72 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
     const auto bu = absbits_native(du), bv = absbits_native(dv);
     const auto bm = bu > bv ? bu : bv;
     mymax_n = bm > mymax_n ? bm : mymax_n;
+  };
+  if constexpr (sizeof(T) == 4) {
+    // FP32: the Arakawa Jacobian (jacobian_lev, src/domain.h:17-27)
+    // straight from the tiles, two vertically adjacent points per thread
+    // sharing their 4 x 3 neighbourhoods (FP32 arithmetic is cheap; the
+    // instructions that move data are not)
+    const int y0 = 2 * ty;
+    T P[4][3], Q[4][3];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        P[r][c] = PS(x + c - 1, y0 + r - 1);
+        Q[r][c] = QS(x + c - 1, y0 + r - 1);
+      }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int y = y0 + h;
+      if (EDGE && (i0 + x >= nx || j0 + y >= ny)) continue;
+      const int r = h + 1;  // centre row in P, Q
+      const T dxp = P[r][2] - P[r][0], dyp = P[r + 1][1] - P[r - 1][1];
+      const T dxq = Q[r][2] - Q[r][0], dyq = Q[r + 1][1] - Q[r - 1][1];
+      T J = dxp * dyq;
+      J = fmaT(-dyp, dxq, J);
+      J = fmaT(P[r][2], Q[r + 1][2] - Q[r - 1][2], J);
+      J = fmaT(-P[r][0], Q[r + 1][0] - Q[r - 1][0], J);
+      J = fmaT(-P[r + 1][1], Q[r + 1][2] - Q[r + 1][0], J);
+      J = fmaT(P[r - 1][1], Q[r - 1][2] - Q[r - 1][0], J);
+      J = fmaT(Q[r + 1][1], P[r + 1][2] - P[r + 1][0], J);
+      J = fmaT(-Q[r - 1][1], P[r - 1][2] - P[r - 1][0], J);
+      J = fmaT(-Q[r][2], P[r + 1][2] - P[r - 1][2], J);
+      J = fmaT(Q[r][0], P[r + 1][0] - P[r - 1][0], J);
+      finish(y, J, dxp, dyp);
+    }
+  } else {
+    // FP64: centred differences shared between neighbouring Jacobian
+    // evaluations (fewer FP64 operations: 2 products + 8 fused terms)
+    for (int w = tid; w < TY * QW; w += NT) {
+      const int y = w / QW, xw = w - y * QW;
+      const int xx = xw - 1;
+      dyp[w] = PS(xx, y + 1) - PS(xx, y - 1);
+      dyq[w] = QS(xx, y + 1) - QS(xx, y - 1);
+    }
+    for (int w = tid; w < QH * TX; w += NT) {
+      const int y = w / TX, xw = w - y * TX;
+      const int yy = y - 1;
+      dxp[w] = PS(xw + 1, yy) - PS(xw - 1, yy);
+      dxq[w] = QS(xw + 1, yy) - QS(xw - 1, yy);
+    }
+    __syncthreads();
+#define DY(arr, x, y) arr[(y) * QW + (x) + 1]
+#define DX(arr, x, y) arr[((y) + 1) * TX + (x)]
+    for (int y = ty; y < TY; y += 8) {
+      if (EDGE && (i0 + x >= nx || j0 + y >= ny)) continue;
+      T J = DX(dxp, x, y) * DY(dyq, x, y);
+      J = fmaT(-DY(dyp, x, y), DX(dxq, x, y), J);
+      J = fmaT(PS(x + 1, y), DY(dyq, x + 1, y), J);
+      J = fmaT(-PS(x - 1, y), DY(dyq, x - 1, y), J);
+      J = fmaT(-PS(x, y + 1), DX(dxq, x, y + 1), J);
+      J = fmaT(PS(x, y - 1), DX(dxq, x, y - 1), J);
+      J = fmaT(QS(x, y + 1), DX(dxp, x, y + 1), J);
+      J = fmaT(-QS(x, y - 1), DX(dxp, x, y - 1), J);
+      J = fmaT(-QS(x + 1, y), DY(dyp, x + 1, y), J);
+      J = fmaT(QS(x - 1, y), DY(dyp, x - 1, y), J);
+      finish(y, J, DX(dxp, x, y), DY(dyp, x, y));
+    }
   }
 #undef DY
 #undef DX
