@@ -2,6 +2,8 @@
 // boundary copies in the reference layout, the device-resident step loop
 // and diagnostics.  All device memory of a run is allocated in qgw_create
 // and released in qgw_destroy.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -95,6 +97,37 @@ int mode_group(int nl, int M, size_t elem, size_t budget, int rows_per_mode, int
   if (g < 1) g = 1;
   const int ngroups = (nl + g - 1) / g;
   return (nl + ngroups - 1) / ngroups;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no
+// libcuda link dependency); null when the driver does not provide it
+PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* ptr = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+    return (PFN_cuTensorMapEncodeTiled_v12000)ptr;
+  }();
+  return fn;
+}
+
+// 3-D map (x, y, layer) of a run field for the RHS kernel's tile boxes:
+// rhs_box_width() columns x `rows` rows x 1 layer; out-of-range elements
+// read as zero.  The driver checks the base alignment, strides and box.
+template <typename T>
+bool encode_tile_map(CUtensorMap* m, const T* base, const qgw_run* r, int rows) {
+  const cuuint64_t dims[3] = {(cuuint64_t)r->nx, (cuuint64_t)r->ny, (cuuint64_t)r->nl};
+  const cuuint64_t strides[2] = {(cuuint64_t)r->pitch * sizeof(T), (cuuint64_t)r->lstride * sizeof(T)};
+  const cuuint32_t box[3] = {(cuuint32_t)qgw::rhs_box_width(), (cuuint32_t)rows, 1};
+  const cuuint32_t es[3] = {1, 1, 1};
+  const CUresult e = tmap_encoder()(m, sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                                    3, (void*)base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return e == CUDA_SUCCESS;
 }
 
 template <typename T>
@@ -321,6 +354,19 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   float* fi;
   if ((rc = upload<float>(r, &fi, r->iRd2))) return rc;
   a.iRd2f = fi;
+  // TMA tensor maps of the RHS kernel's interior tiles (psi with halo R, q
+  // with halo 1, zeta over the first sweep's region); element-wise
+  // asynchronous copies when the driver cannot encode them, or when
+  // QGW_RHS_TILE_LOADS=copies asks for that path
+  std::memset(a.tm, 0, sizeof(a.tm));
+  a.use_tma = 0;
+  const char* loads = std::getenv("QGW_RHS_TILE_LOADS");
+  if (tmap_encoder() && !(loads && !std::strcmp(loads, "copies"))) {
+    const int R = a.nsweep > 0 ? a.nsweep : 1, HH = qgw::rhs_tile_y() + 2 * R;
+    bool ok = encode_tile_map<T>(&a.tm[0], a.psi, r, HH) && encode_tile_map<T>(&a.tm[1], a.q, r, qgw::rhs_tile_y() + 2);
+    if (ok && a.zeta_mode && a.nsweep >= 1) ok = encode_tile_map<T>(&a.tm[2], a.zeta, r, HH - 2);
+    a.use_tma = ok ? 1 : 0;
+  }
   return QGW_OK;
 }
 
@@ -496,6 +542,7 @@ static int reset_history(qgw_run* r) {
   CK(cudaMemsetAsync(&d->step_index, 0, sizeof(int), r->stream));
   CK(cudaMemsetAsync(&d->forc_step, 0, sizeof(int), r->stream));
   CK(cudaMemsetAsync(&d->nonfinite, 0, sizeof(int), r->stream));
+  CK(cudaMemsetAsync(&d->dev_error, 0, sizeof(int), r->stream));
   return QGW_OK;
 }
 
@@ -651,6 +698,7 @@ int qgw_step(qgw_run* r, int nsteps, double t_out, double tend, qgw_step_info* i
     info->stop_reason = s.stop_reason;
     info->nonfinite = s.nonfinite;
   }
+  if (s.dev_error) return QGW_ERR_TIMEOUT;  // a bounded device wait ran out
   return s.nonfinite ? QGW_ERR_NAN : QGW_OK;
 }
 

@@ -283,10 +283,11 @@ int qgw_ensemble_step(qgw_ensemble* ens, int nsteps, const int* max_steps, int u
   int rc = qgw::ens_core_step(e, nsteps, max_steps, use_graph != 0);
   if (rc) return rc;
   if ((rc = qgw::ens_core_finish(e))) return rc;
-  bool bad = false;
+  bool bad = false, timeout = false;
   for (int i = 0; i < n; ++i) {
     const qgw::DevState& s = e->h_states[i];
     bad = bad || s.nonfinite;
+    timeout = timeout || s.dev_error;
     if (infos) {
       infos[i].time.t = s.t;
       infos[i].time.dt = s.dt;
@@ -298,6 +299,7 @@ int qgw_ensemble_step(qgw_ensemble* ens, int nsteps, const int* max_steps, int u
       infos[i].nonfinite = s.nonfinite;
     }
   }
+  if (timeout) return QGW_ERR_TIMEOUT;  // a bounded device wait ran out
   return bad ? QGW_ERR_NAN : QGW_OK;
 }
 

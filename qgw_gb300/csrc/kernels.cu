@@ -167,6 +167,46 @@ __device__ __forceinline__ void cp_async_elem(T* smem_dst, const T* gsrc) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// Tensor-memory-accelerator tile loads completing on a shared-memory
+// mbarrier (one elected thread issues them; every thread waits, bounded).
+__device__ __forceinline__ unsigned int smem_u32(const void* p) { return (unsigned int)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned int bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned int parity) {
+  unsigned int ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait: false when the limit ran out (the caller records an error)
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned int parity) {
+  for (int it = 0; it < (1 << 22); ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z,
+                                            unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::
+          "r"(smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+// order this thread's earlier generic shared-memory accesses before later
+// asynchronous-proxy (TMA) writes to the same memory
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+
 // Records and weights of the 4-D forcing at time t (calc_4d_forcing,
 // src/forcing.h:259-287): q_forc = w1 rec[i1] + w2 rec[i2].
 struct Forc4D {
@@ -752,16 +792,37 @@ __device__ __forceinline__ int wrap_index(int g, int n) {
 // plus its halo touches a wall, so loads are bounds-checked and ghost values
 // follow adjust_bc; interior tiles (the vast majority) skip all of that.
 // Returns this thread's CFL maximum |dpsi| as bits in the arithmetic width.
+// Shared-memory layout of the RHS tile: psi-shaped arrays (psi, the two
+// chain buffers) have HH = TY + 2R rows of TW = TX + 8 columns, tile column
+// xx at TW offset TOX = 4 (xx = -4..TX+3, the span of one TMA box starting at
+// the 16-byte aligned x = i0 - 4); the q tile has QH = TY + 2 rows of TW
+// columns with the same column offset.  Each array starts 128-byte aligned.
+constexpr int TW = TX + 8, TOX = 4;
+template <typename T> __host__ __device__ constexpr int tile_round(int n) {
+  return (n + (128 / (int)sizeof(T)) - 1) / (128 / (int)sizeof(T)) * (128 / (int)sizeof(T));
+}
+
+// RHS tile of TX x TY points of one layer; block (32, 8); R = halo radius
+// of psi (the number of hyperviscosity sweeps, at least 1).  EDGE: the tile
+// plus its halo touches a wall, so loads are bounds-checked and ghost values
+// follow adjust_bc (or wrap around, periodic); interior tiles (the vast
+// majority) arrive by TMA (tm != null, bar: the block's mbarrier, *phase its
+// parity) or by element-wise asynchronous copies.  Returns this thread's CFL
+// maximum |dpsi| as bits in the arithmetic width.
 template <typename T, bool COMP, int R, bool EDGE>
 __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArgs<T>& a, int i0, int j0, int k,
-                                                                    int step_index, unsigned char* smem_raw) {
-  constexpr int W = TX + 2 * R, HH = TY + 2 * R;
+                                                                    int step_index, unsigned char* smem_raw,
+                                                                    const CUtensorMap* tm, unsigned long long* bar,
+                                                                    unsigned int* phase, bool* failed) {
+  constexpr int W = TW, HH = TY + 2 * R;
   constexpr int QW = TX + 2, QH = TY + 2;
+  constexpr int XO = TOX;  // column of tile x = 0
+  constexpr int TS = tile_round<T>(W * HH), QS_ = tile_round<T>(W * QH);
   T* ps = (T*)smem_raw;       // HH x W, psi with halo R
-  T* L0 = ps + W * HH;        // chain ping-pong
-  T* L1 = L0 + W * HH;
-  T* qs = L1 + W * HH;        // QH x QW
-  T* dyp = qs + QW * QH;      // TY x QW
+  T* L0 = ps + TS;            // chain ping-pong
+  T* L1 = L0 + TS;
+  T* qs = L1 + TS;            // QH x W
+  T* dyp = qs + QS_;          // TY x QW (FP64 only)
   T* dyq = dyp + QW * TY;
   T* dxp = dyq + QW * TY;     // QH x TX
   T* dxq = dxp + TX * QH;
@@ -777,48 +838,73 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
   const T m_inv12 = pick<T>(-a.inv12d2, a.fc[FC_MINV12]), b2d = pick<T>(a.b2d, a.fc[FC_B2D]);
   const T nu_d2 = pick<T>(a.nu_d2, a.fc[FC_NUD2]), nuh = pick<T>(a.nuh_scaled, a.fc[FC_NUH]);
   const T drag = pick<T>(a.drag_d2, a.fc[FC_DRAG]), topo_c = pick<T>(-(a.inv12d2 * a.topo_fac), a.fc[FC_TOPOC]);
-#define PS(x, y) ps[((y) + R) * W + (x) + R]
-#define QS(x, y) qs[((y) + 1) * QW + (x) + 1]
+#define PS(x, y) ps[((y) + R) * W + (x) + XO]
+#define QS(x, y) qs[((y) + 1) * W + (x) + XO]
   const int tid = tx + ty * 32;
   const bool per = a.periodic != 0;
   if (EDGE && per) {
     // periodic: every halo value is an interior value of the other side
     // (src/domain.h:225-256); tiles may be wider than the domain
-    for (int w = tid; w < HH * W; w += NT) {
-      const int y = w / W, x = w - y * W;
-      ps[w] = psiL[(size_t)wrap_index(j0 + y - R, ny) * pitch + wrap_index(i0 + x - R, nx)];
+    for (int w = tid; w < HH * (TX + 2 * R); w += NT) {
+      const int y = w / (TX + 2 * R), xx = w - y * (TX + 2 * R) - R;
+      ps[y * W + xx + XO] = psiL[(size_t)wrap_index(j0 + y - R, ny) * pitch + wrap_index(i0 + xx, nx)];
     }
     for (int w = tid; w < QH * QW; w += NT) {
-      const int y = w / QW, x = w - y * QW;
-      qs[w] = qL[(size_t)wrap_index(j0 + y - 1, ny) * pitch + wrap_index(i0 + x - 1, nx)];
+      const int y = w / QW, xx = w - y * QW - 1;
+      qs[y * W + xx + XO] = qL[(size_t)wrap_index(j0 + y - 1, ny) * pitch + wrap_index(i0 + xx, nx)];
     }
   } else if (EDGE) {
-    for (int w = tid; w < HH * W; w += NT) {
-      const int y = w / W, x = w - y * W;
-      const int gi = i0 + x - R, gj = j0 + y - R;
+    for (int w = tid; w < HH * (TX + 2 * R); w += NT) {
+      const int y = w / (TX + 2 * R), xx = w - y * (TX + 2 * R) - R;
+      const int gi = i0 + xx, gj = j0 + y - R;
       T v = T(0);
       if (gi >= 0 && gi < nx && gj >= 0 && gj < ny) v = psiL[(size_t)gj * pitch + gi];
-      ps[w] = v;
+      ps[y * W + xx + XO] = v;
     }
+  } else if (tm) {
+    // interior tile by TMA: psi (HH rows), q (QH rows) and, in zeta mode,
+    // the raw zeta of the first sweep's region (HH - 2 rows, into L1 from
+    // its row 0; L1 is free until the second sweep), each box TW columns
+    // from x = i0 - 4; one mbarrier collects the bytes
+    if (tid == 0) {
+      fence_proxy_async_smem();
+      const bool z1 = zm && a.nsweep >= 1;
+      const unsigned int bytes = (unsigned int)sizeof(T) * W * (HH + QH + (z1 ? HH - 2 : 0));
+      mbar_expect_tx(bar, bytes);
+      tma_load_3d(ps, &tm[0], i0 - XO, j0 - R, k, bar);
+      tma_load_3d(qs, &tm[1], i0 - XO, j0 - 1, k, bar);
+      if (z1) tma_load_3d(L1, &tm[2], i0 - XO, j0 + 1 - R, k, bar);
+    }
+    // block-uniform outcome of the bounded wait
+    const bool ok = __syncthreads_and(mbar_wait_bounded(bar, *phase)) != 0;
+    if (!ok) {
+      // the copies did not arrive: flag the run, give them one more bounded
+      // wait (they may still land in this block's shared memory), skip
+      *failed = true;
+      (void)mbar_wait_bounded(bar, *phase);
+      if (tid == 0) a.state->dev_error = 1;
+      *phase ^= 1u;
+      return 0;
+    }
+    *phase ^= 1u;
   } else {
-    // interior tile: psi, q and (zeta mode) the raw zeta of the first
-    // sweep's region are independent, so all three copies go out together
+    // interior tile by element-wise asynchronous copies (all three together)
     const T* src = psiL + (size_t)(j0 - R) * pitch + (i0 - R);
-    for (int w = tid; w < HH * W; w += NT) {
-      const int y = w / W, x = w - y * W;
-      cp_async_elem(ps + w, src + y * pitch + x);
+    for (int w = tid; w < HH * (TX + 2 * R); w += NT) {
+      const int y = w / (TX + 2 * R), x = w - y * (TX + 2 * R);
+      cp_async_elem(ps + y * W + x - R + XO, src + y * pitch + x);
     }
     const T* qsrc = qL + (size_t)(j0 - 1) * pitch + (i0 - 1);
     for (int w = tid; w < QH * QW; w += NT) {
       const int y = w / QW, x = w - y * QW;
-      cp_async_elem(qs + w, qsrc + y * pitch + x);
+      cp_async_elem(qs + y * W + x - 1 + XO, qsrc + y * pitch + x);
     }
     if (zm && a.nsweep >= 1) {
-      constexpr int W1 = W - 2, H1 = HH - 2;
+      constexpr int W1 = TX + 2 * R - 2, H1 = HH - 2;
       const T* zsrc = zetaL + (size_t)(j0 + 1 - R) * pitch + (i0 + 1 - R);
       for (int w = tid; w < W1 * H1; w += NT) {
         const int yr = w / W1, xr = w - yr * W1;
-        cp_async_elem(L0 + (yr + 1) * W + xr + 1, zsrc + yr * pitch + xr);
+        cp_async_elem(L1 + yr * W + xr + 1 - R + XO, zsrc + yr * pitch + xr);
       }
     }
     cp_async_wait_all();
@@ -837,26 +923,28 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
       else if (iny && gi == nx) v = cbc * PS(xx - 1, yy);
       else if (inx && gj == -1) v = cbc * PS(xx, yy + 1);
       else if (inx && gj == ny) v = cbc * PS(xx, yy - 1);
-      qs[w] = v;
+      qs[y * W + xx + XO] = v;
     }
   }
   // hyperviscosity chain (calc_diff, src/dynamics.h:13-44) on the tile with
   // a shrinking halo; sweeps are unscaled (no 1/Delta^2), the scale is in
   // nuh_scaled and in the ghost factors gh[s]; in zeta mode the first
   // sweep is the spectral zeta.  Unrolled over s so that every region
-  // width is a compile-time constant.
+  // width is a compile-time constant.  Region of sweep s: tile rows
+  // yy = s-R .. TY+R-s-1 (smem row yy + R), columns xx likewise (xx + XO).
   const T* Lp = ps;
   T* Lc = L0;
 #pragma unroll
   for (int s = 1; s <= R; ++s) {
     if (s <= a.nsweep) {
       __syncthreads();
-      const int Ws = W - 2 * s, Hs = HH - 2 * s;
+      const int Ws = TX + 2 * R - 2 * s, Hs = HH - 2 * s;
+      const int cx = s - R + XO;  // smem column of the region's first point
       if (EDGE && per) {
         // periodic: no walls, the sweep is the Laplacian everywhere
         for (int w = tid; w < Ws * Hs; w += NT) {
           const int yr = w / Ws, xr = w - yr * Ws;
-          const int o = (yr + s) * W + xr + s;
+          const int o = (yr + s) * W + xr + cx;
           if (s == 1 && zm) {
             Lc[o] = d2 * zetaL[(size_t)wrap_index(j0 + yr + s - R, ny) * pitch + wrap_index(i0 + xr + s - R, nx)];
           } else {
@@ -868,11 +956,10 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
         const T ghs = pick<T>(a.gh[s], a.fc[FC_GH1 + s - 1]);
         for (int w = tid; w < Ws * Hs; w += NT) {
           const int yr = w / Ws, xr = w - yr * Ws;
-          const int x = xr + s, y = yr + s;
-          const int xx = x - R, yy = y - R;
+          const int xx = xr + s - R, yy = yr + s - R;
           const int gi = i0 + xx, gj = j0 + yy;
           const bool inx = gi >= 0 && gi < nx, iny = gj >= 0 && gj < ny;
-          const int o = y * W + x;
+          const int o = (yr + s) * W + xr + cx;
           T v = T(0);
           if (inx && iny) {
             if (s == 1 && zm) {
@@ -888,18 +975,22 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
           Lc[o] = v;
         }
       } else if (s == 1 && zm) {
-        // the raw zeta is already in place (L0 == Lc): scale it
+        // the raw zeta arrived in L1, one row up (its row 0 is the region's
+        // first row): scale it into L0 (== Lc)
         for (int w = tid; w < Ws * Hs; w += NT) {
           const int yr = w / Ws, xr = w - yr * Ws;
-          const int o = (yr + s) * W + xr + s;
-          Lc[o] = d2 * Lc[o];
+          const int o = (yr + s) * W + xr + cx;
+          Lc[o] = d2 * L1[o - W];
         }
       } else {
-        for (int w = tid; w < Ws * Hs; w += NT) {
-          const int yr = w / Ws, xr = w - yr * Ws;
-          const int o = (yr + s) * W + xr + s;
-          const T sum = (Lp[o + 1] + Lp[o - 1]) + (Lp[o + W] + Lp[o - W]);
-          Lc[o] = fmaT(T(-4), Lp[o], sum);
+        // two vertically adjacent points per item (Hs is even), sharing
+        // their column of four values; same arithmetic per point
+        for (int w = tid; w < Ws * (Hs / 2); w += NT) {
+          const int yp = w / Ws, xr = w - yp * Ws;
+          const int o = (2 * yp + s) * W + xr + cx;
+          const T c0 = Lp[o - W], c1 = Lp[o], c2 = Lp[o + W], c3 = Lp[o + 2 * W];
+          Lc[o] = fmaT(T(-4), c1, (Lp[o + 1] + Lp[o - 1]) + (c2 + c0));
+          Lc[o + W] = fmaT(T(-4), c2, (Lp[o + W + 1] + Lp[o + W - 1]) + (c3 + c1));
         }
       }
       Lp = Lc;
@@ -925,7 +1016,7 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
       const T lq = fmaT(T(-4), QS(x, y), (QS(x + 1, y) + QS(x - 1, y)) + (QS(x, y + 1) + QS(x, y - 1)));
       f = fmaT(nu_d2, lq, f);
     }
-    if (a.nsweep > 0) f = fmaT(nuh, Lp[(y + R) * W + x + R], f);
+    if (a.nsweep > 0) f = fmaT(nuh, Lp[(y + R) * W + x + XO], f);
     // surface wind (src/dynamics.h:66) and bottom drag + topography (:67-69)
     if (k == 0 && a.has_wind) f += a.wind[gj];
     if (bottom) {
@@ -1033,7 +1124,8 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
 
 template <typename T, bool COMP, int R>
 __device__ __forceinline__ void body_rhs(const StepArgs<T>& a, int bx, int by, int k, unsigned int total,
-                                         unsigned char* smem_raw) {
+                                         unsigned char* smem_raw, const CUtensorMap* tm,
+                                         unsigned long long* bar, unsigned int* phase) {
   DevState* st = a.state;
   if (!st->active) return;
   __shared__ unsigned long long wmax[NT / 32];
@@ -1041,9 +1133,10 @@ __device__ __forceinline__ void body_rhs(const StepArgs<T>& a, int bx, int by, i
   const int i0 = bx * TX, j0 = by * TY;
   const bool edge = i0 < R || j0 < R || i0 + TX + R > a.nx || j0 + TY + R > a.ny;
   const int si = st->step_index;
+  bool failed = false;
   const unsigned long long mymax_w =
-      widen_absbits<T>(edge ? rhs_tile<T, COMP, R, true>(a, i0, j0, k, si, smem_raw)
-                            : rhs_tile<T, COMP, R, false>(a, i0, j0, k, si, smem_raw));
+      widen_absbits<T>(edge ? rhs_tile<T, COMP, R, true>(a, i0, j0, k, si, smem_raw, tm, bar, phase, &failed)
+                            : rhs_tile<T, COMP, R, false>(a, i0, j0, k, si, smem_raw, tm, bar, phase, &failed));
   unsigned long long mymax = mymax_w;
   const int tid = threadIdx.x + threadIdx.y * 32;
   for (int o = 16; o > 0; o >>= 1) {
@@ -1090,9 +1183,16 @@ __global__ void __launch_bounds__(NT, 3) k_rows_inv(StepArgs<T> a, int step_mode
   body_rows_inv<T, COMP, PER>(a, step_mode, blockIdx.x, smem_raw, tot, cst);
 }
 template <typename T, bool COMP, int R>
-__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 1) k_rhs(StepArgs<T> a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  body_rhs<T, COMP, R>(a, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x * gridDim.y * gridDim.z, smem_raw);
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 1) k_rhs(const __grid_constant__ StepArgs<T> a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ unsigned long long bar;
+  // TMA destinations are 128-byte aligned (the launch adds 128 bytes)
+  unsigned char* base = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+  if (threadIdx.x == 0 && threadIdx.y == 0) mbar_init(&bar);
+  __syncthreads();
+  unsigned int phase = 0;
+  body_rhs<T, COMP, R>(a, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x * gridDim.y * gridDim.z, base,
+                       a.use_tma ? &a.tm[0] : nullptr, &bar, &phase);
 }
 
 // --------------------------------------------------- ensemble wrappers
@@ -1194,16 +1294,23 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 2) k_rows_inv_ens(Ens
 // so each launch runs the same specialised body as a single run.
 template <typename T, bool COMP, int R>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 3) k_rhs_ens(EnsArgs<T> e) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ StepArgs<T> sa;
   __shared__ int cur;
+  __shared__ unsigned long long bar;
+  unsigned char* base = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+  if (threadIdx.x == 0 && threadIdx.y == 0) mbar_init(&bar);
+  unsigned int phase = 0;
   ens_init_cur(&cur);
   for (int item = blockIdx.x; item < e.total[3]; item += gridDim.x) {
     const int local = ens_item(e, e.start_rhs, item, &sa, &cur);
     const int ntx = (sa.nx + TX - 1) / TX, nty = (sa.ny + TY - 1) / TY;
     const int bx = local % ntx, rest = local / ntx, by = rest % nty, bz = rest / nty;
     const unsigned int total = (unsigned int)(ntx * nty * sa.nl);
-    body_rhs<T, COMP, R>(sa, bx, by, bz, total, smem_raw);
+    // the tensor maps are read from the member table in global memory (TMA
+    // takes them from the parameter, constant or global space, not shared);
+    // only thread 0, which wrote cur, issues the copies
+    body_rhs<T, COMP, R>(sa, bx, by, bz, total, base, sa.use_tma ? &e.members[cur].tm[0] : nullptr, &bar, &phase);
     __syncthreads();
   }
 }
@@ -1547,8 +1654,11 @@ static size_t smem_rows_inv(const StepArgs<T>& a) {
 }
 template <typename T>
 static size_t smem_rhs_r(int r) {
-  const size_t W = TX + 2 * r, Hh = TY + 2 * r;
-  return sizeof(T) * (3 * W * Hh + (TX + 2) * (TY + 2) + 2 * (TX + 2) * TY + 2 * TX * (TY + 2));
+  // rhs_tile's layout: psi and two chain buffers, the q tile, the FP64
+  // centred differences, plus 128 bytes to align the TMA destinations
+  const int HH = TY + 2 * r;
+  const size_t TS = tile_round<T>(TW * HH), QS = tile_round<T>(TW * (TY + 2));
+  return sizeof(T) * (3 * TS + QS + 2 * (TX + 2) * TY + 2 * TX * (TY + 2)) + 128;
 }
 template <typename T>
 static int rhs_halo(const StepArgs<T>& a) { return a.nsweep > 0 ? a.nsweep : 1; }
@@ -1831,6 +1941,7 @@ void ens_flush_f32c(const EnsArgs<float>& e, int grid, cudaStream_t s) {
 int cols_per_tile_f64() { return ColsPer<double>::value; }
 int cols_per_tile_f32c() { return ColsPer<float>::value; }
 int rhs_tile_x() { return TX; }
+int rhs_box_width() { return TW; }
 int rhs_tile_y() { return TY; }
 
 size_t smem_bytes_rows_f64(const StepArgs<double>& a) { return smem_rows<double, false>(a); }

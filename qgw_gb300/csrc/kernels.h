@@ -76,6 +76,8 @@ int rhs_halo_of_f32c(const StepArgs<float>& a);
 int cols_per_tile_f64();
 int cols_per_tile_f32c();
 int rhs_tile_x();
+// TMA box width (columns) of the RHS kernel's interior tiles
+int rhs_box_width();
 int rhs_tile_y();
 
 size_t smem_bytes_rows_f64(const StepArgs<double>& a);

@@ -17,6 +17,7 @@
 // pitch = NX + 4 (room for the NX/2 + 1 complex values of a spectral row).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -44,6 +45,7 @@ struct DevState {
   int max_steps;                   // > 0: stop after this many steps in the call
   int forc_step;                   // step_index of the current stochastic forcing field
   double t_prev;                   // t before the last step's increment (4-D forcing time)
+  int dev_error;                   // 1: a bounded device wait ran out (tile skipped)
 };
 
 // Stochastic thin-ring forcing (src/forcing.h:67-201): each step a new
@@ -129,6 +131,11 @@ template <typename T> struct StepArgs {
   const T* frec;
   int nrec;                        // 0: no 4-D forcing
   double dt_forc;
+  // TMA tensor maps of the RHS kernel's interior tiles (psi, q, zeta), boxes
+  // of 40 columns starting at x = i0 - 4 (16-byte aligned); use_tma = 0:
+  // the element-wise asynchronous copies instead
+  CUtensorMap tm[3];
+  int use_tma;
   // doubly periodic basin (bc_fac = -1): nx = NX, ny = NY interior points,
   // pitch = NX + 4; gx has M = NX (real FFT of length NX as a complex FFT
   // of NX/2), gy has M = 2 NY (complex FFT of length NY); spectral rows hold

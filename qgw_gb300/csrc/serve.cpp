@@ -201,13 +201,14 @@ void worker_loop(qgw_pool* pl) {
             r->remaining -= st.steps_taken;
             pl->lgp_steps += (double)lgp_of(r->p) * st.steps_taken;
             if (st.nonfinite) r->remaining = -1;
+            if (st.dev_error) r->remaining = -2;  // a bounded device wait ran out
             if (r->remaining <= 0) finished.push_back(r);
           }
     }
     pl->ticks += 1;
     if (!finished.empty()) {
       for (auto& r : finished) {
-        retire(pl, r, r->remaining < 0 ? QGW_ERR_NAN : QGW_OK);
+        retire(pl, r, r->remaining == -2 ? QGW_ERR_TIMEOUT : (r->remaining < 0 ? QGW_ERR_NAN : QGW_OK));
         pl->resident.erase(std::find(pl->resident.begin(), pl->resident.end(), r));
       }
       rebuild(pl);
