@@ -1183,7 +1183,7 @@ __global__ void __launch_bounds__(NT, 3) k_rows_inv(StepArgs<T> a, int step_mode
   body_rows_inv<T, COMP, PER>(a, step_mode, blockIdx.x, smem_raw, tot, cst);
 }
 template <typename T, bool COMP, int R>
-__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 1) k_rhs(const __grid_constant__ StepArgs<T> a) {
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 4) k_rhs(const __grid_constant__ StepArgs<T> a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ unsigned long long bar;
   // TMA destinations are 128-byte aligned (the launch adds 128 bytes)
