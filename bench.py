@@ -49,6 +49,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32c", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=0, help="0: same as --steps")
+    ap.add_argument("--variant-steps", type=int, default=50,
+                    help="steps of the periodic / forcing variant lines (0: skip)")
     ap.add_argument("--ensemble-steps", type=int, default=40, help="0: skip the ensemble measurement")
     ap.add_argument("--ensemble-members", type=int, default=64)
     ap.add_argument("--serve-requests", type=int, default=64, help="0: skip the serving measurement")
@@ -364,6 +366,11 @@ def run_ours(args, rank, world, local_rank):
                               "step_frac": step_bytes / hbm_peak},
                  "error_vs_fp64": errs, "dtype": "f32 (q as f32 hi+lo)"}
 
+    # the other boundary kind and the forcing add-ons at the same size
+    variants = None
+    if args.variant_steps > 0:
+        variants = run_variants(args, capi, configs, torch, max_over_ranks, world)
+
     ensemble = None
     if args.ensemble_steps > 0:
         ensemble = run_ensemble(args, capi, configs, torch, barrier, max_over_ranks, world)
@@ -391,10 +398,53 @@ def run_ours(args, rank, world, local_rank):
         "roofline": roofline, "roofline_fp64": roofline_fp64,
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": cl,
         "fp32c": fp32c,
+        "variants": variants,
         "ensemble": ensemble,
         "serving": serving,
         "fp64_tflops_measured": fp64_peak, "fp32_tflops_measured": fp32_peak,
     }
+    return out
+
+
+def run_variants(args, capi, configs, torch, max_over_ranks, world):
+    """Step rate of the doubly periodic basin (both precisions) and the cost
+    of the forcing add-ons (stochastic ring forcing, 4-D forcing) at the
+    workload's size, device-timed like the main line."""
+    import numpy as np
+    K = args.variant_steps
+    base = workload(args.nx, args.nl)
+
+    def rate(params, precision, records=None):
+        run = capi.Run(params, precision)
+        if records is not None:
+            run.set_forcing_records(records)
+        run.set_q(configs.noise_ic(params, 2100))
+        run.fix_dt(600.0)
+        run.step(3)
+        stream = torch.cuda.ExternalStream(run.stream())
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        info = run.step(K)
+        e1.record(stream)
+        e1.synchronize()
+        assert info.steps_taken == K
+        ms = max_over_ranks(e0.elapsed_time(e1)) / K
+        run.close()
+        return {"ms_per_step": ms, "value": world * lgp_of(params) / (ms / 1e3), "unit": "lgp-steps/s"}
+
+    per = dict(base, bc_fac=-1.0)
+    out = {"steps": K, "periodic_fp64": rate(per, 0), "periodic_fp32c": rate(per, 1)}
+    # stochastic ring forcing at k_f = 2 pi * 40 / Lx (a ring of radius 40
+    # wavenumbers), sigma_f = 1e-12
+    st = dict(per, k_f=2 * np.pi * 40 / base["Lx"], sigma_f=1e-12)
+    out["periodic_stochastic_fp64"] = rate(st, 0)
+    # 4-D forcing, 4 records interpolated in time
+    f4 = dict(base, dt_forc=3600.0, dt_forc_period=4 * 3600.0)
+    shape = (4,) + tuple(configs.noise_ic(base, 1).shape)
+    rec = np.random.Generator(np.random.PCG64(7)).normal(0.0, 1e-12, size=shape)
+    out["forcing4d_fp64"] = rate(f4, 0, rec)
     return out
 
 
