@@ -6,6 +6,7 @@
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -306,6 +307,9 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
       f.nring = NP;
       f.NF = p.NX;
       f.fpitch = p.NX + 4;
+      int imax = 0;
+      for (size_t k = 0; k < ij.size(); k += 2) imax = std::max(imax, ij[k]);
+      f.col_blocks = imax / 2 + 1;
       f.gx = qgw::make_geom(f.NF);
       f.gy = qgw::make_geom(2 * f.NF);
       for (int dim = 0; dim < 2; ++dim) {

@@ -266,9 +266,10 @@ __device__ __forceinline__ int group_width(int G) { return G <= 1 ? 1 : G <= 2 ?
 // accumulates the G modes of its points in registers, layer by layer.
 // frow (optional): the stochastic forcing of row j, added to layer 0 as
 // frow * sqdt after the AB3 update (src/timestep.h:415-421)
-// FORCED: the stochastic or 4-D forcing is on (a separate instantiation, so
-// that the unforced loop carries none of it)
-template <typename T, bool COMP, int GB, bool FORCED>
+// FK: 0 no forcing, 1 stochastic forcing only (layer 0), 2 either or both
+// -- separate instantiations, so that each loop carries only the forcing it
+// applies
+template <typename T, bool COMP, int GB, int FK>
 __device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool upd, T c0, T c1, T c2, const T* f0,
                                             const T* f1, const T* f2, int G, T* A, int ld, const T* cst,
                                             const T* frow, T sqdt, const T* r1, const T* r2, T w1, T w2,
@@ -286,7 +287,8 @@ __device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool up
           float lo = (float)a.qlo[o];
           const float d = ab3_increment((float)c0, (float)c1, (float)c2, (float)f0[o], (float)f1[o], (float)f2[o]);
           comp_add(hi, lo, d);
-          if (FORCED) {
+          if (FK == 1 && l == 0) comp_add(hi, lo, (float)frow[i] * (float)sqdt);
+          if (FK == 2) {
             if (frow && l == 0) comp_add(hi, lo, (float)frow[i] * (float)sqdt);
             if (r1) comp_add(hi, lo, (float)forc4d_term<T>(r1, r2, o, w1, w2, dtf));
           }
@@ -298,9 +300,10 @@ __device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool up
         v = a.q[o];
         if (upd) {
           v = ab3_plain<T>(v, c0, c1, c2, f0[o], f1[o], f2[o]);
-          if (FORCED) {
+          if (FK == 1 && l == 0) v = v + frow[i] * sqdt;
+          if (FK == 2) {
             if (frow && l == 0) v = v + frow[i] * sqdt;
-            if (r1) v = v + forc4d_term<T>(r1, r2, o, w1, w2, dtf);
+            v = v + forc4d_term<T>(r1, r2, o, w1, w2, dtf);
           }
           a.q[o] = v;
         }
@@ -359,26 +362,26 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
       cst[w] = g < G ? a.cl2m[(size_t)(m0 + g) * a.nl + l] : T(0);
     }
     __syncthreads();
-    const bool forced = upd && (frow || r1);
+    const int fk = !upd ? 0 : r1 ? 2 : frow ? 1 : 0;
 #define QGW_PF(GBV, F) project_fwd<T, COMP, GBV, F>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt, r1, \
                                                   r2, w1, w2, dtf)
-    if (forced) {
-      switch (GB) {
-        case 1: QGW_PF(1, true); break;
-        case 2: QGW_PF(2, true); break;
-        case 4: QGW_PF(4, true); break;
-        case 8: QGW_PF(8, true); break;
-        default: QGW_PF(16, true); break;
-      }
+#define QGW_PF_GB(F)                 \
+  switch (GB) {                      \
+    case 1: QGW_PF(1, F); break;     \
+    case 2: QGW_PF(2, F); break;     \
+    case 4: QGW_PF(4, F); break;     \
+    case 8: QGW_PF(8, F); break;     \
+    default: QGW_PF(16, F); break;   \
+  }
+    // the compensated path has registers for one forced loop only
+    if (fk == 2 || (COMP && fk == 1)) {
+      QGW_PF_GB(2)
+    } else if (fk == 1) {
+      if constexpr (!COMP) QGW_PF_GB(1)
     } else {
-      switch (GB) {
-        case 1: QGW_PF(1, false); break;
-        case 2: QGW_PF(2, false); break;
-        case 4: QGW_PF(4, false); break;
-        case 8: QGW_PF(8, false); break;
-        default: QGW_PF(16, false); break;
-      }
+      QGW_PF_GB(0)
     }
+#undef QGW_PF_GB
 #undef QGW_PF
     __syncthreads();
     T* O = PER ? rfft_block<T>(A, B, G, ld, a.gx, a.tx) : dst_block<T>(A, B, G, ld, a.gx, a.tx, tot);
@@ -1486,7 +1489,8 @@ __global__ void __launch_bounds__(NT) k_forc_modes(StepArgs<T> a) {
 }
 
 // F2: backward complex FFT along j of two complex columns i per block
-// (the first dimension of the NF x NF c2r, unnormalised).
+// (the first dimension of the NF x NF c2r, unnormalised); only the columns
+// up to the ring's largest i: the others stay zero in both buffers.
 template <typename T>
 __global__ void __launch_bounds__(NT) k_forc_cols(StepArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1536,7 +1540,7 @@ static void launch_forcing(const StepArgs<T>& a, cudaStream_t s) {
   const ForcArgs<T>& f = a.fr;
   if (!f.on) return;
   k_forc_modes<T><<<1, NT, 0, s>>>(a);
-  k_forc_cols<T><<<(f.NF / 2 + 2) / 2, NT, (size_t)4 * padded_len(f.gy.M) * sizeof(T), s>>>(a);
+  k_forc_cols<T><<<f.col_blocks, NT, (size_t)4 * padded_len(f.gy.M) * sizeof(T), s>>>(a);
   k_forc_rows<T><<<a.ny, NT, (size_t)2 * padded_len(f.gx.M) * sizeof(T), s>>>(a);
 }
 

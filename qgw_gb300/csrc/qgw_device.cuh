@@ -57,6 +57,8 @@ template <typename T> struct ForcArgs {
   int nring;                       // ring points (i, j)
   int NF;                          // transform size
   int fpitch;                      // row pitch (reals) of the spectral buffers
+  int col_blocks;                  // column pairs holding ring points: the
+                                   // transform along j skips the zero columns
   DstGeom gx, gy;                  // real FFT of NF along i; complex FFT of NF along j
   DstTables<T> tx, ty;
   const int* ring;                 // 2 * nring: i, j
