@@ -92,7 +92,7 @@ int inv_group(int zeta) {
 // takes rows_per_mode rows in each of the two DST work buffers), at most
 // gmax and at most want, then balanced over the resulting number of groups.
 int mode_group(int nl, int M, size_t elem, size_t budget, int rows_per_mode, int gmax, int want) {
-  int g = (int)(budget / (2 * (size_t)rows_per_mode * qgw::padded_len(M) * elem));
+  int g = (int)(budget / (2 * (size_t)rows_per_mode * (elem == 4 ? qgw::padded_len<float>(M) : qgw::padded_len<double>(M)) * elem));
   if (g > want) g = want;
   if (g > gmax) g = gmax;
   if (g < 1) g = 1;

@@ -57,14 +57,29 @@ QGW_HD float fmaT(float a, float b, float c) {
 #endif
 }
 
-// Padded layout of a row buffer in shared memory: one pad slot after every
-// 8 complex values (16 reals), so that the stride-8 stores of the first
-// Stockham pass and the transposed column loads hit distinct banks.
-// Complex index e lives at pc(e), real index i at pr(i).
-QGW_HD int pc(int e) { return e + (e >> 3); }
-QGW_HD int pr(int i) { return i + ((i >> 4) << 1); }
-// reals occupied by a padded row of M reals
-QGW_HD int padded_len(int M) { return M + ((M >> 4) << 1) + 2; }
+// Padded layout of a row buffer in shared memory: after every 128 bytes of
+// data (2^LG complex values) come W complex pad slots -- one 16-byte slot
+// for doubles (8 complex values per period), two 8-byte slots for floats
+// (16 per period).  A warp's contiguous access then starts and ends inside
+// whole 128-byte periods (one wavefront per 128 bytes), the stride-R stores
+// of the first Stockham pass spread over all banks, and every 16-byte
+// aligned group of reals stays contiguous and 16-byte aligned.
+// Complex index e lives at pc<T>(e), real index i at pr<T>(i).
+template <typename T> struct Pad {
+  static constexpr int LG = sizeof(T) == 8 ? 3 : 4;  // log2 complex values per period
+  static constexpr int W = sizeof(T) == 8 ? 1 : 2;   // pad slots (complex) per period
+  static constexpr int P = 1 << LG;
+};
+template <typename T> QGW_HD int pc(int e) { return e + Pad<T>::W * (e >> Pad<T>::LG); }
+template <typename T> QGW_HD int pr(int i) { return i + 2 * Pad<T>::W * (i >> (Pad<T>::LG + 1)); }
+// reals occupied by a padded row of M reals (room for reals M and M+1, the
+// last complex value of a real FFT), rounded up to whole 16-byte vectors so
+// that every row of a buffer starts 16-byte aligned
+template <typename T> QGW_HD int padded_len(int M) {
+  const int n = pr<T>(M + 1) + 1;
+  constexpr int V = 16 / (int)sizeof(T);
+  return (n + V - 1) / V * V;
+}
 
 // Static shape of one DST length.
 struct DstGeom {
@@ -105,11 +120,11 @@ template <typename T> struct DstTables {
 template <typename T>
 QGW_HD void dst_pre_item(const T* __restrict__ x, T* __restrict__ y, int j, const DstGeom& g,
                          const C2<T>* __restrict__ pre) {
-  const T a = x[pr(j - 1)];
-  const T b = x[pr(g.M - j - 1)];
+  const T a = x[pr<T>(j - 1)];
+  const T b = x[pr<T>(g.M - j - 1)];
   const C2<T> w = pre[j];
-  y[pr(j)] = fmaT(w.x, a, w.y * b);
-  y[pr(g.M - j)] = fmaT(w.y, a, w.x * b);
+  y[pr<T>(j)] = fmaT(w.x, a, w.y * b);
+  y[pr<T>(g.M - j)] = fmaT(w.y, a, w.x * b);
   if (j == 1) y[0] = T(0);
 }
 
@@ -222,7 +237,7 @@ QGW_HD void stockham_item(const C2<T>* __restrict__ src, C2<T>* __restrict__ dst
   const int stride = H / R;
   C2<T> v[R];
 #pragma unroll
-  for (int q = 0; q < R; ++q) v[q] = src[pc(b + q * stride)];
+  for (int q = 0; q < R; ++q) v[q] = src[pc<T>(b + q * stride)];
   const int k = b & (Ns - 1);
   if (Ns > 1) {
     const int step = k * (H / (Ns * R));
@@ -244,7 +259,7 @@ QGW_HD void stockham_item(const C2<T>* __restrict__ src, C2<T>* __restrict__ dst
   }
   const int base = (b - k) * R + k;
 #pragma unroll
-  for (int q = 0; q < R; ++q) dst[pc(base + q * Ns)] = v[q];
+  for (int q = 0; q < R; ++q) dst[pc<T>(base + q * Ns)] = v[q];
 }
 
 template <typename T>
@@ -266,18 +281,18 @@ QGW_HD void dst_split_item(const C2<T>* __restrict__ Z, T* __restrict__ out, int
     out[0] = a.x + a.y;  // R_0
     return;
   }
-  const C2<T> A = Z[pc(k)];
-  const C2<T> Bc = Z[pc(H - k)];
+  const C2<T> A = Z[pc<T>(k)];
+  const C2<T> Bc = Z[pc<T>(H - k)];
   const T br = Bc.x, bi = -Bc.y;
   const C2<T> cs = spl[k];
   const T sr = A.x + br, si = A.y + bi, dr = A.x - br, di = A.y - bi;
   const T P = fmaT(cs.x, di, -(cs.y * dr));
   const T Q = fmaT(cs.x, dr, cs.y * di);
-  out[pr(2 * k)] = sr + P;          // 2 R_k
-  out[pr(2 * k - 1)] = Q - si;      // Y_{2k} = -2 I_k
+  out[pr<T>(2 * k)] = sr + P;          // 2 R_k
+  out[pr<T>(2 * k - 1)] = Q - si;      // Y_{2k} = -2 I_k
   if (2 * k != H) {
-    out[pr(2 * (H - k))] = sr - P;      // 2 R_{H-k}
-    out[pr(2 * (H - k) - 1)] = Q + si;  // Y_{2(H-k)}
+    out[pr<T>(2 * (H - k))] = sr - P;      // 2 R_{H-k}
+    out[pr<T>(2 * (H - k) - 1)] = Q + si;  // Y_{2(H-k)}
   }
 }
 
@@ -287,10 +302,10 @@ template <typename T>
 QGW_HD T dst_scan_chunk(T* out, int c, const DstGeom& g) {
   T acc = T(0);
   const int k0 = c * g.chunk;
-  acc = out[pr(2 * k0)];
+  acc = out[pr<T>(2 * k0)];
   for (int t = 1; t < g.chunk; ++t) {
-    acc = acc + out[pr(2 * (k0 + t))];
-    out[pr(2 * (k0 + t))] = acc;
+    acc = acc + out[pr<T>(2 * (k0 + t))];
+    out[pr<T>(2 * (k0 + t))] = acc;
   }
   return acc;
 }
@@ -298,7 +313,7 @@ QGW_HD T dst_scan_chunk(T* out, int c, const DstGeom& g) {
 template <typename T>
 QGW_HD void dst_scan_fix(T* out, int c, T prefix, const DstGeom& g) {
   const int k0 = c * g.chunk;
-  for (int t = 0; t < g.chunk; ++t) out[pr(2 * (k0 + t))] += prefix;
+  for (int t = 0; t < g.chunk; ++t) out[pr<T>(2 * (k0 + t))] += prefix;
 }
 
 }  // namespace qgw

@@ -1,16 +1,18 @@
 // dst_fixed.cuh -- the batched DST-I of dst_core.h specialised at compile
 // time for one transform length (M = 2H = 2^(LGH+1)), used by the step
-// kernels for the common lengths.  Same phases, same arithmetic as the
-// generic block DST (kernels.cu), so results agree bit for bit with it:
+// kernels for the common lengths.  Same phases and arithmetic as the generic
+// block DST (kernels.cu); the FP32 prefix sum runs here as a warp scan (so
+// FP32 results agree with the generic DST to round-off, FP64 ones bit for
+// bit):
 //   pre-processing -> Stockham radix-8 passes (+ one radix-4/2 pass)
 //   -> split -> prefix sum of the odd outputs.
-// With the geometry fixed, every padded shared-memory index is one base
-// computation plus immediate offsets (strides that are multiples of 8
-// complex values keep the pad pattern: pc(e + 8m) = pc(e) + 9m), and the
-// prefix sum runs one warp per row without block barriers.  The blocks have
-// DST_NT threads and every phase has a power-of-two item count per row, so a
-// thread meets the same in-row items in every row: their indices, table
-// values and twiddles are computed once per transform, outside the row loop.
+// With the geometry fixed, a padded shared-memory index is one base
+// computation plus immediate offsets wherever a stride is a whole number of
+// pad periods (pc(e + P m) = pc(e) + (P + W) m), and the prefix sum runs one
+// warp per row without block barriers.  The blocks have DST_NT threads and
+// every phase has a power-of-two item count per row, so a thread meets the
+// same in-row items in every row: their indices, table values and twiddles
+// are computed once per transform, outside the row loop.
 #pragma once
 
 #include "dst_core.h"
@@ -23,25 +25,27 @@ template <int LGH> struct DstShape {
   static constexpr int H = 1 << LGH, M = 2 * H;
   static constexpr int NP8 = LGH / 3;                 // radix-8 passes
   static constexpr int RLAST = 1 << (LGH % 3);        // 1: none, 2 or 4
-  static constexpr int CHUNK = H >= 256 ? H / 32 : 8; // prefix-sum chunk
-  static constexpr int NCHUNK = H / CHUNK;
   static_assert(LGH >= 6, "fixed DST needs H >= 64");
 };
 
 // One Stockham pass over all rows: item b of a row reads inputs b + q*(H/R)
 // and writes outputs base + q*NS; the twiddles of item b are loaded once.
+// With R, NS, H/R and the pad period P all powers of two, adding q*stride to
+// the item's base never carries across a pad period beyond what q*stride
+// itself crosses (the base's offset inside its period plus that of q*stride
+// stays below P), so pc(base + q*stride) = pc(base) + pc(q*stride): one
+// padded base per item, compile-time offsets per q.
 template <typename T, int R, int NS, int H>
 struct StockhamItem {
   static constexpr int S = H / R;
-  static constexpr int OS = NS == 1 ? 1 : NS + NS / 8;
-  static_assert(S % 8 == 0, "input stride must keep the pad pattern");
-  static_assert(NS == 1 || NS % 8 == 0, "output stride must keep the pad pattern");
+  static constexpr int LG = Pad<T>::LG, W = Pad<T>::W;
+  static constexpr int pco(int e) { return e + W * (e >> LG); }
   int in0, out0;
   C2<T> w[R];
   __device__ __forceinline__ void init(int b, const C2<T>* __restrict__ tw) {
-    in0 = pc(b);
+    in0 = pc<T>(b);
     const int k = b & (NS - 1);
-    out0 = pc((b - k) * R + k);
+    out0 = pc<T>((b - k) * R + k);
     if constexpr (NS > 1) {
       const int step = k * (H / (NS * R));
 #pragma unroll
@@ -51,7 +55,7 @@ struct StockhamItem {
   __device__ __forceinline__ void run(const C2<T>* __restrict__ src, C2<T>* __restrict__ dst) const {
     C2<T> v[R];
 #pragma unroll
-    for (int q = 0; q < R; ++q) v[q] = src[in0 + q * (S + S / 8)];
+    for (int q = 0; q < R; ++q) v[q] = src[in0 + pco(q * S)];
     if constexpr (NS > 1) {
       if constexpr (R == 8) {
         dft8_tw(v, w);
@@ -67,7 +71,7 @@ struct StockhamItem {
       else dft2(v);
     }
 #pragma unroll
-    for (int q = 0; q < R; ++q) dst[out0 + q * OS] = v[q];
+    for (int q = 0; q < R; ++q) dst[out0 + pco(q * NS)] = v[q];
   }
 };
 
@@ -106,10 +110,10 @@ __device__ T* dst_block_fixed(T* A, T* B, int nrows, int ld, const DstTables<T>&
 #pragma unroll
     for (int c = 0; c < C; ++c) {
       const int j = tid + 1 + c * DST_NT;
-      ia[c] = pr(j - 1);
-      ib[c] = pr(M - j - 1);
-      oa[c] = pr(j);
-      ob[c] = pr(M - j);
+      ia[c] = pr<T>(j - 1);
+      ib[c] = pr<T>(M - j - 1);
+      oa[c] = pr<T>(j);
+      ob[c] = pr<T>(M - j);
       wp[c] = tb.pre[j];
     }
     for (int r = 0; r < nrows; ++r) {
@@ -125,7 +129,7 @@ __device__ T* dst_block_fixed(T* A, T* B, int nrows, int ld, const DstTables<T>&
     }
   } else {
     const int j = (tid & (H - 1)) + 1;
-    const int ia = pr(j - 1), ib = pr(M - j - 1), oa = pr(j), ob = pr(M - j);
+    const int ia = pr<T>(j - 1), ib = pr<T>(M - j - 1), oa = pr<T>(j), ob = pr<T>(M - j);
     const C2<T> wp = tb.pre[j];
     for (int r = tid >> LGH; r < nrows; r += DST_NT / H) {
       const T* x = A + r * ld;
@@ -175,12 +179,12 @@ __device__ T* dst_block_fixed(T* A, T* B, int nrows, int ld, const DstTables<T>&
     for (int c = 0; c < C; ++c) {
       const int k = kb + c * DST_NT;
       const int kk = k == 0 ? H / 2 : k;  // item 0 runs the k = H/2 butterfly
-      za[c] = pc(kk);
-      zb[c] = pc(H - kk);
-      o0[c] = pr(2 * kk);
-      o1[c] = pr(2 * kk - 1);
-      o2[c] = pr(2 * (H - kk));
-      o3[c] = pr(2 * (H - kk) - 1);
+      za[c] = pc<T>(kk);
+      zb[c] = pc<T>(H - kk);
+      o0[c] = pr<T>(2 * kk);
+      o1[c] = pr<T>(2 * kk - 1);
+      o2[c] = pr<T>(2 * (H - kk));
+      o3[c] = pr<T>(2 * (H - kk) - 1);
       cs[c] = tb.spl[kk];
     }
     for (int r = KI >= DST_NT ? 0 : tid / KI; r < nrows; r += RS) {
@@ -207,32 +211,74 @@ __device__ T* dst_block_fixed(T* A, T* B, int nrows, int ld, const DstTables<T>&
     }
   }
   __syncthreads();
-  // phase 4: prefix sum of the odd outputs (indices 0, 2, 4, ...): one warp
-  // per row, lane c scans chunk c, the chunk totals are scanned by shuffles
-  const int warp = tid >> 5, lane = tid & 31, nwarp = DST_NT >> 5;
-  constexpr int CH = S::CHUNK, NC = S::NCHUNK;
-  static_assert((2 * CH) % 16 == 0, "chunk start must be pad-aligned");
-  for (int r = warp; r < nrows; r += nwarp) {
-    T* o = dst + r * ld + pr(2 * CH * lane);
-    T acc = T(0);
-    if (lane < NC) {
-      acc = o[0];
+  // phase 4: prefix sum of the odd outputs (indices 0, 2, 4, ...), one warp
+  // per row.
+  if constexpr (sizeof(T) == 8) {
+    // FP64 (the FP64 pipe bounds these kernels, so the fewest additions):
+    // lane c scans chunk c sequentially, the chunk totals are scanned by
+    // shuffles and added back -- two additions per value
+    constexpr int CH = H >= 256 ? H / 32 : 8, NC = H / CH;
+    static_assert((2 * CH) % (2 * Pad<T>::P) == 0, "chunk start must be pad-aligned");
+    const int warp = tid >> 5, lane = tid & 31, nwarp = DST_NT >> 5;
+    for (int r = warp; r < nrows; r += nwarp) {
+      T* o = dst + r * ld + pr<T>(2 * CH * lane);
+      T acc = T(0);
+      if (lane < NC) {
+        acc = o[0];
 #pragma unroll
-      for (int t = 1; t < CH; ++t) {
-        acc = acc + o[2 * t + ((2 * t) >> 4) * 2];
-        o[2 * t + ((2 * t) >> 4) * 2] = acc;
+        for (int t = 1; t < CH; ++t) {
+          acc = acc + o[pr<T>(2 * t)];
+          o[pr<T>(2 * t)] = acc;
+        }
+      }
+      T incl = acc;
+#pragma unroll
+      for (int of = 1; of < 32; of <<= 1) {
+        const T u = __shfl_up_sync(0xffffffffu, incl, of);
+        if (lane >= of) incl += u;
+      }
+      T ex = __shfl_up_sync(0xffffffffu, incl, 1);
+      if (lane > 0 && lane < NC) {
+#pragma unroll
+        for (int t = 0; t < CH; ++t) o[pr<T>(2 * t)] += ex;
       }
     }
-    T incl = acc;
+  } else {
+    // FP32: each lane loads one 16-byte vector of V reals (E = V/2 odd
+    // outputs), scans it, the lane totals are scanned by shuffles, and a
+    // running carry joins the 32 V reals of one iteration to the next:
+    //   out = (carry + exclusive lane prefix) + inclusive in-lane prefix;
+    // every access is a whole, conflict-free 16-byte vector
+    constexpr int V = 16 / (int)sizeof(T), E = V / 2, SPAN = 32 * V;
+    static_assert(M % SPAN == 0, "whole iterations (M >= 128)");
+    static_assert((2 * Pad<T>::P) % V == 0, "vectors stay inside one pad period");
+    const int warp = tid >> 5, lane = tid & 31, nwarp = DST_NT >> 5;
+    for (int r = warp; r < nrows; r += nwarp) {
+      T* row = dst + r * ld;
+      T carry = T(0);
+#pragma unroll 1
+      for (int it = 0; it < M / SPAN; ++it) {
+        const int i = it * SPAN + lane * V;
+        float4 u = *reinterpret_cast<const float4*>(row + pr<T>(i));
+        T* e = reinterpret_cast<T*>(&u);
+        T s[E];
+        s[0] = e[0];
 #pragma unroll
-    for (int of = 1; of < 32; of <<= 1) {
-      const T u = __shfl_up_sync(0xffffffffu, incl, of);
-      if (lane >= of) incl += u;
-    }
-    T ex = __shfl_up_sync(0xffffffffu, incl, 1);
-    if (lane > 0 && lane < NC) {
+        for (int q = 1; q < E; ++q) s[q] = s[q - 1] + e[2 * q];
+        T incl = s[E - 1];
 #pragma unroll
-      for (int t = 0; t < CH; ++t) o[2 * t + ((2 * t) >> 4) * 2] += ex;
+        for (int of = 1; of < 32; of <<= 1) {
+          const T t = __shfl_up_sync(0xffffffffu, incl, of);
+          if (lane >= of) incl += t;
+        }
+        T ex = __shfl_up_sync(0xffffffffu, incl, 1);
+        if (lane == 0) ex = T(0);
+        const T base = carry + ex;
+#pragma unroll
+        for (int q = 0; q < E; ++q) e[2 * q] = base + s[q];
+        *reinterpret_cast<float4*>(row + pr<T>(i)) = u;
+        carry = carry + __shfl_sync(0xffffffffu, incl, 31);
+      }
     }
   }
   __syncthreads();

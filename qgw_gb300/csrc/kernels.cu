@@ -313,7 +313,7 @@ __device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool up
 #pragma unroll
       for (int g = 0; g < GB; ++g) acc[g] = fmaT(c[g], v, acc[g]);
     }
-    const int pi = pr(i);
+    const int pi = pr<T>(i);
 #pragma unroll
     for (int g = 0; g < GB; ++g)
       if (g < G) A[g * ld + pi] = acc[g];
@@ -327,7 +327,7 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
                                               T* tot, T* cst) {
   DevState* st = a.state;
   if (step_mode && !st->active) return;
-  const int ld = padded_len(a.gx.M);
+  const int ld = padded_len<T>(a.gx.M);
   T* A = (T*)smem_raw;
   T* B = A + (size_t)a.G1 * ld;
   const bool ab3 = step_mode && st->pending;
@@ -388,7 +388,7 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
     const int nout = PER ? a.nx + 2 : a.nx;
     for (int gg = 0; gg < G; ++gg) {
       T* dstrow = a.spec + (size_t)(m0 + gg) * a.lstride + (size_t)j * a.pitch;
-      for (int i = threadIdx.x; i < nout; i += NT) dstrow[i] = O[gg * ld + pr(i)];
+      for (int i = threadIdx.x; i < nout; i += NT) dstrow[i] = O[gg * ld + pr<T>(i)];
     }
     __syncthreads();
   }
@@ -433,7 +433,7 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
   if (step_mode && !st->active) return;
   const int k0 = bx * CT;
   const int CTb = min(CT, a.nx - k0);
-  const int ld = padded_len(a.gy.M);
+  const int ld = padded_len<T>(a.gy.M);
   T* A = (T*)smem_raw;
   T* B = A + (size_t)CT * ld;
   T* C = B + (size_t)CT * ld;  // zeta mode only
@@ -448,7 +448,7 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
     if (vec) load_cols<T, CT>(src, v);
     else
       for (int c = 0; c < CT; ++c) v[c] = c < CTb ? src[c] : T(0);
-    const int pj = pr(jj);
+    const int pj = pr<T>(jj);
 #pragma unroll
     for (int c = 0; c < CT; ++c) A[c * ld + pj] = v[c];
   }
@@ -459,7 +459,7 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
   const float ird2f = COMP ? a.iRd2f[m] : 0.f;
   const float normf = a.fc[FC_NORM], lx2f = a.fc[FC_LX2], ly2f = a.fc[FC_LY2];
   for (int jj = threadIdx.x; jj < ny; jj += NT) {
-    const int pj = pr(jj);
+    const int pj = pr<T>(jj);
     if (!COMP) {
       const T* hrow = (const T*)(a.hinv + (size_t)m * a.lstride + (size_t)jj * a.pitch + k0);
       T h[CT];
@@ -497,7 +497,7 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
   T* Oth = (O == A) ? B : A;
   T* O2 = dst_block<T>(O, Oth, CT, ld, a.gy, a.ty, tot);
   for (int jj = threadIdx.x; jj < ny; jj += NT) {
-    const int pj = pr(jj);
+    const int pj = pr<T>(jj);
 #pragma unroll
     for (int c = 0; c < CT; ++c) v[c] = c < CTb ? O2[c * ld + pj] : T(0);
     T* dst = S + (size_t)jj * a.pitch + k0;
@@ -510,7 +510,7 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
     T* O3 = dst_block<T>(C, O2 == A ? B : A, CT, ld, a.gy, a.ty, tot);
     T* S2 = a.spec2 + (size_t)m * a.lstride;
     for (int jj = threadIdx.x; jj < ny; jj += NT) {
-      const int pj = pr(jj);
+      const int pj = pr<T>(jj);
 #pragma unroll
       for (int c = 0; c < CT; ++c) v[c] = c < CTb ? O3[c * ld + pj] : T(0);
       T* dst = S2 + (size_t)jj * a.pitch + k0;
@@ -533,7 +533,7 @@ __device__ __forceinline__ void body_cols_per(const StepArgs<T>& a, int step_mod
   if (step_mode && !st->active) return;
   const int H = a.gx.H;  // x: complex columns k = 0..H
   const int k0 = bx * CC;
-  const int ld = padded_len(a.gy.M);
+  const int ld = padded_len<T>(a.gy.M);
   T* A = (T*)smem_raw;
   T* B = A + (size_t)CC * ld;
   T* C = B + (size_t)CC * ld;  // zeta mode only
@@ -543,7 +543,7 @@ __device__ __forceinline__ void body_cols_per(const StepArgs<T>& a, int step_mod
   for (int jj = tid; jj < ny; jj += NT) {
     T v[4];
     load_cols<T, 4>(S + (size_t)jj * a.pitch + 2 * k0, v);
-    const int pj = pc(jj);
+    const int pj = pc<T>(jj);
     C2<T>* A0 = (C2<T>*)A;
     C2<T>* A1 = (C2<T>*)(A + ld);
     C2<T> z0, z1;
@@ -561,7 +561,7 @@ __device__ __forceinline__ void body_cols_per(const StepArgs<T>& a, int step_mod
     const int c = w / ny, jj = w - c * ny;
     const int k = k0 + c;
     C2<T>* Oc = (C2<T>*)(O + c * ld);
-    const int pj = pc(jj);
+    const int pj = pc<T>(jj);
     C2<T> X = Oc[pj];
     if (k > H || (k == 0 && jj == 0)) {
       // padding columns; the mean is removed (src/elliptic.h:114-117)
@@ -599,7 +599,7 @@ __device__ __forceinline__ void body_cols_per(const StepArgs<T>& a, int step_mod
   T* Oth = (O == A) ? B : A;
   T* O2 = cfft_block<T>(O, Oth, CC, ld, a.gy, a.ty.tw);
   for (int jj = tid; jj < ny; jj += NT) {
-    const int pj = pc(jj);
+    const int pj = pc<T>(jj);
     const C2<T> z0 = ((const C2<T>*)O2)[pj];
     const C2<T> z1 = ((const C2<T>*)(O2 + ld))[pj];
     T v[4] = {z0.x, -z0.y, z1.x, -z1.y};
@@ -610,7 +610,7 @@ __device__ __forceinline__ void body_cols_per(const StepArgs<T>& a, int step_mod
     T* O3 = cfft_block<T>(C, O2 == A ? B : A, CC, ld, a.gy, a.ty.tw);
     T* S2 = a.spec2 + (size_t)m * a.lstride;
     for (int jj = tid; jj < ny; jj += NT) {
-      const int pj = pc(jj);
+      const int pj = pc<T>(jj);
       const C2<T> z0 = ((const C2<T>*)O3)[pj];
       const C2<T> z1 = ((const C2<T>*)(O3 + ld))[pj];
       T v[4] = {z0.x, -z0.y, z1.x, -z1.y};
@@ -650,7 +650,7 @@ __device__ __forceinline__ void project_spec(const StepArgs<T>& a, int j, int G,
         for (int g = 0; g < GB; ++g) zacc[g] = fmaT(c[g], z, zacc[g]);
       }
     }
-    const int pi = pr(i);
+    const int pi = pr<T>(i);
 #pragma unroll
     for (int g = 0; g < GB; ++g)
       if (g < G) {
@@ -665,7 +665,7 @@ __device__ __forceinline__ void body_rows_inv(const StepArgs<T>& a, int step_mod
                                               T* tot, T* cst) {
   DevState* st = a.state;
   if (step_mode && !st->active) return;
-  const int ld = padded_len(a.gx.M);
+  const int ld = padded_len<T>(a.gx.M);
   const bool zm = COMP && a.zeta_mode;
   const int Gb = a.G3;
   T* A = (T*)smem_raw;
@@ -702,11 +702,11 @@ __device__ __forceinline__ void body_rows_inv(const StepArgs<T>& a, int step_mod
     const T odd = PER ? T(-1) : T(1);
     for (int g = 0; g < G; ++g) {
       T* prow = a.psi + (size_t)(l0 + g) * a.lstride + (size_t)j * a.pitch;
-      for (int i = threadIdx.x; i < a.nx; i += NT) prow[i] = (i & 1) ? odd * O[g * ld + pr(i)] : O[g * ld + pr(i)];
+      for (int i = threadIdx.x; i < a.nx; i += NT) prow[i] = (i & 1) ? odd * O[g * ld + pr<T>(i)] : O[g * ld + pr<T>(i)];
       if (zm) {
         T* zrow = a.zeta + (size_t)(l0 + g) * a.lstride + (size_t)j * a.pitch;
         for (int i = threadIdx.x; i < a.nx; i += NT)
-          zrow[i] = (i & 1) ? odd * O[(G + g) * ld + pr(i)] : O[(G + g) * ld + pr(i)];
+          zrow[i] = (i & 1) ? odd * O[(G + g) * ld + pr<T>(i)] : O[(G + g) * ld + pr<T>(i)];
       }
     }
     __syncthreads();
@@ -1495,7 +1495,7 @@ template <typename T>
 __global__ void __launch_bounds__(NT) k_forc_cols(StepArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const ForcArgs<T>& f = a.fr;
-  const int ld = padded_len(f.gy.M);
+  const int ld = padded_len<T>(f.gy.M);
   T* A = (T*)smem_raw;
   T* B = A + 2 * ld;
   const int c4 = 4 * blockIdx.x;
@@ -1504,14 +1504,14 @@ __global__ void __launch_bounds__(NT) k_forc_cols(StepArgs<T> a) {
     load_cols<T, 4>(f.spec + (size_t)j * f.fpitch + c4, v);
     C2<T> z0, z1;
     z0.x = v[0]; z0.y = -v[1]; z1.x = v[2]; z1.y = -v[3];
-    ((C2<T>*)A)[pc(j)] = z0;
-    ((C2<T>*)(A + ld))[pc(j)] = z1;
+    ((C2<T>*)A)[pc<T>(j)] = z0;
+    ((C2<T>*)(A + ld))[pc<T>(j)] = z1;
   }
   __syncthreads();
   T* O = cfft_block<T>(A, B, 2, ld, f.gy, f.ty.tw);
   for (int j = threadIdx.x; j < f.NF; j += NT) {
-    const C2<T> z0 = ((const C2<T>*)O)[pc(j)];
-    const C2<T> z1 = ((const C2<T>*)(O + ld))[pc(j)];
+    const C2<T> z0 = ((const C2<T>*)O)[pc<T>(j)];
+    const C2<T> z1 = ((const C2<T>*)(O + ld))[pc<T>(j)];
     T v[4] = {z0.x, -z0.y, z1.x, -z1.y};
     store_cols<T, 4>(f.spec2 + (size_t)j * f.fpitch + c4, v);
   }
@@ -1524,15 +1524,15 @@ __global__ void __launch_bounds__(NT) k_forc_rows(StepArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const ForcArgs<T>& f = a.fr;
   const int j = blockIdx.x;
-  const int ld = padded_len(f.gx.M);
+  const int ld = padded_len<T>(f.gx.M);
   T* A = (T*)smem_raw;
   T* B = A + ld;
   const T* src = f.spec2 + (size_t)j * f.fpitch;
-  for (int i = threadIdx.x; i < f.NF + 2; i += NT) A[pr(i)] = src[i];
+  for (int i = threadIdx.x; i < f.NF + 2; i += NT) A[pr<T>(i)] = src[i];
   __syncthreads();
   T* O = irfft_block<T>(A, B, 1, ld, f.gx, f.tx);
   T* dst = f.field + (size_t)j * a.pitch;
-  for (int i = threadIdx.x; i < a.nx; i += NT) dst[i] = (i & 1) ? -O[pr(i)] : O[pr(i)];
+  for (int i = threadIdx.x; i < a.nx; i += NT) dst[i] = (i & 1) ? -O[pr<T>(i)] : O[pr<T>(i)];
 }
 
 template <typename T>
@@ -1540,8 +1540,8 @@ static void launch_forcing(const StepArgs<T>& a, cudaStream_t s) {
   const ForcArgs<T>& f = a.fr;
   if (!f.on) return;
   k_forc_modes<T><<<1, NT, 0, s>>>(a);
-  k_forc_cols<T><<<f.col_blocks, NT, (size_t)4 * padded_len(f.gy.M) * sizeof(T), s>>>(a);
-  k_forc_rows<T><<<a.ny, NT, (size_t)2 * padded_len(f.gx.M) * sizeof(T), s>>>(a);
+  k_forc_cols<T><<<f.col_blocks, NT, (size_t)4 * padded_len<T>(f.gy.M) * sizeof(T), s>>>(a);
+  k_forc_rows<T><<<a.ny, NT, (size_t)2 * padded_len<T>(f.gx.M) * sizeof(T), s>>>(a);
 }
 
 // Boundary copies: the reference layout (nl, ny+2, nx+2) in one contiguous
@@ -1639,12 +1639,12 @@ __global__ void k_budget_final(const double* part, int nblk, double scale, doubl
 
 // ------------------------------------------------------------- launchers
 template <typename T, bool COMP>
-static size_t smem_rows(const StepArgs<T>& a) { return (size_t)2 * a.G1 * padded_len(a.gx.M) * sizeof(T); }
+static size_t smem_rows(const StepArgs<T>& a) { return (size_t)2 * a.G1 * padded_len<T>(a.gx.M) * sizeof(T); }
 template <typename T, bool COMP>
 static size_t smem_cols(const StepArgs<T>& a) {
   // periodic: two complex columns of ny values (padded rows of 2 ny reals)
   const size_t rows = a.periodic ? 2 : ColsPer<T>::value;
-  return (size_t)((COMP && a.zeta_mode) ? 3 : 2) * rows * padded_len(a.gy.M) * sizeof(T);
+  return (size_t)((COMP && a.zeta_mode) ? 3 : 2) * rows * padded_len<T>(a.gy.M) * sizeof(T);
 }
 // column tiles of one mode: four real columns (DST) or two complex columns
 // k = 0..nx/2 (periodic)
@@ -1654,7 +1654,7 @@ static int col_tiles(const StepArgs<T>& a) {
 }
 template <typename T, bool COMP>
 static size_t smem_rows_inv(const StepArgs<T>& a) {
-  return (size_t)((COMP && a.zeta_mode) ? 4 : 2) * a.G3 * padded_len(a.gx.M) * sizeof(T);
+  return (size_t)((COMP && a.zeta_mode) ? 4 : 2) * a.G3 * padded_len<T>(a.gx.M) * sizeof(T);
 }
 template <typename T>
 static size_t smem_rhs_r(int r) {

@@ -225,7 +225,7 @@ extern "C" int qgw_invert_pv_noalloc(const qgw_params* p, const double* cl2m, co
   a.norm = norm;
   // same grouping rule as the library's runs (96 KiB of work buffers)
   const size_t budget = 96 * 1024;
-  int g = (int)(budget / (2 * (size_t)qgw::padded_len(nx + 1) * sizeof(double)));
+  int g = (int)(budget / (2 * (size_t)qgw::padded_len<double>(nx + 1) * sizeof(double)));
   g = g < 1 ? 1 : (g > 16 ? 16 : g);
   const int ngroups = (nl + g - 1) / g;
   a.G1 = (nl + ngroups - 1) / ngroups;

@@ -21,7 +21,7 @@
 
 namespace qgw {
 
-// forward complex FFT of length g.H on nrows rows (complex values at pc(e)
+// forward complex FFT of length g.H on nrows rows (complex values at pc<T>(e)
 // of row r at A + r*ld); B is the work buffer; returns the output buffer
 template <typename T>
 __device__ __forceinline__ T* cfft_block(T* A, T* B, int nrows, int ld, const DstGeom& g, const C2<T>* tw) {
@@ -44,8 +44,8 @@ __device__ __forceinline__ T* cfft_block(T* A, T* B, int nrows, int ld, const Ds
   return src;
 }
 
-// Real FFT of rows of N = 2 g.H reals (x_i at pr(i) of A), unnormalised:
-// X_k, k = 0..H, at pc(k) of the returned buffer.
+// Real FFT of rows of N = 2 g.H reals (x_i at pr<T>(i) of A), unnormalised:
+// X_k, k = 0..H, at pc<T>(k) of the returned buffer.
 template <typename T>
 __device__ __forceinline__ T* rfft_block(T* A, T* B, int nrows, int ld, const DstGeom& g, const DstTables<T>& tb) {
   const int tid = threadIdx.x + threadIdx.y * blockDim.x, nth = blockDim.x * blockDim.y;
@@ -57,8 +57,8 @@ __device__ __forceinline__ T* rfft_block(T* A, T* B, int nrows, int ld, const Ds
     const int r = w / nk, k = w - r * nk;
     const C2<T>* Z = (const C2<T>*)(Zb + r * ld);
     C2<T>* X = (C2<T>*)(Xb + r * ld);
-    const C2<T> A1 = Z[pc(k)];
-    const C2<T> B1 = Z[pc(k == 0 ? 0 : H - k)];  // Z_H = Z_0
+    const C2<T> A1 = Z[pc<T>(k)];
+    const C2<T> B1 = Z[pc<T>(k == 0 ? 0 : H - k)];  // Z_H = Z_0
     const T Pr = A1.x + B1.x, Pi = A1.y - B1.y;  // P = Z_k + conj Z_{H-k}
     const T Qr = A1.x - B1.x, Qi = A1.y + B1.y;  // Q = Z_k - conj Z_{H-k}
     const C2<T> cs = tb.spl[k];                  // (cos, sin)(2 pi k / N)
@@ -70,16 +70,16 @@ __device__ __forceinline__ T* rfft_block(T* A, T* B, int nrows, int ld, const Ds
     xk.y = T(0.5) * (Pi + Vi);
     xh.x = T(0.5) * (Pr - Vr);
     xh.y = -(T(0.5) * (Pi - Vi));
-    X[pc(k)] = xk;
-    if (k != H - k) X[pc(H - k)] = xh;
+    X[pc<T>(k)] = xk;
+    if (k != H - k) X[pc<T>(H - k)] = xh;
   }
   __syncthreads();
   return Xb;
 }
 
 // Inverse real FFT (FFTW c2r, unnormalised) of rows holding X_k, k = 0..H,
-// at pc(k) of A; returns the buffer F with x_{2m} = F[pc(m)].x and
-// x_{2m+1} = -F[pc(m)].y.  The imaginary parts of X_0 and X_H are ignored.
+// at pc<T>(k) of A; returns the buffer F with x_{2m} = F[pc<T>(m)].x and
+// x_{2m+1} = -F[pc<T>(m)].y.  The imaginary parts of X_0 and X_H are ignored.
 template <typename T>
 __device__ __forceinline__ T* irfft_block(T* A, T* B, int nrows, int ld, const DstGeom& g, const DstTables<T>& tb) {
   const int tid = threadIdx.x + threadIdx.y * blockDim.x, nth = blockDim.x * blockDim.y;
@@ -89,7 +89,7 @@ __device__ __forceinline__ T* irfft_block(T* A, T* B, int nrows, int ld, const D
     const int r = w / nk, k = w - r * nk;
     const C2<T>* X = (const C2<T>*)(A + r * ld);
     C2<T>* Zc = (C2<T>*)(B + r * ld);
-    C2<T> a = X[pc(k)], b = X[pc(H - k)];
+    C2<T> a = X[pc<T>(k)], b = X[pc<T>(H - k)];
     if (k == 0) { a.y = T(0); b.y = T(0); }
     const T Pr = a.x + b.x, Pi = a.y - b.y;  // P' = X_k + conj X_{H-k}
     const T Qr = a.x - b.x, Qi = a.y + b.y;  // Q' = X_k - conj X_{H-k}
@@ -104,8 +104,8 @@ __device__ __forceinline__ T* irfft_block(T* A, T* B, int nrows, int ld, const D
     zk.y = -(Pi + Ui);
     zh.x = Pr - Ur;
     zh.y = Pi - Ui;
-    if (k < H) Zc[pc(k)] = zk;
-    if (k != H - k && k > 0) Zc[pc(H - k)] = zh;
+    if (k < H) Zc[pc<T>(k)] = zk;
+    if (k != H - k && k > 0) Zc[pc<T>(H - k)] = zh;
   }
   __syncthreads();
   return cfft_block<T>(B, A, nrows, ld, g, tb.tw);

@@ -16,12 +16,12 @@ static void run(int M, int howmany, T* data) {
   const C2<T>* TW = (const C2<T>*)tw.data();
   const C2<T>* PRE = (const C2<T>*)pre.data();
   const C2<T>* SPL = (const C2<T>*)spl.data();
-  std::vector<T> A(padded_len(M)), B(padded_len(M));
+  std::vector<T> A(padded_len<T>(M)), B(padded_len<T>(M));
   for (int r = 0; r < howmany; ++r) {
     T* x = data + (size_t)r * (M - 1);
     for (size_t j = 0; j < A.size(); ++j) A[j] = B[j] = T(777);  // pad slots must never be read
-    for (int j = 0; j < M - 1; ++j) A[pr(j)] = x[j];
-    A[pr(M - 1)] = T(12345);  // padding must never be read
+    for (int j = 0; j < M - 1; ++j) A[pr<T>(j)] = x[j];
+    A[pr<T>(M - 1)] = T(12345);  // padding must never be read
     for (int j = 1; j <= g.H; ++j) dst_pre_item<T>(A.data(), B.data(), j, g, PRE);
     T* src = B.data();
     T* dst = A.data();
@@ -42,7 +42,7 @@ static void run(int M, int howmany, T* data) {
       if (c > 0) dst_scan_fix<T>(dst, c, pref, g);
       pref += tot[c];
     }
-    for (int j = 0; j < M - 1; ++j) x[j] = dst[pr(j)];
+    for (int j = 0; j < M - 1; ++j) x[j] = dst[pr<T>(j)];
   }
 }
 
