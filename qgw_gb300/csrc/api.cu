@@ -152,14 +152,16 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   for (int dim = 0; dim < 2; ++dim) {
     const int M = dim == 0 ? Mx : My;
     qgw::DstTablesHost th = qgw::build_dst_tables(M);
-    T *tw, *pre, *spl;
+    T *tw, *pre, *spl, *twp;
     if ((rc = upload<T>(r, &tw, th.tw))) return rc;
     if ((rc = upload<T>(r, &pre, th.pre))) return rc;
     if ((rc = upload<T>(r, &spl, th.spl))) return rc;
+    if ((rc = upload<T>(r, &twp, th.twp))) return rc;
     qgw::DstTables<T>& t = dim == 0 ? a.tx : a.ty;
     t.tw = (const qgw::C2<T>*)tw;
     t.pre = (const qgw::C2<T>*)pre;
     t.spl = (const qgw::C2<T>*)spl;
+    t.twp = (const qgw::C2<T>*)twp;
   }
   T *cl, *cm;
   if ((rc = upload<T>(r, &cl, r->cl2m))) return rc;

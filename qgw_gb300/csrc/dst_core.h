@@ -105,14 +105,39 @@ inline DstGeom make_geom(int M) {
   return g;
 }
 
+// Twiddles of the Stockham passes with Ns > 1 in the order the passes read
+// them: pass (R, Ns) holds w_H^(q k H/(Ns R)) at (Ns - R0) + (q-1) Ns + k for
+// q = 1..R-1, k = 0..Ns-1 (R0 = the first radix; the pass sizes telescope,
+// sum (R-1) Ns = H - R0), so the consecutive items k of a warp read
+// consecutive entries.  tw holds the H values w_H^m in FP64 pairs; twp gets
+// 2 (H - R0) values.
+inline void fill_pass_twiddles(const DstGeom& g, const double* tw, double* twp) {
+  if (g.npass == 0) return;
+  const int R0 = g.radix[0];
+  int Ns = R0;
+  for (int p = 1; p < g.npass; ++p) {
+    const int R = g.radix[p];
+    for (int q = 1; q < R; ++q)
+      for (int k = 0; k < Ns; ++k) {
+        const int e = (Ns - R0) + (q - 1) * Ns + k;
+        const int m = q * k * (g.H / (Ns * R));
+        twp[2 * e] = tw[2 * m];
+        twp[2 * e + 1] = tw[2 * m + 1];
+      }
+    Ns *= R;
+  }
+}
+
 // Tables (host-computed in FP64, stored per real type):
 //   tw[m]  = (cos, -sin)(2 pi m / H),            m < H     (FFT twiddles)
+//   twp    = tw reordered per Stockham pass (fill_pass_twiddles)
 //   pre[j] = (s_j + 1/2, s_j - 1/2), s_j = sin(pi j/M), j <= H
 //   spl[k] = (cos, sin)(2 pi k / M),             k <= H/2
 template <typename T> struct DstTables {
   const C2<T>* tw;
   const C2<T>* pre;
   const C2<T>* spl;
+  const C2<T>* twp;
 };
 
 // ---- phase 1: pre-processing, items j = 1..H per row -------------------

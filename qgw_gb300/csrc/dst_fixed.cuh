@@ -29,7 +29,8 @@ template <int LGH> struct DstShape {
 };
 
 // One Stockham pass over all rows: item b of a row reads inputs b + q*(H/R)
-// and writes outputs base + q*NS; the twiddles of item b are loaded once.
+// and writes outputs base + q*NS; the twiddles of item b are loaded once,
+// from the pass-ordered table (consecutive items, consecutive entries).
 // With R, NS, H/R and the pad period P all powers of two, adding q*stride to
 // the item's base never carries across a pad period beyond what q*stride
 // itself crosses (the base's offset inside its period plus that of q*stride
@@ -42,14 +43,14 @@ struct StockhamItem {
   static constexpr int pco(int e) { return e + W * (e >> LG); }
   int in0, out0;
   C2<T> w[R];
-  __device__ __forceinline__ void init(int b, const C2<T>* __restrict__ tw) {
+  // twp: the pass-ordered twiddles (fill_pass_twiddles; first radix 8)
+  __device__ __forceinline__ void init(int b, const C2<T>* __restrict__ twp) {
     in0 = pc<T>(b);
     const int k = b & (NS - 1);
     out0 = pc<T>((b - k) * R + k);
     if constexpr (NS > 1) {
-      const int step = k * (H / (NS * R));
 #pragma unroll
-      for (int q = 1; q < R; ++q) w[q] = tw[q * step];
+      for (int q = 1; q < R; ++q) w[q] = twp[(NS - 8) + (q - 1) * NS + k];
     }
   }
   __device__ __forceinline__ void run(const C2<T>* __restrict__ src, C2<T>* __restrict__ dst) const {
@@ -145,24 +146,24 @@ __device__ T* dst_block_fixed(T* A, T* B, int nrows, int ld, const DstTables<T>&
   T* src = B;
   T* dst = A;
   if constexpr (S::NP8 >= 1) {
-    stockham_pass_fixed<T, 8, 1, H>(src, dst, nrows, ld, tb.tw);
+    stockham_pass_fixed<T, 8, 1, H>(src, dst, nrows, ld, tb.twp);
     __syncthreads();
     T* t = src; src = dst; dst = t;
   }
   if constexpr (S::NP8 >= 2) {
-    stockham_pass_fixed<T, 8, 8, H>(src, dst, nrows, ld, tb.tw);
+    stockham_pass_fixed<T, 8, 8, H>(src, dst, nrows, ld, tb.twp);
     __syncthreads();
     T* t = src; src = dst; dst = t;
   }
   if constexpr (S::NP8 >= 3) {
-    stockham_pass_fixed<T, 8, 64, H>(src, dst, nrows, ld, tb.tw);
+    stockham_pass_fixed<T, 8, 64, H>(src, dst, nrows, ld, tb.twp);
     __syncthreads();
     T* t = src; src = dst; dst = t;
   }
   static_assert(S::NP8 <= 3, "fixed DST covers H <= 2048");
   if constexpr (S::RLAST > 1) {
     constexpr int NS = 1 << (3 * S::NP8);
-    stockham_pass_fixed<T, S::RLAST, NS, H>(src, dst, nrows, ld, tb.tw);
+    stockham_pass_fixed<T, S::RLAST, NS, H>(src, dst, nrows, ld, tb.twp);
     __syncthreads();
     T* t = src; src = dst; dst = t;
   }

@@ -22,10 +22,10 @@ inline double sinpi_frac(long m, long N) {
 inline double cospi_frac(long m, long N) { return sinpi_frac(2 * m + N, 2 * N); }
 
 struct DstTablesHost {
-  std::vector<double> tw, pre, spl;  // interleaved (x, y) pairs
+  std::vector<double> tw, pre, spl, twp;  // interleaved (x, y) pairs
 };
 
-// tw: H entries, pre: H+1 entries, spl: H/2+1 entries
+// tw: H entries, twp: H - R0 entries, pre: H+1 entries, spl: H/2+1 entries
 inline DstTablesHost build_dst_tables(int M) {
   const int H = M / 2;
   DstTablesHost t;
@@ -35,6 +35,9 @@ inline DstTablesHost build_dst_tables(int M) {
     t.tw[2 * m] = cospi_frac(2L * m, H);
     t.tw[2 * m + 1] = -sinpi_frac(2L * m, H);
   }
+  const DstGeom g = make_geom(M);
+  t.twp.assign(2 * (size_t)(g.npass ? H - g.radix[0] : 0) + 2, 0.0);
+  fill_pass_twiddles(g, t.tw.data(), t.twp.data());
   t.pre.resize(2 * (size_t)(H + 1));
   for (int j = 0; j <= H; ++j) {
     const double s = sinpi_frac(j, M);

@@ -33,8 +33,9 @@ constexpr size_t kFieldMax = (size_t)1 << 21;  // doubles: nl*(NX+1)*(NY+1) limi
 constexpr int kMMax = 1024;                     // NX, NY limit (DST length + 1)
 constexpr int kNlMax = QGW_NL_GPU_MAX;
 constexpr int kDevMax = 16;
-// DST tables of one dimension: tw (H), pre (H+1), spl (H/2+1) complex values
-constexpr size_t kTab = 2 * ((size_t)kMMax / 2 + ((size_t)kMMax / 2 + 1) + ((size_t)kMMax / 4 + 1));
+// DST tables of one dimension: tw (H), pre (H+1), spl (H/2+1), twp (< H)
+// complex values
+constexpr size_t kTab = 2 * (2 * ((size_t)kMMax / 2) + ((size_t)kMMax / 2 + 1) + ((size_t)kMMax / 4 + 1));
 constexpr size_t kStateD = (sizeof(qgw::DevState) + 7) / 8;
 
 // offsets (in doubles) inside the scratch array
@@ -129,6 +130,7 @@ void fill_tables(int M, double* dst) {
     spl[2 * k] = sinpi_r(4L * k + M, 2L * M);
     spl[2 * k + 1] = sinpi_r(2L * k, M);
   }
+  qgw::fill_pass_twiddles(qgw::make_geom(M), tw, spl + 2 * (H / 2 + 1));
 }
 
 bool pow2_in(int v) { return v >= 4 && v <= kMMax && (v & (v - 1)) == 0; }
@@ -207,9 +209,11 @@ extern "C" int qgw_invert_pv_noalloc(const qgw_params* p, const double* cl2m, co
   a.tx.tw = (const qgw::C2<double>*)(base + oTx);
   a.tx.pre = (const qgw::C2<double>*)(base + oTx + 2 * Hx);
   a.tx.spl = (const qgw::C2<double>*)(base + oTx + 2 * Hx + 2 * (Hx + 1));
+  a.tx.twp = (const qgw::C2<double>*)(base + oTx + 2 * Hx + 2 * (Hx + 1) + 2 * (Hx / 2 + 1));
   a.ty.tw = (const qgw::C2<double>*)(base + oTy);
   a.ty.pre = (const qgw::C2<double>*)(base + oTy + 2 * Hy);
   a.ty.spl = (const qgw::C2<double>*)(base + oTy + 2 * Hy + 2 * (Hy + 1));
+  a.ty.twp = (const qgw::C2<double>*)(base + oTy + 2 * Hy + 2 * (Hy + 1) + 2 * (Hy / 2 + 1));
   a.cl2m = base + oCl;
   a.cm2l = base + oCm;
   a.iRd2 = base + oIrd;

@@ -1,6 +1,7 @@
 // CPU check of the device DST-I building blocks (qgw_gb300/csrc/dst_core.h):
 // runs every phase's work items in a plain loop, exactly as the kernels
 // spread them over threads, and exposes the result through a C function.
+#include <cmath>
 #include <vector>
 #include <cstring>
 #include "../../qgw_gb300/csrc/dst_tables.h"
@@ -48,3 +49,26 @@ static void run(int M, int howmany, T* data) {
 
 extern "C" void dst_core_run_f64(int M, int howmany, double* data) { run<double>(M, howmany, data); }
 extern "C" void dst_core_run_f32(int M, int howmany, float* data) { run<float>(M, howmany, data); }
+
+// pass-ordered twiddles (fill_pass_twiddles) against their definition:
+// returns the number of mismatching entries, or -1 if the count is wrong
+extern "C" int dst_core_check_twp(int M) {
+  DstGeom g = make_geom(M);
+  DstTablesHost th = build_dst_tables(M);
+  const int H = g.H;
+  int bad = 0, count = 0, Ns = g.radix[0];
+  for (int p = 1; p < g.npass; ++p) {
+    const int R = g.radix[p];
+    for (int q = 1; q < R; ++q)
+      for (int k = 0; k < Ns; ++k) {
+        const int e = (Ns - g.radix[0]) + (q - 1) * Ns + k;
+        const double ang = 2.0 * M_PI * ((double)q * k * (H / (Ns * R))) / H;
+        if (std::fabs(th.twp[2 * e] - std::cos(ang)) > 1e-15 || std::fabs(th.twp[2 * e + 1] + std::sin(ang)) > 1e-15)
+          ++bad;
+        ++count;
+      }
+    Ns *= R;
+  }
+  if (count != (g.npass > 1 ? H - g.radix[0] : 0)) return -1;
+  return bad;
+}

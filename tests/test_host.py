@@ -148,6 +148,13 @@ def test_device_dst_blocks_on_host(dstcore, M):
     assert np.linalg.norm(yf - ref) <= 1e-5 * np.linalg.norm(ref)
 
 
+@pytest.mark.parametrize("M", [16, 64, 128, 256, 512, 1024, 2048])
+def test_pass_ordered_twiddles(dstcore, M):
+    """The Stockham passes' lane-ordered twiddle table holds w_H^(q k H/(Ns R))
+    at (Ns - R0) + (q-1) Ns + k, H - R0 entries in all."""
+    assert dstcore.dst_core_check_twp(M) == 0
+
+
 @pytest.mark.parametrize("seed", [1, 7, 12345, 0])
 def test_forcing_generator_is_the_c_library_rand(tmp_path, seed):
     """The stochastic forcing's generator restates the C library's rand()
