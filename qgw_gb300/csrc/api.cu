@@ -67,25 +67,27 @@ int upload(qgw_run* r, T** out, const std::vector<double>& host) {
 // 1024^2 x 10 on GB300: 64 KiB (3 blocks/SM) is fastest for FP64 and 40 KiB
 // (4-5 blocks/SM) for FP32; QGW_ROW_SMEM_KB overrides it (tuning knob).
 // Shared-memory budget of the work buffers of the forward rows kernel (K1):
-// 48 KiB (FP64) / 56 KiB (FP32), which keeps four blocks per SM; measured
-// at 1024^2 and 2048^2 x 10 on GB300.  QGW_ROW_SMEM_KB overrides it.
-size_t row_budget(size_t elem) {
+// 48 KiB (FP64) / 56 KiB (FP32), which keeps four blocks per SM, and 40 KiB
+// for FP32 rows of 2048 and more; measured at 512^2, 1024^2 and 2048^2 x 10
+// on GB300.  QGW_ROW_SMEM_KB overrides it.
+size_t row_budget(size_t elem, int M) {
   const char* e = std::getenv("QGW_ROW_SMEM_KB");
   const long v = e ? std::atol(e) : 0;
   if (v >= 16 && v <= 220) return (size_t)v * 1024;
+  if (elem == 4 && M >= 2048) return (size_t)40 * 1024;
   return (size_t)(elem == 8 ? 48 : 56) * 1024;
 }
 
 // Layers per block of the inverse rows kernel (K3): the measured optimum is
 // a fixed group size rather than a byte budget (each group re-reads the
-// row's spectral data, while larger groups cost occupancy): 3 layers with
-// the zeta rows, 2 without, within 110 KiB of work buffers.
-// QGW_INV_GROUP overrides the size.
-int inv_group(int zeta) {
+// row's spectral data, while larger groups cost occupancy): with the zeta
+// rows 3 layers, 5 for rows of 512 and less; 2 without; within 110 KiB of
+// work buffers.  QGW_INV_GROUP overrides the size.
+int inv_group(int zeta, int M) {
   const char* e = std::getenv("QGW_INV_GROUP");
   const int v = e ? std::atoi(e) : 0;
   if (v >= 1 && v <= 16) return v;
-  return zeta ? 3 : 2;
+  return zeta ? (M <= 512 ? 5 : 3) : 2;
 }
 
 // Modes (layers) per block of a row kernel: as many as the budget holds (each
@@ -252,8 +254,8 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   a.topo_fac = p.f0 / dhb;
   a.has_topo = 0;
   a.has_wind = p.tau0 != 0;
-  a.G1 = mode_group(r->nl, Mx, sizeof(T), row_budget(sizeof(T)), 1, 16, 16);
-  a.G3 = mode_group(r->nl, Mx, sizeof(T), 110 * 1024, 1, 16, inv_group(0));
+  a.G1 = mode_group(r->nl, Mx, sizeof(T), row_budget(sizeof(T), Mx), 1, 16, 16);
+  a.G3 = mode_group(r->nl, Mx, sizeof(T), 110 * 1024, 1, 16, inv_group(0, Mx));
   a.CT = 0;
   a.low_k64 = 8;
   // 16-byte column vectors: rows 16-byte aligned and a whole number of
@@ -273,7 +275,7 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
     if ((rc = dalloc(r, &a.spec2, field))) return rc;
     if ((rc = dalloc(r, &a.zeta, field))) return rc;
     // K3 transforms psi and zeta rows of each mode: two rows per mode
-    a.G3 = mode_group(r->nl, Mx, sizeof(T), 110 * 1024, 2, 8, inv_group(1));
+    a.G3 = mode_group(r->nl, Mx, sizeof(T), 110 * 1024, 2, 8, inv_group(1, Mx));
     // symbol of the 5-point Laplacian: DST-I basis sin^2(pi k / 2(n+1));
     // periodic Fourier basis sin^2(pi k / N)
     std::vector<double> sx(r->nx, 0.0), sy(r->ny);
