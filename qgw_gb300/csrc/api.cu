@@ -38,7 +38,9 @@ int cuda_fail(cudaError_t e) {
     if (e_ != cudaSuccess) return cuda_fail(e_); \
   } while (0)
 
-bool pow2(int v) { return v >= 4 && (v & (v - 1)) == 0; }
+// row pitch of a periodic run's fields (and of the forcing spectra): the
+// NX/2 + 1 complex values of a spectral row, rounded up to 16-byte rows
+int periodic_pitch(int NX) { return (NX + 2 + 3) & ~3; }
 
 template <typename T>
 int dalloc(qgw_run* r, T** out, size_t count) {
@@ -310,7 +312,7 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
       f.on = 1;
       f.nring = NP;
       f.NF = p.NX;
-      f.fpitch = p.NX + 4;
+      f.fpitch = periodic_pitch(p.NX);
       int imax = 0;
       for (size_t k = 0; k < ij.size(); k += 2) imax = std::max(imax, ij[k]);
       f.col_blocks = imax / 2 + 1;
@@ -406,12 +408,12 @@ int qgw_footprint(const qgw_params* p, int precision, size_t* bytes) {
   if (!p || !bytes) return QGW_ERR_PARAM;
   const bool per = p->bc_fac == -1;
   const size_t nx = p->NX - (per ? 0 : 1), ny = p->NY - (per ? 0 : 1);
-  const size_t field = (size_t)p->nl * ny * (nx + (per ? 4 : 1));
+  const size_t field = (size_t)p->nl * ny * (per ? (size_t)periodic_pitch(p->NX) : nx + 1);
   size_t b;
   if (precision == QGW_FP64) b = field * 8 * 7;  // q psi spec f0 f1 f2 hinv
   else b = field * 4 * 9;                        // q_hi q_lo psi spec spec2 zeta f0 f1 f2
   b += (size_t)p->nl * (ny + 2) * (nx + 2) * 8;  // reference-layout staging for host copies
-  if (p->k_f != 0) b += (size_t)3 * p->NX * (p->NX + 4) * (precision == QGW_FP64 ? 8 : 4);  // forcing
+  if (p->k_f != 0) b += (size_t)3 * p->NX * periodic_pitch(p->NX) * (precision == QGW_FP64 ? 8 : 4);  // forcing
   *bytes = b + (size_t)(nx + ny) * 64 + (1 << 20);
   return QGW_OK;
 }
@@ -434,7 +436,11 @@ int qgw_create(const qgw_params* pin, const double* cl2m, const double* cm2l, co
     const int n_rec = (int)std::floor(p.dt_forc_period / p.dt_forc);
     if (n_rec < 1 || n_rec * p.dt_forc != p.dt_forc_period) return QGW_ERR_PARAM;
   }
-  if (!pow2(p.NX) || !pow2(p.NY) || p.NX > 8192 || p.NY > 8192) return QGW_ERR_UNSUPPORTED;
+  // transform lengths: closed DST-I of M = NX, NY; periodic real FFT of NX and
+  // complex FFT of NY (M = 2 NY); M even, M/2 a product of 2, 3, 5 and 7
+  if (p.NX > 8192 || p.NY > 8192) return QGW_ERR_UNSUPPORTED;
+  if (!qgw::transform_length_ok(p.NX) || !qgw::transform_length_ok(per ? 2 * p.NY : p.NY))
+    return QGW_ERR_UNSUPPORTED;
   if (p.nl < 1 || p.nl > QGW_NL_GPU_MAX) return QGW_ERR_UNSUPPORTED;
   if (!(p.Lx > 0) || !(p.cfl > 0)) return QGW_ERR_PARAM;
   qgw_run* r = new qgw_run();
@@ -444,7 +450,7 @@ int qgw_create(const qgw_params* pin, const double* cl2m, const double* cm2l, co
   r->ny = per ? p.NY : p.NY - 1;
   r->nl = p.nl;
   // periodic rows also hold the NX/2 + 1 complex values of a spectral row
-  r->pitch = per ? r->nx + 4 : r->nx + 1;
+  r->pitch = per ? periodic_pitch(p.NX) : r->nx + 1;
   r->lstride = (size_t)r->ny * r->pitch;
   r->Delta = p.Lx / p.NX;
   r->Ly = p.NY * r->Delta;

@@ -2,7 +2,8 @@
 // inversion (the reference takes it from FFTW's RODFT00 plans,
 // src/elliptic.h:136-139,174,204).
 //
-// Definition (FFTW RODFT00, unnormalised), length n = M-1, M = 2H = 2^p:
+// Definition (FFTW RODFT00, unnormalised), length n = M-1, M = 2H, H a
+// product of 2, 3, 5 and 7:
 //     Y_k = 2 sum_{j=1}^{M-1} x_j sin(pi j k / M),   k = 1..M-1.
 // Method (published: the sine transform through a half-length complex FFT,
 // e.g. Press et al., Numerical Recipes, section 12.3):
@@ -83,12 +84,13 @@ template <typename T> QGW_HD int padded_len(int M) {
 
 // Static shape of one DST length.
 struct DstGeom {
-  int M;          // DST length + 1 (power of two, >= 4)
+  int M;          // DST length + 1 (even, >= 4)
   int H;          // M / 2, complex FFT length
   int npass;      // Stockham passes
-  int radix[8];   // radix of each pass (8, then 4 or 2); first pass has Ns = 1
+  int radix[12];  // radix of each pass: 8s, then 4 or 2, then 3s, 5s, 7s; first pass has Ns = 1
   int chunk;      // prefix-sum chunk length (values per work item)
-  int nchunk;     // H / chunk (<= 32)
+  int nchunk;     // ceil(H / chunk) (<= 32)
+  int ok;         // 1 when H factors into 2, 3, 5 and 7
 };
 
 inline DstGeom make_geom(int M) {
@@ -96,14 +98,20 @@ inline DstGeom make_geom(int M) {
   g.M = M;
   g.H = M / 2;
   int rem = g.H, p = 0;
-  while (rem >= 8) { g.radix[p++] = 8; rem /= 8; }
-  if (rem == 4) g.radix[p++] = 4;
-  else if (rem == 2) g.radix[p++] = 2;
+  while (rem % 8 == 0 && rem >= 8) { g.radix[p++] = 8; rem /= 8; }
+  if (rem % 4 == 0) { g.radix[p++] = 4; rem /= 4; }
+  else if (rem % 2 == 0) { g.radix[p++] = 2; rem /= 2; }
+  for (int f : {3, 5, 7})
+    while (rem % f == 0 && p < 12) { g.radix[p++] = f; rem /= f; }
   g.npass = p;
-  g.chunk = g.H >= 256 ? g.H / 32 : (g.H >= 8 ? 8 : g.H);
-  g.nchunk = g.H / g.chunk;
+  g.ok = (rem == 1 && M % 2 == 0 && M >= 4) ? 1 : 0;
+  g.chunk = g.H < 8 ? g.H : (g.H >= 256 ? (g.H + 31) / 32 : 8);
+  g.nchunk = g.chunk > 0 ? (g.H + g.chunk - 1) / g.chunk : 0;
   return g;
 }
+
+// Lengths the transforms support: even, half-length a product of 2, 3, 5, 7
+inline bool transform_length_ok(int M) { return M >= 4 && make_geom(M).ok == 1; }
 
 // Twiddles of the Stockham passes with Ns > 1 in the order the passes read
 // them: pass (R, Ns) holds w_H^(q k H/(Ns R)) at (Ns - R0) + (q-1) Ns + k for
@@ -256,6 +264,64 @@ template <typename T> QGW_HD void dft8_tw(C2<T>* v, const C2<T>* w) {
   }
 }
 
+// forward DFTs of odd length (the published symmetric forms: outputs k and
+// R-k share the sums over x_n + x_{R-n} and the differences x_n - x_{R-n})
+template <typename T> QGW_HD void dft3(C2<T>* v) {
+  const T s = T(0.86602540378443864676);  // sin(2 pi / 3)
+  const C2<T> t = cadd(v[1], v[2]), d = csub(v[1], v[2]);
+  C2<T> m;
+  m.x = fmaT(T(-0.5), t.x, v[0].x);
+  m.y = fmaT(T(-0.5), t.y, v[0].y);
+  v[0] = cadd(v[0], t);
+  // y1 = m - i s d, y2 = m + i s d
+  v[1].x = fmaT(s, d.y, m.x);  v[1].y = fmaT(-s, d.x, m.y);
+  v[2].x = fmaT(-s, d.y, m.x); v[2].y = fmaT(s, d.x, m.y);
+}
+template <typename T> QGW_HD void dft5(C2<T>* v) {
+  const T c1 = T(0.30901699437494742410), c2 = T(-0.80901699437494742410);  // cos(2 pi/5), cos(4 pi/5)
+  const T s1 = T(0.95105651629515357212), s2 = T(0.58778525229247312917);   // sin(2 pi/5), sin(4 pi/5)
+  const C2<T> t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
+  const C2<T> d1 = csub(v[1], v[4]), d2 = csub(v[2], v[3]);
+  C2<T> a, b, p, q;
+  a.x = fmaT(c2, t2.x, fmaT(c1, t1.x, v[0].x)); a.y = fmaT(c2, t2.y, fmaT(c1, t1.y, v[0].y));
+  b.x = fmaT(c1, t2.x, fmaT(c2, t1.x, v[0].x)); b.y = fmaT(c1, t2.y, fmaT(c2, t1.y, v[0].y));
+  p.x = fmaT(s2, d2.x, s1 * d1.x); p.y = fmaT(s2, d2.y, s1 * d1.y);     // s1 d1 + s2 d2
+  q.x = fmaT(-s1, d2.x, s2 * d1.x); q.y = fmaT(-s1, d2.y, s2 * d1.y);   // s2 d1 - s1 d2
+  v[0] = cadd(v[0], cadd(t1, t2));
+  // y1 = a - i p, y4 = a + i p, y2 = b - i q, y3 = b + i q
+  v[1].x = a.x + p.y; v[1].y = a.y - p.x;
+  v[4].x = a.x - p.y; v[4].y = a.y + p.x;
+  v[2].x = b.x + q.y; v[2].y = b.y - q.x;
+  v[3].x = b.x - q.y; v[3].y = b.y + q.x;
+}
+template <typename T> QGW_HD void dft7(C2<T>* v) {
+  // cos and sin of 2 pi n / 7, n = 1, 2, 3
+  const T c[3] = {T(0.62348980185873353053), T(-0.22252093395631440429), T(-0.90096886790241912624)};
+  const T s[3] = {T(0.78183148246802980871), T(0.97492791218182360702), T(0.43388373911755812048)};
+  C2<T> t[3], d[3];
+  for (int n = 0; n < 3; ++n) { t[n] = cadd(v[n + 1], v[6 - n]); d[n] = csub(v[n + 1], v[6 - n]); }
+  C2<T> y[7];
+  y[0] = cadd(v[0], cadd(t[0], cadd(t[1], t[2])));
+  for (int k = 1; k <= 3; ++k) {
+    C2<T> a = v[0], p;
+    p.x = T(0); p.y = T(0);
+    for (int n = 1; n <= 3; ++n) {
+      const int e = (n * k) % 7;                 // angle index of w^(n k)
+      const T cn = e <= 3 ? c[e - 1] : c[7 - e - 1];
+      const T sn = e <= 3 ? s[e - 1] : -s[7 - e - 1];
+      a.x = fmaT(cn, t[n - 1].x, a.x); a.y = fmaT(cn, t[n - 1].y, a.y);
+      p.x = fmaT(sn, d[n - 1].x, p.x); p.y = fmaT(sn, d[n - 1].y, p.y);
+    }
+    // y_k = a - i p, y_{7-k} = a + i p
+    y[k].x = a.x + p.y; y[k].y = a.y - p.x;
+    y[7 - k].x = a.x - p.y; y[7 - k].y = a.y + p.x;
+  }
+  for (int k = 0; k < 7; ++k) v[k] = y[k];
+}
+
+// One Stockham autosort pass of radix R over a row (Govindaraju et al.'s
+// formulation, any mix of radices): item b reads b + q H/R, k = b mod Ns,
+// multiplies by w_H^(q k H/(Ns R)) and writes (b - k) R + k + q Ns.
 template <int R, typename T>
 QGW_HD void stockham_item(const C2<T>* __restrict__ src, C2<T>* __restrict__ dst, int b, int Ns, int H,
                           const C2<T>* __restrict__ tw) {
@@ -263,7 +329,7 @@ QGW_HD void stockham_item(const C2<T>* __restrict__ src, C2<T>* __restrict__ dst
   C2<T> v[R];
 #pragma unroll
   for (int q = 0; q < R; ++q) v[q] = src[pc<T>(b + q * stride)];
-  const int k = b & (Ns - 1);
+  const int k = b % Ns;
   if (Ns > 1) {
     const int step = k * (H / (Ns * R));
     if (R == 8) {
@@ -275,12 +341,18 @@ QGW_HD void stockham_item(const C2<T>* __restrict__ src, C2<T>* __restrict__ dst
 #pragma unroll
       for (int q = 1; q < R; ++q) v[q] = cmul(v[q], tw[q * step]);
       if (R == 4) dft4(v);
-      else dft2(v);
+      else if (R == 2) dft2(v);
+      else if (R == 3) dft3(v);
+      else if (R == 5) dft5(v);
+      else dft7(v);
     }
   } else {
     if (R == 8) dft8(v);
     else if (R == 4) dft4(v);
-    else dft2(v);
+    else if (R == 2) dft2(v);
+    else if (R == 3) dft3(v);
+    else if (R == 5) dft5(v);
+    else dft7(v);
   }
   const int base = (b - k) * R + k;
 #pragma unroll
@@ -289,9 +361,14 @@ QGW_HD void stockham_item(const C2<T>* __restrict__ src, C2<T>* __restrict__ dst
 
 template <typename T>
 QGW_HD void stockham_dispatch(int R, const C2<T>* src, C2<T>* dst, int b, int Ns, int H, const C2<T>* tw) {
-  if (R == 8) stockham_item<8, T>(src, dst, b, Ns, H, tw);
-  else if (R == 4) stockham_item<4, T>(src, dst, b, Ns, H, tw);
-  else stockham_item<2, T>(src, dst, b, Ns, H, tw);
+  switch (R) {
+    case 8: stockham_item<8, T>(src, dst, b, Ns, H, tw); break;
+    case 4: stockham_item<4, T>(src, dst, b, Ns, H, tw); break;
+    case 2: stockham_item<2, T>(src, dst, b, Ns, H, tw); break;
+    case 3: stockham_item<3, T>(src, dst, b, Ns, H, tw); break;
+    case 5: stockham_item<5, T>(src, dst, b, Ns, H, tw); break;
+    default: stockham_item<7, T>(src, dst, b, Ns, H, tw); break;
+  }
 }
 
 // ---- phase 3: split, items k = 0..H/2 per row --------------------------
@@ -327,8 +404,9 @@ template <typename T>
 QGW_HD T dst_scan_chunk(T* out, int c, const DstGeom& g) {
   T acc = T(0);
   const int k0 = c * g.chunk;
+  const int n = g.H - k0 < g.chunk ? g.H - k0 : g.chunk;  // the last chunk may be short
   acc = out[pr<T>(2 * k0)];
-  for (int t = 1; t < g.chunk; ++t) {
+  for (int t = 1; t < n; ++t) {
     acc = acc + out[pr<T>(2 * (k0 + t))];
     out[pr<T>(2 * (k0 + t))] = acc;
   }
@@ -338,7 +416,8 @@ QGW_HD T dst_scan_chunk(T* out, int c, const DstGeom& g) {
 template <typename T>
 QGW_HD void dst_scan_fix(T* out, int c, T prefix, const DstGeom& g) {
   const int k0 = c * g.chunk;
-  for (int t = 0; t < g.chunk; ++t) out[pr<T>(2 * (k0 + t))] += prefix;
+  const int n = g.H - k0 < g.chunk ? g.H - k0 : g.chunk;
+  for (int t = 0; t < n; ++t) out[pr<T>(2 * (k0 + t))] += prefix;
 }
 
 }  // namespace qgw

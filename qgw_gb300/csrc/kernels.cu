@@ -50,9 +50,9 @@ template <typename T>
 __device__ __forceinline__ T* dst_block_generic(T* A, T* B, int nrows, int ld, const DstGeom& g,
                                                 const DstTables<T>& tb, T* tot) {
   const int tid = threadIdx.x + threadIdx.y * blockDim.x, nth = blockDim.x * blockDim.y;
-  const int H = g.H, lgH = __ffs(H) - 1;
-  for (int w = tid; w < (nrows << lgH); w += nth) {
-    const int r = w >> lgH, j = (w & (H - 1)) + 1;
+  const int H = g.H;
+  for (int w = tid; w < nrows * H; w += nth) {
+    const int r = w / H, j = w - r * H + 1;
     dst_pre_item<T>(A + r * ld, B + r * ld, j, g, tb.pre);
   }
   __syncthreads();
@@ -61,26 +61,25 @@ __device__ __forceinline__ T* dst_block_generic(T* A, T* B, int nrows, int ld, c
   int Ns = 1;
   for (int p = 0; p < g.npass; ++p) {
     const int R = g.radix[p];
-    const int nb = H / R, lgnb = __ffs(nb) - 1;
-    for (int w = tid; w < (nrows << lgnb); w += nth) {
-      const int r = w >> lgnb, b = w & (nb - 1);
+    const int nb = H / R;
+    for (int w = tid; w < nrows * nb; w += nth) {
+      const int r = w / nb, b = w - r * nb;
       stockham_dispatch<T>(R, (const C2<T>*)(src + r * ld), (C2<T>*)(dst + r * ld), b, Ns, H, tb.tw);
     }
     __syncthreads();
     Ns *= R;
     T* t = src; src = dst; dst = t;
   }
-  // split: items k = 0..H/2-1 per row; item 0 also does k = H/2
-  const int lgh = lgH - 1;
-  for (int w = tid; w < (nrows << lgh); w += nth) {
-    const int r = w >> lgh, k = w & ((H >> 1) - 1);
+  // split: items k = 0..H/2 per row
+  const int nk = H / 2 + 1;
+  for (int w = tid; w < nrows * nk; w += nth) {
+    const int r = w / nk, k = w - r * nk;
     dst_split_item<T>((const C2<T>*)(src + r * ld), dst + r * ld, k, g, tb.spl);
-    if (k == 0) dst_split_item<T>((const C2<T>*)(src + r * ld), dst + r * ld, H >> 1, g, tb.spl);
   }
   __syncthreads();
-  const int nc = g.nchunk, lgnc = __ffs(nc) - 1;
-  for (int w = tid; w < (nrows << lgnc); w += nth) {
-    const int r = w >> lgnc, c = w & (nc - 1);
+  const int nc = g.nchunk;
+  for (int w = tid; w < nrows * nc; w += nth) {
+    const int r = w / nc, c = w - r * nc;
     tot[r * 32 + c] = dst_scan_chunk<T>(dst + r * ld, c, g);
   }
   __syncthreads();
@@ -98,16 +97,17 @@ __device__ __forceinline__ T* dst_block_generic(T* A, T* B, int nrows, int ld, c
     if (lane < nc) tot[r * 32 + lane] = ex;
   }
   __syncthreads();
-  for (int w = tid; w < (nrows << lgnc); w += nth) {
-    const int r = w >> lgnc, c = w & (nc - 1);
+  for (int w = tid; w < nrows * nc; w += nth) {
+    const int r = w / nc, c = w - r * nc;
     if (c > 0) dst_scan_fix<T>(dst + r * ld, c, tot[r * 32 + c], g);
   }
   __syncthreads();
   return dst;
 }
 
-// Block DST of any supported length: lengths M = 128..2048 use the
-// compile-time specialisations of dst_fixed.cuh, others the generic loops.
+// Block DST of any supported length: the power-of-two lengths M = 128..2048
+// use the compile-time specialisations of dst_fixed.cuh, others (mixed
+// radix 2, 3, 5, 7) the generic loops.
 template <typename T>
 __device__ __forceinline__ T* dst_block(T* A, T* B, int nrows, int ld, const DstGeom& g, const DstTables<T>& tb,
                                         T* tot) {

@@ -13,7 +13,7 @@
 //   P' = X_k + conj X_{H-k},  Q' = X_k - conj X_{H-k},
 // takes the backward FFT of Z' as conj(FFT(conj Z')) and reads
 // x_{2m} = Re, x_{2m+1} = Im of the result.  The Stockham passes are the
-// runtime-geometry ones of dst_core.h, so every power-of-two length works.
+// runtime-geometry ones of dst_core.h (mixed radix 2, 3, 5, 7).
 #pragma once
 
 #include "dst_core.h"
@@ -32,9 +32,9 @@ __device__ __forceinline__ T* cfft_block(T* A, T* B, int nrows, int ld, const Ds
   int Ns = 1;
   for (int p = 0; p < g.npass; ++p) {
     const int R = g.radix[p];
-    const int nb = H / R, lgnb = __ffs(nb) - 1;
-    for (int w = tid; w < (nrows << lgnb); w += nth) {
-      const int r = w >> lgnb, b = w & (nb - 1);
+    const int nb = H / R;
+    for (int w = tid; w < nrows * nb; w += nth) {
+      const int r = w / nb, b = w - r * nb;
       stockham_dispatch<T>(R, (const C2<T>*)(src + r * ld), (C2<T>*)(dst + r * ld), b, Ns, H, tw);
     }
     __syncthreads();

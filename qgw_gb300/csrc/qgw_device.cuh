@@ -14,7 +14,8 @@
 //   hinv   FP64 path only: 1 / (-(L^2 + K^2 + iRd2_m) * norm) per (m, j, k)
 //   topo   (ny+2) x (nx+2) reference layout (only when non-zero)
 // The doubly periodic basin keeps the same layout with nx = NX, ny = NY and
-// pitch = NX + 4 (room for the NX/2 + 1 complex values of a spectral row).
+// pitch = NX + 2 rounded up to a multiple of 4 (room for the NX/2 + 1
+// complex values of a spectral row, 16-byte aligned rows).
 #pragma once
 
 #include <cuda.h>
@@ -139,7 +140,7 @@ template <typename T> struct StepArgs {
   CUtensorMap tm[3];
   int use_tma;
   // doubly periodic basin (bc_fac = -1): nx = NX, ny = NY interior points,
-  // pitch = NX + 4; gx has M = NX (real FFT of length NX as a complex FFT
+  // pitch = NX + 2 rounded up to 4; gx has M = NX (real FFT of length NX as a complex FFT
   // of NX/2), gy has M = 2 NY (complex FFT of length NY); spectral rows hold
   // X_0..X_{NX/2} as (re, im) pairs; ghost values wrap around
   int periodic;

@@ -96,6 +96,17 @@ def cases():
         rng = np.random.Generator(np.random.PCG64(8100 + int(nx) + int(bc)))
         frec = (rng.normal(0.0, 1e-11, size=O.forcing_file_shape(p, 3))).astype(np.float32)
         out.append((name, p, 40, 1200.0, None, frec))
+    # grids that are not powers of two (FFTW plans any length): DST-I of
+    # 95 x 59 points (half-lengths 48 = 8*2*3, 30 = 2*3*5), hyperviscous
+    # 49^2 x 10 (25 = 5*5), a periodic 48^2 basin (24 = 8*3, 48)
+    p = C.cfg1(96)
+    p["NY"] = 60
+    out.append(("mixed_radix_nx96_ny60", p, 50, 1200.0, None))
+    p = C.cfg2(50, 10)
+    out.append(("mixed_radix_nx50_nl10_hyper", p, 40, 600.0, None))
+    p = C.cfg1(48)
+    p.update(bc_fac=-1.0)
+    out.append(("periodic_nx48", p, 40, 1200.0, None))
     return out
 
 

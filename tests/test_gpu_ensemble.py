@@ -10,7 +10,9 @@ pytestmark = pytest.mark.gpu
 
 
 def members():
-    return [C.cfg1(64), C.cfg2(128, 5), dict(C.cfg1(64), NY=32), C.cfg2(64, 10), C.basin_params(32, 2, dt=900.0)]
+    # the last two are not powers of two (mixed-radix transforms)
+    return [C.cfg1(64), C.cfg2(128, 5), dict(C.cfg1(64), NY=32), C.cfg2(64, 10), C.basin_params(32, 2, dt=900.0),
+            dict(C.cfg1(96), NY=60), C.cfg2(70, 5)]
 
 
 def alone(capi, p, prec, q0, n):
@@ -33,7 +35,7 @@ def test_ensemble_members_equal_alone(qgwlib, prec, graph):
     for i, (p, q0) in enumerate(zip(ps, q0s)):
         ens.set_q(i, q0)
         ens.fix_dt(i, p["dt"])
-    caps = [12, 0, 5, 12, 9]  # 0: no cap (12 steps)
+    caps = [12, 0, 5, 12, 9, 7, 0]  # 0: no cap (12 steps)
     infos = ens.step(12, max_steps=caps, graph=graph)
     for i, (p, q0) in enumerate(zip(ps, q0s)):
         n = caps[i] or 12

@@ -103,6 +103,36 @@ def test_fp64_vs_port_100_steps(qgwlib, oracle_mod, case):
     assert rel(psi, o["psi"]) <= TOL64, rel(psi, o["psi"])
 
 
+@pytest.mark.parametrize("case", ["closed_384x240", "closed_70_nl5_hyper", "periodic_96", "periodic_60_hyper"])
+def test_fp64_mixed_radix_vs_port(qgwlib, oracle_mod, case):
+    """Grids that are not powers of two: the transforms run Stockham passes
+    of radix 2, 3, 5 and 7 (half-lengths 192 = 8*8*3, 120 = 8*3*5, 35 = 5*7,
+    48 = 8*2*3, 96 = 8*4*3, 30 = 2*3*5)."""
+    if case == "closed_384x240":
+        p, dt, n = dict(C.cfg1(384), NY=240), 1200.0, 10
+    elif case == "closed_70_nl5_hyper":
+        p, dt, n = C.cfg2(70, 5), 600.0, 50
+    elif case == "periodic_96":
+        p, dt, n = dict(C.cfg1(96), bc_fac=-1.0), 1200.0, 30
+    else:
+        p, dt, n = dict(C.cfg2(60, 5), bc_fac=-1.0), 600.0, 30
+    q0 = C.noise_ic(p, 1101)
+    o = oracle_mod.run_port(p, q0, n, dt_fixed=dt)
+    psi, q, tm = gpu_run(qgwlib, p, q0, n, dt)
+    assert rel(q, o["q"]) <= TOL64, rel(q, o["q"])
+    assert rel(psi, o["psi"]) <= TOL64, rel(psi, o["psi"])
+
+
+def test_fp32c_vs_fp64_mixed_radix(qgwlib):
+    """FP32c against FP64 on a 768^2 x 10 grid (half-length 384 = 8*8*2*3)."""
+    p = C.cfg2(768, 10)
+    q0 = C.noise_ic(p, 34)
+    psi64, q64, _ = gpu_run(qgwlib, p, q0, 100, 600.0, precision=0)
+    psi32, q32, _ = gpu_run(qgwlib, p, q0, 100, 600.0, precision=1)
+    assert rel(q32, q64) <= TOL32C, rel(q32, q64)
+    assert rel(psi32, psi64) <= TOL32C, rel(psi32, psi64)
+
+
 def test_fp64_adaptive_dt_vs_port(qgwlib, oracle_mod):
     p = dict(C.cfg1(128))
     p.pop("dt")
@@ -198,7 +228,8 @@ def test_step_stops_at_t_out_and_tend(qgwlib):
 
 def test_unsupported_configs_fail_loudly(qgwlib):
     deep = dict(C.cfg2(64, 33))  # more layers than the GPU kernels hold (32)
-    for bad in (dict(C.cfg1(64), NX=100), dict(C.cfg1(64), bc_fac=-0.5), deep):
+    # NX = 22: half-length 11 (a prime beyond the radices 2, 3, 5, 7); NX = 99: odd
+    for bad in (dict(C.cfg1(64), NX=22), dict(C.cfg1(64), NX=99), dict(C.cfg1(64), bc_fac=-0.5), deep):
         with pytest.raises(qgwlib.QgwError) as e:
             qgwlib.Run(bad)
         assert e.value.status == -6

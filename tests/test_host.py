@@ -136,7 +136,8 @@ def dstcore(tmp_path_factory):
     return lib
 
 
-@pytest.mark.parametrize("M", [4, 8, 16, 32, 64, 128, 256, 512, 1024, 2048, 4096])
+@pytest.mark.parametrize("M", [4, 8, 16, 32, 64, 128, 256, 512, 1024, 2048, 4096,
+                               6, 10, 12, 14, 30, 42, 96, 100, 250, 384, 490, 1000, 1536, 2430])
 def test_device_dst_blocks_on_host(dstcore, M):
     x = np.random.default_rng(M).standard_normal((3, M - 1))
     ref = sf.dst(x, type=1, axis=1)
@@ -148,7 +149,7 @@ def test_device_dst_blocks_on_host(dstcore, M):
     assert np.linalg.norm(yf - ref) <= 1e-5 * np.linalg.norm(ref)
 
 
-@pytest.mark.parametrize("M", [16, 64, 128, 256, 512, 1024, 2048])
+@pytest.mark.parametrize("M", [16, 64, 128, 256, 512, 1024, 2048, 96, 1000])
 def test_pass_ordered_twiddles(dstcore, M):
     """The Stockham passes' lane-ordered twiddle table holds w_H^(q k H/(Ns R))
     at (Ns - R0) + (q-1) Ns + k, H - R0 entries in all."""
