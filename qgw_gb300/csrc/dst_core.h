@@ -30,9 +30,11 @@
 
 #ifdef __CUDACC__
 #define QGW_HD __host__ __device__ __forceinline__
+#define QGW_HD_NOINLINE __host__ __device__ __noinline__
 #define QGW_ALIGN(n) __align__(n)
 #else
 #define QGW_HD inline
+#define QGW_HD_NOINLINE __attribute__((noinline))
 #define QGW_ALIGN(n) alignas(n)
 #endif
 
@@ -147,6 +149,25 @@ template <typename T> struct DstTables {
   const C2<T>* spl;
   const C2<T>* twp;
 };
+
+// Work-item loop of a block over nrows rows of n items each: f(r, i) for
+// every row r and item i, spread over the block's threads; shifts when n is
+// a power of two (the common case), one division per item otherwise.
+#ifdef __CUDACC__
+template <typename F>
+__device__ __forceinline__ void block_items(int nrows, int n, F f) {
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x, nth = blockDim.x * blockDim.y;
+  if ((n & (n - 1)) == 0) {
+    const int lg = __ffs(n) - 1;
+    for (int w = tid; w < (nrows << lg); w += nth) f(w >> lg, w & (n - 1));
+  } else {
+    for (int w = tid; w < nrows * n; w += nth) {
+      const int r = w / n;
+      f(r, w - r * n);
+    }
+  }
+}
+#endif
 
 // ---- phase 1: pre-processing, items j = 1..H per row -------------------
 // reads x (input format) of row r, writes y (work format) of row r.
@@ -322,16 +343,16 @@ template <typename T> QGW_HD void dft7(C2<T>* v) {
 // One Stockham autosort pass of radix R over a row (Govindaraju et al.'s
 // formulation, any mix of radices): item b reads b + q H/R, k = b mod Ns,
 // multiplies by w_H^(q k H/(Ns R)) and writes (b - k) R + k + q Ns.
+// k = b mod Ns and hs = H / (Ns R) come from the caller (uniform per pass).
 template <int R, typename T>
-QGW_HD void stockham_item(const C2<T>* __restrict__ src, C2<T>* __restrict__ dst, int b, int Ns, int H,
-                          const C2<T>* __restrict__ tw) {
+QGW_HD void stockham_item_k(const C2<T>* __restrict__ src, C2<T>* __restrict__ dst, int b, int k, int Ns, int H,
+                            int hs, const C2<T>* __restrict__ tw) {
   const int stride = H / R;
   C2<T> v[R];
 #pragma unroll
   for (int q = 0; q < R; ++q) v[q] = src[pc<T>(b + q * stride)];
-  const int k = b % Ns;
   if (Ns > 1) {
-    const int step = k * (H / (Ns * R));
+    const int step = k * hs;
     if (R == 8) {
       C2<T> w[8];
 #pragma unroll
@@ -359,17 +380,48 @@ QGW_HD void stockham_item(const C2<T>* __restrict__ src, C2<T>* __restrict__ dst
   for (int q = 0; q < R; ++q) dst[pc<T>(base + q * Ns)] = v[q];
 }
 
+// the odd radices as separate functions: their registers do not weigh on
+// the power-of-two paths the kernels inline
+template <int R, typename T>
+QGW_HD_NOINLINE void stockham_item_odd(const C2<T>* __restrict__ src, C2<T>* __restrict__ dst, int b, int k, int Ns,
+                                       int H, int hs, const C2<T>* __restrict__ tw) {
+  stockham_item_k<R, T>(src, dst, b, k, Ns, H, hs, tw);
+}
 template <typename T>
-QGW_HD void stockham_dispatch(int R, const C2<T>* src, C2<T>* dst, int b, int Ns, int H, const C2<T>* tw) {
+QGW_HD void stockham_dispatch_k(int R, const C2<T>* src, C2<T>* dst, int b, int k, int Ns, int H, int hs,
+                                const C2<T>* tw) {
   switch (R) {
-    case 8: stockham_item<8, T>(src, dst, b, Ns, H, tw); break;
-    case 4: stockham_item<4, T>(src, dst, b, Ns, H, tw); break;
-    case 2: stockham_item<2, T>(src, dst, b, Ns, H, tw); break;
-    case 3: stockham_item<3, T>(src, dst, b, Ns, H, tw); break;
-    case 5: stockham_item<5, T>(src, dst, b, Ns, H, tw); break;
-    default: stockham_item<7, T>(src, dst, b, Ns, H, tw); break;
+    case 8: stockham_item_k<8, T>(src, dst, b, k, Ns, H, hs, tw); break;
+    case 4: stockham_item_k<4, T>(src, dst, b, k, Ns, H, hs, tw); break;
+    case 2: stockham_item_k<2, T>(src, dst, b, k, Ns, H, hs, tw); break;
+    case 3: stockham_item_odd<3, T>(src, dst, b, k, Ns, H, hs, tw); break;
+    case 5: stockham_item_odd<5, T>(src, dst, b, k, Ns, H, hs, tw); break;
+    default: stockham_item_odd<7, T>(src, dst, b, k, Ns, H, hs, tw); break;
   }
 }
+template <typename T>
+QGW_HD void stockham_dispatch(int R, const C2<T>* src, C2<T>* dst, int b, int Ns, int H, const C2<T>* tw) {
+  stockham_dispatch_k<T>(R, src, dst, b, b % Ns, Ns, H, H / (Ns * R), tw);
+}
+
+#ifdef __CUDACC__
+// one Stockham pass of radix R over nrows rows by the whole block
+template <typename T>
+__device__ __forceinline__ void stockham_pass_block(int R, const T* src, T* dst, int nrows, int ld, int Ns, int H,
+                                                    const C2<T>* tw) {
+  const int hs = H / (Ns * R);
+  if ((Ns & (Ns - 1)) == 0) {
+    block_items(nrows, H / R, [&](int r, int b) {
+      stockham_dispatch_k<T>(R, (const C2<T>*)(src + r * ld), (C2<T>*)(dst + r * ld), b, b & (Ns - 1), Ns, H, hs,
+                             tw);
+    });
+  } else {
+    block_items(nrows, H / R, [&](int r, int b) {
+      stockham_dispatch_k<T>(R, (const C2<T>*)(src + r * ld), (C2<T>*)(dst + r * ld), b, b % Ns, Ns, H, hs, tw);
+    });
+  }
+}
+#endif
 
 // ---- phase 3: split, items k = 0..H/2 per row --------------------------
 // reads the FFT result Z (work format) and writes the output format, with

@@ -51,37 +51,24 @@ __device__ __forceinline__ T* dst_block_generic(T* A, T* B, int nrows, int ld, c
                                                 const DstTables<T>& tb, T* tot) {
   const int tid = threadIdx.x + threadIdx.y * blockDim.x, nth = blockDim.x * blockDim.y;
   const int H = g.H;
-  for (int w = tid; w < nrows * H; w += nth) {
-    const int r = w / H, j = w - r * H + 1;
-    dst_pre_item<T>(A + r * ld, B + r * ld, j, g, tb.pre);
-  }
+  block_items(nrows, H, [&](int r, int i) { dst_pre_item<T>(A + r * ld, B + r * ld, i + 1, g, tb.pre); });
   __syncthreads();
   T* src = B;
   T* dst = A;
   int Ns = 1;
   for (int p = 0; p < g.npass; ++p) {
     const int R = g.radix[p];
-    const int nb = H / R;
-    for (int w = tid; w < nrows * nb; w += nth) {
-      const int r = w / nb, b = w - r * nb;
-      stockham_dispatch<T>(R, (const C2<T>*)(src + r * ld), (C2<T>*)(dst + r * ld), b, Ns, H, tb.tw);
-    }
+    stockham_pass_block<T>(R, src, dst, nrows, ld, Ns, H, tb.tw);
     __syncthreads();
     Ns *= R;
     T* t = src; src = dst; dst = t;
   }
   // split: items k = 0..H/2 per row
-  const int nk = H / 2 + 1;
-  for (int w = tid; w < nrows * nk; w += nth) {
-    const int r = w / nk, k = w - r * nk;
-    dst_split_item<T>((const C2<T>*)(src + r * ld), dst + r * ld, k, g, tb.spl);
-  }
+  block_items(nrows, H / 2 + 1,
+              [&](int r, int k) { dst_split_item<T>((const C2<T>*)(src + r * ld), dst + r * ld, k, g, tb.spl); });
   __syncthreads();
   const int nc = g.nchunk;
-  for (int w = tid; w < nrows * nc; w += nth) {
-    const int r = w / nc, c = w - r * nc;
-    tot[r * 32 + c] = dst_scan_chunk<T>(dst + r * ld, c, g);
-  }
+  block_items(nrows, nc, [&](int r, int c) { tot[r * 32 + c] = dst_scan_chunk<T>(dst + r * ld, c, g); });
   __syncthreads();
   const int warp = tid >> 5, lane = tid & 31, nwarp = nth >> 5;
   for (int r = warp; r < nrows; r += nwarp) {
@@ -97,10 +84,9 @@ __device__ __forceinline__ T* dst_block_generic(T* A, T* B, int nrows, int ld, c
     if (lane < nc) tot[r * 32 + lane] = ex;
   }
   __syncthreads();
-  for (int w = tid; w < nrows * nc; w += nth) {
-    const int r = w / nc, c = w - r * nc;
+  block_items(nrows, nc, [&](int r, int c) {
     if (c > 0) dst_scan_fix<T>(dst + r * ld, c, tot[r * 32 + c], g);
-  }
+  });
   __syncthreads();
   return dst;
 }
@@ -1172,7 +1158,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 3) k_rows_fwd(StepArg
   body_rows_fwd<T, COMP, PER>(a, step_mode, blockIdx.x, smem_raw, tot, cst);
 }
 template <typename T, bool COMP, bool PER>
-__global__ void __launch_bounds__(NT) k_cols(StepArgs<T> a, int step_mode) {
+__global__ void __launch_bounds__(NT, (PER && sizeof(T) == 8) ? 4 : 3) k_cols(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
   if (PER) body_cols_per<T, COMP>(a, step_mode, blockIdx.x, blockIdx.y, smem_raw);

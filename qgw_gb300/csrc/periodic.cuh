@@ -25,18 +25,13 @@ namespace qgw {
 // of row r at A + r*ld); B is the work buffer; returns the output buffer
 template <typename T>
 __device__ __forceinline__ T* cfft_block(T* A, T* B, int nrows, int ld, const DstGeom& g, const C2<T>* tw) {
-  const int tid = threadIdx.x + threadIdx.y * blockDim.x, nth = blockDim.x * blockDim.y;
   const int H = g.H;
   T* src = A;
   T* dst = B;
   int Ns = 1;
   for (int p = 0; p < g.npass; ++p) {
     const int R = g.radix[p];
-    const int nb = H / R;
-    for (int w = tid; w < nrows * nb; w += nth) {
-      const int r = w / nb, b = w - r * nb;
-      stockham_dispatch<T>(R, (const C2<T>*)(src + r * ld), (C2<T>*)(dst + r * ld), b, Ns, H, tw);
-    }
+    stockham_pass_block<T>(R, src, dst, nrows, ld, Ns, H, tw);
     __syncthreads();
     Ns *= R;
     T* t = src; src = dst; dst = t;
