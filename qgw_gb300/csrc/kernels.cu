@@ -340,8 +340,10 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
     w2 = (T)fw.w2;
     dtf = (T)st->dt;
   }
-  for (int m0 = 0; m0 < a.nl; m0 += a.G1) {
-    const int G = min(a.G1, a.nl - m0);
+  // ceil(nl / G1) groups of balanced sizes (at most G1 each)
+  const int ng = (a.nl + a.G1 - 1) / a.G1, gq = a.nl / ng, gr = a.nl - gq * ng;
+  for (int gi = 0, m0 = 0; gi < ng; m0 += gq + (gi < gr), ++gi) {
+    const int G = gq + (gi < gr);
     const bool upd = ab3 && m0 == 0;
     for (int w = tid; w < a.nl * GMAX; w += NT) {
       const int l = w / GMAX, g = w - l * GMAX;
@@ -657,8 +659,10 @@ __device__ __forceinline__ void body_rows_inv(const StepArgs<T>& a, int step_mod
   T* A = (T*)smem_raw;
   T* B = A + (size_t)(zm ? 2 * Gb : Gb) * ld;
   const int GB = group_width(Gb);
-  for (int l0 = 0; l0 < a.nl; l0 += Gb) {
-    const int G = min(Gb, a.nl - l0);
+  // ceil(nl / Gb) layer groups of balanced sizes (at most Gb each)
+  const int ng = (a.nl + Gb - 1) / Gb, gq = a.nl / ng, gr = a.nl - gq * ng;
+  for (int gi = 0, l0 = 0; gi < ng; l0 += gq + (gi < gr), ++gi) {
+    const int G = gq + (gi < gr);
     for (int w = threadIdx.x; w < a.nl * GMAX; w += NT) {
       const int m = w / GMAX, g = w - m * GMAX;
       cst[w] = g < G ? a.cm2l[(size_t)(l0 + g) * a.nl + m] : T(0);
