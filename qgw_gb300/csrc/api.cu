@@ -70,26 +70,29 @@ int upload(qgw_run* r, T** out, const std::vector<double>& host) {
 // (4-5 blocks/SM) for FP32; QGW_ROW_SMEM_KB overrides it (tuning knob).
 // Shared-memory budget of the work buffers of the forward rows kernel (K1):
 // 48 KiB (FP64) / 56 KiB (FP32), which keeps four blocks per SM, and 40 KiB
-// for FP32 rows of 2048 and more; measured at 512^2, 1024^2 and 2048^2 x 10
-// on GB300.  QGW_ROW_SMEM_KB overrides it.
-size_t row_budget(size_t elem, int M) {
+// for FP32 rows of 2048 and more or more than 10 layers; measured at 512^2,
+// 1024^2 and 2048^2 with 10, 16 and 20 layers on GB300 (1024^2 x 16 FP32:
+// 0.254 -> 0.197 ms).  QGW_ROW_SMEM_KB overrides it.
+size_t row_budget(size_t elem, int M, int nl) {
   const char* e = std::getenv("QGW_ROW_SMEM_KB");
   const long v = e ? std::atol(e) : 0;
   if (v >= 16 && v <= 220) return (size_t)v * 1024;
-  if (elem == 4 && M >= 2048) return (size_t)40 * 1024;
+  if (elem == 4 && (M >= 2048 || nl > 10)) return (size_t)40 * 1024;
   return (size_t)(elem == 8 ? 48 : 56) * 1024;
 }
 
 // Layers per block of the inverse rows kernel (K3): the measured optimum is
 // a fixed group size rather than a byte budget (each group re-reads the
-// row's spectral data, while larger groups cost occupancy): with the zeta
-// rows 3 layers, 5 for rows of 512 and less; 2 without; within 110 KiB of
-// work buffers.  QGW_INV_GROUP overrides the size.
-int inv_group(int zeta, int M) {
+// row's spectral data, while larger groups cost occupancy).  With the zeta
+// rows: 3 layers, 5 for rows of 512 and less or more than 10 layers
+// (1024^2 x 20 FP32: 0.477 -> 0.430 ms); without: 2, 4 for more than 10
+// layers on rows of 1024 and less; within 110 KiB of work buffers.  QGW_INV_GROUP overrides the size.
+int inv_group(int zeta, int M, int nl) {
   const char* e = std::getenv("QGW_INV_GROUP");
   const int v = e ? std::atoi(e) : 0;
   if (v >= 1 && v <= 16) return v;
-  return zeta ? (M <= 512 ? 5 : 3) : 2;
+  if (zeta) return (M <= 512 || nl > 10) ? 5 : 3;
+  return (nl > 10 && M <= 1024) ? 4 : 2;
 }
 
 // Modes (layers) per block of a row kernel: as many as the budget holds (each
@@ -102,6 +105,27 @@ int mode_group(int nl, int M, size_t elem, size_t budget, int rows_per_mode, int
   if (g < 1) g = 1;
   const int ngroups = (nl + g - 1) / g;
   return (nl + ngroups - 1) / ngroups;
+}
+
+// The same for a kernel bound by its projection FMAs (the FP64 forward rows
+// kernel): each group's loop runs at the compile-time width GB = the power
+// of two at or above its size, so a group of 5 costs 8 FMAs per layer and
+// point, and each group costs about 1.5 such FMAs more in fixed work (its
+// pass over the layers, its barriers).  Among the sizes the budget allows,
+// take the one of least groups x (GB + 1.5), then the fewest groups
+// (fitted to GB300 sweeps of 256^2 and 512^2 x 5, 10, 20 layers: groups of
+// 4 for 10 and 20 layers, one group for 5; 512^2 x 20: 0.579 -> 0.461 ms).
+int mode_group_fma(int nl, int M, size_t elem, size_t budget, int gmax) {
+  const int gfit = mode_group(1 << 30, M, elem, budget, 1, gmax, gmax);  // largest size that fits
+  int best = 1, best_cost = 1 << 30, best_ng = 1 << 30;
+  for (int g = 1; g <= gfit; ++g) {
+    const int ng = (nl + g - 1) / g, s = (nl + ng - 1) / ng;
+    int gb = 1;
+    while (gb < s) gb <<= 1;
+    const int cost = ng * (2 * gb + 3);
+    if (cost < best_cost || (cost == best_cost && ng < best_ng)) { best = s; best_cost = cost; best_ng = ng; }
+  }
+  return best;
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no
@@ -256,8 +280,16 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   a.topo_fac = p.f0 / dhb;
   a.has_topo = 0;
   a.has_wind = p.tau0 != 0;
-  a.G1 = mode_group(r->nl, Mx, sizeof(T), row_budget(sizeof(T), Mx), 1, 16, 16);
-  a.G3 = mode_group(r->nl, Mx, sizeof(T), 110 * 1024, 1, 16, inv_group(0, Mx));
+  {
+    // QGW_ROW_GROUP overrides the modes per forward-rows block (tuning knob)
+    const char* e = std::getenv("QGW_ROW_GROUP");
+    const int want = e ? std::atoi(e) : 0;
+    const size_t budget = row_budget(sizeof(T), Mx, r->nl);
+    if (want >= 1 && want <= 16) a.G1 = mode_group(r->nl, Mx, sizeof(T), budget, 1, 16, want);
+    else if (sizeof(T) == 8) a.G1 = mode_group_fma(r->nl, Mx, sizeof(T), budget, 16);
+    else a.G1 = mode_group(r->nl, Mx, sizeof(T), budget, 1, 16, 16);
+  }
+  a.G3 = mode_group(r->nl, Mx, sizeof(T), 110 * 1024, 1, 16, inv_group(0, Mx, r->nl));
   a.CT = 0;
   a.low_k64 = 8;
   // 16-byte column vectors: rows 16-byte aligned and a whole number of
@@ -277,7 +309,7 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
     if ((rc = dalloc(r, &a.spec2, field))) return rc;
     if ((rc = dalloc(r, &a.zeta, field))) return rc;
     // K3 transforms psi and zeta rows of each mode: two rows per mode
-    a.G3 = mode_group(r->nl, Mx, sizeof(T), 110 * 1024, 2, 8, inv_group(1, Mx));
+    a.G3 = mode_group(r->nl, Mx, sizeof(T), 110 * 1024, 2, 8, inv_group(1, Mx, r->nl));
     // symbol of the 5-point Laplacian: DST-I basis sin^2(pi k / 2(n+1));
     // periodic Fourier basis sin^2(pi k / N)
     std::vector<double> sx(r->nx, 0.0), sy(r->ny);
