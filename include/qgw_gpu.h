@@ -140,7 +140,10 @@ int qgw_topo(const qgw_params* p, double* topo);
  * analytic shelf of qgw_topo() when h_topo != 0); otherwise it is a
  * (ny+2, nx+2) reference-layout array.  The time scalars start as the
  * reference's init_timestep leaves them (src/timestep.h:328-339), or at the
- * fixed dt when p->dt > 0.  q starts at zero. */
+ * fixed dt when p->dt > 0.  q starts at zero.  Grids: NX and NY even, up to
+ * 8192, with NX/2 and NY/2 products of 2, 3, 5 and 7 (the transforms'
+ * radices); periodic grids square; 1..32 layers.  Anything else returns
+ * QGW_ERR_UNSUPPORTED. */
 int qgw_create(const qgw_params* p, const double* cl2m, const double* cm2l,
                const double* iRd2, const double* topo, int precision,
                qgw_run** out);

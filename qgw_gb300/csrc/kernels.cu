@@ -16,9 +16,9 @@
 // step's K1 (or by the flush kernel at the end of a call), which saves one
 // full pass over q, f0, f1, f2.
 //
-// Shared-memory rows use the padded layout of dst_core.h (pr/pc); every
-// work loop walks a power-of-two item count per row, so item -> (row, index)
-// is a shift and a mask.
+// Shared-memory rows use the padded layout of dst_core.h (pr/pc); work
+// loops map item -> (row, index) by a shift and a mask when the item count
+// per row is a power of two (block_items), by one division otherwise.
 #include <cuda_runtime.h>
 
 #include <algorithm>
