@@ -29,9 +29,9 @@ def forced(p, nrec=4, dt_forc=3600.0, seed=5):
     return p, frec
 
 
-@pytest.mark.parametrize("bc", [0.0, -1.0])
-def test_forcing4d_fp64_vs_port(qgwlib, oracle_mod, bc):
-    p, frec = forced(dict(C.cfg2(128, 5), bc_fac=bc))
+@pytest.mark.parametrize("bc,nx", [(0.0, 128), (-1.0, 128), (0.0, 96)])
+def test_forcing4d_fp64_vs_port(qgwlib, oracle_mod, bc, nx):
+    p, frec = forced(dict(C.cfg2(nx, 5), bc_fac=bc))
     q0 = C.noise_ic(p, 41)
     o = oracle_mod.run_port(p, q0, 50, dt_fixed=600.0, forcing_records=frec)
     psi, q, _ = gpu_run(qgwlib, p, q0, 50, 600.0, frec=frec)

@@ -24,9 +24,11 @@ def stochastic(NX, bc_fac, **kw):
     return p
 
 
-@pytest.mark.parametrize("bc", [-1.0, 0.0])
-def test_stochastic_fp64_vs_port(qgwlib, oracle_mod, bc):
-    p = stochastic(128, bc, k_f=40.0)
+@pytest.mark.parametrize("bc,nx", [(-1.0, 128), (0.0, 128), (-1.0, 96), (0.0, 120)])
+def test_stochastic_fp64_vs_port(qgwlib, oracle_mod, bc, nx):
+    """128: power of two; 96 and 120: the forcing transforms on mixed-radix
+    lengths (96 = 8*4*3 complex points along j, 48 along i; 120 = 8*3*5)."""
+    p = stochastic(nx, bc, k_f=40.0)
     q0 = np.zeros(C.halo_shape(p))
     o = oracle_mod.run_port(p, q0, 60, dt_fixed=2e-4)
     psi, q, _ = gpu_run(qgwlib, p, q0, 60, 2e-4)
