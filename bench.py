@@ -9,8 +9,9 @@ step is one model time step (the reference's timestep(), src/timestep.h:386).
 Metric: layer-gridpoint-steps/s = nl * (NX-1)^2 * steps / seconds, for the
 plain FP64 path (``value``), with the FP32-compensated path reported beside it
 (``fp32c``).  ``value`` is device-timed with the state resident in HBM;
-``e2e`` goes through the C ABI with host buffers: every step copies q in
-from pinned memory (qgw_put_q), steps, and copies q out (qgw_get).
+``e2e`` goes through the C ABI with host buffers: every step takes q in
+from pinned host memory and returns q to it (qgw_step_host: the first kernel
+reads the host array across the C2C link, q goes out as qgw_get does).
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 
@@ -320,20 +321,16 @@ def run_ours(args, rank, world, local_rank):
     qo = torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
     run64.get(q=qh, want=("q",))
     for _ in range(2):
-        run64.put_q(qh)
-        run64.step(1)
-        run64.get(q=qo, want=("q",))
+        run64.step_host(1, qh, qo)
     barrier()
     t0 = time.perf_counter()
     for _ in range(E):
-        run64.put_q(qh)
-        run64.step(1)
-        run64.get(q=qo, want=("q",))
+        run64.step_host(1, qh, qo)
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     # the host arrays cross the link whole: the reference layout with its ghost ring
     e2e = {"value": world * lgp * E / e2e_s, "unit": "lgp-steps/s", "steps": E,
            "h2d_bytes_per_step": int(qh.nbytes), "d2h_bytes_per_step": int(qo.nbytes),
-           "api": "qgw_put_q + qgw_step(1) + qgw_get(q) per step, pinned host buffers"}
+           "api": "qgw_step_host(1 step, q in and q out) per step, pinned host buffers"}
     run64.close()
 
     fp32c = None

@@ -197,6 +197,16 @@ int qgw_set_forcing_records(qgw_run* run, const double* records, int nrec);
 int qgw_step(qgw_run* run, int nsteps, double t_out, double tend,
              qgw_step_info* info);
 
+/* The reference's timestep(q) on the caller's host array, nsteps times:
+ * q_in (reference layout, or NULL) replaces q keeping the AB3 history, as
+ * qgw_put_q; q_out (or NULL) receives q after the steps, as qgw_get.  The
+ * two may be the same array.  Where the device can address q_in (pinned
+ * memory, or any host memory on a Grace host), the first kernel of the call
+ * reads it across the C2C link itself, so the transfer overlaps that
+ * kernel's arithmetic instead of preceding it. */
+int qgw_step_host(qgw_run* run, int nsteps, double t_out, double tend,
+                  const double* q_in, double* q_out, qgw_step_info* info);
+
 /* Recompute psi from the current q (invert_pv, src/elliptic.h:149). */
 int qgw_invert(qgw_run* run);
 

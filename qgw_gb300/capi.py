@@ -41,7 +41,7 @@ EXPORTS = [
     "qgw_params_default", "qgw_params_read", "qgw_eigmode", "qgw_check_timestep", "qgw_topo",
     "qgw_create", "qgw_destroy", "qgw_set_q", "qgw_set_q_device", "qgw_put_q", "qgw_get_time", "qgw_set_time",
     "qgw_set_forcing_seed", "qgw_set_forcing_records", "qgw_ensemble_set_forcing_records",
-    "qgw_step", "qgw_invert", "qgw_get", "qgw_budget", "qgw_footprint", "qgw_stream",
+    "qgw_step", "qgw_step_host", "qgw_invert", "qgw_get", "qgw_budget", "qgw_footprint", "qgw_stream",
     "qgw_kernels_per_step", "qgw_profile_kernels", "qgw_probe_fp_rates", "qgw_strerror", "qgw_abi_version",
     "qgw_invert_pv_noalloc", "qgw_nc_create", "qgw_nc_write", "qgw_nc_close", "qgw_nc_read",
     "qgw_ensemble_create", "qgw_ensemble_destroy", "qgw_ensemble_size", "qgw_ensemble_member",
@@ -86,6 +86,7 @@ def load(path: str = LIB_PATH):
     lib.qgw_get_time.argtypes = [V, P(QgwTime)]
     lib.qgw_set_time.argtypes = [V, P(QgwTime)]
     lib.qgw_step.argtypes = [V, I, ctypes.c_double, ctypes.c_double, P(QgwStepInfo)]
+    lib.qgw_step_host.argtypes = [V, I, ctypes.c_double, ctypes.c_double, D, D, P(QgwStepInfo)]
     lib.qgw_invert.argtypes = [V]
     lib.qgw_get.argtypes = [V, D, D]
     lib.qgw_budget.argtypes = [V, P(QgwBudget)]
@@ -376,6 +377,18 @@ class Run:
     def put_q(self, q: np.ndarray):
         """Replace q, keeping the AB3 history (per-step host driver)."""
         _check(self.lib.qgw_put_q(self.h, _dp(q)), "qgw_put_q")
+
+    def step_host(self, n: int, q_in: Optional[np.ndarray], q_out: Optional[np.ndarray],
+                  t_out: float = 0.0, tend: float = 0.0) -> "QgwStepInfo":
+        """qgw_step with the caller's q in and out (timestep(q) on a host
+        array); q_in / q_out in the reference layout, either may be None or
+        both the same array."""
+        info = QgwStepInfo()
+        _check(self.lib.qgw_step_host(self.h, int(n), float(t_out), float(tend),
+                                      None if q_in is None else _dp(q_in),
+                                      None if q_out is None else _dp(q_out), ctypes.byref(info)),
+               "qgw_step_host")
+        return info
 
     def set_q_device(self, ptr: int):
         _check(self.lib.qgw_set_q_device(self.h, ctypes.c_void_p(ptr)), "qgw_set_q_device")

@@ -169,6 +169,8 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   a.lstride = (long long)r->lstride;
   const bool per = p.bc_fac == -1;
   a.periodic = per ? 1 : 0;
+  a.qin = nullptr;
+  a.qout = nullptr;
   // closed basin: DST-I of length n along x and y (M = n + 1); periodic:
   // real FFT of length NX along x (a complex FFT of NX/2: M = NX) and
   // complex FFT of length NY along y (M = 2 NY)
@@ -592,11 +594,42 @@ static int reset_history(qgw_run* r) {
   return QGW_OK;
 }
 
-// q in the reference layout -> the run layout: one contiguous copy into the
-// staging buffer (or the caller's device array directly), then a kernel
+// A device-usable address of a host array, or null: pinned (registered)
+// memory through its mapped address; pageable memory itself where the GPU
+// reads host page tables (the Grace C2C link's address translation).
+// QGW_HOST_ACCESS=copy turns this off (every host array then crosses the
+// link as one copy-engine transfer through the staging buffer).
+static const void* device_view(const qgw_run* r, const void* host) {
+  static const int mode = [] {
+    const char* e = std::getenv("QGW_HOST_ACCESS");
+    return (e && !std::strcmp(e, "copy")) ? 0 : 1;
+  }();
+  if (!mode || !host) return nullptr;
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type == cudaMemoryTypeHost) return at.devicePointer;
+  if (at.type == cudaMemoryTypeUnregistered) {
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccessUsesHostPageTables, r->device) ==
+            cudaSuccess &&
+        pageable)
+      return host;
+  }
+  return nullptr;
+}
+
+// q in the reference layout -> the run layout: the unpack kernel reads the
+// caller's array where the device can address it (host arrays over the
+// C2C link), else one contiguous copy into the staging buffer first
 static int load_q(qgw_run* r, const double* q, bool device_src) {
   const double* full = q;
-  if (!device_src) {
+  const double* view = device_src ? nullptr : (const double*)device_view(r, q);
+  if (view) {
+    full = view;
+  } else if (!device_src) {
     const size_t nfull = (size_t)r->nl * (r->ny + 2) * (r->nx + 2);
     CK(cudaMemcpyAsync(r->d_full, q, sizeof(double) * nfull, cudaMemcpyHostToDevice, r->stream));
     full = r->d_full;
@@ -719,6 +752,9 @@ int qgw_step(qgw_run* r, int nsteps, double t_out, double tend, qgw_step_info* i
     for (int s = 0; s < n; ++s) {
       if (r->precision == QGW_FP64) qgw::enqueue_step_f64(r->a64, r->stream);
       else qgw::enqueue_step_f32c(r->a32, r->stream);
+      // a host q (qgw_step_host) is read by the first step only
+      r->a64.qin = nullptr;
+      r->a32.qin = nullptr;
     }
     launched += n;
     if (launched < nsteps) {
@@ -748,6 +784,43 @@ int qgw_step(qgw_run* r, int nsteps, double t_out, double tend, qgw_step_info* i
   return s.nonfinite ? QGW_ERR_NAN : QGW_OK;
 }
 
+static void fill_ghosts(const qgw_run* r, double* psi, double* q, const double* ps);
+
+// qgw_step with the caller's q going in and out (the reference's
+// timestep(q) on a host array, n times): q_in replaces q keeping the AB3
+// history (as qgw_put_q), read by the first kernel of the call straight from
+// the host array where the device can address it; q_out receives q after
+// the steps (as qgw_get).  q_in and q_out may be the same array.
+int qgw_step_host(qgw_run* r, int nsteps, double t_out, double tend, const double* q_in, double* q_out,
+                  qgw_step_info* info) {
+  if (!r) return QGW_ERR_PARAM;
+  if (!r->has_q) return QGW_ERR_STATE;
+  int rc;
+  // the direct read needs the first step to run: no t_out / tend stop
+  const bool direct = q_in && nsteps > 0 && t_out == 0 && tend == 0;
+  const double* view = direct ? (const double*)device_view(r, q_in) : nullptr;
+  if (q_in && !view && (rc = load_q(r, q_in, false))) return rc;
+  // q out: the end-of-call flush writes the interior into the caller's array
+  // where the device can address it and the ghost ring needs no psi
+  // (free-slip or periodic); otherwise as qgw_get
+  double* oview = q_out && (r->p.bc_fac == 0 || r->p.bc_fac == -1) ? (double*)device_view(r, q_out) : nullptr;
+  if (r->precision == QGW_FP64) {
+    r->a64.qin = view;
+    r->a64.qout = oview;
+  } else {
+    r->a32.qin = view;
+    r->a32.qout = oview;
+  }
+  rc = qgw_step(r, nsteps, t_out, tend, info);
+  r->a64.qin = r->a32.qin = nullptr;
+  r->a64.qout = r->a32.qout = nullptr;
+  if (rc != QGW_OK && rc != QGW_ERR_NAN) return rc;
+  int rc2 = QGW_OK;
+  if (oview) fill_ghosts(r, nullptr, q_out, nullptr);
+  else if (q_out) rc2 = qgw_get(r, nullptr, q_out);
+  return rc2 != QGW_OK ? rc2 : rc;
+}
+
 int qgw_invert(qgw_run* r) {
   if (!r) return QGW_ERR_PARAM;
   if (!r->has_q) return QGW_ERR_STATE;
@@ -757,31 +830,10 @@ int qgw_invert(qgw_run* r) {
   return QGW_OK;
 }
 
-int qgw_get(qgw_run* r, double* psi, double* q) {
-  if (!r) return QGW_ERR_PARAM;
-  if (!r->has_q) return QGW_ERR_STATE;
-  // psi is the inversion of the current q; q alone needs it only for the
-  // ghost values of a no-slip or partial-slip wall
-  if (psi || (r->p.bc_fac != 0 && r->p.bc_fac != -1)) enqueue_invert(r);
-  const size_t nfull = (size_t)r->nl * (r->ny + 2) * (r->nx + 2);
-  // one field out through the staging buffer: pack (interior), contiguous copy
-  auto fetch = [&](bool want_psi, double* host) -> int {
-    if (r->precision == QGW_FP64)
-      qgw::enqueue_pack_f64(want_psi ? r->a64.psi : r->a64.q, r->d_full, r->nx, r->ny, r->nl, r->pitch, r->stream);
-    else
-      qgw::enqueue_pack_join(want_psi ? r->a32.psi : r->a32.q, want_psi ? nullptr : r->a32.qlo, r->d_full, r->nx,
-                             r->ny, r->nl, r->pitch, r->stream);
-    CK(cudaMemcpyAsync(host, r->d_full, sizeof(double) * nfull, cudaMemcpyDeviceToHost, r->stream));
-    CK(cudaStreamSynchronize(r->stream));
-    return QGW_OK;
-  };
-  int rc;
-  if (psi && (rc = fetch(true, psi))) return rc;
-  if (q && (rc = fetch(false, q))) return rc;
-  CK(cudaGetLastError());
-  std::vector<double> psi_tmp;
-  // ghost rings as adjust_bc leaves them after invert_pv
-  // (src/elliptic.h:225-226, src/domain.h:308-348)
+// Ghost rings as adjust_bc leaves them after invert_pv (src/elliptic.h:225-226,
+// src/domain.h:308-348): periodic copies; at walls psi = 0 and
+// q = 2 bc_fac / Delta^2 * psi_adjacent (ps: psi, needed when bc_fac != 0).
+static void fill_ghosts(const qgw_run* r, double* psi, double* q, const double* ps) {
   const int nxp2 = r->nx + 2, nyp2 = r->ny + 2;
   const size_t L = (size_t)nxp2 * nyp2;
   if (r->p.bc_fac == -1) {
@@ -796,15 +848,9 @@ int qgw_get(qgw_run* r, double* psi, double* q) {
         for (int j = 0; j < nyp2; ++j) f[(size_t)j * nxp2 + nxp2 - 1] = f[(size_t)j * nxp2 + 1];
       }
     }
-    return QGW_OK;
+    return;
   }
   const double c = 2 * r->p.bc_fac / (r->Delta * r->Delta);
-  const double* ps = psi;
-  if (q && !psi && c != 0) {
-    psi_tmp.resize(L * r->nl);
-    if ((rc = fetch(true, psi_tmp.data()))) return rc;
-    ps = psi_tmp.data();
-  }
   for (int k = 0; k < r->nl; ++k) {
     double* P = psi ? psi + k * L : nullptr;
     double* Q = q ? q + k * L : nullptr;
@@ -830,6 +876,43 @@ int qgw_get(qgw_run* r, double* psi, double* q) {
       }
     }
   }
+}
+
+int qgw_get(qgw_run* r, double* psi, double* q) {
+  if (!r) return QGW_ERR_PARAM;
+  if (!r->has_q) return QGW_ERR_STATE;
+  // psi is the inversion of the current q; q alone needs it only for the
+  // ghost values of a no-slip or partial-slip wall
+  if (psi || (r->p.bc_fac != 0 && r->p.bc_fac != -1)) enqueue_invert(r);
+  const size_t nfull = (size_t)r->nl * (r->ny + 2) * (r->nx + 2);
+  // one field out through the staging buffer: pack (interior), contiguous copy
+  // (the pack kernel writes the caller's array directly where the device
+  // can address it)
+  auto fetch = [&](bool want_psi, double* host) -> int {
+    double* view = (double*)device_view(r, host);
+    double* dst = view ? view : r->d_full;
+    if (r->precision == QGW_FP64)
+      qgw::enqueue_pack_f64(want_psi ? r->a64.psi : r->a64.q, dst, r->nx, r->ny, r->nl, r->pitch, r->stream);
+    else
+      qgw::enqueue_pack_join(want_psi ? r->a32.psi : r->a32.q, want_psi ? nullptr : r->a32.qlo, dst, r->nx, r->ny,
+                             r->nl, r->pitch, r->stream);
+    if (!view) CK(cudaMemcpyAsync(host, r->d_full, sizeof(double) * nfull, cudaMemcpyDeviceToHost, r->stream));
+    CK(cudaStreamSynchronize(r->stream));
+    return QGW_OK;
+  };
+  int rc;
+  if (psi && (rc = fetch(true, psi))) return rc;
+  if (q && (rc = fetch(false, q))) return rc;
+  CK(cudaGetLastError());
+  const double c = 2 * r->p.bc_fac / (r->Delta * r->Delta);
+  std::vector<double> psi_tmp;
+  const double* ps = psi;
+  if (r->p.bc_fac != -1 && q && !psi && c != 0) {
+    psi_tmp.resize((size_t)(r->nx + 2) * (r->ny + 2) * r->nl);
+    if ((rc = fetch(true, psi_tmp.data()))) return rc;
+    ps = psi_tmp.data();
+  }
+  fill_ghosts(r, psi, q, ps);
   return QGW_OK;
 }
 

@@ -254,12 +254,56 @@ __device__ __forceinline__ int group_width(int G) { return G <= 1 ? 1 : G <= 2 ?
 // frow * sqdt after the AB3 update (src/timestep.h:415-421)
 // FK: 0 no forcing, 1 stochastic forcing only (layer 0), 2 either or both
 // -- separate instantiations, so that each loop carries only the forcing it
-// applies
+// applies; 3: no update pending, q comes from the caller's array a.qin
+// (reference layout) and is stored into the run's field on the way
 template <typename T, bool COMP, int GB, int FK>
 __device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool upd, T c0, T c1, T c2, const T* f0,
                                             const T* f1, const T* f2, int G, T* A, int ld, const T* cst,
                                             const T* frow, T sqdt, const T* r1, const T* r2, T w1, T w2,
                                             T dtf) {
+  if constexpr (FK == 3) {
+    // q from the caller's host array: four layers' loads in flight per
+    // point (the link's latency is several microseconds), then the stores
+    // into the run's field and the projection
+    const size_t hs = (size_t)(a.ny + 2) * (a.nx + 2);
+    for (int i = threadIdx.x; i < a.nx; i += NT) {
+      T acc[GB];
+#pragma unroll
+      for (int g = 0; g < GB; ++g) acc[g] = T(0);
+      const double* __restrict__ src = a.qin + (size_t)(j + 1) * (a.nx + 2) + (i + 1);
+      const size_t o0 = (size_t)j * a.pitch + i;
+      for (int l0 = 0; l0 < a.nl; l0 += 4) {
+        double x[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) x[u] = l0 + u < a.nl ? src[(size_t)(l0 + u) * hs] : 0.0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int l = l0 + u;
+          if (l >= a.nl) break;
+          const size_t o = o0 + (size_t)l * a.lstride;
+          T v;
+          if constexpr (COMP) {
+            const float hi = (float)x[u];
+            a.q[o] = (T)hi;
+            a.qlo[o] = (T)(float)(x[u] - (double)hi);
+            v = (T)hi;
+          } else {
+            v = (T)x[u];
+            a.q[o] = v;
+          }
+          T c[GB];
+          ld_coefs<GB, T>(cst + l * GMAX, c);
+#pragma unroll
+          for (int g = 0; g < GB; ++g) acc[g] = fmaT(c[g], v, acc[g]);
+        }
+      }
+      const int pi = pr<T>(i);
+#pragma unroll
+      for (int g = 0; g < GB; ++g)
+        if (g < G) A[g * ld + pi] = acc[g];
+    }
+    return;
+  }
   for (int i = threadIdx.x; i < a.nx; i += NT) {
     T acc[GB];
 #pragma unroll
@@ -350,7 +394,7 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
       cst[w] = g < G ? a.cl2m[(size_t)(m0 + g) * a.nl + l] : T(0);
     }
     __syncthreads();
-    const int fk = !upd ? 0 : r1 ? 2 : frow ? 1 : 0;
+    const int fk = (a.qin && m0 == 0) ? 3 : !upd ? 0 : r1 ? 2 : frow ? 1 : 0;
 #define QGW_PF(GBV, F) project_fwd<T, COMP, GBV, F>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt, r1, \
                                                   r2, w1, w2, dtf)
 #define QGW_PF_GB(F)                 \
@@ -362,7 +406,9 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
     default: QGW_PF(16, F); break;   \
   }
     // the compensated path has registers for one forced loop only
-    if (fk == 2 || (COMP && fk == 1)) {
+    if (fk == 3) {
+      QGW_PF_GB(3)
+    } else if (fk == 2 || (COMP && fk == 1)) {
       QGW_PF_GB(2)
     } else if (fk == 1) {
       if constexpr (!COMP) QGW_PF_GB(1)
@@ -1333,9 +1379,12 @@ __global__ void k_end_ens(EnsArgs<T> e) {
 }
 
 template <typename T, bool COMP>
+// (a.qout: also writes the final q, joined to FP64, into the caller's array
+// in the reference layout -- the interior; the host fills the ghost ring)
 __global__ void __launch_bounds__(NT) k_flush(StepArgs<T> a) {
   DevState* st = a.state;
-  if (!st->pending) return;
+  const bool pend = st->pending != 0;
+  if (!pend && !a.qout) return;
   int s0, s1, s2;
   slabs(st->step_index, s0, s1, s2);
   const double c0 = st->c0, c1 = st->c1, c2 = st->c2;
@@ -1361,19 +1410,31 @@ __global__ void __launch_bounds__(NT) k_flush(StepArgs<T> a) {
     const size_t o = row * a.pitch + i;
     // layer 0 also takes the stochastic forcing (src/timestep.h:415-421)
     const T* fo = (a.fr.on && row < (size_t)a.ny) ? a.fr.field + o : nullptr;
+    double out;
     if (COMP) {
       float hi = (float)a.q[o], lo = (float)a.qlo[o];
-      const float d = ab3_increment((float)c0, (float)c1, (float)c2, (float)f0[o], (float)f1[o], (float)f2[o]);
-      comp_add(hi, lo, d);
-      if (fo) comp_add(hi, lo, (float)*fo * (float)sqdt);
-      if (r1) comp_add(hi, lo, (float)forc4d_term<T>(r1, r2, o, w1, w2, (T)st->dt));
-      a.q[o] = (T)hi;
-      a.qlo[o] = (T)lo;
+      if (pend) {
+        const float d = ab3_increment((float)c0, (float)c1, (float)c2, (float)f0[o], (float)f1[o], (float)f2[o]);
+        comp_add(hi, lo, d);
+        if (fo) comp_add(hi, lo, (float)*fo * (float)sqdt);
+        if (r1) comp_add(hi, lo, (float)forc4d_term<T>(r1, r2, o, w1, w2, (T)st->dt));
+        a.q[o] = (T)hi;
+        a.qlo[o] = (T)lo;
+      }
+      out = (double)hi + (double)lo;
     } else {
-      T v = ab3_plain<T>(a.q[o], (T)c0, (T)c1, (T)c2, f0[o], f1[o], f2[o]);
-      if (fo) v = v + *fo * (T)sqdt;
-      if (r1) v = v + forc4d_term<T>(r1, r2, o, w1, w2, (T)st->dt);
-      a.q[o] = v;
+      T v = a.q[o];
+      if (pend) {
+        v = ab3_plain<T>(v, (T)c0, (T)c1, (T)c2, f0[o], f1[o], f2[o]);
+        if (fo) v = v + *fo * (T)sqdt;
+        if (r1) v = v + forc4d_term<T>(r1, r2, o, w1, w2, (T)st->dt);
+        a.q[o] = v;
+      }
+      out = (double)v;
+    }
+    if (a.qout) {
+      const size_t l = row / a.ny, jj = row - l * a.ny;
+      a.qout[(l * (a.ny + 2) + jj + 1) * (a.nx + 2) + i + 1] = out;
     }
   }
 }

@@ -144,6 +144,13 @@ template <typename T> struct StepArgs {
   // of NX/2), gy has M = 2 NY (complex FFT of length NY); spectral rows hold
   // X_0..X_{NX/2} as (re, im) pairs; ghost values wrap around
   int periodic;
+  // the first forward-rows pass of a call may read q straight from the
+  // caller's host array (reference layout, an address the device can use;
+  // null: q is already in the run's field)
+  const double* qin;
+  // the flush of a call may also write q to the caller's host array
+  // (reference layout interior; null: none)
+  double* qout;
 };
 
 // indices into StepArgs::fc

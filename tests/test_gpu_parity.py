@@ -133,6 +133,38 @@ def test_fp32c_vs_fp64_mixed_radix(qgwlib):
     assert rel(psi32, psi64) <= TOL32C, rel(psi32, psi64)
 
 
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("bc,pinned", [(0.0, False), (0.5, True), (-1.0, True)])
+def test_step_host_equals_put_step_get(qgwlib, prec, bc, pinned):
+    """qgw_step_host (the first kernel reading the caller's host q directly,
+    in place) gives bitwise what qgw_put_q + qgw_step + qgw_get give."""
+    p = dict(C.cfg1(64), bc_fac=bc)
+    q0, q1 = C.noise_ic(p, 71), C.noise_ic(p, 72)
+    out = []
+    for mode in ("put", "host"):
+        r = qgwlib.Run(p, prec)
+        r.set_q(q0)
+        r.fix_dt(1200.0)
+        r.step(3)  # an AB3 history that the new q keeps
+        if mode == "put":
+            r.put_q(q1)
+            r.step(2)
+            _, q = r.get(want=("q",))
+        else:
+            if pinned:
+                torch = pytest.importorskip("torch")
+                buf = torch.empty(q1.shape, dtype=torch.float64, pin_memory=True).numpy()
+            else:
+                buf = np.empty_like(q1)
+            buf[...] = q1
+            info = r.step_host(2, buf, buf)
+            assert info.steps_taken == 2
+            q = buf.copy()
+        r.close()
+        out.append(q)
+    assert np.array_equal(out[0], out[1]), np.abs(out[0] - out[1]).max()
+
+
 def test_fp64_adaptive_dt_vs_port(qgwlib, oracle_mod):
     p = dict(C.cfg1(128))
     p.pop("dt")
