@@ -4,6 +4,8 @@ Tolerances: the plain FP64 path must match the reference's CPU step to
 rel-L2 <= 1e-12 on psi and q after 100 steps (rel-L2 = ||a-b||_2/||b||_2
 over the full reference-layout arrays); the compensated FP32 path must stay
 within 1e-5 of the FP64 result after 100 steps."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -163,6 +165,26 @@ def test_step_host_equals_put_step_get(qgwlib, prec, bc, pinned):
         r.close()
         out.append(q)
     assert np.array_equal(out[0], out[1]), np.abs(out[0] - out[1]).max()
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_nonfinite_state_stops_the_call(qgwlib, prec):
+    """A NaN in q reaches psi through the inversion and the CFL maximum; the
+    call stops after that step and reports QGW_ERR_NAN (the state is the
+    caller's to inspect), instead of running on."""
+    p = C.cfg1(64)
+    q0 = C.noise_ic(p, 5)
+    q0[1, 20, 30] = np.nan
+    r = qgwlib.Run(p, prec)
+    r.set_q(q0)
+    r.fix_dt(1200.0)
+    with pytest.raises(qgwlib.QgwError) as e:
+        r.step(10)
+    assert e.value.status == -5
+    info = qgwlib.QgwStepInfo()
+    assert r.lib.qgw_step(r.h, 3, 0.0, 0.0, ctypes.byref(info)) == -5
+    assert info.steps_taken == 1 and info.stop_reason == 3 and info.nonfinite == 1
+    r.close()
 
 
 def test_fp64_adaptive_dt_vs_port(qgwlib, oracle_mod):
