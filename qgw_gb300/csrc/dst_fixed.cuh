@@ -96,6 +96,41 @@ __device__ __forceinline__ void stockham_pass_fixed(const T* src, T* dst, int nr
   }
 }
 
+// The complex FFT of H = 2^LGH points (the Stockham passes alone) on nrows
+// rows by the whole block: input in X, Y the second buffer; returns the
+// buffer that holds the output.  The same passes and arithmetic as the
+// runtime-geometry loops of dst_core.h (bit-identical results).
+template <typename T, int LGH>
+__device__ T* cfft_block_fixed(T* X, T* Y, int nrows, int ld, const C2<T>* __restrict__ twp) {
+  using S = DstShape<LGH>;
+  constexpr int H = S::H;
+  static_assert(S::NP8 <= 3, "fixed passes cover H <= 4096");
+  T* src = X;
+  T* dst = Y;
+  if constexpr (S::NP8 >= 1) {
+    stockham_pass_fixed<T, 8, 1, H>(src, dst, nrows, ld, twp);
+    __syncthreads();
+    T* t = src; src = dst; dst = t;
+  }
+  if constexpr (S::NP8 >= 2) {
+    stockham_pass_fixed<T, 8, 8, H>(src, dst, nrows, ld, twp);
+    __syncthreads();
+    T* t = src; src = dst; dst = t;
+  }
+  if constexpr (S::NP8 >= 3) {
+    stockham_pass_fixed<T, 8, 64, H>(src, dst, nrows, ld, twp);
+    __syncthreads();
+    T* t = src; src = dst; dst = t;
+  }
+  if constexpr (S::RLAST > 1) {
+    constexpr int NS = 1 << (3 * S::NP8);
+    stockham_pass_fixed<T, S::RLAST, NS, H>(src, dst, nrows, ld, twp);
+    __syncthreads();
+    T* t = src; src = dst; dst = t;
+  }
+  return src;
+}
+
 template <typename T, int LGH>
 __device__ T* dst_block_fixed(T* A, T* B, int nrows, int ld, const DstTables<T>& tb) {
   using S = DstShape<LGH>;
@@ -143,30 +178,8 @@ __device__ T* dst_block_fixed(T* A, T* B, int nrows, int ld, const DstTables<T>&
   }
   __syncthreads();
   // phase 2: Stockham passes B -> A -> B ...
-  T* src = B;
-  T* dst = A;
-  if constexpr (S::NP8 >= 1) {
-    stockham_pass_fixed<T, 8, 1, H>(src, dst, nrows, ld, tb.twp);
-    __syncthreads();
-    T* t = src; src = dst; dst = t;
-  }
-  if constexpr (S::NP8 >= 2) {
-    stockham_pass_fixed<T, 8, 8, H>(src, dst, nrows, ld, tb.twp);
-    __syncthreads();
-    T* t = src; src = dst; dst = t;
-  }
-  if constexpr (S::NP8 >= 3) {
-    stockham_pass_fixed<T, 8, 64, H>(src, dst, nrows, ld, tb.twp);
-    __syncthreads();
-    T* t = src; src = dst; dst = t;
-  }
-  static_assert(S::NP8 <= 3, "fixed DST covers H <= 2048");
-  if constexpr (S::RLAST > 1) {
-    constexpr int NS = 1 << (3 * S::NP8);
-    stockham_pass_fixed<T, S::RLAST, NS, H>(src, dst, nrows, ld, tb.twp);
-    __syncthreads();
-    T* t = src; src = dst; dst = t;
-  }
+  T* src = cfft_block_fixed<T, LGH>(B, A, nrows, ld, tb.twp);
+  T* dst = src == A ? B : A;
   // phase 3: split (dst_split_item), items k = 0..H/2-1; item 0 also does
   // k = H/2 (and R_0); thread tid handles k = tid + c * DST_NT of every row
   {

@@ -586,7 +586,7 @@ __device__ __forceinline__ void body_cols_per(const StepArgs<T>& a, int step_mod
     A1[pj] = z1;
   }
   __syncthreads();
-  T* O = cfft_block<T>(A, B, CC, ld, a.gy, a.ty.tw);
+  T* O = cfft_block<T>(A, B, CC, ld, a.gy, a.ty.tw, a.ty.twp);
   const bool zm = COMP && a.zeta_mode;
   const double iRd2 = a.iRd2[m];
   const float ird2f = COMP ? a.iRd2f[m] : 0.f;
@@ -631,7 +631,7 @@ __device__ __forceinline__ void body_cols_per(const StepArgs<T>& a, int step_mod
   }
   __syncthreads();
   T* Oth = (O == A) ? B : A;
-  T* O2 = cfft_block<T>(O, Oth, CC, ld, a.gy, a.ty.tw);
+  T* O2 = cfft_block<T>(O, Oth, CC, ld, a.gy, a.ty.tw, a.ty.twp);
   for (int jj = tid; jj < ny; jj += NT) {
     const int pj = pc<T>(jj);
     const C2<T> z0 = ((const C2<T>*)O2)[pj];
@@ -641,7 +641,7 @@ __device__ __forceinline__ void body_cols_per(const StepArgs<T>& a, int step_mod
   }
   if (zm) {
     __syncthreads();
-    T* O3 = cfft_block<T>(C, O2 == A ? B : A, CC, ld, a.gy, a.ty.tw);
+    T* O3 = cfft_block<T>(C, O2 == A ? B : A, CC, ld, a.gy, a.ty.tw, a.ty.twp);
     T* S2 = a.spec2 + (size_t)m * a.lstride;
     for (int jj = tid; jj < ny; jj += NT) {
       const int pj = pc<T>(jj);
@@ -1208,7 +1208,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 3) k_rows_fwd(StepArg
   body_rows_fwd<T, COMP, PER>(a, step_mode, blockIdx.x, smem_raw, tot, cst);
 }
 template <typename T, bool COMP, bool PER>
-__global__ void __launch_bounds__(NT, (PER && sizeof(T) == 8) ? 4 : 3) k_cols(StepArgs<T> a, int step_mode) {
+__global__ void __launch_bounds__(NT, 3) k_cols(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
   if (PER) body_cols_per<T, COMP>(a, step_mode, blockIdx.x, blockIdx.y, smem_raw);

@@ -17,14 +17,27 @@
 #pragma once
 
 #include "dst_core.h"
+#include "dst_fixed.cuh"
 #include "qgw_device.cuh"
 
 namespace qgw {
 
 // forward complex FFT of length g.H on nrows rows (complex values at pc<T>(e)
-// of row r at A + r*ld); B is the work buffer; returns the output buffer
+// of row r at A + r*ld); B is the work buffer; returns the output buffer.
+// With the pass-ordered table twp, the lengths 256, 512 and 1024 (grids of
+// 512^2 to 2048^2) run the compile-time passes of dst_fixed.cuh (the same
+// arithmetic).
 template <typename T>
-__device__ __forceinline__ T* cfft_block(T* A, T* B, int nrows, int ld, const DstGeom& g, const C2<T>* tw) {
+__device__ __forceinline__ T* cfft_block(T* A, T* B, int nrows, int ld, const DstGeom& g, const C2<T>* tw,
+                                         const C2<T>* twp = nullptr) {
+  if (twp) {
+    switch (g.H) {
+      case 256: return cfft_block_fixed<T, 8>(A, B, nrows, ld, twp);
+      case 512: return cfft_block_fixed<T, 9>(A, B, nrows, ld, twp);
+      case 1024: return cfft_block_fixed<T, 10>(A, B, nrows, ld, twp);
+      default: break;
+    }
+  }
   const int H = g.H;
   T* src = A;
   T* dst = B;
@@ -45,7 +58,7 @@ template <typename T>
 __device__ __forceinline__ T* rfft_block(T* A, T* B, int nrows, int ld, const DstGeom& g, const DstTables<T>& tb) {
   const int tid = threadIdx.x + threadIdx.y * blockDim.x, nth = blockDim.x * blockDim.y;
   const int H = g.H;
-  T* Zb = cfft_block<T>(A, B, nrows, ld, g, tb.tw);
+  T* Zb = cfft_block<T>(A, B, nrows, ld, g, tb.tw, tb.twp);
   T* Xb = (Zb == A) ? B : A;
   const int nk = H / 2 + 1;  // k = 0..H/2 pairs with H-k
   for (int w = tid; w < nrows * nk; w += nth) {
@@ -103,7 +116,7 @@ __device__ __forceinline__ T* irfft_block(T* A, T* B, int nrows, int ld, const D
     if (k != H - k && k > 0) Zc[pc<T>(H - k)] = zh;
   }
   __syncthreads();
-  return cfft_block<T>(B, A, nrows, ld, g, tb.tw);
+  return cfft_block<T>(B, A, nrows, ld, g, tb.tw, tb.twp);
 }
 
 }  // namespace qgw
