@@ -258,28 +258,39 @@ __device__ T* dst_block_fixed(T* A, T* B, int nrows, int ld, const DstTables<T>&
       }
     }
   } else {
-    // FP32: each lane loads one 16-byte vector of V reals (E = V/2 odd
-    // outputs), scans it, the lane totals are scanned by shuffles, and a
-    // running carry joins the 32 V reals of one iteration to the next:
-    //   out = (carry + exclusive lane prefix) + inclusive in-lane prefix;
-    // every access is a whole, conflict-free 16-byte vector
-    constexpr int V = 16 / (int)sizeof(T), E = V / 2, SPAN = 32 * V;
-    static_assert(M % SPAN == 0, "whole iterations (M >= 128)");
-    static_assert((2 * Pad<T>::P) % V == 0, "vectors stay inside one pad period");
+    // FP32: each lane scans NV consecutive 16-byte vectors (4 NV reals,
+    // 2 NV odd outputs) in registers, the lane totals are scanned by
+    // shuffles, and a running carry joins the 128 NV reals of one round to
+    // the next:  out = (carry + exclusive lane prefix) + in-lane prefix.
+    // A lane's vectors start 4 NV reals (plus the pads) after its
+    // neighbour's, which spreads the 8 lanes of each 128-byte wavefront
+    // over all banks (the pad layout of 16 complex floats per 128 bytes).
+    constexpr int NV = M >= 512 ? 4 : M / 128, SPAN = 128 * NV;
+    static_assert(NV >= 1 && M % SPAN == 0, "whole rounds (M >= 128)");
+    static_assert((2 * Pad<T>::P) % 4 == 0, "vectors stay inside one pad period");
     const int warp = tid >> 5, lane = tid & 31, nwarp = DST_NT >> 5;
     for (int r = warp; r < nrows; r += nwarp) {
       T* row = dst + r * ld;
       T carry = T(0);
 #pragma unroll 1
       for (int it = 0; it < M / SPAN; ++it) {
-        const int i = it * SPAN + lane * V;
-        float4 u = *reinterpret_cast<const float4*>(row + pr<T>(i));
-        T* e = reinterpret_cast<T*>(&u);
-        T s[E];
-        s[0] = e[0];
+        const int i0 = it * SPAN + lane * 4 * NV;
+        float4 u[NV];
 #pragma unroll
-        for (int q = 1; q < E; ++q) s[q] = s[q - 1] + e[2 * q];
-        T incl = s[E - 1];
+        for (int v = 0; v < NV; ++v) u[v] = *reinterpret_cast<const float4*>(row + pr<T>(i0 + 4 * v));
+        T pre[2 * NV];
+        T run = u[0].x;
+        pre[0] = run;
+        run = run + u[0].z;
+        pre[1] = run;
+#pragma unroll
+        for (int v = 1; v < NV; ++v) {
+          run = run + u[v].x;
+          pre[2 * v] = run;
+          run = run + u[v].z;
+          pre[2 * v + 1] = run;
+        }
+        T incl = run;
 #pragma unroll
         for (int of = 1; of < 32; of <<= 1) {
           const T t = __shfl_up_sync(0xffffffffu, incl, of);
@@ -289,8 +300,11 @@ __device__ T* dst_block_fixed(T* A, T* B, int nrows, int ld, const DstTables<T>&
         if (lane == 0) ex = T(0);
         const T base = carry + ex;
 #pragma unroll
-        for (int q = 0; q < E; ++q) e[2 * q] = base + s[q];
-        *reinterpret_cast<float4*>(row + pr<T>(i)) = u;
+        for (int v = 0; v < NV; ++v) {
+          u[v].x = base + pre[2 * v];
+          u[v].z = base + pre[2 * v + 1];
+          *reinterpret_cast<float4*>(row + pr<T>(i0 + 4 * v)) = u[v];
+        }
         carry = carry + __shfl_sync(0xffffffffu, incl, 31);
       }
     }
