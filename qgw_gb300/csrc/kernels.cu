@@ -302,8 +302,7 @@ __device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool up
       for (int g = 0; g < GB; ++g)
         if (g < G) A[g * ld + pi] = acc[g];
     }
-    return;
-  }
+  } else {
   for (int i = threadIdx.x; i < a.nx; i += NT) {
     T acc[GB];
 #pragma unroll
@@ -347,6 +346,7 @@ __device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool up
 #pragma unroll
     for (int g = 0; g < GB; ++g)
       if (g < G) A[g * ld + pi] = acc[g];
+  }
   }
 }
 
