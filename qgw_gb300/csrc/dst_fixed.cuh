@@ -1,15 +1,15 @@
 // dst_fixed.cuh -- the batched DST-I of dst_core.h specialised at compile
 // time for one transform length (M = 2H = 2^(LGH+1)), used by the step
-// kernels for the common lengths.  Same phases and arithmetic as the generic
-// block DST (kernels.cu); the FP32 prefix sum runs here as a warp scan (so
-// FP32 results agree with the generic DST to round-off, FP64 ones bit for
-// bit):
+// kernels for the common lengths, and its complex FFT alone (the periodic
+// transforms).  Same phases and arithmetic as the generic block DST
+// (step_device.cuh); the FP32 prefix sum runs here as a vector scan per lane
+// (so FP32 results agree with the generic DST to round-off, FP64 ones and
+// the FFT bit for bit):
 //   pre-processing -> Stockham radix-8 passes (+ one radix-4/2 pass)
 //   -> split -> prefix sum of the odd outputs.
 // With the geometry fixed, a padded shared-memory index is one base
-// computation plus immediate offsets wherever a stride is a whole number of
-// pad periods (pc(e + P m) = pc(e) + (P + W) m), and the prefix sum runs one
-// warp per row without block barriers.  The blocks have DST_NT threads and
+// computation plus compile-time offsets (StockhamItem), and the prefix sum
+// runs one warp per row without block barriers.  The blocks have DST_NT threads and
 // every phase has a power-of-two item count per row, so a thread meets the
 // same in-row items in every row: their indices, table values and twiddles
 // are computed once per transform, outside the row loop.

@@ -1,4 +1,4 @@
-// kernels.h -- host-side launchers of the step kernels (kernels.cu).
+// kernels.h -- host-side launchers of the step kernels (kernels.cu, kernels_ens.cu).
 #pragma once
 
 #include <cuda_runtime.h>

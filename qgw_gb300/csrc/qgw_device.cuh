@@ -170,7 +170,7 @@ enum FcIndex {
   FC_COUNT
 };
 
-// A batch of runs advanced by one launch per stage (see kernels.cu).
+// A batch of runs advanced by one launch per stage (see kernels_ens.cu).
 template <typename T> struct EnsArgs {
   const StepArgs<T>* members;  // device array, n entries
   const int* start_rows;       // n+1 prefix sums of per-member work items (rows, ny)
