@@ -167,6 +167,36 @@ def test_step_host_equals_put_step_get(qgwlib, prec, bc, pinned):
     assert np.array_equal(out[0], out[1]), np.abs(out[0] - out[1]).max()
 
 
+def test_step_host_staging_path(tmp_path):
+    """With QGW_HOST_ACCESS=copy every host array goes through the staging
+    copies: qgw_step_host must still give what qgw_put_q + qgw_step +
+    qgw_get give (checked in a fresh process; the mode is read once)."""
+    import os
+    import subprocess
+    import sys
+    script = tmp_path / "staging.py"
+    script.write_text(
+        "import numpy as np\n"
+        "from qgw_gb300 import capi, configs as C\n"
+        "p = C.cfg1(64)\n"
+        "q0, q1 = C.noise_ic(p, 81), C.noise_ic(p, 82)\n"
+        "out = []\n"
+        "for mode in ('put', 'host'):\n"
+        "    r = capi.Run(p, 0)\n"
+        "    r.set_q(q0); r.fix_dt(1200.0); r.step(3)\n"
+        "    if mode == 'put':\n"
+        "        r.put_q(q1); r.step(2); q = r.get(want=('q',))[1]\n"
+        "    else:\n"
+        "        q = q1.copy(); r.step_host(2, q, q)\n"
+        "    r.close(); out.append(q)\n"
+        "assert np.array_equal(out[0], out[1]), np.abs(out[0] - out[1]).max()\n"
+        "print('ok')\n")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, QGW_HOST_ACCESS="copy", PYTHONPATH=root)
+    res = subprocess.run([sys.executable, str(script)], env=env, capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0 and "ok" in res.stdout, res.stdout + res.stderr
+
+
 @pytest.mark.parametrize("prec", [0, 1])
 def test_nonfinite_state_stops_the_call(qgwlib, prec):
     """A NaN in q reaches psi through the inversion and the CFL maximum; the
