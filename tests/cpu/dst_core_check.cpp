@@ -72,3 +72,6 @@ extern "C" int dst_core_check_twp(int M) {
   if (count != (g.npass > 1 ? H - g.radix[0] : 0)) return -1;
   return bad;
 }
+
+// the transform lengths the library accepts (M even, M/2 a product of 2, 3, 5, 7)
+extern "C" int dst_core_length_ok(int M) { return transform_length_ok(M) ? 1 : 0; }

@@ -149,6 +149,19 @@ def test_device_dst_blocks_on_host(dstcore, M):
     assert np.linalg.norm(yf - ref) <= 1e-5 * np.linalg.norm(ref)
 
 
+def test_supported_transform_lengths(dstcore):
+    """Even lengths whose half factors into 2, 3, 5 and 7 run on the GPU; the
+    rest is refused (QGW_ERR_UNSUPPORTED at qgw_create)."""
+    def smooth(n):
+        for f in (2, 3, 5, 7):
+            while n % f == 0:
+                n //= f
+        return n == 1
+    for M in range(4, 4100):
+        expect = M % 2 == 0 and smooth(M // 2)
+        assert dstcore.dst_core_length_ok(M) == int(expect), M
+
+
 @pytest.mark.parametrize("M", [16, 64, 128, 256, 512, 1024, 2048, 96, 1000])
 def test_pass_ordered_twiddles(dstcore, M):
     """The Stockham passes' lane-ordered twiddle table holds w_H^(q k H/(Ns R))
