@@ -34,6 +34,21 @@ def test_library_exports_every_declared_symbol(qgwlib):
     assert lib.qgw_strerror(-6) == b"configuration not supported by the GPU kernels"
 
 
+def test_header_is_plain_c(tmp_path):
+    """The boundary header compiles as C99 and C11 without warnings (the
+    reference's driver is C) and declares every entry point with a
+    prototype a C caller can take the address of."""
+    names = declared_functions()
+    src = tmp_path / "uses_header.c"
+    src.write_text('#include "qgw_gpu.h"\n'
+                   "void* const table[] = {\n" + ",\n".join(f"  (void*){n}" for n in names) + "\n};\n"
+                   "int main(void) { return table[0] == 0; }\n")
+    for std in ("c99", "c11"):
+        subprocess.check_call(["gcc", f"-std={std}", "-Wall", "-Wextra", "-Werror", "-pedantic",
+                               "-Wno-pedantic", "-I", os.path.join(ROOT, "include"), "-c", str(src),
+                               "-o", str(tmp_path / f"u_{std}.o")])
+
+
 PARAM_TEXTS = [
     "NX = 256\nNY=128\n nl = 3\nLx = 4000e3\ndh = [350., 750., 2900.]\nN2 = [4.5e-05, 6.8e-06]\n",
     "#!sh\n# comment = 5\nNX  = 64\nNY  = 64\nnl = 3\nunknown_key = 7\nDT_max = 1e-2;\nbeta = 1.7e-11\n",
