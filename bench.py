@@ -586,11 +586,15 @@ def main():
         workers = os.cpu_count() or 1
         pool = cpu_pool(args.nx, args.nl, workers)
         v, wall = cpu_measure(pool, workers, lgp_of(p), steps=2, warmup=1)
+        # one core: one run stepping alone (the reference's serial build)
+        v1, wall1 = cpu_measure(pool, 1, lgp_of(p), steps=2, warmup=0)
         pool.close()
         pool.join()
         args._cpu = {"value": v, "unit": "lgp-steps/s", "cores": workers, "kind": "port",
                      "sample": f"{workers} concurrent full-size runs, 1 warm-up + 2 timed model steps each "
-                               f"({wall:.1f} s); oracle/qgw_port.c, the C restatement of the reference step"}
+                               f"({wall:.1f} s); oracle/qgw_port.c, the C restatement of the reference step",
+                     "one_core": {"value": v1, "unit": "lgp-steps/s", "cores": 1,
+                                  "sample": f"one full-size run alone, 2 timed model steps ({wall1:.1f} s)"}}
     if world > 1:
         import torch
         torch.distributed.init_process_group(backend="nccl", init_method="env://")
