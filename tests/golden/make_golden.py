@@ -107,6 +107,14 @@ def cases():
     p = C.cfg1(48)
     p.update(bc_fac=-1.0)
     out.append(("periodic_nx48", p, 40, 1200.0, None))
+    # many layers: 20 stretched layers with hyperviscosity (the row kernels'
+    # mode and layer groups for more than 10 layers); dh and N2 to 6 digits,
+    # since the reference reads params.in lines into 300 characters
+    # (src/extra.h:121-122) and would cut a longer list short
+    p = C.cfg2(32, 20)
+    p["dh"] = [float(f"{x:.6g}") for x in p["dh"]]
+    p["N2"] = [float(f"{x:.6g}") for x in p["N2"]]
+    out.append(("cfg2_nx32_nl20_hyper", p, 40, 600.0, None))
     return out
 
 

@@ -263,9 +263,10 @@ def test_analytic_mode_inversion_full_size(qgwlib):
         assert rel(psi, expect) <= 1e-12, (a, b, m, rel(psi, expect))
 
 
-@pytest.mark.parametrize("nx", [256, 1024])
-def test_fp32c_vs_fp64_100_steps(qgwlib, nx):
-    p = C.cfg2(nx, 10)
+@pytest.mark.parametrize("nx,nl", [(256, 10), (1024, 10), (256, 16)])
+def test_fp32c_vs_fp64_100_steps(qgwlib, nx, nl):
+    """(256, 16): the row kernels' groups for more than 10 layers."""
+    p = C.cfg2(nx, nl)
     q0 = C.noise_ic(p, 33)
     psi64, q64, _ = gpu_run(qgwlib, p, q0, 100, 600.0, precision=0)
     psi32, q32, _ = gpu_run(qgwlib, p, q0, 100, 600.0, precision=1)
