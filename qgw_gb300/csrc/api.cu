@@ -236,7 +236,7 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   a.hinv = nullptr;
   if (r->precision == QGW_FP64) {
     // 1 / (fact * norm), fact = -(sq(L[i]) + sq(K[j]) + iRd2[k]) as in
-    // invert_pv, src/elliptic.h:195-200 and the /norm of :207-211
+    // invert_pv, src/elliptic.h:122-127 and the /norm of :134-138
     // periodic: one factor per complex value k <= NX/2; the mean is removed
     // (src/elliptic.h:103-117), a zero factor elsewhere is never hit
     std::vector<double> h(field, 0.0);
@@ -411,6 +411,15 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
     if (ok && a.zeta_mode && a.nsweep >= 1) ok = encode_tile_map<T>(&a.tm[2], a.zeta, r, HH - 2);
     a.use_tma = ok ? 1 : 0;
   }
+  // QGW_TEST_FIRST_WAIT_ITERS (tests of the timeout path only) lowers the
+  // limit of the first wait for a tile's TMA bytes, down to 0 polls; the
+  // second wait keeps the full limit, so the bytes still land before the
+  // block moves on
+  a.wait_iters = qgw::kWaitIters;
+  if (const char* w = std::getenv("QGW_TEST_FIRST_WAIT_ITERS")) {
+    const long v = std::strtol(w, nullptr, 10);
+    a.wait_iters = v < 0 ? 0 : v > qgw::kWaitIters ? qgw::kWaitIters : (int)v;
+  }
   return QGW_OK;
 }
 
@@ -461,7 +470,7 @@ int qgw_create(const qgw_params* pin, const double* cl2m, const double* cm2l, co
   const bool per = p.bc_fac == -1;
   // negative bc_fac other than the periodic flag has no meaning in the reference
   if (p.bc_fac < 0 && !per) return QGW_ERR_UNSUPPORTED;
-  // periodic: the reference's r2c layout (src/elliptic.h:21,41) is only
+  // periodic: the reference's r2c layout (src/elliptic.h:26,45) is only
   // consistent for a square grid; the real FFT needs NX >= 8
   if (per && (p.NX != p.NY || p.NX < 8)) return QGW_ERR_UNSUPPORTED;
   if (p.dt_forc_period != 0) {
@@ -549,7 +558,7 @@ int qgw_create(const qgw_params* pin, const double* cl2m, const double* cm2l, co
   r->budget_blocks = 304;
   if ((rc = dalloc(r, &r->d_part, (size_t)4 * r->budget_blocks))) return fail(rc);
   if ((rc = dalloc(r, &r->d_bout, 4))) return fail(rc);
-  // initial time scalars: init_timestep (src/timestep.h:328-339), or the
+  // initial time scalars: init_timestep (src/timestep.h:56-67), or the
   // fixed dt of the optional `dt` key
   DevState s{};
   double DT, dt0;
@@ -830,7 +839,7 @@ int qgw_invert(qgw_run* r) {
   return QGW_OK;
 }
 
-// Ghost rings as adjust_bc leaves them after invert_pv (src/elliptic.h:225-226,
+// Ghost rings as adjust_bc leaves them after invert_pv (src/elliptic.h:152-153,
 // src/domain.h:308-348): periodic copies; at walls psi = 0 and
 // q = 2 bc_fac / Delta^2 * psi_adjacent (ps: psi, needed when bc_fac != 0).
 static void fill_ghosts(const qgw_run* r, double* psi, double* q, const double* ps) {

@@ -27,8 +27,13 @@
 
 namespace qgw {
 
+// try_wait polls of a bounded mbarrier wait (each poll may itself suspend the
+// thread for a hardware-defined interval): far longer than any tile load
+// takes, short enough that a lost copy ends the kernel with an error status
+constexpr int kWaitIters = 1 << 22;
+
 // Scalars that evolve on the device (the reference globals t, dt, dt0,
-// dt1 of src/qg.c:63-64 and src/timestep.h:286, plus the control flags of
+// dt1 of src/qg.c:63-64 and src/timestep.h:14, plus the control flags of
 // the device-side driver loop).
 struct DevState {
   double t, dt, dt0, dt1, DT_max;
@@ -52,7 +57,7 @@ struct DevState {
 // Stochastic thin-ring forcing (src/forcing.h:67-201): each step a new
 // field of random complex amplitudes on the ring of the NF x (NF/2+1) half
 // spectrum, transformed by a 2-D c2r of size NF x NF (NF = NX), added to
-// layer 0 as forc * sqrt(dt) after the AB3 update (src/timestep.h:415-421).
+// layer 0 as forc * sqrt(dt) after the AB3 update (src/timestep.h:143-150).
 template <typename T> struct ForcArgs {
   int on;                          // k_f != 0 and more than one ring point
   int nring;                       // ring points (i, j)
@@ -130,7 +135,7 @@ template <typename T> struct StepArgs {
   ForcArgs<T> fr;                  // stochastic forcing (fr.on = 0: none)
   // 4-D forcing (src/forcing.h:226-288): nrec records [nrec][nl][ny][pitch],
   // interpolated linearly in time with period nrec * dt_forc, added to every
-  // layer as q_forc * dt after the AB3 update (src/timestep.h:423-433)
+  // layer as q_forc * dt after the AB3 update (src/timestep.h:152-163)
   const T* frec;
   int nrec;                        // 0: no 4-D forcing
   double dt_forc;
@@ -139,6 +144,11 @@ template <typename T> struct StepArgs {
   // the element-wise asynchronous copies instead
   CUtensorMap tm[3];
   int use_tma;
+  // iterations of the first bounded wait for a tile's TMA bytes (normally
+  // kWaitIters; lowered only by tests, to make that wait run out -- the
+  // second wait, which lets the bytes land before the block moves on, always
+  // keeps kWaitIters)
+  int wait_iters;
   // doubly periodic basin (bc_fac = -1): nx = NX, ny = NY interior points,
   // pitch = NX + 2 rounded up to 4; gx has M = NX (real FFT of length NX as a complex FFT
   // of NX/2), gy has M = 2 NY (complex FFT of length NY); spectral rows hold

@@ -7,7 +7,7 @@
 // FP64 path (T = double) and the compensated FP32 path (T = float, q held
 // as hi + lo).
 //
-// One reference step (timestep, src/timestep.h:386-439) is
+// One reference step (timestep, src/timestep.h:114-167) is
 //   K1 rows   : apply the pending AB3 update of the previous step, project
 //               layers onto vertical modes, forward DST-I along x
 //   K2 columns: forward DST-I along y, Helmholtz divide, inverse DST-I
@@ -39,7 +39,7 @@ constexpr int NT = 256;          // threads per block in every step kernel
 constexpr int GMAX = 16;         // max rows of one batched DST in a block
 constexpr int NLMAX = 32;        // max layers on the GPU path
 constexpr int TX = 32, TY = 16;  // RHS tile (interior points)
-constexpr double TEPS = 1e-9;    // src/timestep.h:288
+constexpr double TEPS = 1e-9;    // src/timestep.h:16
 constexpr double HUGEV = 1e30;   // src/qg.c:43
 
 // columns per block of the column kernel (one or two 16-byte vectors per row):
@@ -119,7 +119,7 @@ __device__ __forceinline__ void slabs(int si, int& s0, int& s1, int& s2) {
   s2 = (5 - m) % 3;
 }
 
-// The AB3 update q + c0 f0 + c1 f1 + c2 f2 (src/timestep.h:410), with the
+// The AB3 update q + c0 f0 + c1 f1 + c2 f2 (src/timestep.h:138), with the
 // FMAs written out so that every kernel that applies it rounds the same way.
 template <typename T>
 __device__ __forceinline__ T ab3_plain(T q, T c0, T c1, T c2, T f0, T f1, T f2) {
@@ -179,8 +179,9 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
   return ok != 0;
 }
 // bounded wait: false when the limit ran out (the caller records an error)
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned int parity) {
-  for (int it = 0; it < (1 << 22); ++it)
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned int parity,
+                                                  int limit = kWaitIters) {
+  for (int it = 0; it < limit; ++it)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
@@ -256,7 +257,7 @@ __device__ __forceinline__ int group_width(int G) { return G <= 1 ? 1 : G <= 2 ?
 // block ever reads a q value another block may be updating.  Each thread
 // accumulates the G modes of its points in registers, layer by layer.
 // frow (optional): the stochastic forcing of row j, added to layer 0 as
-// frow * sqdt after the AB3 update (src/timestep.h:415-421)
+// frow * sqdt after the AB3 update (src/timestep.h:143-150)
 // FK: 0 no forcing, 1 stochastic forcing only (layer 0), 2 either or both
 // -- separate instantiations, so that each loop carries only the forcing it
 // applies; 3: no update pending, q comes from the caller's array a.qin
@@ -603,7 +604,7 @@ __device__ __forceinline__ void body_cols_per(const StepArgs<T>& a, int step_mod
     const int pj = pc<T>(jj);
     C2<T> X = Oc[pj];
     if (k > H || (k == 0 && jj == 0)) {
-      // padding columns; the mean is removed (src/elliptic.h:114-117)
+      // padding columns; the mean is removed (src/elliptic.h:115-118)
       X.x = T(0);
       X.y = T(0);
     } else if (!COMP) {
@@ -768,8 +769,8 @@ template <> __device__ __forceinline__ unsigned long long widen_absbits<float>(u
   return absbits((double)__uint_as_float((unsigned int)b));
 }
 
-// adjust_timestep's dt rule (src/timestep.h:341-383) and the AB3
-// coefficients (src/timestep.h:398-405), by one thread.
+// adjust_timestep's dt rule (src/timestep.h:69-111) and the AB3
+// coefficients (src/timestep.h:130-133), by one thread.
 static __device__ void scalar_update(DevState* st, double Delta, double cfl) {
   const unsigned long long bits = atomicMax(&st->maxbits, 0ULL);
   const bool bad = bits >= 0x7ff0000000000000ULL;
@@ -920,12 +921,13 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
       if (z1) tma_load_3d(L1, &tm[2], i0 - XO, j0 + 1 - R, k, bar);
     }
     // block-uniform outcome of the bounded wait
-    const bool ok = __syncthreads_and(mbar_wait_bounded(bar, *phase)) != 0;
+    const bool ok = __syncthreads_and(mbar_wait_bounded(bar, *phase, a.wait_iters)) != 0;
     if (!ok) {
       // the copies did not arrive: flag the run, give them one more bounded
-      // wait (they may still land in this block's shared memory), skip
+      // wait with the full limit (they may still land in this block's shared
+      // memory), skip
       *failed = true;
-      (void)mbar_wait_bounded(bar, *phase);
+      (void)mbar_wait_bounded(bar, *phase, kWaitIters);
       if (tid == 0) a.state->dev_error = 1;
       *phase ^= 1u;
       return 0;
@@ -1086,7 +1088,7 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
       }
     }
     fout[(size_t)gj * pitch + gi] = f;
-    // CFL (adjust_timestep, src/timestep.h:346-359): one-sided differences
+    // CFL (adjust_timestep, src/timestep.h:74-87): one-sided differences
     const T du = PS(x + 1, y) - PS(x, y);
     const T dv = PS(x, y + 1) - PS(x, y);
     const auto bu = absbits_native(du), bv = absbits_native(dv);
