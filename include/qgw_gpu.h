@@ -5,13 +5,13 @@
  * The reference program keeps its whole state in globals and advances it
  * with four C functions that the driver calls directly:
  *
- *   invert_pv(q, psi)        src/elliptic.h:149   (called at src/qg.c:167,188)
- *   timestep(q)              src/timestep.h:386   (called at src/qg.c:197)
+ *   invert_pv(q, psi)        src/elliptic.h:76    (called at src/qg.c:167,188)
+ *   timestep(q)              src/timestep.h:114   (called at src/qg.c:197)
  *   rhs(q, f)                src/dynamics.h:47    (inside timestep)
- *   adjust_timestep(psi)     src/timestep.h:341   (inside timestep)
+ *   adjust_timestep(psi)     src/timestep.h:69    (inside timestep)
  *
  * plus the host-side set-up read_params (src/extra.h:118),
- * compute_eigmode (src/eigmode.h:87) and check_timestep (src/timestep.h:290).
+ * compute_eigmode (src/eigmode.h:87) and check_timestep (src/timestep.h:18).
  * This header replaces that global-state interface with an opaque run handle.
  * A host driver that used to call the functions above calls the entry points
  * below instead; fields cross the boundary in the reference's own array
@@ -84,7 +84,7 @@ typedef struct qgw_params {
 } qgw_params;
 
 /* Time-stepping scalars of a run (the reference globals t, dt, dt0, dt1,
- * DT_max, src/qg.c:63-69 and src/timestep.h:286). */
+ * DT_max, src/qg.c:63-69 and src/timestep.h:14). */
 typedef struct qgw_time {
   double t, dt, dt0, dt1, DT_max;
 } qgw_time;
@@ -126,7 +126,7 @@ int qgw_params_read(qgw_params* p, const char* path);
 int qgw_eigmode(const qgw_params* p, double* cl2m, double* cm2l, double* iRd2);
 
 /* Maximum and initial time step: replaces check_timestep,
- * src/timestep.h:290-326, including its operator-precedence quirks. */
+ * src/timestep.h:18-54, including its operator-precedence quirks. */
 int qgw_check_timestep(const qgw_params* p, double* DT_max, double* dt);
 
 /* Topography on the reference layout (ny+2, nx+2): init_vars,
@@ -139,7 +139,7 @@ int qgw_topo(const qgw_params* p, double* topo);
  * which case qgw_eigmode() is used.  topo may be NULL (flat bottom, or the
  * analytic shelf of qgw_topo() when h_topo != 0); otherwise it is a
  * (ny+2, nx+2) reference-layout array.  The time scalars start as the
- * reference's init_timestep leaves them (src/timestep.h:328-339), or at the
+ * reference's init_timestep leaves them (src/timestep.h:56-67), or at the
  * fixed dt when p->dt > 0.  q starts at zero.  Grids: NX and NY even, up to
  * 8192, with NX/2 and NY/2 products of 2, 3, 5 and 7 (the transforms'
  * radices); periodic grids square; 1..32 layers.  Anything else returns
@@ -159,7 +159,7 @@ int qgw_set_q(qgw_run* run, const double* q);
 int qgw_set_q_device(qgw_run* run, const double* q_dev);
 
 /* Replace q but keep the AB3 history: the reference's timestep(q)
- * (src/timestep.h:386) works on the caller's q array while f0/f1/f2 stay in
+ * (src/timestep.h:114-167) works on the caller's q array while f0/f1/f2 stay in
  * globals, so a driver that owns q on the host calls qgw_put_q, qgw_step(1),
  * qgw_get(NULL, q) per step.  Requires a prior qgw_set_q. */
 int qgw_put_q(qgw_run* run, const double* q);
@@ -188,9 +188,9 @@ int qgw_set_forcing_seed(qgw_run* run, unsigned int seed);
  * to step (QGW_ERR_STATE) until its records are set. */
 int qgw_set_forcing_records(qgw_run* run, const double* records, int nrec);
 
-/* Advance up to nsteps reference time steps (timestep(), src/timestep.h:386).
+/* Advance up to nsteps reference time steps (timestep(), src/timestep.h:114-167).
  * t_out is the next output time used by the dt snapping of
- * adjust_timestep (src/timestep.h:369-381); pass 0 for none.  Mirrors the
+ * adjust_timestep (src/timestep.h:97-109); pass 0 for none.  Mirrors the
  * driver loop src/qg.c:181-199: before each step, stop if t >= tend
  * (tend <= 0: no limit) or |t - t_out| < 1e-9*dt.  Work stays on the device
  * between steps; the call returns after the last step has finished. */
@@ -207,7 +207,7 @@ int qgw_step(qgw_run* run, int nsteps, double t_out, double tend,
 int qgw_step_host(qgw_run* run, int nsteps, double t_out, double tend,
                   const double* q_in, double* q_out, qgw_step_info* info);
 
-/* Recompute psi from the current q (invert_pv, src/elliptic.h:149). */
+/* Recompute psi from the current q (invert_pv, src/elliptic.h:76-155). */
 int qgw_invert(qgw_run* run);
 
 /* Copy psi and/or q out in the reference layout (either may be NULL).  The
@@ -235,7 +235,7 @@ int qgw_kernels_per_step(qgw_run* run);
 int qgw_profile_kernels(qgw_run* run, int nsteps, float* ms4);
 
 /* PV inversion without any allocation (no counterpart in the reference,
- * whose invert_pv, src/elliptic.h:149, allocates nothing only because its
+ * whose invert_pv, src/elliptic.h:76-155, allocates nothing only because its
  * work array is a global made at start-up).  For callers that cannot
  * allocate device memory -- a host model whose memory manager owns every
  * device buffer, or a loop that must not call cudaMalloc/cudaFree, which
@@ -245,11 +245,15 @@ int qgw_profile_kernels(qgw_run* run, int nsteps, float* ms4);
  * psi with a zero ghost ring and q_dev's ghost ring is set as invert_pv sets
  * it.  cl2m, cm2l, iRd2 are host arrays (e.g. from qgw_eigmode).  Scratch
  * is one file-scope device array of 32 MiB held by every GPU that loads the
- * library: sizes beyond nl*(NX+1)*(NY+1) <= 2097152, NX, NY <= 1024 or
- * nl > 32 are rejected with QGW_ERR_UNSUPPORTED.  The first call on a device
- * looks up the array's device address (with that device current) and should
- * come before any stream capture.  Calls share the array: calls that
- * overlap on the GPU, or come from several host threads at once, race. */
+ * library.  Accepted: closed basins (bc_fac >= 0; the periodic basin is
+ * QGW_ERR_UNSUPPORTED here) on grids the run path accepts (NX, NY even, NX/2
+ * and NY/2 products of 2, 3, 5 and 7) with 4 <= NX, NY <= 1024, 1 <= nl <= 32
+ * and nl*(NX+1)*(NY+1) <= 2097152; anything else returns
+ * QGW_ERR_UNSUPPORTED.  A launch error already pending in the calling thread
+ * makes the call return QGW_ERR_CUDA without clearing it.  The first call on
+ * a device looks up the array's device address (with that device current)
+ * and should come before any stream capture.  Calls share the array: calls
+ * that overlap on the GPU, or come from several host threads at once, race. */
 int qgw_invert_pv_noalloc(const qgw_params* p, const double* cl2m, const double* cm2l,
                           const double* iRd2, double* q_dev, double* psi_dev, void* stream);
 

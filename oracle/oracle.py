@@ -31,16 +31,21 @@ from qgw_gb300.params import QgwParams, QgwTime, halo_shape, to_struct, write_pa
 
 PORT_SO = os.path.join(HERE, "_build", "libqgw_port.so")
 REF_BIN = os.path.join(HERE, "_ref", "qgw_ref")
-REF_SRC_DEFAULT = "/root/reference/src"
 
 
 def build(ref: bool = True) -> None:
-    """Compile the port (always) and the in-place reference build (when the
-    reference sources exist)."""
+    """Compile the port (always) and the in-place reference build (the
+    recipe, oracle/Makefile, builds it where the reference sources exist --
+    QGW_REF_SRC names their directory -- and skips it elsewhere)."""
     subprocess.check_call(["make", "-s", "-C", HERE, "port"])
-    src = os.environ.get("QGW_REF_SRC", REF_SRC_DEFAULT)
-    if ref and os.path.exists(os.path.join(src, "qg.c")):
-        subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF_SRC={src}"])
+    if ref:
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref"], stdout=subprocess.DEVNULL)
+
+
+def ref_source_dir() -> str:
+    """The reference source directory the recipe reads (QGW_REF_SRC, or the
+    recipe's usual location)."""
+    return subprocess.check_output(["make", "-s", "-C", HERE, "print-ref-src"], text=True).strip()
 
 
 def ref_available() -> bool:

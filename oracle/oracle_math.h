@@ -4,7 +4,7 @@
  * never by the product library).
  *
  * - DST-I (FFTW's RODFT00 definition, the transform the reference plans at
- *   src/elliptic.h:136-139):  Y_k = 2 sum_{j=0}^{n-1} X_j sin(pi (j+1)(k+1)/(n+1)).
+ *   src/elliptic.h:63-66):  Y_k = 2 sum_{j=0}^{n-1} X_j sin(pi (j+1)(k+1)/(n+1)).
  *   Two implementations: a direct O(n^2) sum with an exactly reduced sine
  *   table, and an O(n log n) one through a half-length complex FFT (used when
  *   n+1 is a power of two).

@@ -17,7 +17,7 @@
 #include <string.h>
 
 static const double PORT_PI = 3.141592653589793;  /* src/qg.c:44 */
-static const double PORT_TEPS = 1e-9;            /* src/timestep.h:288 */
+static const double PORT_TEPS = 1e-9;            /* src/timestep.h:16 */
 static const double PORT_HUGE = 1e30;            /* src/qg.c:43 */
 
 struct port_run {
@@ -179,7 +179,7 @@ static int port_eigmode(port_run* r) {
 
 /* ------------------------------------------------------------- set-up */
 
-/* check_timestep, src/timestep.h:290-326, with the unparenthesised min/max
+/* check_timestep, src/timestep.h:18-54, with the unparenthesised min/max
  * macros of src/qg.c:40-41: max(max(a,b),c) is (a<b) ? b : (a<c ? c : a)
  * and 1e-3*min(A,B) is (1e-3*A > B) ? B : A. */
 static void port_check_timestep(port_run* r) {
@@ -234,7 +234,7 @@ port_run* port_create(const qgw_params* pin, int fast_dst) {
     for (int j = 1; j < r->ny + 1; ++j) r->K[j] = PORT_PI * j / p->Lx;
     for (int i = 1; i < r->nx + 1; ++i) r->L[i] = PORT_PI * i / p->Lx;
   }
-  /* init_elliptic, src/elliptic.h:102-147: periodic rows of Nx+2 doubles
+  /* init_elliptic, src/elliptic.h:29-74: periodic rows of Nx+2 doubles
    * (the in-place r2c layout), bounded rows of Nx */
   r->norm = periodic ? (double)p->NX * p->NY : 4.0 * (r->nx + 1) * (r->ny + 1);
   r->wrk = calloc((size_t)(r->nx + 2) * r->ny, sizeof(double));
@@ -257,7 +257,7 @@ port_run* port_create(const qgw_params* pin, int fast_dst) {
 #undef SHELF
     }
   r->nu_hyper = pow(-1, p->n_hyper / 2 - 1) * fabs(p->nu_hyper);
-  /* init_timestep, src/timestep.h:328-339 */
+  /* init_timestep, src/timestep.h:56-67 */
   for (int s = 0; s < 3; ++s) r->fab[s] = calloc(n3, sizeof(double));
   port_check_timestep(r);
   r->dt0 = r->dt;
@@ -431,7 +431,7 @@ static void port_invert_periodic(port_run* r) {
   port_adjust_bc(r, q, 1);
 }
 
-/* invert_pv, src/elliptic.h:149-228 (bounded branch). */
+/* invert_pv, src/elliptic.h:76-155 (bounded branch). */
 void port_invert(port_run* r) {
   const int nl = r->nl, nx = r->nx, ny = r->ny;
   double *q = r->q, *psi = r->psi, *w = r->wrk;
@@ -530,7 +530,7 @@ static void port_rhs(port_run* r, double* f) {
 
 /* ----------------------------------------------------------- time step */
 
-/* adjust_timestep, src/timestep.h:341-383. */
+/* adjust_timestep, src/timestep.h:69-111. */
 static double port_adjust_timestep(port_run* r) {
   double dt_max = PORT_HUGE;
   const double* psi = r->psi;
@@ -564,7 +564,7 @@ static double port_adjust_timestep(port_run* r) {
   return dt;
 }
 
-/* timestep, src/timestep.h:386-439, with the stochastic and 4-D forcing
+/* timestep, src/timestep.h:114-167, with the stochastic and 4-D forcing
  * add-ons. */
 void port_timestep(port_run* r) {
   double* swap = r->fab[2];
@@ -586,12 +586,12 @@ void port_timestep(port_run* r) {
         const size_t s = IDX(r, i, j, k);
         r->q[s] = r->q[s] + c0 * f0[s] + c1 * f1[s] + c2 * f2[s];
       }
-  if (r->p.k_f != 0) { /* src/timestep.h:415-421 */
+  if (r->p.k_f != 0) { /* src/timestep.h:143-150 */
     port_calc_forc(r);
     for (int j = 1; j < r->ny + 1; ++j)
       for (int i = 1; i < r->nx + 1; ++i) r->q[IDX(r, i, j, 0)] += r->forc[IDX(r, i, j, 0)] * sqrt(dt);
   }
-  if (r->p.dt_forc_period != 0 && r->nrec > 0) { /* src/timestep.h:423-433 */
+  if (r->p.dt_forc_period != 0 && r->nrec > 0) { /* src/timestep.h:152-163 */
     /* calc_4d_forcing, src/forcing.h:259-287: linear interpolation in t
      * (the time before this step's increment) between records irec1, irec2 */
     const int n_rec = (int)floor(r->p.dt_forc_period / r->p.dt_forc);

@@ -1,6 +1,6 @@
 /*
  * fftw3.h (oracle shim) -- declares the subset of the FFTW 3 API that the
- * reference calls (src/elliptic.h:102-147,149-242, src/forcing.h:67-219), so
+ * reference calls (src/elliptic.h:29-74,76-155,157-169, src/forcing.h:67-219), so
  * that the reference compiles unchanged when FFTW is not installed.  The
  * implementation in shim.c is project code (oracle_math.c); it is test
  * infrastructure only.  Names and signatures follow FFTW's public API.

@@ -3,7 +3,7 @@
  * reference makes, so that the reference's own src/qg.c can be compiled and
  * run in place as the oracle (test infrastructure only).
  *
- * FFTW: the closed-basin 2-D RODFT00 plan (src/elliptic.h:136-139), the
+ * FFTW: the closed-basin 2-D RODFT00 plans (src/elliptic.h:63-66), the
  * periodic in-place r2c/c2r plans (src/elliptic.h:32-47) and the
  * out-of-place c2r of the stochastic forcing (src/forcing.h:124).
  * The DST uses direct sums with an exactly reduced sine table unless

@@ -1,6 +1,6 @@
 // dst_core.h -- building blocks of the batched DST-I used by the PV
 // inversion (the reference takes it from FFTW's RODFT00 plans,
-// src/elliptic.h:136-139,174,204).
+// src/elliptic.h:63-66, executed at :101 and :131).
 //
 // Definition (FFTW RODFT00, unnormalised), length n = M-1, M = 2H, H a
 // product of 2, 3, 5 and 7:

@@ -245,7 +245,7 @@ double qgw_host_nu_hyper(const qgw_params* p) {
   return std::pow(-1, p->n_hyper / 2 - 1) * std::fabs(p->nu_hyper);
 }
 
-// check_timestep, src/timestep.h:290-326.  Its min/max come from the
+// check_timestep, src/timestep.h:18-54.  Its min/max come from the
 // unparenthesised macros of src/qg.c:40-41, so
 //   max(max(a,b),c) == (a < b) ? b : ((a < c) ? c : a)
 //   1e-3*min(A,B)   == (1e-3*A > B) ? B : A

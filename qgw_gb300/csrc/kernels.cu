@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(NT) k_flush(StepArgs<T> a) {
     const size_t row = w / a.nx;
     const int i = (int)(w - row * a.nx);
     const size_t o = row * a.pitch + i;
-    // layer 0 also takes the stochastic forcing (src/timestep.h:415-421)
+    // layer 0 also takes the stochastic forcing (src/timestep.h:143-150)
     const T* fo = (a.fr.on && row < (size_t)a.ny) ? a.fr.field + o : nullptr;
     double out;
     if (COMP) {

@@ -66,7 +66,7 @@ static __device__ __align__(256) double g_noalloc_scratch[kTotal];
 namespace {
 
 // 1 / (fact * norm) with fact = -(sq(L[i]) + sq(K[j]) + iRd2[m])
-// (src/elliptic.h:195-200, :207-211), on the caller's pitched layout
+// (src/elliptic.h:122-127, normalisation :134-138), on the caller's pitched layout
 __global__ void k_noalloc_hinv(double* hinv, const double* Lsq, const double* Ksq, const double* ird, int nx,
                                int ny, int nl, int pitch, long long lstride, double norm) {
   const size_t n = (size_t)nl * ny * nx;
@@ -81,7 +81,7 @@ __global__ void k_noalloc_hinv(double* hinv, const double* Lsq, const double* Ks
 }
 
 // Ghost rings as adjust_bc leaves them at the end of invert_pv
-// (src/elliptic.h:225-226, src/domain.h:308-348): psi = 0 on the ring,
+// (src/elliptic.h:152-153, src/domain.h:308-348): psi = 0 on the ring,
 // q = 2 bc_fac / Delta^2 * psi at the adjacent interior point, corners 0.
 __global__ void k_noalloc_ghosts(double* q, double* psi, int nx, int ny, int nl, double c) {
   const int nxp2 = nx + 2, nyp2 = ny + 2;
@@ -133,20 +133,25 @@ void fill_tables(int M, double* dst) {
   qgw::fill_pass_twiddles(qgw::make_geom(M), tw, spl + 2 * (H / 2 + 1));
 }
 
-bool pow2_in(int v) { return v >= 4 && v <= kMMax && (v & (v - 1)) == 0; }
+// a grid size of a closed basin the transforms take (the run path's rule:
+// NX even, NX/2 a product of 2, 3, 5 and 7), up to the scratch tables' limit
+bool length_ok(int v) { return v >= 4 && v <= kMMax && qgw::transform_length_ok(v); }
 
 }  // namespace
 
 extern "C" int qgw_invert_pv_noalloc(const qgw_params* p, const double* cl2m, const double* cm2l,
                                      const double* iRd2, double* q_dev, double* psi_dev, void* stream) {
   if (!p || !cl2m || !cm2l || !iRd2 || !q_dev || !psi_dev) return QGW_ERR_PARAM;
-  if (p->bc_fac < 0) return QGW_ERR_UNSUPPORTED;
-  if (!pow2_in(p->NX) || !pow2_in(p->NY)) return QGW_ERR_UNSUPPORTED;
+  if (p->bc_fac < 0) return QGW_ERR_UNSUPPORTED;  // closed basins only
+  if (!length_ok(p->NX) || !length_ok(p->NY)) return QGW_ERR_UNSUPPORTED;
   if (p->nl < 1 || p->nl > kNlMax) return QGW_ERR_UNSUPPORTED;
   const int nx = p->NX - 1, ny = p->NY - 1, nl = p->nl;
   const int pitch = nx + 2;
   const long long lstride = (long long)(ny + 2) * (nx + 2);
   if ((size_t)nl * (size_t)lstride > kFieldMax) return QGW_ERR_UNSUPPORTED;
+  // A launch error the caller left pending could not be told apart from one
+  // of the launches below: refuse, and leave it for the caller to read.
+  if (cudaPeekAtLastError() != cudaSuccess) return QGW_ERR_CUDA;
   cudaStream_t s = (cudaStream_t)stream;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kDevMax) return QGW_ERR_CUDA;
@@ -179,6 +184,8 @@ extern "C" int qgw_invert_pv_noalloc(const qgw_params* p, const double* cl2m, co
   const bool same = h_key_valid[dev] && std::memcmp(h_key[dev], key, sizeof(double) * klen) == 0;
   const double norm = 4.0 * (nx + 1) * (ny + 1);
   if (!same) {
+    // the scratch no longer holds a complete set-up until this one is in
+    h_key_valid[dev] = false;
     // small tables: DST (x, y), modes, wavenumbers
     std::memset(h_tab, 0, sizeof(h_tab));
     fill_tables(nx + 1, h_tab + (oTx - oTx));
@@ -192,6 +199,8 @@ extern "C" int qgw_invert_pv_noalloc(const qgw_params* p, const double* cl2m, co
       return QGW_ERR_CUDA;
     k_noalloc_hinv<<<304, 256, 0, s>>>(base + oHinv + pitch + 1, base + oLsq, base + oKsq, base + oIrd, nx, ny, nl,
                                        pitch, lstride, norm);
+    // the set-up is marked held only once its divisor launch was accepted
+    if (cudaGetLastError() != cudaSuccess) return QGW_ERR_CUDA;
     std::memcpy(h_key[dev], key, sizeof(double) * klen);
     h_key_valid[dev] = true;
   }

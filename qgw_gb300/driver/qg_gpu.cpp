@@ -25,7 +25,7 @@
 
 namespace {
 
-const double kTeps = 1e-9;  // src/timestep.h:288
+const double kTeps = 1e-9;  // src/timestep.h:16
 
 bool file_exists(const char* p) {
   struct stat st;

@@ -26,7 +26,8 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import oracle as O  # noqa: E402
 from qgw_gb300 import configs as C  # noqa: E402
 
-REF_TEST = os.environ.get("QGW_REF_TEST", "/root/reference/test")
+# the reference's test/ directory beside the src/ that the oracle recipe reads
+REF_TEST = os.environ.get("QGW_REF_TEST") or os.path.join(os.path.dirname(O.ref_source_dir()), "test")
 
 
 def parse_params_in(path):

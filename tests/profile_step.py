@@ -1,6 +1,7 @@
-"""Run a few time steps of one configuration, for profiler captures.
+"""Run a few time steps of one configuration, for profiler captures (the
+commands of the profiles/ summaries run this file).
 
-    python -m qgw_gb300.profile_step --nx 1024 --nl 10 --precision 0 --warmup 2 --steps 3
+    python tests/profile_step.py --nx 1024 --nl 10 --precision 0 --warmup 2 --steps 3
 
 The warm-up steps and the captured steps are separate qgw_step calls, so a
 profiler can skip the warm-up launches by count: each call launches one
@@ -8,11 +9,14 @@ begin kernel, 4 kernels per step (7 with stochastic forcing), and a flush
 pair (2 kernels).
 """
 import argparse
+import os
+import sys
 import time
 
 import numpy as np
 
-from . import build, capi, configs
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+from qgw_gb300 import build, capi, configs  # noqa: E402
 
 
 def main():

@@ -1,6 +1,6 @@
 """4-D forcing on the GPU (dt_forc_period != 0, src/forcing.h:226-288):
 records of q_forcing_3d interpolated linearly in time, added to every layer
-as q_forc * dt after the AB3 update (src/timestep.h:423-433).  The
+as q_forc * dt after the AB3 update (src/timestep.h:152-163).  The
 reference's own golden runs (it reads input_vars.nc itself through the
 oracle's netCDF reader) are covered by
 test_gpu_parity.test_fp64_matches_reference_golden (forcing4d_* cases);

@@ -1,5 +1,5 @@
 """Stochastic thin-ring forcing on the GPU (k_f != 0, src/forcing.h:67-201,
-added after the AB3 update as forc * sqrt(dt), src/timestep.h:415-421).
+added after the AB3 update as forc * sqrt(dt), src/timestep.h:143-150).
 
 The noise is the C library's rand() sequence restated on the device, so
 trajectories can be compared with the oracle (the reference's golden
