@@ -182,16 +182,18 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   for (int dim = 0; dim < 2; ++dim) {
     const int M = dim == 0 ? Mx : My;
     qgw::DstTablesHost th = qgw::build_dst_tables(M);
-    T *tw, *pre, *spl, *twp;
+    T *tw, *pre, *spl, *twp, *sj;
     if ((rc = upload<T>(r, &tw, th.tw))) return rc;
     if ((rc = upload<T>(r, &pre, th.pre))) return rc;
     if ((rc = upload<T>(r, &spl, th.spl))) return rc;
     if ((rc = upload<T>(r, &twp, th.twp))) return rc;
+    if ((rc = upload<T>(r, &sj, th.sj))) return rc;
     qgw::DstTables<T>& t = dim == 0 ? a.tx : a.ty;
     t.tw = (const qgw::C2<T>*)tw;
     t.pre = (const qgw::C2<T>*)pre;
     t.spl = (const qgw::C2<T>*)spl;
     t.twp = (const qgw::C2<T>*)twp;
+    t.sj = sj;
   }
   T *cl, *cm;
   if ((rc = upload<T>(r, &cl, r->cl2m))) return rc;
@@ -301,13 +303,25 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   // compensated path: psi's FP32 round-off is white in wavenumber while psi
   // itself is dominated by the largest scales, so Laplacians of psi taken
   // by stencils lose ~(k_max/k_min)^2 of relative accuracy at grid scale.
-  // The discrete Laplacian zeta is therefore formed spectrally (exact
-  // symbol) and feeds the hyperviscosity chain and the bottom drag.
+  // The Laplacians are therefore formed spectrally with the exact symbol of
+  // the 5-point stencil.  Where every sweep of calc_diff (src/dynamics.h:13-44)
+  // sees zero ghosts (free-slip walls: adjust_bc sets lap_n_diff's ghosts to
+  // 2 bc_fac/Delta^2 psi = 0) or wrapped ones (periodic), the whole chain
+  // L^nsweep psi is diagonal in the transform basis and is formed there
+  // (zeta_mode 2) when there is no bottom drag; otherwise the spectral
+  // zeta = L psi starts the chain and feeds the bottom drag (zeta_mode 1):
+  // the drag's Laplacian taken by the stencil of an FP32 psi raised the
+  // error against FP64 at 1024^2 x 10 from 8.6e-7 to 5.5e-6 (q, 100 steps),
+  // while a third spectral field for it would cost the column kernel one
+  // more inverse transform per column than the tile's sweeps cost.
+  // QGW_FP32C_DISSIPATION=zeta keeps zeta_mode 1 everywhere (comparisons).
   a.zeta_mode = 0;
   a.spec2 = nullptr;
   a.zeta = nullptr;
+  const char* dmode = std::getenv("QGW_FP32C_DISSIPATION");
+  const bool chain_diag = (p.bc_fac == 0 || per) && !a.has_drag && !(dmode && !std::strcmp(dmode, "zeta"));
   if (r->precision == QGW_FP32C && (a.nsweep > 0 || a.has_drag)) {
-    a.zeta_mode = 1;
+    a.zeta_mode = (chain_diag && a.nsweep > 0) ? 2 : 1;
     if ((rc = dalloc(r, &a.spec2, field))) return rc;
     if ((rc = dalloc(r, &a.zeta, field))) return rc;
     // K3 transforms psi and zeta rows of each mode: two rows per mode
@@ -393,22 +407,28 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   a.fc[qgw::FC_TOPOC] = (float)(-(a.inv12d2 * a.topo_fac));
   for (int g = 1; g <= 4; ++g) a.fc[qgw::FC_GH1 + g - 1] = (float)a.gh[g];
   a.fc[qgw::FC_NORM] = (float)r->norm;
+  a.fc[qgw::FC_NUHS] = (float)nuh;
   a.fc[qgw::FC_LX2] = (float)a.lx2;
   a.fc[qgw::FC_LY2] = (float)a.ly2;
   float* fi;
   if ((rc = upload<float>(r, &fi, r->iRd2))) return rc;
   a.iRd2f = fi;
   // TMA tensor maps of the RHS kernel's interior tiles (psi with halo R, q
-  // with halo 1, zeta over the first sweep's region); element-wise
-  // asynchronous copies when the driver cannot encode them, or when
-  // QGW_RHS_TILE_LOADS=copies asks for that path
+  // with halo 1, in zeta mode 1 zeta over the first sweep's region; zeta
+  // mode 2 reads its field point by point); element-wise asynchronous copies
+  // when the driver cannot encode them, or when QGW_RHS_TILE_LOADS=copies
+  // asks for that path
   std::memset(a.tm, 0, sizeof(a.tm));
   a.use_tma = 0;
+  a.rhs_grid = 0;
   const char* loads = std::getenv("QGW_RHS_TILE_LOADS");
   if (tmap_encoder() && !(loads && !std::strcmp(loads, "copies"))) {
-    const int R = a.nsweep > 0 ? a.nsweep : 1, HH = qgw::rhs_tile_y() + 2 * R;
+    int R;
+    if constexpr (sizeof(T) == 8) R = qgw::rhs_halo_of_f64(a);
+    else R = qgw::rhs_halo_of_f32c(a);
+    const int HH = qgw::rhs_tile_y() + 2 * R;
     bool ok = encode_tile_map<T>(&a.tm[0], a.psi, r, HH) && encode_tile_map<T>(&a.tm[1], a.q, r, qgw::rhs_tile_y() + 2);
-    if (ok && a.zeta_mode && a.nsweep >= 1) ok = encode_tile_map<T>(&a.tm[2], a.zeta, r, HH - 2);
+    if (ok && a.zeta_mode == 1 && a.nsweep >= 1) ok = encode_tile_map<T>(&a.tm[2], a.zeta, r, HH - 2);
     a.use_tma = ok ? 1 : 0;
   }
   // QGW_TEST_FIRST_WAIT_ITERS (tests of the timeout path only) lowers the
@@ -569,6 +589,9 @@ int qgw_create(const qgw_params* pin, const double* cl2m, const double* cm2l, co
     return fail(QGW_ERR_CUDA);
   cudaError_t e = precision == QGW_FP64 ? qgw::prepare_f64(r->a64) : qgw::prepare_f32c(r->a32);
   if (e != cudaSuccess) return fail(cuda_fail(e));
+  // persistent grid of the RHS kernel (after the shared-memory limits are set)
+  if (precision == QGW_FP64) r->a64.rhs_grid = qgw::rhs_grid_f64(r->a64);
+  else r->a32.rhs_grid = qgw::rhs_grid_f32c(r->a32);
   if (cudaStreamSynchronize(r->stream) != cudaSuccess) return fail(QGW_ERR_CUDA);
   *out = r;
   return QGW_OK;

@@ -20,10 +20,11 @@
 // are stored contiguously: row r of a buffer starts at r * ld reals.
 //
 // Buffer formats (reals, every access through the padded index pr/pc):
-//   input   x_j at index j-1 (j = 1..M-1); index M-1 is padding
-//   work    H complex values = M reals
-//   output  Y_k at index k-1 (k = 1..M-1)  -- same as the input format,
-//           so a DST output can feed the next DST directly.
+//   input   x_j at index j (j = 1..M-1); index 0 is not read
+//   work    H complex values = M reals (y_j at index j)
+//   output  Y_k at index k (k = 1..M-1), index 0 = 0 -- the input format,
+//           so a DST output can feed the next DST directly; the split
+//           writes (Y_{2k}, 2 R_k) as one complex pair at complex index k.
 #pragma once
 
 #include <stdint.h>
@@ -143,11 +144,13 @@ inline void fill_pass_twiddles(const DstGeom& g, const double* tw, double* twp) 
 //   twp    = tw reordered per Stockham pass (fill_pass_twiddles)
 //   pre[j] = (s_j + 1/2, s_j - 1/2), s_j = sin(pi j/M), j <= H
 //   spl[k] = (cos, sin)(2 pi k / M),             k <= H/2
+//   sj[j]  = s_j,                                j <= H
 template <typename T> struct DstTables {
   const C2<T>* tw;
   const C2<T>* pre;
   const C2<T>* spl;
   const C2<T>* twp;
+  const T* sj;  // s_j = sin(pi j/M), j <= H (the merged pre-processing pass)
 };
 
 // Work-item loop of a block over nrows rows of n items each: f(r, i) for
@@ -174,8 +177,8 @@ __device__ __forceinline__ void block_items(int nrows, int n, F f) {
 template <typename T>
 QGW_HD void dst_pre_item(const T* __restrict__ x, T* __restrict__ y, int j, const DstGeom& g,
                          const C2<T>* __restrict__ pre) {
-  const T a = x[pr<T>(j - 1)];
-  const T b = x[pr<T>(g.M - j - 1)];
+  const T a = x[pr<T>(j)];
+  const T b = x[pr<T>(g.M - j)];
   const C2<T> w = pre[j];
   y[pr<T>(j)] = fmaT(w.x, a, w.y * b);
   y[pr<T>(g.M - j)] = fmaT(w.y, a, w.x * b);
@@ -425,14 +428,19 @@ __device__ __forceinline__ void stockham_pass_block(int R, const T* src, T* dst,
 
 // ---- phase 3: split, items k = 0..H/2 per row --------------------------
 // reads the FFT result Z (work format) and writes the output format, with
-// the odd outputs still as increments (2R_k; R_0 at index 0).
+// the odd outputs still as increments (2R_k at index 2k+1; R_0 at index 1),
+// each (Y_{2k}, 2R_k) pair as one complex value at complex index k.
 template <typename T>
 QGW_HD void dst_split_item(const C2<T>* __restrict__ Z, T* __restrict__ out, int k, const DstGeom& g,
                            const C2<T>* __restrict__ spl) {
   const int H = g.H;
+  C2<T>* o = (C2<T>*)out;
   if (k == 0) {
     const C2<T> a = Z[0];
-    out[0] = a.x + a.y;  // R_0
+    C2<T> z0;
+    z0.x = T(0);       // index 0 (no output)
+    z0.y = a.x + a.y;  // R_0
+    o[0] = z0;
     return;
   }
   const C2<T> A = Z[pc<T>(k)];
@@ -442,25 +450,29 @@ QGW_HD void dst_split_item(const C2<T>* __restrict__ Z, T* __restrict__ out, int
   const T sr = A.x + br, si = A.y + bi, dr = A.x - br, di = A.y - bi;
   const T P = fmaT(cs.x, di, -(cs.y * dr));
   const T Q = fmaT(cs.x, dr, cs.y * di);
-  out[pr<T>(2 * k)] = sr + P;          // 2 R_k
-  out[pr<T>(2 * k - 1)] = Q - si;      // Y_{2k} = -2 I_k
+  C2<T> lo;
+  lo.x = Q - si;  // Y_{2k} = -2 I_k
+  lo.y = sr + P;  // 2 R_k
+  o[pc<T>(k)] = lo;
   if (2 * k != H) {
-    out[pr<T>(2 * (H - k))] = sr - P;      // 2 R_{H-k}
-    out[pr<T>(2 * (H - k) - 1)] = Q + si;  // Y_{2(H-k)}
+    C2<T> hi;
+    hi.x = Q + si;  // Y_{2(H-k)}
+    hi.y = sr - P;  // 2 R_{H-k}
+    o[pc<T>(H - k)] = hi;
   }
 }
 
-// ---- phase 4: prefix sum of the odd outputs (indices 0, 2, 4, ...) ------
+// ---- phase 4: prefix sum of the odd outputs (indices 1, 3, 5, ...) ------
 // 4a: items c = 0..nchunk-1: inclusive scan inside chunk c, returns total
 template <typename T>
 QGW_HD T dst_scan_chunk(T* out, int c, const DstGeom& g) {
   T acc = T(0);
   const int k0 = c * g.chunk;
   const int n = g.H - k0 < g.chunk ? g.H - k0 : g.chunk;  // the last chunk may be short
-  acc = out[pr<T>(2 * k0)];
+  acc = out[pr<T>(2 * k0 + 1)];
   for (int t = 1; t < n; ++t) {
-    acc = acc + out[pr<T>(2 * (k0 + t))];
-    out[pr<T>(2 * (k0 + t))] = acc;
+    acc = acc + out[pr<T>(2 * (k0 + t) + 1)];
+    out[pr<T>(2 * (k0 + t) + 1)] = acc;
   }
   return acc;
 }
@@ -469,7 +481,7 @@ template <typename T>
 QGW_HD void dst_scan_fix(T* out, int c, T prefix, const DstGeom& g) {
   const int k0 = c * g.chunk;
   const int n = g.H - k0 < g.chunk ? g.H - k0 : g.chunk;
-  for (int t = 0; t < n; ++t) out[pr<T>(2 * (k0 + t))] += prefix;
+  for (int t = 0; t < n; ++t) out[pr<T>(2 * (k0 + t) + 1)] += prefix;
 }
 
 }  // namespace qgw

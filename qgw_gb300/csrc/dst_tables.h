@@ -23,6 +23,7 @@ inline double cospi_frac(long m, long N) { return sinpi_frac(2 * m + N, 2 * N); 
 
 struct DstTablesHost {
   std::vector<double> tw, pre, spl, twp;  // interleaved (x, y) pairs
+  std::vector<double> sj;                 // sin(pi j / M), j = 0..H
 };
 
 // tw: H entries, twp: H - R0 entries, pre: H+1 entries, spl: H/2+1 entries
@@ -39,10 +40,12 @@ inline DstTablesHost build_dst_tables(int M) {
   t.twp.assign(2 * (size_t)(g.npass ? H - g.radix[0] : 0) + 2, 0.0);
   fill_pass_twiddles(g, t.tw.data(), t.twp.data());
   t.pre.resize(2 * (size_t)(H + 1));
+  t.sj.resize((size_t)H + 1);
   for (int j = 0; j <= H; ++j) {
     const double s = sinpi_frac(j, M);
     t.pre[2 * j] = s + 0.5;
     t.pre[2 * j + 1] = s - 0.5;
+    t.sj[j] = s;
   }
   t.spl.resize(2 * (size_t)(H / 2 + 1));
   for (int k = 0; k <= H / 2; ++k) {

@@ -27,17 +27,23 @@ __global__ void __launch_bounds__(NT, 3) k_rows_inv(StepArgs<T> a, int step_mode
   __shared__ __align__(16) T cst[NLMAX * GMAX];
   body_rows_inv<T, COMP, PER>(a, step_mode, blockIdx.x, smem_raw, tot, cst);
 }
+// The RHS of a step: a persistent grid (a.rhs_grid blocks) over the
+// ntx x nty x nl tiles (body_rhs_tiles); the FP64 path launches one block
+// per tile (its tiles keep the FP64 pipe busy, and blocks that each load
+// one tile overlap one another's loads without a second buffer).
 template <typename T, bool COMP, int R>
-__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 4) k_rhs(const __grid_constant__ StepArgs<T> a) {
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 4) k_rhs(const __grid_constant__ StepArgs<T> a, int ntx,
+                                                                    int nty) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  __shared__ unsigned long long bar;
+  __shared__ unsigned long long bar[2];
   // TMA destinations are 128-byte aligned (the launch adds 128 bytes)
   unsigned char* base = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
-  if (threadIdx.x == 0 && threadIdx.y == 0) mbar_init(&bar);
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    mbar_init(&bar[0]);
+    mbar_init(&bar[1]);
+  }
   __syncthreads();
-  unsigned int phase = 0;
-  body_rhs<T, COMP, R>(a, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x * gridDim.y * gridDim.z, base,
-                       a.use_tma ? &a.tm[0] : nullptr, &bar, &phase);
+  body_rhs_tiles<T, COMP, R, rhs_nbuf<T>()>(a, ntx, nty, base, a.use_tma ? &a.tm[0] : nullptr, bar);
 }
 
 // ------------------------------------------------------- small kernels
@@ -316,7 +322,7 @@ static cudaError_t set_attrs(const StepArgs<T>& a) {
   const size_t static_tot = sizeof(T) * (GMAX * 32 + NLMAX * GMAX) + 64;
   if (smem_rows<T, COMP>(a) + static_tot > (size_t)optin || smem_cols<T, COMP>(a) + static_tot > (size_t)optin ||
       smem_rows_inv<T, COMP>(a) + static_tot > (size_t)optin || rhs_halo(a) > RHS_RMAX ||
-      smem_rhs<T>(a) + 1024 > (size_t)optin)
+      smem_rhs<T>(a) + 1024 > (size_t)optin || smem_rhs_tiles<T>(a) + 1024 > (size_t)optin)
     return cudaErrorInvalidValue;
   const int lim = optin - (int)static_tot;
   if ((e = cudaFuncSetAttribute(k_rows_fwd<T, COMP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
@@ -353,16 +359,40 @@ static void launch_k3(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
   if (a.periodic) k_rows_inv<T, COMP, true><<<dim3(a.ny), NT, smem_rows_inv<T, COMP>(a), s>>>(a, step_mode);
   else k_rows_inv<T, COMP, false><<<dim3(a.ny), NT, smem_rows_inv<T, COMP>(a), s>>>(a, step_mode);
 }
+// tiles of the RHS kernel along x and y
+template <typename T> static int rhs_ntx(const StepArgs<T>& a) { return (a.nx + TX - 1) / TX; }
+template <typename T> static int rhs_nty(const StepArgs<T>& a) { return (a.ny + TY - 1) / TY; }
+
 template <typename T, bool COMP>
 static void launch_rhs(const StepArgs<T>& a, cudaStream_t s) {
-  const dim3 grid((a.nx + TX - 1) / TX, (a.ny + TY - 1) / TY, a.nl), blk(32, 8);
-  const size_t sm = smem_rhs(a);
+  const int ntx = rhs_ntx(a), nty = rhs_nty(a), ntiles = ntx * nty * a.nl;
+  const int grid = (a.rhs_grid > 0 && a.rhs_grid < ntiles) ? a.rhs_grid : ntiles;
+  const dim3 blk(32, 8);
+  const size_t sm = smem_rhs_tiles(a);
   switch (rhs_halo(a)) {
-    case 1: k_rhs<T, COMP, 1><<<grid, blk, sm, s>>>(a); break;
-    case 2: k_rhs<T, COMP, 2><<<grid, blk, sm, s>>>(a); break;
-    case 3: k_rhs<T, COMP, 3><<<grid, blk, sm, s>>>(a); break;
-    default: k_rhs<T, COMP, 4><<<grid, blk, sm, s>>>(a); break;
+    case 1: k_rhs<T, COMP, 1><<<grid, blk, sm, s>>>(a, ntx, nty); break;
+    case 2: k_rhs<T, COMP, 2><<<grid, blk, sm, s>>>(a, ntx, nty); break;
+    case 3: k_rhs<T, COMP, 3><<<grid, blk, sm, s>>>(a, ntx, nty); break;
+    default: k_rhs<T, COMP, 4><<<grid, blk, sm, s>>>(a, ntx, nty); break;
   }
+}
+
+// Persistent grid of the RHS kernel: as many blocks as stay resident on the
+// device at once (the occupancy of the run's halo and shared memory).
+template <typename T, bool COMP>
+static int rhs_grid(const StepArgs<T>& a) {
+  int dev = 0, sms = 0, per = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  const size_t sm = smem_rhs_tiles(a);
+  cudaError_t e;
+  switch (rhs_halo(a)) {
+    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rhs<T, COMP, 1>, NT, sm); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rhs<T, COMP, 2>, NT, sm); break;
+    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rhs<T, COMP, 3>, NT, sm); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rhs<T, COMP, 4>, NT, sm); break;
+  }
+  return (e == cudaSuccess && per > 0) ? per * sms : 0;
 }
 
 template <typename T, bool COMP>
@@ -392,6 +422,8 @@ static void launch_one(const StepArgs<T>& a, int which, cudaStream_t s) {
 // ---- entry points used by api.cu (see kernels.h)
 cudaError_t prepare_f64(const StepArgs<double>& a) { return set_attrs<double, false>(a); }
 cudaError_t prepare_f32c(const StepArgs<float>& a) { return set_attrs<float, true>(a); }
+int rhs_grid_f64(const StepArgs<double>&) { return 0; }  // one block per tile
+int rhs_grid_f32c(const StepArgs<float>& a) { return rhs_grid<float, true>(a); }
 
 void enqueue_begin(DevState* st, double t_out, double tend, cudaStream_t s) { k_begin<<<1, 1, 0, s>>>(st, t_out, tend); }
 
@@ -455,9 +487,9 @@ int rhs_tile_y() { return TY; }
 
 size_t smem_bytes_rows_f64(const StepArgs<double>& a) { return smem_rows<double, false>(a); }
 size_t smem_bytes_cols_f64(const StepArgs<double>& a) { return smem_cols<double, false>(a); }
-size_t smem_bytes_rhs_f64(const StepArgs<double>& a) { return smem_rhs<double>(a); }
+size_t smem_bytes_rhs_f64(const StepArgs<double>& a) { return smem_rhs_tiles<double>(a); }
 size_t smem_bytes_rows_f32c(const StepArgs<float>& a) { return smem_rows<float, true>(a); }
 size_t smem_bytes_cols_f32c(const StepArgs<float>& a) { return smem_cols<float, true>(a); }
-size_t smem_bytes_rhs_f32c(const StepArgs<float>& a) { return smem_rhs<float>(a); }
+size_t smem_bytes_rhs_f32c(const StepArgs<float>& a) { return smem_rhs_tiles<float>(a); }
 
 }  // namespace qgw

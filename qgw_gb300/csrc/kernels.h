@@ -10,6 +10,10 @@ namespace qgw {
 
 cudaError_t prepare_f64(const StepArgs<double>& a);
 cudaError_t prepare_f32c(const StepArgs<float>& a);
+// blocks of the persistent RHS kernel (resident blocks per SM x SMs; 0:
+// one block per tile, as the FP64 path runs); after prepare_*
+int rhs_grid_f64(const StepArgs<double>& a);
+int rhs_grid_f32c(const StepArgs<float>& a);
 
 void enqueue_begin(DevState* st, double t_out, double tend, cudaStream_t s);
 void enqueue_step_f64(const StepArgs<double>& a, cudaStream_t s);

@@ -116,7 +116,14 @@ template <typename T> struct StepArgs {
   // grouping
   int G1;                          // modes per block in the row passes
   int G3;                          // modes per block in K3 (zeta doubles the rows)
-  int zeta_mode;                   // 1: K2/K3 also produce zeta, K4 uses it
+  // compensated path: a second spectral field formed in K2, transformed by
+  // K3 into `zeta`, read by K4.  0: none.  1: zeta = L psi (the 5-point
+  // Laplacian), which K4 continues into the hyperviscosity chain and uses
+  // for the bottom drag.  2: zeta = L^nsweep psi, the whole hyperviscosity
+  // chain, which is diagonal in the transform basis when every sweep sees
+  // zero ghosts (free-slip walls) or wrapped ones (periodic): K4 runs no
+  // sweeps and needs a halo of 1 (runs without bottom drag).
+  int zeta_mode;
   double lx2, ly2;                 // -4/Delta^2 factors of the discrete symbol
   const double* sx2;               // sin^2(pi k / (2 Mx)), k = 1..nx
   const double* sy2;               // sin^2(pi j / (2 My)), j = 1..ny
@@ -144,6 +151,7 @@ template <typename T> struct StepArgs {
   // the element-wise asynchronous copies instead
   CUtensorMap tm[3];
   int use_tma;
+  int rhs_grid;                    // blocks of the persistent RHS kernel (0: one per tile)
   // iterations of the first bounded wait for a tile's TMA bytes (normally
   // kWaitIters; lowered only by tests, to make that wait run out -- the
   // second wait, which lets the bytes land before the block moves on, always
@@ -177,8 +185,10 @@ enum FcIndex {
   FC_NORM = FC_GH1 + 4,
   FC_LX2,
   FC_LY2,
+  FC_NUHS,        // nu_hyper itself (zeta_mode 2: the field is scaled)
   FC_COUNT
 };
+static_assert(FC_COUNT <= (int)(sizeof(StepArgs<float>::fc) / sizeof(float)), "fc holds every constant");
 
 // A batch of runs advanced by one launch per stage (see kernels_ens.cu).
 template <typename T> struct EnsArgs {

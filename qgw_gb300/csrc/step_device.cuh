@@ -158,6 +158,24 @@ __device__ __forceinline__ void cp_async_elem(T* smem_dst, const T* gsrc) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// Start bringing a transform's tables into L1 (the s_j table, the pass
+// twiddles, the split's cos/sin: ~8 KiB at M = 1024, read by every thread
+// at each transform), one 128-byte line per thread, without waiting.
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+  asm volatile("prefetch.global.L1 [%0];\n" ::"l"(p));
+}
+template <typename T>
+__device__ __forceinline__ void prefetch_tables_l1(const DstTables<T>& t, int M) {
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x, nth = blockDim.x * blockDim.y;
+  const int H = M / 2;
+  const char* base[3] = {(const char*)t.sj, (const char*)t.twp, (const char*)t.spl};
+  const int bytes[3] = {(H + 1) * (int)sizeof(T), H * (int)sizeof(C2<T>), (H / 2 + 1) * (int)sizeof(C2<T>)};
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+    if (base[r])
+      for (int off = tid * 128; off < bytes[r]; off += nth * 128) prefetch_l1(base[r] + off);
+}
+
 // Tensor-memory-accelerator tile loads completing on a shared-memory
 // mbarrier (one elected thread issues them; every thread waits, bounded).
 __device__ __forceinline__ unsigned int smem_u32(const void* p) { return (unsigned int)__cvta_generic_to_shared(p); }
@@ -261,12 +279,14 @@ __device__ __forceinline__ int group_width(int G) { return G <= 1 ? 1 : G <= 2 ?
 // FK: 0 no forcing, 1 stochastic forcing only (layer 0), 2 either or both
 // -- separate instantiations, so that each loop carries only the forcing it
 // applies; 3: no update pending, q comes from the caller's array a.qin
-// (reference layout) and is stored into the run's field on the way
+// (reference layout) and is stored into the run's field on the way.
+// Point i of the row goes to index i + xo of its mode row (xo = 1: the DST's
+// x_{i+1} at index i+1; xo = 0: the real FFT's x_i at index i).
 template <typename T, bool COMP, int GB, int FK>
 __device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool upd, T c0, T c1, T c2, const T* f0,
                                             const T* f1, const T* f2, int G, T* A, int ld, const T* cst,
                                             const T* frow, T sqdt, const T* r1, const T* r2, T w1, T w2,
-                                            T dtf) {
+                                            T dtf, int xo) {
   if constexpr (FK == 3) {
     // q from the caller's host array: four layers' loads in flight per
     // point (the link's latency is several microseconds), then the stores
@@ -303,55 +323,91 @@ __device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool up
           for (int g = 0; g < GB; ++g) acc[g] = fmaT(c[g], v, acc[g]);
         }
       }
-      const int pi = pr<T>(i);
+      const int pi = pr<T>(i + xo);
 #pragma unroll
       for (int g = 0; g < GB; ++g)
         if (g < G) A[g * ld + pi] = acc[g];
     }
   } else {
-  for (int i = threadIdx.x; i < a.nx; i += NT) {
-    T acc[GB];
+  // FP32: two points per pass (i and i + NT, the second absent past the
+  // row's end), every layer's loads of both issued before either is used:
+  // the fields stream from HBM/L2 and one point's chain of layers alone
+  // leaves the loads' latency exposed.  FP64 (bound by its FP64 pipe, and
+  // without registers for a second point's 16-wide groups): one point.
+  constexpr int PP = sizeof(T) == 4 ? 2 : 1;
+  T* __restrict__ qh = a.q;
+  T* __restrict__ ql = a.qlo;
+  const T* __restrict__ g0 = f0;
+  const T* __restrict__ g1 = f1;
+  const T* __restrict__ g2 = f2;
+  // one layer of one point: the pending AB3 update (and forcing) of q,
+  // stored back, and the value the projection takes
+  auto layer = [&](int i, size_t o, int l, T qv, T lov, T a0, T a1, T a2) -> T {
+    if (COMP) {
+      float hi = (float)qv;
+      if (upd) {
+        float lo = (float)lov;
+        const float d = ab3_increment((float)c0, (float)c1, (float)c2, (float)a0, (float)a1, (float)a2);
+        comp_add(hi, lo, d);
+        if (FK == 1 && l == 0) comp_add(hi, lo, (float)frow[i] * (float)sqdt);
+        if (FK == 2) {
+          if (frow && l == 0) comp_add(hi, lo, (float)frow[i] * (float)sqdt);
+          if (r1) comp_add(hi, lo, (float)forc4d_term<T>(r1, r2, o, w1, w2, dtf));
+        }
+        qh[o] = (T)hi;
+        ql[o] = (T)lo;
+      }
+      return (T)hi;
+    } else {
+      T v = qv;
+      if (upd) {
+        v = ab3_plain<T>(v, c0, c1, c2, a0, a1, a2);
+        if (FK == 1 && l == 0) v = v + frow[i] * sqdt;
+        if (FK == 2) {
+          if (frow && l == 0) v = v + frow[i] * sqdt;
+          v = v + forc4d_term<T>(r1, r2, o, w1, w2, dtf);
+        }
+        qh[o] = v;
+      }
+      return v;
+    }
+  };
+  for (int i = threadIdx.x; i < a.nx; i += PP * NT) {
+    const int i2 = i + NT;
+    const bool two = PP == 2 && i2 < a.nx;
+    T acc[GB], acc2[GB];
 #pragma unroll
-    for (int g = 0; g < GB; ++g) acc[g] = T(0);
+    for (int g = 0; g < GB; ++g) acc[g] = acc2[g] = T(0);
     size_t o = (size_t)j * a.pitch + i;
     for (int l = 0; l < a.nl; ++l, o += a.lstride) {
-      T v;
-      if (COMP) {
-        float hi = (float)a.q[o];
-        if (upd) {
-          float lo = (float)a.qlo[o];
-          const float d = ab3_increment((float)c0, (float)c1, (float)c2, (float)f0[o], (float)f1[o], (float)f2[o]);
-          comp_add(hi, lo, d);
-          if (FK == 1 && l == 0) comp_add(hi, lo, (float)frow[i] * (float)sqdt);
-          if (FK == 2) {
-            if (frow && l == 0) comp_add(hi, lo, (float)frow[i] * (float)sqdt);
-            if (r1) comp_add(hi, lo, (float)forc4d_term<T>(r1, r2, o, w1, w2, dtf));
-          }
-          a.q[o] = (T)hi;
-          a.qlo[o] = (T)lo;
-        }
-        v = (T)hi;
-      } else {
-        v = a.q[o];
-        if (upd) {
-          v = ab3_plain<T>(v, c0, c1, c2, f0[o], f1[o], f2[o]);
-          if (FK == 1 && l == 0) v = v + frow[i] * sqdt;
-          if (FK == 2) {
-            if (frow && l == 0) v = v + frow[i] * sqdt;
-            v = v + forc4d_term<T>(r1, r2, o, w1, w2, dtf);
-          }
-          a.q[o] = v;
-        }
+      const size_t o2 = o + NT;
+      const T x = qh[o], x2 = two ? qh[o2] : T(0);
+      T lo = T(0), lo2 = T(0), a0 = T(0), a1 = T(0), a2 = T(0), b0 = T(0), b1 = T(0), b2 = T(0);
+      if (upd) {
+        if (COMP) { lo = ql[o]; if (two) lo2 = ql[o2]; }
+        a0 = g0[o]; a1 = g1[o]; a2 = g2[o];
+        if (two) { b0 = g0[o2]; b1 = g1[o2]; b2 = g2[o2]; }
       }
+      const T v = layer(i, o, l, x, lo, a0, a1, a2);
+      const T v2 = two ? layer(i2, o2, l, x2, lo2, b0, b1, b2) : T(0);
       T c[GB];
       ld_coefs<GB, T>(cst + l * GMAX, c);
 #pragma unroll
-      for (int g = 0; g < GB; ++g) acc[g] = fmaT(c[g], v, acc[g]);
+      for (int g = 0; g < GB; ++g) {
+        acc[g] = fmaT(c[g], v, acc[g]);
+        acc2[g] = fmaT(c[g], v2, acc2[g]);
+      }
     }
-    const int pi = pr<T>(i);
+    const int pi = pr<T>(i + xo);
 #pragma unroll
     for (int g = 0; g < GB; ++g)
       if (g < G) A[g * ld + pi] = acc[g];
+    if (two) {
+      const int pi2 = pr<T>(i2 + xo);
+#pragma unroll
+      for (int g = 0; g < GB; ++g)
+        if (g < G) A[g * ld + pi2] = acc2[g];
+    }
   }
   }
 }
@@ -376,6 +432,7 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
   const T* f2 = a.fab + s2 * fs;
   const int tid = threadIdx.x;
   const int GB = group_width(a.G1);
+  if (!PER) prefetch_tables_l1(a.tx, a.gx.M);
   const T* frow = (ab3 && a.fr.on) ? a.fr.field + (size_t)j * a.pitch : nullptr;
   const T sqdt = frow ? (T)sqrt(st->dt) : T(0);
   const T* r1 = nullptr;
@@ -402,7 +459,7 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
     __syncthreads();
     const int fk = (a.qin && m0 == 0) ? 3 : !upd ? 0 : r1 ? 2 : frow ? 1 : 0;
 #define QGW_PF(GBV, F) project_fwd<T, COMP, GBV, F>(a, j, upd, c0, c1, c2, f0, f1, f2, G, A, ld, cst, frow, sqdt, r1, \
-                                                  r2, w1, w2, dtf)
+                                                  r2, w1, w2, dtf, PER ? 0 : 1)
 #define QGW_PF_GB(F)                 \
   switch (GB) {                      \
     case 1: QGW_PF(1, F); break;     \
@@ -425,10 +482,12 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
 #undef QGW_PF
     __syncthreads();
     T* O = PER ? rfft_block<T>(A, B, G, ld, a.gx, a.tx) : dst_block<T>(A, B, G, ld, a.gx, a.tx, tot);
-    const int nout = PER ? a.nx + 2 : a.nx;
+    // spectral row: the real FFT's X_0..X_H as (re, im) pairs from index 0,
+    // or the DST's Y_1..Y_{M-1} from index 1
+    const int nout = PER ? a.nx + 2 : a.nx, yo = PER ? 0 : 1;
     for (int gg = 0; gg < G; ++gg) {
       T* dstrow = a.spec + (size_t)(m0 + gg) * a.lstride + (size_t)j * a.pitch;
-      for (int i = threadIdx.x; i < nout; i += NT) dstrow[i] = O[gg * ld + pr<T>(i)];
+      for (int i = threadIdx.x; i < nout; i += NT) dstrow[i] = O[gg * ld + pr<T>(i + yo)];
     }
     __syncthreads();
   }
@@ -446,6 +505,20 @@ __device__ __forceinline__ void load_cols(const T* __restrict__ src, T* v) {
 #pragma unroll
   for (int n = 0; n < NV; ++n) {
     const uint4 u = p[n];
+    const T* a = reinterpret_cast<const T*>(&u);
+#pragma unroll
+    for (int c = 0; c < PV; ++c) v[n * PV + c] = a[c];
+  }
+}
+// load_cols with streaming (evict-first) loads: data read once
+template <typename T, int CT>
+__device__ __forceinline__ void load_cols_stream(const T* __restrict__ src, T* v) {
+  constexpr int NV = CT * (int)sizeof(T) / 16, PV = 16 / (int)sizeof(T);
+  static_assert(NV >= 1 && CT * sizeof(T) == 16 * NV, "whole 16-byte vectors");
+  const uint4* p = reinterpret_cast<const uint4*>(src);
+#pragma unroll
+  for (int n = 0; n < NV; ++n) {
+    const uint4 u = __ldcs(p + n);
     const T* a = reinterpret_cast<const T*>(&u);
 #pragma unroll
     for (int c = 0; c < PV; ++c) v[n * PV + c] = a[c];
@@ -474,89 +547,139 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
   const int k0 = bx * CT;
   const int CTb = min(CT, a.nx - k0);
   const int ld = padded_len<T>(a.gy.M);
+  const bool zm = COMP && a.zeta_mode;
+  // Two pairs of CT-row buffers, [A | C] and [B | D]: the forward DST runs on
+  // A with B as work buffer; the divide overwrites its output O with psi_hat
+  // and, in zeta mode, writes the second field into the CT rows after O; the
+  // inverse DST then transforms both at once (2 CT rows) with the other pair
+  // as work buffer.  Column jj + 1 of a tile row holds point jj (x_{jj+1}).
   T* A = (T*)smem_raw;
-  T* B = A + (size_t)CT * ld;
-  T* C = B + (size_t)CT * ld;  // zeta mode only
+  T* B = A + (size_t)(zm ? 2 : 1) * CT * ld;
   T* S = a.spec + (size_t)m * a.lstride;
   const int ny = a.ny;
+  prefetch_tables_l1(a.ty, a.gy.M);
   // 16-byte vectors need 16-byte aligned rows (vec_cols); the last tile then
-  // reads the padding column (index nx < pitch), never past the row
+  // reads the padding column (index nx < pitch), never past the row.  RB
+  // rows per pass, all their loads in flight before any store (FP32 four,
+  // FP64 two: its rows take twice the registers); streaming loads (the tile
+  // is read once), which leave L1 to the tables.
+  constexpr int RB = sizeof(T) == 4 ? 4 : 2;
   const bool vec = a.vec_cols != 0;
-  T v[CT];
-  for (int jj = threadIdx.x; jj < ny; jj += NT) {
-    const T* src = S + (size_t)jj * a.pitch + k0;
-    if (vec) load_cols<T, CT>(src, v);
-    else
-      for (int c = 0; c < CT; ++c) v[c] = c < CTb ? src[c] : T(0);
-    const int pj = pr<T>(jj);
+  for (int j0 = threadIdx.x; j0 < ny; j0 += RB * NT) {
+    T vv[RB][CT];
 #pragma unroll
-    for (int c = 0; c < CT; ++c) A[c * ld + pj] = v[c];
+    for (int u = 0; u < RB; ++u) {
+      const int jj = j0 + u * NT;
+      if (jj < ny) {
+        const T* src = S + (size_t)jj * a.pitch + k0;
+        if (vec) load_cols_stream<T, CT>(src, vv[u]);
+        else
+          for (int c = 0; c < CT; ++c) vv[u][c] = c < CTb ? src[c] : T(0);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < RB; ++u) {
+      const int jj = j0 + u * NT;
+      if (jj < ny) {
+        const int pj = pr<T>(jj + 1);
+#pragma unroll
+        for (int c = 0; c < CT; ++c) A[c * ld + pj] = vv[u][c];
+      }
+    }
   }
   __syncthreads();
   T* O = dst_block<T>(A, B, CT, ld, a.gy, a.ty, tot);
+  T* C = O + (size_t)CT * ld;  // the second field's rows (zeta mode)
   const double iRd2 = a.iRd2[m];
-  const bool zm = COMP && a.zeta_mode;
+  // power of the 5-point symbol in the second field: L psi (zeta mode 1) or
+  // the whole hyperviscosity chain L^nsweep psi (zeta mode 2)
+  const int zpow = (COMP && a.zeta_mode == 2) ? a.nsweep : 1;
   const float ird2f = COMP ? a.iRd2f[m] : 0.f;
   const float normf = a.fc[FC_NORM], lx2f = a.fc[FC_LX2], ly2f = a.fc[FC_LY2];
-  for (int jj = threadIdx.x; jj < ny; jj += NT) {
-    const int pj = pr<T>(jj);
-    if (!COMP) {
-      const T* hrow = (const T*)(a.hinv + (size_t)m * a.lstride + (size_t)jj * a.pitch + k0);
-      T h[CT];
-      if (vec) load_cols<T, CT>(hrow, h);
-      else
-        for (int c = 0; c < CT; ++c) h[c] = c < CTb ? hrow[c] : T(0);
+  // the tile's per-column table values, the same for every row
+  int kc[CT];
+  float lsqc[CT], sxc[CT];
 #pragma unroll
-      for (int c = 0; c < CT; ++c) O[c * ld + pj] *= h[c];
-    } else {
-      const float ksq = a.Ksqf[jj], sy = a.sy2f[jj];
+  for (int c = 0; c < CT; ++c) {
+    kc[c] = min(k0 + c, a.nx - 1);
+    lsqc[c] = COMP ? a.Lsqf[kc[c]] : 0.f;
+    sxc[c] = zm ? a.sx2f[kc[c]] : 0.f;
+  }
+  // RB rows per pass, their per-row loads issued before any is used
+  for (int j0 = threadIdx.x; j0 < ny; j0 += RB * NT) {
+    T h4[RB][CT];
+    float ksq4[RB], sy4[RB];
 #pragma unroll
-      for (int c = 0; c < CT; ++c) {
-        const int k = min(k0 + c, a.nx - 1);
-        float x;
-        if (m == 0 && jj < a.low_k64 && k < a.low_k64) {
-          // barotropic mode, lowest wavenumbers: divide in FP64
-          const double fact = -(a.Lsq[k] + a.Ksq[jj] + iRd2);
-          x = (float)((double)O[c * ld + pj] / fact / a.norm);
-        } else {
-          const float fact = -((a.Lsqf[k] + ksq) + ird2f);
-          x = (float)O[c * ld + pj] / (fact * normf);
-        }
-        O[c * ld + pj] = (T)x;
-        if (zm) {
-          // spectral discrete Laplacian of psi: lambda(k, j) * psi_hat with
-          // lambda = -4/Delta^2 (sin^2 kx + sin^2 ky), the exact symbol of
-          // the 5-point Laplacian with zero ghosts in the DST basis
-          const float lam = lx2f * a.sx2f[k] + ly2f * sy;
-          C[c * ld + pj] = (T)(lam * x);
+    for (int u = 0; u < RB; ++u) {
+      const int jj = j0 + u * NT;
+      if (jj >= ny) continue;
+      if (!COMP) {
+        const T* hrow = (const T*)(a.hinv + (size_t)m * a.lstride + (size_t)jj * a.pitch + k0);
+        if (vec) load_cols<T, CT>(hrow, h4[u]);
+        else
+          for (int c = 0; c < CT; ++c) h4[u][c] = c < CTb ? hrow[c] : T(0);
+      } else {
+        ksq4[u] = a.Ksqf[jj];
+        sy4[u] = zm ? a.sy2f[jj] : 0.f;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < RB; ++u) {
+      const int jj = j0 + u * NT;
+      if (jj >= ny) continue;
+      const int pj = pr<T>(jj + 1);
+      if (!COMP) {
+#pragma unroll
+        for (int c = 0; c < CT; ++c) O[c * ld + pj] *= h4[u][c];
+      } else {
+#pragma unroll
+        for (int c = 0; c < CT; ++c) {
+          const int k = kc[c];
+          float x;
+          if (m == 0 && jj < a.low_k64 && k < a.low_k64) {
+            // barotropic mode, lowest wavenumbers: divide in FP64
+            const double fact = -(a.Lsq[k] + a.Ksq[jj] + iRd2);
+            x = (float)((double)O[c * ld + pj] / fact / a.norm);
+          } else {
+            const float fact = -((lsqc[c] + ksq4[u]) + ird2f);
+            x = (float)O[c * ld + pj] / (fact * normf);
+          }
+          O[c * ld + pj] = (T)x;
+          if (zm) {
+            // spectral discrete Laplacian of psi: lambda(k, j) * psi_hat with
+            // lambda = -4/Delta^2 (sin^2 kx + sin^2 ky), the exact symbol of
+            // the 5-point Laplacian with zero ghosts in the DST basis; applied
+            // zpow times, one factor after the other (no underflow of
+            // lambda^zpow at the lowest wavenumbers)
+            const float lam = lx2f * sxc[c] + ly2f * sy4[u];
+            float z = lam * x;
+            for (int s = 1; s < zpow; ++s) z = z * lam;
+            C[c * ld + pj] = (T)z;
+          }
         }
       }
     }
   }
   __syncthreads();
   T* Oth = (O == A) ? B : A;
-  T* O2 = dst_block<T>(O, Oth, CT, ld, a.gy, a.ty, tot);
+  T* O2 = dst_block<T>(O, Oth, zm ? 2 * CT : CT, ld, a.gy, a.ty, tot);
+  T* S2 = zm ? a.spec2 + (size_t)m * a.lstride : nullptr;
+  T v[CT];
   for (int jj = threadIdx.x; jj < ny; jj += NT) {
-    const int pj = pr<T>(jj);
+    const int pj = pr<T>(jj + 1);
 #pragma unroll
     for (int c = 0; c < CT; ++c) v[c] = c < CTb ? O2[c * ld + pj] : T(0);
     T* dst = S + (size_t)jj * a.pitch + k0;
     if (vec) store_cols<T, CT>(dst, v);
     else
       for (int c = 0; c < CTb; ++c) dst[c] = v[c];
-  }
-  if (zm) {
-    __syncthreads();
-    T* O3 = dst_block<T>(C, O2 == A ? B : A, CT, ld, a.gy, a.ty, tot);
-    T* S2 = a.spec2 + (size_t)m * a.lstride;
-    for (int jj = threadIdx.x; jj < ny; jj += NT) {
-      const int pj = pr<T>(jj);
+    if (zm) {
 #pragma unroll
-      for (int c = 0; c < CT; ++c) v[c] = c < CTb ? O3[c * ld + pj] : T(0);
-      T* dst = S2 + (size_t)jj * a.pitch + k0;
-      if (vec) store_cols<T, CT>(dst, v);
+      for (int c = 0; c < CT; ++c) v[c] = c < CTb ? O2[(CT + c) * ld + pj] : T(0);
+      T* dst2 = S2 + (size_t)jj * a.pitch + k0;
+      if (vec) store_cols<T, CT>(dst2, v);
       else
-        for (int c = 0; c < CTb; ++c) dst[c] = v[c];
+        for (int c = 0; c < CTb; ++c) dst2[c] = v[c];
     }
   }
 }
@@ -594,6 +717,7 @@ __device__ __forceinline__ void body_cols_per(const StepArgs<T>& a, int step_mod
   __syncthreads();
   T* O = cfft_block<T>(A, B, CC, ld, a.gy, a.ty.tw, a.ty.twp);
   const bool zm = COMP && a.zeta_mode;
+  const int zpow = (COMP && a.zeta_mode == 2) ? a.nsweep : 1;  // as in body_cols
   const double iRd2 = a.iRd2[m];
   const float ird2f = COMP ? a.iRd2f[m] : 0.f;
   const float normf = a.fc[FC_NORM], lx2f = a.fc[FC_LX2], ly2f = a.fc[FC_LY2];
@@ -627,9 +751,14 @@ __device__ __forceinline__ void body_cols_per(const StepArgs<T>& a, int step_mod
     if (zm) {
       const int kk = k > H ? H : k;
       const float lam = lx2f * a.sx2f[kk] + ly2f * a.sy2f[jj];
+      float zx = lam * (float)X.x, zy = lam * (float)X.y;
+      for (int s = 1; s < zpow; ++s) {
+        zx = zx * lam;
+        zy = zy * lam;
+      }
       C2<T> Z;
-      Z.x = (T)(lam * (float)X.x);
-      Z.y = -(T)(lam * (float)X.y);
+      Z.x = (T)zx;
+      Z.y = -(T)zy;
       ((C2<T>*)(C + c * ld))[pj] = Z;
     }
     X.y = -X.y;  // conjugate: backward FFT = conj(FFT(conj))
@@ -665,37 +794,56 @@ __device__ __forceinline__ void body_cols_per(const StepArgs<T>& a, int step_mod
 // group first forms the spectral rows of its layers, sum_m cm2l[l][m] *
 // spec_m (and of zeta from spec2 in zeta mode), then inverse-transforms them
 // and writes psi_l (zeta_l) once.  The spectral rows of row j are re-read by
-// each group (from cache); nothing is accumulated in global memory.
+// each group (from cache); nothing is accumulated in global memory.  Column
+// i goes to index i + xo of its row (xo = 1: the DST's input format).
 template <typename T, bool ZM, int GB>
 __device__ __forceinline__ void project_spec(const StepArgs<T>& a, int j, int G, T* A, int ld, const T* cst,
-                                             int ncols) {
-  for (int i = threadIdx.x; i < ncols; i += NT) {
-    T acc[GB], zacc[ZM ? GB : 1];
+                                             int ncols, int xo) {
+  // FP32: two columns per pass (i and i + NT), each mode's loads of both
+  // issued before either is used (the spectral rows come from L2); FP64
+  // (FP64-pipe bound, registers for one column's groups): one column
+  constexpr int PP = sizeof(T) == 4 ? 2 : 1;
+  const T* __restrict__ sp = a.spec;
+  const T* __restrict__ sp2 = a.spec2;
+  for (int i = threadIdx.x; i < ncols; i += PP * NT) {
+    const bool two = PP == 2 && i + NT < ncols;
+    T acc[GB], zacc[ZM ? GB : 1], acc2[GB], zacc2[ZM ? GB : 1];
 #pragma unroll
     for (int g = 0; g < GB; ++g) {
-      acc[g] = T(0);
-      if (ZM) zacc[g] = T(0);
+      acc[g] = acc2[g] = T(0);
+      if (ZM) zacc[g] = zacc2[g] = T(0);
     }
     size_t o = (size_t)j * a.pitch + i;
 #pragma unroll 2
     for (int m = 0; m < a.nl; ++m, o += a.lstride) {
+      const T v = sp[o], v2 = two ? sp[o + NT] : T(0);
+      T z = T(0), z2 = T(0);
+      if (ZM) {
+        z = sp2[o];
+        z2 = two ? sp2[o + NT] : T(0);
+      }
       T c[GB];
       ld_coefs<GB, T>(cst + m * GMAX, c);
-      const T v = a.spec[o];
 #pragma unroll
-      for (int g = 0; g < GB; ++g) acc[g] = fmaT(c[g], v, acc[g]);
-      if (ZM) {
-        const T z = a.spec2[o];
-#pragma unroll
-        for (int g = 0; g < GB; ++g) zacc[g] = fmaT(c[g], z, zacc[g]);
+      for (int g = 0; g < GB; ++g) {
+        acc[g] = fmaT(c[g], v, acc[g]);
+        acc2[g] = fmaT(c[g], v2, acc2[g]);
+        if (ZM) {
+          zacc[g] = fmaT(c[g], z, zacc[g]);
+          zacc2[g] = fmaT(c[g], z2, zacc2[g]);
+        }
       }
     }
-    const int pi = pr<T>(i);
+    const int pi = pr<T>(i + xo), pi2 = pr<T>(i + NT + xo);
 #pragma unroll
     for (int g = 0; g < GB; ++g)
       if (g < G) {
         A[g * ld + pi] = acc[g];
         if (ZM) A[(G + g) * ld + pi] = zacc[g];
+        if (two) {
+          A[g * ld + pi2] = acc2[g];
+          if (ZM) A[(G + g) * ld + pi2] = zacc2[g];
+        }
       }
   }
 }
@@ -711,6 +859,7 @@ __device__ __forceinline__ void body_rows_inv(const StepArgs<T>& a, int step_mod
   T* A = (T*)smem_raw;
   T* B = A + (size_t)(zm ? 2 * Gb : Gb) * ld;
   const int GB = group_width(Gb);
+  if (!PER) prefetch_tables_l1(a.tx, a.gx.M);
   // ceil(nl / Gb) layer groups of balanced sizes (at most Gb each)
   const int ng = (a.nl + Gb - 1) / Gb, gq = a.nl / ng, gr = a.nl - gq * ng;
   for (int gi = 0, l0 = 0; gi < ng; l0 += gq + (gi < gr), ++gi) {
@@ -720,35 +869,41 @@ __device__ __forceinline__ void body_rows_inv(const StepArgs<T>& a, int step_mod
       cst[w] = g < G ? a.cm2l[(size_t)(l0 + g) * a.nl + m] : T(0);
     }
     __syncthreads();
-    const int ncols = PER ? a.nx + 2 : a.nx;
+    const int ncols = PER ? a.nx + 2 : a.nx, xo = PER ? 0 : 1;
     if (zm) {
       switch (GB) {
-        case 1: project_spec<T, true, 1>(a, j, G, A, ld, cst, ncols); break;
-        case 2: project_spec<T, true, 2>(a, j, G, A, ld, cst, ncols); break;
-        case 4: project_spec<T, true, 4>(a, j, G, A, ld, cst, ncols); break;
-        default: project_spec<T, true, 8>(a, j, G, A, ld, cst, ncols); break;
+        case 1: project_spec<T, true, 1>(a, j, G, A, ld, cst, ncols, xo); break;
+        case 2: project_spec<T, true, 2>(a, j, G, A, ld, cst, ncols, xo); break;
+        case 4: project_spec<T, true, 4>(a, j, G, A, ld, cst, ncols, xo); break;
+        default: project_spec<T, true, 8>(a, j, G, A, ld, cst, ncols, xo); break;
       }
     } else {
       switch (GB) {
-        case 1: project_spec<T, false, 1>(a, j, G, A, ld, cst, ncols); break;
-        case 2: project_spec<T, false, 2>(a, j, G, A, ld, cst, ncols); break;
-        case 4: project_spec<T, false, 4>(a, j, G, A, ld, cst, ncols); break;
-        case 8: project_spec<T, false, 8>(a, j, G, A, ld, cst, ncols); break;
-        default: project_spec<T, false, 16>(a, j, G, A, ld, cst, ncols); break;
+        case 1: project_spec<T, false, 1>(a, j, G, A, ld, cst, ncols, xo); break;
+        case 2: project_spec<T, false, 2>(a, j, G, A, ld, cst, ncols, xo); break;
+        case 4: project_spec<T, false, 4>(a, j, G, A, ld, cst, ncols, xo); break;
+        case 8: project_spec<T, false, 8>(a, j, G, A, ld, cst, ncols, xo); break;
+        default: project_spec<T, false, 16>(a, j, G, A, ld, cst, ncols, xo); break;
       }
     }
     __syncthreads();
     const int nrow = zm ? 2 * G : G;
     T* O = PER ? irfft_block<T>(A, B, nrow, ld, a.gx, a.tx) : dst_block<T>(A, B, nrow, ld, a.gx, a.tx, tot);
     // periodic: x_{2m+1} is minus the imaginary part of the backward FFT
+    // (x_i at index i); DST: x_{i+1} at index i + 1
     const T odd = PER ? T(-1) : T(1);
     for (int g = 0; g < G; ++g) {
       T* prow = a.psi + (size_t)(l0 + g) * a.lstride + (size_t)j * a.pitch;
-      for (int i = threadIdx.x; i < a.nx; i += NT) prow[i] = (i & 1) ? odd * O[g * ld + pr<T>(i)] : O[g * ld + pr<T>(i)];
+      for (int i = threadIdx.x; i < a.nx; i += NT) {
+        const T v = O[g * ld + pr<T>(i + xo)];
+        prow[i] = (PER && (i & 1)) ? odd * v : v;
+      }
       if (zm) {
         T* zrow = a.zeta + (size_t)(l0 + g) * a.lstride + (size_t)j * a.pitch;
-        for (int i = threadIdx.x; i < a.nx; i += NT)
-          zrow[i] = (i & 1) ? odd * O[(G + g) * ld + pr<T>(i)] : O[(G + g) * ld + pr<T>(i)];
+        for (int i = threadIdx.x; i < a.nx; i += NT) {
+          const T v = O[(G + g) * ld + pr<T>(i + xo)];
+          zrow[i] = (PER && (i & 1)) ? odd * v : v;
+        }
       }
     }
     __syncthreads();
@@ -847,47 +1002,50 @@ template <typename T> __host__ __device__ constexpr int tile_round(int n) {
   return (n + (128 / (int)sizeof(T)) - 1) / (128 / (int)sizeof(T)) * (128 / (int)sizeof(T));
 }
 
-// RHS tile of TX x TY points of one layer; block (32, 8); R = halo radius
-// of psi (the number of hyperviscosity sweeps, at least 1).  EDGE: the tile
-// plus its halo touches a wall, so loads are bounds-checked and ghost values
-// follow adjust_bc (or wrap around, periodic); interior tiles (the vast
-// majority) arrive by TMA (tm != null, bar: the block's mbarrier, *phase its
-// parity) or by element-wise asynchronous copies.  Returns this thread's CFL
-// maximum |dpsi| as bits in the arithmetic width.
+// Shared memory of the RHS kernels: NB input buffers (a TMA box set: psi
+// with halo R, q with halo 1 and, in zeta mode 1, the raw zeta of the first
+// sweep's region) followed by the work buffers (the chain's ping-pong and,
+// for FP64, the centred differences).  Every array starts 128-byte aligned.
+template <typename T, int R> struct RhsShape {
+  static constexpr int HH = TY + 2 * R, QH = TY + 2, QW = TX + 2;
+  static constexpr int TS = tile_round<T>(TW * HH), QS = tile_round<T>(TW * QH), ZS = tile_round<T>(TW * (HH - 2));
+  static constexpr int IS = TS + QS + ZS;  // one input buffer
+  static constexpr int DIFFS = sizeof(T) == 8 ? tile_round<T>(2 * QW * TY + 2 * TX * QH) : 0;
+  static constexpr int WS = 2 * TS + DIFFS;  // work buffers
+  static constexpr size_t bytes(int nb) { return sizeof(T) * ((size_t)nb * IS + WS) + 128; }
+};
+template <typename T> struct RhsIn {
+  T* ps;  // HH x TW: psi with halo R
+  T* qs;  // QH x TW: q with halo 1
+  T* zt;  // (HH - 2) x TW: zeta over the first sweep's region (zeta mode 1)
+};
+template <typename T, int R> __device__ __forceinline__ RhsIn<T> rhs_in(unsigned char* base, int b) {
+  using S = RhsShape<T, R>;
+  T* p = (T*)base + (size_t)b * S::IS;
+  return RhsIn<T>{p, p + S::TS, p + S::TS + S::QS};
+}
+template <typename T, int R> __device__ __forceinline__ T* rhs_work(unsigned char* base, int nb) {
+  return (T*)base + (size_t)nb * RhsShape<T, R>::IS;
+}
+
+// Loads of one tile that do not go through TMA, into `in`: edge tiles
+// (bounds-checked psi; periodic tiles also q, wrapped) and, where no tensor
+// map exists, interior tiles by element-wise asynchronous copies (all three
+// fields together).  A closed edge tile's q (with its ghost rule) is formed
+// by rhs_tile_compute, which needs the whole psi tile.  The caller
+// synchronises the block afterwards.
 template <typename T, bool COMP, int R, bool EDGE>
-__device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArgs<T>& a, int i0, int j0, int k,
-                                                                    int step_index, unsigned char* smem_raw,
-                                                                    const CUtensorMap* tm, unsigned long long* bar,
-                                                                    unsigned int* phase, bool* failed) {
+__device__ __forceinline__ void rhs_tile_fetch(const StepArgs<T>& a, int i0, int j0, int k, const RhsIn<T>& in) {
   constexpr int W = TW, HH = TY + 2 * R;
   constexpr int QW = TX + 2, QH = TY + 2;
-  constexpr int XO = TOX;  // column of tile x = 0
-  constexpr int TS = tile_round<T>(W * HH), QS_ = tile_round<T>(W * QH);
-  T* ps = (T*)smem_raw;       // HH x W, psi with halo R
-  T* L0 = ps + TS;            // chain ping-pong
-  T* L1 = L0 + TS;
-  T* qs = L1 + TS;            // QH x W
-  T* dyp = qs + QS_;          // TY x QW (FP64 only)
-  T* dyq = dyp + QW * TY;
-  T* dxp = dyq + QW * TY;     // QH x TX
-  T* dxq = dxp + TX * QH;
-  const int tx = threadIdx.x, ty = threadIdx.y;
+  constexpr int XO = TOX;
+  const int tid = threadIdx.x + threadIdx.y * 32;
   const int nx = a.nx, ny = a.ny, pitch = a.pitch;
   const T* psiL = a.psi + (size_t)k * a.lstride;
   const T* qL = a.q + (size_t)k * a.lstride;
-  const bool zm = COMP && a.zeta_mode;
-  const T* zetaL = zm ? a.zeta + (size_t)k * a.lstride : nullptr;
-  // every double parameter converted once (conversions run on the FP64 pipe)
-  const T d2 = pick<T>(a.Delta * a.Delta, a.fc[FC_D2]);
-  const T cbc = pick<T>(a.cbc, a.fc[FC_CBC]);
-  const T m_inv12 = pick<T>(-a.inv12d2, a.fc[FC_MINV12]), b2d = pick<T>(a.b2d, a.fc[FC_B2D]);
-  const T nu_d2 = pick<T>(a.nu_d2, a.fc[FC_NUD2]), nuh = pick<T>(a.nuh_scaled, a.fc[FC_NUH]);
-  const T drag = pick<T>(a.drag_d2, a.fc[FC_DRAG]), topo_c = pick<T>(-(a.inv12d2 * a.topo_fac), a.fc[FC_TOPOC]);
-#define PS(x, y) ps[((y) + R) * W + (x) + XO]
-#define QS(x, y) qs[((y) + 1) * W + (x) + XO]
-  const int tid = tx + ty * 32;
-  const bool per = a.periodic != 0;
-  if (EDGE && per) {
+  T* ps = in.ps;
+  T* qs = in.qs;
+  if (EDGE && a.periodic) {
     // periodic: every halo value is an interior value of the other side
     // (src/domain.h:225-256); tiles may be wider than the domain
     for (int w = tid; w < HH * (TX + 2 * R); w += NT) {
@@ -906,35 +1064,7 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
       if (gi >= 0 && gi < nx && gj >= 0 && gj < ny) v = psiL[(size_t)gj * pitch + gi];
       ps[y * W + xx + XO] = v;
     }
-  } else if (tm) {
-    // interior tile by TMA: psi (HH rows), q (QH rows) and, in zeta mode,
-    // the raw zeta of the first sweep's region (HH - 2 rows, into L1 from
-    // its row 0; L1 is free until the second sweep), each box TW columns
-    // from x = i0 - 4; one mbarrier collects the bytes
-    if (tid == 0) {
-      fence_proxy_async_smem();
-      const bool z1 = zm && a.nsweep >= 1;
-      const unsigned int bytes = (unsigned int)sizeof(T) * W * (HH + QH + (z1 ? HH - 2 : 0));
-      mbar_expect_tx(bar, bytes);
-      tma_load_3d(ps, &tm[0], i0 - XO, j0 - R, k, bar);
-      tma_load_3d(qs, &tm[1], i0 - XO, j0 - 1, k, bar);
-      if (z1) tma_load_3d(L1, &tm[2], i0 - XO, j0 + 1 - R, k, bar);
-    }
-    // block-uniform outcome of the bounded wait
-    const bool ok = __syncthreads_and(mbar_wait_bounded(bar, *phase, a.wait_iters)) != 0;
-    if (!ok) {
-      // the copies did not arrive: flag the run, give them one more bounded
-      // wait with the full limit (they may still land in this block's shared
-      // memory), skip
-      *failed = true;
-      (void)mbar_wait_bounded(bar, *phase, kWaitIters);
-      if (tid == 0) a.state->dev_error = 1;
-      *phase ^= 1u;
-      return 0;
-    }
-    *phase ^= 1u;
   } else {
-    // interior tile by element-wise asynchronous copies (all three together)
     const T* src = psiL + (size_t)(j0 - R) * pitch + (i0 - R);
     for (int w = tid; w < HH * (TX + 2 * R); w += NT) {
       const int y = w / (TX + 2 * R), x = w - y * (TX + 2 * R);
@@ -945,17 +1075,104 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
       const int y = w / QW, x = w - y * QW;
       cp_async_elem(qs + y * W + x - 1 + XO, qsrc + y * pitch + x);
     }
-    if (zm && a.nsweep >= 1) {
+    if (COMP && a.zeta_mode == 1 && a.nsweep >= 1) {
       constexpr int W1 = TX + 2 * R - 2, H1 = HH - 2;
-      const T* zsrc = zetaL + (size_t)(j0 + 1 - R) * pitch + (i0 + 1 - R);
+      const T* zsrc = a.zeta + (size_t)k * a.lstride + (size_t)(j0 + 1 - R) * pitch + (i0 + 1 - R);
       for (int w = tid; w < W1 * H1; w += NT) {
         const int yr = w / W1, xr = w - yr * W1;
-        cp_async_elem(L1 + yr * W + xr + 1 - R + XO, zsrc + yr * pitch + xr);
+        cp_async_elem(in.zt + yr * W + xr + 1 - R + XO, zsrc + yr * pitch + xr);
       }
     }
     cp_async_wait_all();
   }
-  __syncthreads();
+}
+
+// An interior tile's boxes by TMA (one thread): psi (HH rows), q (QH rows)
+// and, in zeta mode 1, zeta over the first sweep's region (HH - 2 rows), each
+// TW columns from x = i0 - 4; the mbarrier `bar` collects the bytes.  The
+// caller has synchronised the block since the buffers were last read.
+template <typename T, bool COMP, int R>
+__device__ __forceinline__ void rhs_tile_tma(const StepArgs<T>& a, int i0, int j0, int k, const RhsIn<T>& in,
+                                             const CUtensorMap* tm, unsigned long long* bar) {
+  constexpr int W = TW, HH = TY + 2 * R, QH = TY + 2;
+  fence_proxy_async_smem();
+  const bool z1 = COMP && a.zeta_mode == 1 && a.nsweep >= 1;
+  const unsigned int bytes = (unsigned int)sizeof(T) * W * (HH + QH + (z1 ? HH - 2 : 0));
+  mbar_expect_tx(bar, bytes);
+  tma_load_3d(in.ps, &tm[0], i0 - TOX, j0 - R, k, bar);
+  tma_load_3d(in.qs, &tm[1], i0 - TOX, j0 - 1, k, bar);
+  if (z1) tma_load_3d(in.zt, &tm[2], i0 - TOX, j0 + 1 - R, k, bar);
+}
+
+// Block-uniform bounded wait for a tile's TMA bytes.  When the first wait
+// (a.wait_iters polls) runs out, the run is flagged (QGW_ERR_TIMEOUT), the
+// bytes get a second wait with the full limit (they may still land in this
+// block's shared memory) and the tile is to be skipped: returns false.
+template <typename T>
+__device__ __forceinline__ bool rhs_tile_wait(const StepArgs<T>& a, unsigned long long* bar, unsigned int* phase) {
+  const bool ok = __syncthreads_and(mbar_wait_bounded(bar, *phase, a.wait_iters)) != 0;
+  if (!ok) {
+    (void)mbar_wait_bounded(bar, *phase, kWaitIters);
+    if (threadIdx.x == 0 && threadIdx.y == 0) a.state->dev_error = 1;
+  }
+  *phase ^= 1u;
+  return ok;
+}
+
+// RHS tile of TX x TY points of one layer; block (32, 8); R = halo radius
+// of psi (the number of hyperviscosity sweeps the tile runs, at least 1).
+// EDGE: the tile plus its halo touches a wall, so ghost values follow
+// adjust_bc (or wrap around, periodic); interior tiles (the vast majority)
+// skip all of that.  The tile's inputs are in `in` and the block has been
+// synchronised since they arrived; `wk` holds the work buffers.  Returns
+// this thread's CFL maximum |dpsi| as bits in the arithmetic width.
+template <typename T, bool COMP, int R, bool EDGE>
+__device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile_compute(const StepArgs<T>& a, int i0, int j0,
+                                                                            int k, int step_index,
+                                                                            const RhsIn<T>& in, T* wk) {
+  constexpr int W = TW, HH = TY + 2 * R;
+  constexpr int QW = TX + 2, QH = TY + 2;
+  constexpr int XO = TOX;  // column of tile x = 0
+  constexpr int TS = RhsShape<T, R>::TS;
+  T* ps = in.ps;              // HH x W, psi with halo R
+  T* qs = in.qs;              // QH x W
+  T* L0 = wk;                 // chain ping-pong
+  T* L1 = L0 + TS;
+  T* dyp = L1 + TS;           // TY x QW (FP64 only)
+  T* dyq = dyp + QW * TY;
+  T* dxp = dyq + QW * TY;     // QH x TX
+  T* dxq = dxp + TX * QH;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int nx = a.nx, ny = a.ny, pitch = a.pitch;
+  const T* qL = a.q + (size_t)k * a.lstride;
+  // zeta mode 1: the spectral L psi starts the chain and gives the drag;
+  // zeta mode 2: the field is the whole chain L^nsweep psi (no sweeps here)
+  const bool zm = COMP && a.zeta_mode == 1;
+  const bool zm2 = COMP && a.zeta_mode == 2;
+  const int ksweep = zm2 ? 0 : a.nsweep;  // Laplacian sweeps run on the tile
+  const T* zetaL = (COMP && a.zeta_mode) ? a.zeta + (size_t)k * a.lstride : nullptr;
+  // every double parameter converted once (conversions run on the FP64 pipe)
+  const T d2 = pick<T>(a.Delta * a.Delta, a.fc[FC_D2]);
+  const T cbc = pick<T>(a.cbc, a.fc[FC_CBC]);
+  const T m_inv12 = pick<T>(-a.inv12d2, a.fc[FC_MINV12]), b2d = pick<T>(a.b2d, a.fc[FC_B2D]);
+  const T nu_d2 = pick<T>(a.nu_d2, a.fc[FC_NUD2]), nuh = pick<T>(a.nuh_scaled, a.fc[FC_NUH]);
+  const T nuhs = pick<T>(0.0, a.fc[FC_NUHS]);
+  const T drag = pick<T>(a.drag_d2, a.fc[FC_DRAG]), topo_c = pick<T>(-(a.inv12d2 * a.topo_fac), a.fc[FC_TOPOC]);
+#define PS(x, y) ps[((y) + R) * W + (x) + XO]
+#define QS(x, y) qs[((y) + 1) * W + (x) + XO]
+  const int tid = tx + ty * 32;
+  const bool per = a.periodic != 0;
+  // zeta mode 2: the chain value at this thread's two points (x = tx,
+  // y = 2 ty + h; the FP32 Jacobian's mapping), loaded first so that its
+  // latency overlaps the tile's shared-memory work
+  T hv[2] = {T(0), T(0)};
+  if (zm2) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int gi = i0 + tx, gj = j0 + 2 * ty + h;
+      if (!EDGE || (gi < nx && gj < ny)) hv[h] = zetaL[(size_t)gj * pitch + gi];
+    }
+  }
   // q with one ghost point: adjust_bc(q, 1, psi), src/domain.h:308-348
   if (EDGE && !per) {
     for (int w = tid; w < QH * QW; w += NT) {
@@ -982,7 +1199,7 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
   T* Lc = L0;
 #pragma unroll
   for (int s = 1; s <= R; ++s) {
-    if (s <= a.nsweep) {
+    if (s <= ksweep) {
       __syncthreads();
       const int Ws = TX + 2 * R - 2 * s, Hs = HH - 2 * s;
       const int cx = s - R + XO;  // smem column of the region's first point
@@ -1021,12 +1238,13 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
           Lc[o] = v;
         }
       } else if (s == 1 && zm) {
-        // the raw zeta arrived in L1, one row up (its row 0 is the region's
-        // first row): scale it into L0 (== Lc)
+        // the raw zeta arrived in in.zt, one row up (its row 0 is the
+        // region's first row): scale it into L0 (== Lc)
+        const T* zt = in.zt;
         for (int w = tid; w < Ws * Hs; w += NT) {
           const int yr = w / Ws, xr = w - yr * Ws;
           const int o = (yr + s) * W + xr + cx;
-          Lc[o] = d2 * L1[o - W];
+          Lc[o] = d2 * zt[o - W];
         }
       } else {
         // two vertically adjacent points per item (Hs is even), sharing
@@ -1053,8 +1271,9 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
   const int x = tx;
   // the rest of the RHS at one point (src/dynamics.h:55-69) given its
   // Jacobian J and the centred differences dxp = psi_E - psi_W,
-  // dyp = psi_N - psi_S; then the CFL maximum
-  auto finish = [&](int y, T J, T dxp, T dyp) {
+  // dyp = psi_N - psi_S (and, in zeta mode 2, the spectral chain value
+  // hchain at the point); then the CFL maximum
+  auto finish = [&](int y, T J, T dxp, T dyp, T hchain) {
     const int gi = i0 + x, gj = j0 + y;
     // rhs, src/dynamics.h:55-58: -J - beta psi_x + nu lap q + nu_h lap^n psi
     T f = fmaT(m_inv12, J, -(b2d * dxp));
@@ -1062,7 +1281,8 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
       const T lq = fmaT(T(-4), QS(x, y), (QS(x + 1, y) + QS(x - 1, y)) + (QS(x, y + 1) + QS(x, y - 1)));
       f = fmaT(nu_d2, lq, f);
     }
-    if (a.nsweep > 0) f = fmaT(nuh, Lp[(y + R) * W + x + XO], f);
+    if (zm2) f = fmaT(nuhs, hchain, f);
+    else if (a.nsweep > 0) f = fmaT(nuh, Lp[(y + R) * W + x + XO], f);
     // surface wind (src/dynamics.h:66) and bottom drag + topography (:67-69)
     if (k == 0 && a.has_wind) f += a.wind[gj];
     if (bottom) {
@@ -1126,7 +1346,7 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
       J = fmaT(-Q[r - 1][1], P[r - 1][2] - P[r - 1][0], J);
       J = fmaT(-Q[r][2], P[r + 1][2] - P[r - 1][2], J);
       J = fmaT(Q[r][0], P[r + 1][0] - P[r - 1][0], J);
-      finish(y, J, dxp, dyp);
+      finish(y, J, dxp, dyp, hv[h]);
     }
   } else {
     // FP64: centred differences shared between neighbouring Jacobian
@@ -1158,7 +1378,7 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
       J = fmaT(-QS(x, y - 1), DX(dxp, x, y - 1), J);
       J = fmaT(-QS(x + 1, y), DY(dyp, x + 1, y), J);
       J = fmaT(QS(x - 1, y), DY(dyp, x - 1, y), J);
-      finish(y, J, DX(dxp, x, y), DY(dyp, x, y));
+      finish(y, J, DX(dxp, x, y), DY(dyp, x, y), T(0));
     }
   }
 #undef DY
@@ -1168,22 +1388,13 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile(const StepArg
   return mymax_n;
 }
 
-template <typename T, bool COMP, int R>
-__device__ __forceinline__ void body_rhs(const StepArgs<T>& a, int bx, int by, int k, unsigned int total,
-                                         unsigned char* smem_raw, const CUtensorMap* tm,
-                                         unsigned long long* bar, unsigned int* phase) {
-  DevState* st = a.state;
-  if (!st->active) return;
+// End of a block's RHS work: the block's CFL maximum joins the run's
+// (atomicMax on the bits), and the last of `total` blocks to finish runs
+// the time-step update (adjust_timestep, src/timestep.h:74-87).
+__device__ __forceinline__ void rhs_block_done(DevState* st, unsigned long long mymax, unsigned int total,
+                                               double Delta, double cfl) {
   __shared__ unsigned long long wmax[NT / 32];
   __shared__ int is_last;
-  const int i0 = bx * TX, j0 = by * TY;
-  const bool edge = i0 < R || j0 < R || i0 + TX + R > a.nx || j0 + TY + R > a.ny;
-  const int si = st->step_index;
-  bool failed = false;
-  const unsigned long long mymax_w =
-      widen_absbits<T>(edge ? rhs_tile<T, COMP, R, true>(a, i0, j0, k, si, smem_raw, tm, bar, phase, &failed)
-                            : rhs_tile<T, COMP, R, false>(a, i0, j0, k, si, smem_raw, tm, bar, phase, &failed));
-  unsigned long long mymax = mymax_w;
   const int tid = threadIdx.x + threadIdx.y * 32;
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long u = __shfl_xor_sync(0xffffffffu, mymax, o);
@@ -1202,8 +1413,110 @@ __device__ __forceinline__ void body_rhs(const StepArgs<T>& a, int bx, int by, i
   __syncthreads();
   if (is_last && tid == 0) {
     __threadfence();
-    scalar_update(st, a.Delta, a.cfl);
+    scalar_update(st, Delta, cfl);
   }
+}
+
+// the tile at (i0, j0) plus its psi halo R touches a wall (or wraps)
+__device__ __forceinline__ bool rhs_edge_tile(int i0, int j0, int R, int nx, int ny) {
+  return i0 < R || j0 < R || i0 + TX + R > nx || j0 + TY + R > ny;
+}
+
+// The RHS stage of one run: tiles t = blockIdx.x, blockIdx.x + gridDim.x,
+// ... over (x tile, y tile, layer).  NB == 2 (FP32, a persistent grid): two
+// input buffers, the next interior tile's TMA boxes are issued before the
+// current tile is computed, so that its copy overlaps the computation.
+// NB == 1: one tile per block, loaded and then computed.
+template <typename T, bool COMP, int R, int NB>
+__device__ __forceinline__ void body_rhs_tiles(const StepArgs<T>& a, int ntx, int nty, unsigned char* base,
+                                               const CUtensorMap* tm, unsigned long long* bar) {
+  DevState* st = a.state;
+  if (!st->active) return;
+  T* wk = rhs_work<T, R>(base, NB);
+  unsigned int ph[2] = {0u, 0u};
+  const int tid = threadIdx.x + threadIdx.y * 32;
+  const int ntiles = ntx * nty * a.nl;
+  const int si = st->step_index;
+  const int step = (int)gridDim.x;
+  auto tile_of = [&](int t, int& i0, int& j0, int& k) {
+    const int bx = t % ntx, r = t / ntx;
+    i0 = bx * TX;
+    j0 = (r % nty) * TY;
+    k = r / nty;
+  };
+  // prologue: the first tile's boxes into buffer 0
+  if (NB == 2 && tm && tid == 0 && (int)blockIdx.x < ntiles) {
+    int i0, j0, k;
+    tile_of((int)blockIdx.x, i0, j0, k);
+    if (!rhs_edge_tile(i0, j0, R, a.nx, a.ny)) rhs_tile_tma<T, COMP, R>(a, i0, j0, k, rhs_in<T, R>(base, 0), tm, &bar[0]);
+  }
+  decltype(absbits_native(T(0))) mymax = 0;
+  int it = 0;
+  for (int t = (int)blockIdx.x; t < ntiles; t += step, ++it) {
+    const int cur = NB == 2 ? (it & 1) : 0;
+    int i0, j0, k;
+    tile_of(t, i0, j0, k);
+    const bool edge = rhs_edge_tile(i0, j0, R, a.nx, a.ny);
+    const RhsIn<T> in = rhs_in<T, R>(base, cur);
+    if (NB == 2 && tm && tid == 0 && t + step < ntiles) {
+      // the next tile's boxes into the other buffer (last read by the
+      // previous tile, which every thread has finished: the trailing
+      // __syncthreads of the previous iteration)
+      int i1, j1, k1;
+      tile_of(t + step, i1, j1, k1);
+      if (!rhs_edge_tile(i1, j1, R, a.nx, a.ny))
+        rhs_tile_tma<T, COMP, R>(a, i1, j1, k1, rhs_in<T, R>(base, cur ^ 1), tm, &bar[cur ^ 1]);
+    }
+    bool ok = true;
+    if (edge) {
+      rhs_tile_fetch<T, COMP, R, true>(a, i0, j0, k, in);
+    } else if (!tm) {
+      rhs_tile_fetch<T, COMP, R, false>(a, i0, j0, k, in);
+    } else {
+      if (NB == 1 && tid == 0) rhs_tile_tma<T, COMP, R>(a, i0, j0, k, in, tm, &bar[0]);
+      ok = rhs_tile_wait(a, &bar[cur], &ph[cur]);
+    }
+    __syncthreads();
+    if (ok) {
+      const auto m = edge ? rhs_tile_compute<T, COMP, R, true>(a, i0, j0, k, si, in, wk)
+                          : rhs_tile_compute<T, COMP, R, false>(a, i0, j0, k, si, in, wk);
+      mymax = m > mymax ? m : mymax;
+    }
+    __syncthreads();
+  }
+  rhs_block_done(st, widen_absbits<T>(mymax), gridDim.x, a.Delta, a.cfl);
+}
+
+// One RHS tile (bx, by, layer k) of an ensemble member, in one input
+// buffer; `total` blocks share the member's CFL reduction.
+template <typename T, bool COMP, int R>
+__device__ __forceinline__ void body_rhs(const StepArgs<T>& a, int bx, int by, int k, unsigned int total,
+                                         unsigned char* smem_raw, const CUtensorMap* tm,
+                                         unsigned long long* bar, unsigned int* phase) {
+  DevState* st = a.state;
+  if (!st->active) return;
+  const int i0 = bx * TX, j0 = by * TY;
+  const bool edge = rhs_edge_tile(i0, j0, R, a.nx, a.ny);
+  const int si = st->step_index;
+  const int tid = threadIdx.x + threadIdx.y * 32;
+  const RhsIn<T> in = rhs_in<T, R>(smem_raw, 0);
+  T* wk = rhs_work<T, R>(smem_raw, 1);
+  bool ok = true;
+  if (edge) {
+    rhs_tile_fetch<T, COMP, R, true>(a, i0, j0, k, in);
+  } else if (!tm) {
+    rhs_tile_fetch<T, COMP, R, false>(a, i0, j0, k, in);
+  } else {
+    if (tid == 0) rhs_tile_tma<T, COMP, R>(a, i0, j0, k, in, tm, bar);
+    ok = rhs_tile_wait(a, bar, phase);
+  }
+  __syncthreads();
+  decltype(absbits_native(T(0))) mymax = 0;
+  if (ok) {
+    mymax = edge ? rhs_tile_compute<T, COMP, R, true>(a, i0, j0, k, si, in, wk)
+                 : rhs_tile_compute<T, COMP, R, false>(a, i0, j0, k, si, in, wk);
+  }
+  rhs_block_done(st, widen_absbits<T>(mymax), total, a.Delta, a.cfl);
 }
 
 // ------------------------------------------------------- small kernels
@@ -1222,8 +1535,11 @@ static size_t smem_rows(const StepArgs<T>& a) { return (size_t)2 * a.G1 * padded
 template <typename T, bool COMP>
 static size_t smem_cols(const StepArgs<T>& a) {
   // periodic: two complex columns of ny values (padded rows of 2 ny reals)
-  const size_t rows = a.periodic ? 2 : ColsPer<T>::value;
-  return (size_t)((COMP && a.zeta_mode) ? 3 : 2) * rows * padded_len<T>(a.gy.M) * sizeof(T);
+  // in two or three buffers; DST: the pairs [A | C] and [B | D] of CT rows
+  // ([A] and [B] without the second field)
+  const bool zm = COMP && a.zeta_mode;
+  const size_t rows = a.periodic ? (size_t)(zm ? 3 : 2) * 2 : (size_t)(zm ? 4 : 2) * ColsPer<T>::value;
+  return rows * padded_len<T>(a.gy.M) * sizeof(T);
 }
 // column tiles of one mode: four real columns (DST) or two complex columns
 // k = 0..nx/2 (periodic)
@@ -1235,18 +1551,29 @@ template <typename T, bool COMP>
 static size_t smem_rows_inv(const StepArgs<T>& a) {
   return (size_t)((COMP && a.zeta_mode) ? 4 : 2) * a.G3 * padded_len<T>(a.gx.M) * sizeof(T);
 }
+// dynamic shared memory of the RHS kernels for halo radius r and nb input
+// buffers (RhsShape)
 template <typename T>
-static size_t smem_rhs_r(int r) {
-  // rhs_tile's layout: psi and two chain buffers, the q tile, the FP64
-  // centred differences, plus 128 bytes to align the TMA destinations
-  const int HH = TY + 2 * r;
-  const size_t TS = tile_round<T>(TW * HH), QS = tile_round<T>(TW * (TY + 2));
-  return sizeof(T) * (3 * TS + QS + 2 * (TX + 2) * TY + 2 * TX * (TY + 2)) + 128;
+static size_t smem_rhs_r(int r, int nb = 1) {
+  switch (r) {
+    case 1: return RhsShape<T, 1>::bytes(nb);
+    case 2: return RhsShape<T, 2>::bytes(nb);
+    case 3: return RhsShape<T, 3>::bytes(nb);
+    default: return RhsShape<T, 4>::bytes(nb);
+  }
 }
+// halo radius of the RHS tiles: the Laplacian sweeps they run (none in zeta
+// mode 2, where the whole chain is spectral), at least 1 (the Jacobian)
 template <typename T>
-static int rhs_halo(const StepArgs<T>& a) { return a.nsweep > 0 ? a.nsweep : 1; }
+static int rhs_halo(const StepArgs<T>& a) { return (a.nsweep > 0 && a.zeta_mode != 2) ? a.nsweep : 1; }
 template <typename T>
 static size_t smem_rhs(const StepArgs<T>& a) { return smem_rhs_r<T>(rhs_halo(a)); }
+// input buffers of the single-run RHS kernel: FP32 double-buffers its
+// persistent loop, FP64 runs one tile per block
+template <typename T>
+constexpr int rhs_nbuf() { return sizeof(T) == 4 ? 2 : 1; }
+template <typename T>
+static size_t smem_rhs_tiles(const StepArgs<T>& a) { return smem_rhs_r<T>(rhs_halo(a), rhs_nbuf<T>()); }
 
 constexpr int RHS_RMAX = 4;  // n_hyper <= 6
 

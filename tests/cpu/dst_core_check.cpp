@@ -21,8 +21,8 @@ static void run(int M, int howmany, T* data) {
   for (int r = 0; r < howmany; ++r) {
     T* x = data + (size_t)r * (M - 1);
     for (size_t j = 0; j < A.size(); ++j) A[j] = B[j] = T(777);  // pad slots must never be read
-    for (int j = 0; j < M - 1; ++j) A[pr<T>(j)] = x[j];
-    A[pr<T>(M - 1)] = T(12345);  // padding must never be read
+    for (int j = 0; j < M - 1; ++j) A[pr<T>(j + 1)] = x[j];      // x_j at index j
+    A[pr<T>(0)] = T(12345);  // index 0 must never be read
     for (int j = 1; j <= g.H; ++j) dst_pre_item<T>(A.data(), B.data(), j, g, PRE);
     T* src = B.data();
     T* dst = A.data();
@@ -43,7 +43,7 @@ static void run(int M, int howmany, T* data) {
       if (c > 0) dst_scan_fix<T>(dst, c, pref, g);
       pref += tot[c];
     }
-    for (int j = 0; j < M - 1; ++j) x[j] = dst[pr<T>(j)];
+    for (int j = 0; j < M - 1; ++j) x[j] = dst[pr<T>(j + 1)];  // Y_k at index k
   }
 }
 
