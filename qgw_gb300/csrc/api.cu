@@ -15,6 +15,7 @@
 
 #include "../../include/qgw_gpu.h"
 #include "dst_tables.h"
+#include "dst_warp.h"
 #include "host.h"
 #include "kernels.h"
 #include "qgw_device.cuh"
@@ -96,10 +97,10 @@ int inv_group(int zeta, int M, int nl) {
 }
 
 // Modes (layers) per block of a row kernel: as many as the budget holds (each
-// takes rows_per_mode rows in each of the two DST work buffers), at most
+// takes rows_per_mode rows in each of the bufs DST work buffers), at most
 // gmax and at most want, then balanced over the resulting number of groups.
-int mode_group(int nl, int M, size_t elem, size_t budget, int rows_per_mode, int gmax, int want) {
-  int g = (int)(budget / (2 * (size_t)rows_per_mode * (elem == 4 ? qgw::padded_len<float>(M) : qgw::padded_len<double>(M)) * elem));
+int mode_group(int nl, int M, size_t elem, size_t budget, int rows_per_mode, int gmax, int want, int bufs = 2) {
+  int g = (int)(budget / (bufs * (size_t)rows_per_mode * (elem == 4 ? qgw::padded_len<float>(M) : qgw::padded_len<double>(M)) * elem));
   if (g > want) g = want;
   if (g > gmax) g = gmax;
   if (g < 1) g = 1;
@@ -182,18 +183,22 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   for (int dim = 0; dim < 2; ++dim) {
     const int M = dim == 0 ? Mx : My;
     qgw::DstTablesHost th = qgw::build_dst_tables(M);
-    T *tw, *pre, *spl, *twp, *sj;
+    T *tw, *pre, *spl, *twp, *sj, *twd, *sjp;
     if ((rc = upload<T>(r, &tw, th.tw))) return rc;
     if ((rc = upload<T>(r, &pre, th.pre))) return rc;
     if ((rc = upload<T>(r, &spl, th.spl))) return rc;
     if ((rc = upload<T>(r, &twp, th.twp))) return rc;
     if ((rc = upload<T>(r, &sj, th.sj))) return rc;
+    if ((rc = upload<T>(r, &twd, th.twd))) return rc;
+    if ((rc = upload<T>(r, &sjp, th.sjp))) return rc;
     qgw::DstTables<T>& t = dim == 0 ? a.tx : a.ty;
     t.tw = (const qgw::C2<T>*)tw;
     t.pre = (const qgw::C2<T>*)pre;
     t.spl = (const qgw::C2<T>*)spl;
     t.twp = (const qgw::C2<T>*)twp;
     t.sj = sj;
+    t.twd = (const qgw::C2<T>*)twd;
+    t.sjp = (const qgw::C2<T>*)sjp;
   }
   T *cl, *cm;
   if ((rc = upload<T>(r, &cl, r->cl2m))) return rc;
@@ -284,16 +289,18 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   a.topo_fac = p.f0 / dhb;
   a.has_topo = 0;
   a.has_wind = p.tau0 != 0;
+  // work buffers per row of the row kernels' transforms (one: in place)
+  const int bufs_x = (!per && qgw::warp_dst_len(Mx / 2, (int)sizeof(T))) ? 1 : 2;
   {
     // QGW_ROW_GROUP overrides the modes per forward-rows block (tuning knob)
     const char* e = std::getenv("QGW_ROW_GROUP");
     const int want = e ? std::atoi(e) : 0;
     const size_t budget = row_budget(sizeof(T), Mx, r->nl);
-    if (want >= 1 && want <= 16) a.G1 = mode_group(r->nl, Mx, sizeof(T), budget, 1, 16, want);
+    if (want >= 1 && want <= 16) a.G1 = mode_group(r->nl, Mx, sizeof(T), budget, 1, 16, want, bufs_x);
     else if (sizeof(T) == 8) a.G1 = mode_group_fma(r->nl, Mx, sizeof(T), budget, 16);
-    else a.G1 = mode_group(r->nl, Mx, sizeof(T), budget, 1, 16, 16);
+    else a.G1 = mode_group(r->nl, Mx, sizeof(T), budget, 1, 16, 16, bufs_x);
   }
-  a.G3 = mode_group(r->nl, Mx, sizeof(T), 110 * 1024, 1, 16, inv_group(0, Mx, r->nl));
+  a.G3 = mode_group(r->nl, Mx, sizeof(T), 110 * 1024, 1, 16, inv_group(0, Mx, r->nl), bufs_x);
   a.CT = 0;
   a.low_k64 = 8;
   // 16-byte column vectors: rows 16-byte aligned and a whole number of
@@ -325,7 +332,7 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
     if ((rc = dalloc(r, &a.spec2, field))) return rc;
     if ((rc = dalloc(r, &a.zeta, field))) return rc;
     // K3 transforms psi and zeta rows of each mode: two rows per mode
-    a.G3 = mode_group(r->nl, Mx, sizeof(T), 110 * 1024, 2, 8, inv_group(1, Mx, r->nl));
+    a.G3 = mode_group(r->nl, Mx, sizeof(T), 110 * 1024, 2, 8, inv_group(1, Mx, r->nl), bufs_x);
     // symbol of the 5-point Laplacian: DST-I basis sin^2(pi k / 2(n+1));
     // periodic Fourier basis sin^2(pi k / N)
     std::vector<double> sx(r->nx, 0.0), sy(r->ny);

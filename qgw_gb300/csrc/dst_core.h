@@ -151,6 +151,8 @@ template <typename T> struct DstTables {
   const C2<T>* spl;
   const C2<T>* twp;
   const T* sj;  // s_j = sin(pi j/M), j <= H (the merged pre-processing pass)
+  const C2<T>* twd;  // the one-warp transform (dst_warp.h, H = 256, 512): DIF twiddles
+  const C2<T>* sjp;  // and (s_{2m}, s_{2m+1}), m < H
 };
 
 // Work-item loop of a block over nrows rows of n items each: f(r, i) for

@@ -20,6 +20,7 @@
 #pragma once
 
 #include "dst_core.h"
+#include "dst_warp.h"
 
 namespace qgw {
 
@@ -75,8 +76,17 @@ struct StockhamItem {
       else if constexpr (R == 4) dft4(v);
       else dft2(v);
     }
+    if constexpr (sizeof(T) == 4 && NS == 1) {
+      // first pass: outputs R b .. R b + R - 1 lie in one pad period and
+      // start 16-byte aligned -- 16-byte stores (8-byte ones at stride R
+      // would meet bank conflicts)
 #pragma unroll
-    for (int q = 0; q < R; ++q) dst[out0 + pco(q * NS)] = v[q];
+      for (int q = 0; q < R; q += 2)
+        *reinterpret_cast<float4*>(dst + out0 + q) = make_float4(v[q].x, v[q].y, v[q + 1].x, v[q + 1].y);
+    } else {
+#pragma unroll
+      for (int q = 0; q < R; ++q) dst[out0 + pco(q * NS)] = v[q];
+    }
   }
 };
 
@@ -175,15 +185,29 @@ struct PrePassItem {
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
       const int o = pro(q * (H / 4));
-      const T xa = x[a0 + o], xb = x[a0 + o + 1];  // x_{2m}, x_{2m+1}
+      // x_{2m}, x_{2m+1}: one aligned pair (2m is even, and an even index
+      // and the next share a pad period)
+      const C2<T> xp = *reinterpret_cast<const C2<T>*>(x + a0 + o);
+      const T xa = xp.x, xb = xp.y;
       const T ya = x[m0 - o], yb = x[m1 - o];      // x_{M-2m}, x_{M-2m-1}
       const T y0 = fmaT(s[q][0], xa + ya, T(0.5) * (xa - ya));
       v[q].x = (q == 0 && first) ? T(0) : y0;
       v[q].y = fmaT(s[q][1], xb + yb, T(0.5) * (xb - yb));
     }
     dft8(v);
+    // outputs 8b .. 8b+7 lie in one pad period and start 16-byte aligned:
+    // four 16-byte stores (eight 8-byte ones at stride 8 would meet 2-way
+    // bank conflicts in each half-warp)
 #pragma unroll
-    for (int q = 0; q < 8; ++q) dst[out0 + q] = v[q];
+    for (int q = 0; q < 8; q += 2) store_pair(dst + out0 + q, v[q], v[q + 1]);
+  }
+  __device__ __forceinline__ static void store_pair(C2<T>* p, C2<T> a, C2<T> b) {
+    if constexpr (sizeof(T) == 4) {
+      *reinterpret_cast<float4*>(p) = make_float4(a.x, a.y, b.x, b.y);
+    } else {
+      p[0] = a;
+      p[1] = b;
+    }
   }
 };
 
@@ -218,36 +242,17 @@ __device__ __forceinline__ void pre_pass1_fixed(const T* src, T* dst, int nrows,
 // 16-byte complex pairs; the hi pairs start at even indices, so each lane
 // stores its pairs H-k0-KPL .. H-k0-1, the first element taken from the next
 // lane (lane 31 from lane 0's k = H/2 item).
+// The split and prefix sum of one row by one warp from the lane's inputs
+// Zl[t] = Z_{k0+t}, Zh[t] = Z_{H-k0-t} (k0 = KPL lane; lane 0's Zh[0] =
+// Z_{H/2}) and split constants cs[t] = spl[k0 + t] (lane 0's cs[0] =
+// spl[H/2]); writes Y_k at index k of orow.  The row's inputs have all been
+// read (the caller synchronises the warp when orow is the input row).
 template <int H>
-__device__ __forceinline__ void split_scan_warp_f32(const float* src, float* dst, int nrows, int ld,
-                                                    const C2<float>* __restrict__ spl) {
+__device__ __forceinline__ void split_scan_lane_f32(int lane, const C2<float>* Zl, const C2<float>* Zh,
+                                                    const C2<float>* cs, float* orow) {
   constexpr int KPL = H / 64;
-  static_assert(KPL == 2 || KPL == 4 || KPL == 8, "H = 128, 256 or 512");
-  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
-  const int warp = tid >> 5, lane = tid & 31, nwarp = DST_NT >> 5;
   const int k0 = KPL * lane;
-  C2<float> cs[KPL];
-#pragma unroll
-  for (int t = 0; t < KPL; ++t) cs[t] = spl[(lane == 0 && t == 0) ? H / 2 : k0 + t];
-  const int hs = lane == 0 ? pc<float>(H / 2) : pc<float>(H - k0);  // t = 0 mirror (or k = H/2)
-  for (int r = warp; r < nrows; r += nwarp) {
-    const C2<float>* Z = (const C2<float>*)(src + r * ld);
-    float* orow = dst + r * ld;
-    C2<float> Zl[KPL], Zh[KPL];
-#pragma unroll
-    for (int p = 0; p < KPL / 2; ++p) {
-      // an even index and the next share a pad period: one 16-byte pair
-      const float4 u = *reinterpret_cast<const float4*>(Z + pc<float>(k0 + 2 * p));
-      Zl[2 * p].x = u.x; Zl[2 * p].y = u.y; Zl[2 * p + 1].x = u.z; Zl[2 * p + 1].y = u.w;
-    }
-#pragma unroll
-    for (int p = 0; p < KPL / 2; ++p) {
-      const int e = H - k0 - KPL + 2 * p;
-      const float4 u = *reinterpret_cast<const float4*>(Z + pc<float>(e));
-      if (p > 0) { Zh[KPL - 2 * p].x = u.x; Zh[KPL - 2 * p].y = u.y; }
-      Zh[KPL - 2 * p - 1].x = u.z; Zh[KPL - 2 * p - 1].y = u.w;
-    }
-    Zh[0] = Z[hs];
+  {
     C2<float> lo[KPL], hi[KPL];
 #pragma unroll
     for (int t = 0; t < KPL; ++t) {
@@ -319,6 +324,97 @@ __device__ __forceinline__ void split_scan_warp_f32(const float* src, float* dst
       *reinterpret_cast<float4*>(orow + 2 * pc<float>(H - k0 - KPL + 2 * p)) = make_float4(e0.x, e0.y, e1.x, e1.y);
     }
   }
+}
+
+template <int H>
+__device__ __forceinline__ void split_scan_warp_f32(const float* src, float* dst, int nrows, int ld,
+                                                    const C2<float>* __restrict__ spl) {
+  constexpr int KPL = H / 64;
+  static_assert(KPL == 2 || KPL == 4 || KPL == 8, "H = 128, 256 or 512");
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+  const int warp = tid >> 5, lane = tid & 31, nwarp = DST_NT >> 5;
+  const int k0 = KPL * lane;
+  C2<float> cs[KPL];
+#pragma unroll
+  for (int t = 0; t < KPL; ++t) cs[t] = spl[(lane == 0 && t == 0) ? H / 2 : k0 + t];
+  const int hs = lane == 0 ? pc<float>(H / 2) : pc<float>(H - k0);  // t = 0 mirror (or k = H/2)
+  for (int r = warp; r < nrows; r += nwarp) {
+    const C2<float>* Z = (const C2<float>*)(src + r * ld);
+    C2<float> Zl[KPL], Zh[KPL];
+#pragma unroll
+    for (int p = 0; p < KPL / 2; ++p) {
+      // an even index and the next share a pad period: one 16-byte pair
+      const float4 u = *reinterpret_cast<const float4*>(Z + pc<float>(k0 + 2 * p));
+      Zl[2 * p].x = u.x; Zl[2 * p].y = u.y; Zl[2 * p + 1].x = u.z; Zl[2 * p + 1].y = u.w;
+    }
+#pragma unroll
+    for (int p = 0; p < KPL / 2; ++p) {
+      const int e = H - k0 - KPL + 2 * p;
+      const float4 u = *reinterpret_cast<const float4*>(Z + pc<float>(e));
+      if (p > 0) { Zh[KPL - 2 * p].x = u.x; Zh[KPL - 2 * p].y = u.y; }
+      Zh[KPL - 2 * p - 1].x = u.z; Zh[KPL - 2 * p - 1].y = u.w;
+    }
+    Zh[0] = Z[hs];
+    split_scan_lane_f32<H>(lane, Zl, Zh, cs, dst + r * ld);
+  }
+}
+
+// One row's DST-I by one warp, in place (dst_warp.h): pre-processing with
+// the first DIF pass, two more passes, then the split with the prefix sum.
+// x_{M-2m} of a pass-1 member comes from the previous member's mirror pair
+// by one shuffle per member: from lane - 1, and for lane 0 from lane 31 at
+// the previous member in (n2, u) order (the value the shuffle of the
+// previous iteration delivered).
+template <int LGH>
+__device__ __forceinline__ void dst_row_warp_f32(float* row, const DstTables<float>& tb, int lane) {
+  using W = WarpDst<LGH>;
+  C2<float>* Z = reinterpret_cast<C2<float>*>(row);
+  C2<float> v[W::IPL][8];
+  {
+    float prev = 0.f;
+#pragma unroll
+    for (int n2 = 0; n2 < 8; ++n2)
+#pragma unroll
+      for (int u = 0; u < W::IPL; ++u) {
+        const int m = lane + 32 * u + W::S0 * n2;
+        C2<float> own, mir;
+        W::p1_read(m, Z, own, mir);
+        const float got = __shfl_sync(0xffffffffu, mir.x, (lane + 31) & 31);
+        const float xm = lane > 0 ? got : prev;  // (lane 0, m = 0): x_M, enters only y_0 = 0
+        prev = got;
+        v[u][n2] = W::p1_pre(m, own, xm, mir.y, tb.sjp[m]);
+      }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int u = 0; u < W::IPL; ++u) W::p1_fft(lane + 32 * u, v[u], tb.twd, Z);
+  __syncwarp();
+#pragma unroll
+  for (int u = 0; u < W::IPL; ++u) W::p2(lane + 32 * u, tb.twd, Z);
+  __syncwarp();
+#pragma unroll
+  for (int u = 0; u < 2; ++u) W::p3(lane + 32 * u, Z);
+  __syncwarp();
+  C2<float> Zl[W::KPL], Zh[W::KPL], cs[W::KPL];
+  W::split_read(lane, Z, Zl, Zh);
+  const int k0 = W::KPL * lane;
+#pragma unroll
+  for (int t = 0; t < W::KPL; ++t) cs[t] = tb.spl[(lane == 0 && t == 0) ? W::H / 2 : k0 + t];
+  __syncwarp();
+  split_scan_lane_f32<W::H>(lane, Zl, Zh, cs, row);
+  __syncwarp();
+}
+
+// DST-I of nrows raw rows in A by one warp per row, in place; the caller
+// has synchronised the block since the rows were written, and the block is
+// synchronised again before the result (in A) is returned.
+template <int LGH>
+__device__ float* dst_block_warp_f32(float* A, int nrows, int ld, const DstTables<float>& tb) {
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+  const int warp = tid >> 5, lane = tid & 31, nwarp = DST_NT >> 5;
+  for (int r = warp; r < nrows; r += nwarp) dst_row_warp_f32<LGH>(A + r * ld, tb, lane);
+  __syncthreads();
+  return A;
 }
 
 // DST-I of nrows raw rows in A (x_j at index j), B the second buffer;

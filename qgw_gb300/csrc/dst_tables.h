@@ -24,6 +24,9 @@ inline double cospi_frac(long m, long N) { return sinpi_frac(2 * m + N, 2 * N); 
 struct DstTablesHost {
   std::vector<double> tw, pre, spl, twp;  // interleaved (x, y) pairs
   std::vector<double> sj;                 // sin(pi j / M), j = 0..H
+  // the warp transform's tables (H = 256, 512; one dummy pair otherwise):
+  std::vector<double> twd;  // DIF twiddles: w_H^(n1 k2) at (k2-1) S0 + n1, then w_H^(8 n1 k2) at 7 S0 + (k2-1) S1 + n1
+  std::vector<double> sjp;  // (s_{2m}, s_{2m+1}), m < H
 };
 
 // tw: H entries, twp: H - R0 entries, pre: H+1 entries, spl: H/2+1 entries
@@ -51,6 +54,30 @@ inline DstTablesHost build_dst_tables(int M) {
   for (int k = 0; k <= H / 2; ++k) {
     t.spl[2 * k] = cospi_frac(2L * k, M);
     t.spl[2 * k + 1] = sinpi_frac(2L * k, M);
+  }
+  t.twd.assign(2, 0.0);
+  t.sjp.assign(2, 0.0);
+  if (H == 256 || H == 512) {
+    const int S0 = H / 8, S1 = H / 64;
+    t.twd.assign(2 * (size_t)7 * (S0 + S1), 0.0);
+    for (int k2 = 1; k2 < 8; ++k2) {
+      for (int n1 = 0; n1 < S0; ++n1) {
+        const int e = (k2 - 1) * S0 + n1, m = (n1 * k2) % H;
+        t.twd[2 * e] = t.tw[2 * m];
+        t.twd[2 * e + 1] = t.tw[2 * m + 1];
+      }
+      for (int n1 = 0; n1 < S1; ++n1) {
+        const int e = 7 * S0 + (k2 - 1) * S1 + n1, m = (8 * n1 * k2) % H;
+        t.twd[2 * e] = t.tw[2 * m];
+        t.twd[2 * e + 1] = t.tw[2 * m + 1];
+      }
+    }
+    t.sjp.resize(2 * (size_t)H);
+    for (int m = 0; m < H; ++m) {
+      const int j0 = 2 * m, j1 = 2 * m + 1;
+      t.sjp[2 * m] = t.sj[j0 <= H ? j0 : M - j0];
+      t.sjp[2 * m + 1] = t.sj[j1 <= H ? j1 : M - j1];
+    }
   }
   return t;
 }

@@ -45,7 +45,8 @@ constexpr double HUGEV = 1e30;   // src/qg.c:43
 // columns per block of the column kernel (one or two 16-byte vectors per row):
 // four, so that the three work buffers of the compensated path leave room
 // for four blocks per SM
-template <typename T> struct ColsPer { static constexpr int value = 4; };
+// columns per K2 tile: 32-byte rows of FP32 (8) and FP64 (4) values
+template <typename T> struct ColsPer { static constexpr int value = 32 / (int)sizeof(T); };
 
 // --------------------------------------------------------------- DST block
 // Batched DST-I of nrows rows (row r at A + r*ld, padded input format) by
@@ -97,16 +98,21 @@ __device__ __forceinline__ T* dst_block_generic(T* A, T* B, int nrows, int ld, c
 }
 
 // Block DST of any supported length: the power-of-two lengths M = 128..2048
-// use the compile-time specialisations of dst_fixed.cuh, others (mixed
-// radix 2, 3, 5, 7) the generic loops.
+// use the compile-time specialisations of dst_fixed.cuh (FP32 M = 512 and
+// 1024: one warp per row, in place, the result in A), others (mixed radix
+// 2, 3, 5, 7) the generic loops.
 template <typename T>
 __device__ __forceinline__ T* dst_block(T* A, T* B, int nrows, int ld, const DstGeom& g, const DstTables<T>& tb,
                                         T* tot) {
   switch (g.H) {
     case 64: return dst_block_fixed<T, 6>(A, B, nrows, ld, tb);
     case 128: return dst_block_fixed<T, 7>(A, B, nrows, ld, tb);
-    case 256: return dst_block_fixed<T, 8>(A, B, nrows, ld, tb);
-    case 512: return dst_block_fixed<T, 9>(A, B, nrows, ld, tb);
+    case 256:
+      if constexpr (sizeof(T) == 4) return dst_block_warp_f32<8>(A, nrows, ld, tb);
+      else return dst_block_fixed<T, 8>(A, B, nrows, ld, tb);
+    case 512:
+      if constexpr (sizeof(T) == 4) return dst_block_warp_f32<9>(A, nrows, ld, tb);
+      else return dst_block_fixed<T, 9>(A, B, nrows, ld, tb);
     case 1024: return dst_block_fixed<T, 10>(A, B, nrows, ld, tb);
     default: return dst_block_generic<T>(A, B, nrows, ld, g, tb, tot);
   }
@@ -560,17 +566,20 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
   prefetch_tables_l1(a.ty, a.gy.M);
   // 16-byte vectors need 16-byte aligned rows (vec_cols); the last tile then
   // reads the padding column (index nx < pitch), never past the row.  RB
-  // rows per pass, all their loads in flight before any store (FP32 four,
-  // FP64 two: its rows take twice the registers); streaming loads (the tile
-  // is read once), which leave L1 to the tables.
-  constexpr int RB = sizeof(T) == 4 ? 4 : 2;
+  // rows per pass, all their loads in flight before any store (two 32-byte
+  // rows); streaming loads (the tile is read once), which leave L1 to the
+  // tables.
+  constexpr int RB = 2;
+  // Thread t takes the points jj = t - 1 + u NT (tile index jj + 1 = t +
+  // u NT), so that each warp's shared-memory accesses cover whole 128-byte
+  // pad periods (one wavefront per access).
   const bool vec = a.vec_cols != 0;
-  for (int j0 = threadIdx.x; j0 < ny; j0 += RB * NT) {
+  for (int j0 = threadIdx.x - 1; j0 < ny; j0 += RB * NT) {
     T vv[RB][CT];
 #pragma unroll
     for (int u = 0; u < RB; ++u) {
       const int jj = j0 + u * NT;
-      if (jj < ny) {
+      if (jj >= 0 && jj < ny) {
         const T* src = S + (size_t)jj * a.pitch + k0;
         if (vec) load_cols_stream<T, CT>(src, vv[u]);
         else
@@ -580,7 +589,7 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
 #pragma unroll
     for (int u = 0; u < RB; ++u) {
       const int jj = j0 + u * NT;
-      if (jj < ny) {
+      if (jj >= 0 && jj < ny) {
         const int pj = pr<T>(jj + 1);
 #pragma unroll
         for (int c = 0; c < CT; ++c) A[c * ld + pj] = vv[u][c];
@@ -597,22 +606,21 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
   const float ird2f = COMP ? a.iRd2f[m] : 0.f;
   const float normf = a.fc[FC_NORM], lx2f = a.fc[FC_LX2], ly2f = a.fc[FC_LY2];
   // the tile's per-column table values, the same for every row
-  int kc[CT];
   float lsqc[CT], sxc[CT];
 #pragma unroll
   for (int c = 0; c < CT; ++c) {
-    kc[c] = min(k0 + c, a.nx - 1);
-    lsqc[c] = COMP ? a.Lsqf[kc[c]] : 0.f;
-    sxc[c] = zm ? a.sx2f[kc[c]] : 0.f;
+    const int k = min(k0 + c, a.nx - 1);
+    lsqc[c] = COMP ? a.Lsqf[k] : 0.f;
+    sxc[c] = zm ? a.sx2f[k] : 0.f;
   }
   // RB rows per pass, their per-row loads issued before any is used
-  for (int j0 = threadIdx.x; j0 < ny; j0 += RB * NT) {
+  for (int j0 = threadIdx.x - 1; j0 < ny; j0 += RB * NT) {
     T h4[RB][CT];
     float ksq4[RB], sy4[RB];
 #pragma unroll
     for (int u = 0; u < RB; ++u) {
       const int jj = j0 + u * NT;
-      if (jj >= ny) continue;
+      if (jj < 0 || jj >= ny) continue;
       if (!COMP) {
         const T* hrow = (const T*)(a.hinv + (size_t)m * a.lstride + (size_t)jj * a.pitch + k0);
         if (vec) load_cols<T, CT>(hrow, h4[u]);
@@ -626,7 +634,7 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
 #pragma unroll
     for (int u = 0; u < RB; ++u) {
       const int jj = j0 + u * NT;
-      if (jj >= ny) continue;
+      if (jj < 0 || jj >= ny) continue;
       const int pj = pr<T>(jj + 1);
       if (!COMP) {
 #pragma unroll
@@ -634,7 +642,7 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
       } else {
 #pragma unroll
         for (int c = 0; c < CT; ++c) {
-          const int k = kc[c];
+          const int k = min(k0 + c, a.nx - 1);
           float x;
           if (m == 0 && jj < a.low_k64 && k < a.low_k64) {
             // barotropic mode, lowest wavenumbers: divide in FP64
@@ -665,7 +673,8 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
   T* O2 = dst_block<T>(O, Oth, zm ? 2 * CT : CT, ld, a.gy, a.ty, tot);
   T* S2 = zm ? a.spec2 + (size_t)m * a.lstride : nullptr;
   T v[CT];
-  for (int jj = threadIdx.x; jj < ny; jj += NT) {
+  for (int jj = threadIdx.x - 1; jj < ny; jj += NT) {
+    if (jj < 0) continue;
     const int pj = pr<T>(jj + 1);
 #pragma unroll
     for (int c = 0; c < CT; ++c) v[c] = c < CTb ? O2[c * ld + pj] : T(0);
@@ -1433,7 +1442,9 @@ __device__ __forceinline__ void body_rhs_tiles(const StepArgs<T>& a, int ntx, in
   DevState* st = a.state;
   if (!st->active) return;
   T* wk = rhs_work<T, R>(base, NB);
-  unsigned int ph[2] = {0u, 0u};
+  // mbarrier parities of the two buffers (two scalars: an array indexed by
+  // the loop's buffer number would live in local memory)
+  unsigned int ph0 = 0u, ph1 = 0u;
   const int tid = threadIdx.x + threadIdx.y * 32;
   const int ntiles = ntx * nty * a.nl;
   const int si = st->step_index;
@@ -1474,7 +1485,7 @@ __device__ __forceinline__ void body_rhs_tiles(const StepArgs<T>& a, int ntx, in
       rhs_tile_fetch<T, COMP, R, false>(a, i0, j0, k, in);
     } else {
       if (NB == 1 && tid == 0) rhs_tile_tma<T, COMP, R>(a, i0, j0, k, in, tm, &bar[0]);
-      ok = rhs_tile_wait(a, &bar[cur], &ph[cur]);
+      ok = cur ? rhs_tile_wait(a, &bar[1], &ph1) : rhs_tile_wait(a, &bar[0], &ph0);
     }
     __syncthreads();
     if (ok) {
@@ -1530,15 +1541,24 @@ __device__ __forceinline__ void begin_state(DevState* st, double t_out, double t
   st->active = ((tend > 0 && !(st->t < tend)) || max_steps < 0) ? 0 : 1;
 }
 
+// work buffers of the transforms: two per row, one where the transform runs
+// in place (the one-warp DST)
+template <typename T>
+static int dst_bufs(const StepArgs<T>& a, const DstGeom& g) {
+  return (!a.periodic && warp_dst_len(g.H, (int)sizeof(T))) ? 1 : 2;
+}
 template <typename T, bool COMP>
-static size_t smem_rows(const StepArgs<T>& a) { return (size_t)2 * a.G1 * padded_len<T>(a.gx.M) * sizeof(T); }
+static size_t smem_rows(const StepArgs<T>& a) {
+  return (size_t)dst_bufs(a, a.gx) * a.G1 * padded_len<T>(a.gx.M) * sizeof(T);
+}
 template <typename T, bool COMP>
 static size_t smem_cols(const StepArgs<T>& a) {
   // periodic: two complex columns of ny values (padded rows of 2 ny reals)
   // in two or three buffers; DST: the pairs [A | C] and [B | D] of CT rows
   // ([A] and [B] without the second field)
   const bool zm = COMP && a.zeta_mode;
-  const size_t rows = a.periodic ? (size_t)(zm ? 3 : 2) * 2 : (size_t)(zm ? 4 : 2) * ColsPer<T>::value;
+  const size_t rows = a.periodic ? (size_t)(zm ? 3 : 2) * 2
+                                 : (size_t)(zm ? 2 : 1) * dst_bufs(a, a.gy) * ColsPer<T>::value;
   return rows * padded_len<T>(a.gy.M) * sizeof(T);
 }
 // column tiles of one mode: four real columns (DST) or two complex columns
@@ -1549,7 +1569,7 @@ static int col_tiles(const StepArgs<T>& a) {
 }
 template <typename T, bool COMP>
 static size_t smem_rows_inv(const StepArgs<T>& a) {
-  return (size_t)((COMP && a.zeta_mode) ? 4 : 2) * a.G3 * padded_len<T>(a.gx.M) * sizeof(T);
+  return (size_t)((COMP && a.zeta_mode) ? 2 : 1) * dst_bufs(a, a.gx) * a.G3 * padded_len<T>(a.gx.M) * sizeof(T);
 }
 // dynamic shared memory of the RHS kernels for halo radius r and nb input
 // buffers (RhsShape)

@@ -5,6 +5,7 @@
 #include <vector>
 #include <cstring>
 #include "../../qgw_gb300/csrc/dst_tables.h"
+#include "../../qgw_gb300/csrc/dst_warp.h"
 
 using namespace qgw;
 
@@ -45,6 +46,85 @@ static void run(int M, int howmany, T* data) {
     }
     for (int j = 0; j < M - 1; ++j) x[j] = dst[pr<T>(j + 1)];  // Y_k at index k
   }
+}
+
+// The one-warp transform (dst_warp.h) with its 32 lanes run one after the
+// other inside each phase, every phase's reads done before its writes where
+// the device code synchronises the warp in between; the lane-to-lane value
+// of pass 1 (x_{M-2m}) taken as the device's shuffle delivers it.  The
+// split's inputs are read through WarpDst::split_read (the digit-reversed
+// positions) into a natural-order row, which the split and scan items of
+// dst_core.h finish.
+template <int LGH>
+static void run_warp(int howmany, float* data) {
+  using W = WarpDst<LGH>;
+  constexpr int H = W::H, M = W::M, IPL = W::IPL, KPL = W::KPL;
+  DstGeom g = make_geom(M);
+  DstTablesHost th = build_dst_tables(M);
+  std::vector<float> twd(th.twd.begin(), th.twd.end()), sjp(th.sjp.begin(), th.sjp.end()),
+      spl(th.spl.begin(), th.spl.end());
+  const C2<float>* TWD = (const C2<float>*)twd.data();
+  const C2<float>* SJP = (const C2<float>*)sjp.data();
+  const C2<float>* SPL = (const C2<float>*)spl.data();
+  const int L = padded_len<float>(M);
+  std::vector<F4> Abuf((L + 3) / 4), Bbuf((L + 3) / 4), Cbuf((L + 3) / 4);
+  float* A = (float*)Abuf.data();
+  float* B = (float*)Bbuf.data();
+  float* Cr = (float*)Cbuf.data();
+  static C2<float> own[32][IPL][8], mir[32][IPL][8], v[32][IPL][8];
+  for (int r = 0; r < howmany; ++r) {
+    float* x = data + (size_t)r * (M - 1);
+    for (int j = 0; j < L; ++j) A[j] = B[j] = Cr[j] = 777.f;  // pad slots must never be read
+    for (int j = 0; j < M - 1; ++j) A[pr<float>(j + 1)] = x[j];
+    A[pr<float>(0)] = 12345.f;  // index 0 must never be read
+    C2<float>* Z = (C2<float>*)A;
+    for (int lane = 0; lane < 32; ++lane)
+      for (int n2 = 0; n2 < 8; ++n2)
+        for (int u = 0; u < IPL; ++u) W::p1_read(lane + 32 * u + W::S0 * n2, Z, own[lane][u][n2], mir[lane][u][n2]);
+    for (int lane = 0; lane < 32; ++lane) {
+      float prev = 0.f;
+      for (int n2 = 0; n2 < 8; ++n2)
+        for (int u = 0; u < IPL; ++u) {
+          const int m = lane + 32 * u + W::S0 * n2;
+          const float got = mir[(lane + 31) & 31][u][n2].x;  // __shfl_sync(.., (lane + 31) & 31)
+          const float xm = lane > 0 ? got : prev;
+          prev = got;
+          v[lane][u][n2] = W::p1_pre(m, own[lane][u][n2], xm, mir[lane][u][n2].y, SJP[m]);
+        }
+    }
+    for (int lane = 0; lane < 32; ++lane)
+      for (int u = 0; u < IPL; ++u) W::p1_fft(lane + 32 * u, v[lane][u], TWD, Z);
+    for (int lane = 0; lane < 32; ++lane)
+      for (int u = 0; u < IPL; ++u) W::p2(lane + 32 * u, TWD, Z);
+    for (int lane = 0; lane < 32; ++lane)
+      for (int u = 0; u < 2; ++u) W::p3(lane + 32 * u, Z);
+    C2<float>* N = (C2<float>*)B;
+    for (int lane = 0; lane < 32; ++lane) {
+      C2<float> Zl[KPL], Zh[KPL];
+      W::split_read(lane, Z, Zl, Zh);
+      for (int t = 0; t < KPL; ++t) {
+        N[pc<float>(KPL * lane + t)] = Zl[t];
+        N[pc<float>((lane == 0 && t == 0) ? H / 2 : H - KPL * lane - t)] = Zh[t];
+      }
+    }
+    for (int k = 0; k <= H / 2; ++k) dst_split_item<float>((const C2<float>*)B, Cr, k, g, SPL);
+    std::vector<float> tot(g.nchunk);
+    for (int c = 0; c < g.nchunk; ++c) tot[c] = dst_scan_chunk<float>(Cr, c, g);
+    float pref = 0.f;
+    for (int c = 0; c < g.nchunk; ++c) {
+      if (c > 0) dst_scan_fix<float>(Cr, c, pref, g);
+      pref += tot[c];
+    }
+    for (int j = 0; j < M - 1; ++j) x[j] = Cr[pr<float>(j + 1)];
+  }
+}
+
+// the one-warp transform for M = 512 and 1024; returns 0 for other lengths
+extern "C" int dst_warp_run_f32(int M, int howmany, float* data) {
+  if (M == 512) run_warp<8>(howmany, data);
+  else if (M == 1024) run_warp<9>(howmany, data);
+  else return 0;
+  return 1;
 }
 
 extern "C" void dst_core_run_f64(int M, int howmany, double* data) { run<double>(M, howmany, data); }

@@ -143,11 +143,15 @@ def test_topography_formula(qgwlib):
 @pytest.fixture(scope="module")
 def dstcore(tmp_path_factory):
     so = str(tmp_path_factory.mktemp("dst") / "dstcore.so")
-    subprocess.check_call(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-o", so,
+    # the work items move a buffer's values as floats, complex pairs and
+    # 16-byte vectors; the device code separates those phases by warp or
+    # block barriers, the loops here by nothing, hence no type-based aliasing
+    subprocess.check_call(["g++", "-O2", "-fno-strict-aliasing", "-std=c++17", "-shared", "-fPIC", "-o", so,
                            os.path.join(ROOT, "tests", "cpu", "dst_core_check.cpp")])
     lib = ctypes.CDLL(so)
     lib.dst_core_run_f64.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
     lib.dst_core_run_f32.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    lib.dst_warp_run_f32.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
     return lib
 
 
@@ -162,6 +166,23 @@ def test_device_dst_blocks_on_host(dstcore, M):
     yf = x.astype(np.float32)
     dstcore.dst_core_run_f32(M, 3, yf.ctypes.data)
     assert np.linalg.norm(yf - ref) <= 1e-5 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("M", [512, 1024])
+def test_warp_dst_on_host(dstcore, M):
+    """The FP32 one-warp in-place transform (three DIF passes, digit-reversed
+    split reads) with its lanes run in turn, against scipy's DST-I."""
+    x = np.random.default_rng(M + 1).standard_normal((3, M - 1))
+    ref = sf.dst(x, type=1, axis=1)
+    yf = x.astype(np.float32)
+    assert dstcore.dst_warp_run_f32(M, 3, yf.ctypes.data) == 1
+    assert np.linalg.norm(yf - ref) <= 1e-5 * np.linalg.norm(ref)
+    # a single impulse and a constant row
+    for row in (np.eye(M - 1)[M // 3], np.ones(M - 1)):
+        ref = sf.dst(row, type=1)
+        yf = row.astype(np.float32).copy()
+        assert dstcore.dst_warp_run_f32(M, 1, yf.ctypes.data) == 1
+        assert np.linalg.norm(yf - ref) <= 1e-5 * np.linalg.norm(ref)
 
 
 def test_supported_transform_lengths(dstcore):
