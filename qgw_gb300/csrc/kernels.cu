@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(NT, 3) k_rows_inv(StepArgs<T> a, int step_mode
 template <typename T, bool COMP, int R>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 4) k_rhs(const __grid_constant__ StepArgs<T> a, int ntx,
                                                                     int nty) {
-  extern __shared__ __align__(128) unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned long long bar[2];
   // TMA destinations are 128-byte aligned (the launch adds 128 bytes)
   unsigned char* base = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);

@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 2) k_rows_inv_ens(Ens
 // so each launch runs the same specialised body as a single run.
 template <typename T, bool COMP, int R>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 3) k_rhs_ens(EnsArgs<T> e) {
-  extern __shared__ __align__(128) unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ StepArgs<T> sa;
   __shared__ int cur;
   __shared__ unsigned long long bar;

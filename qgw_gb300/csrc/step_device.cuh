@@ -1038,11 +1038,13 @@ template <typename T, int R> __device__ __forceinline__ T* rhs_work(unsigned cha
 }
 
 // Loads of one tile that do not go through TMA, into `in`: edge tiles
-// (bounds-checked psi; periodic tiles also q, wrapped) and, where no tensor
-// map exists, interior tiles by element-wise asynchronous copies (all three
-// fields together).  A closed edge tile's q (with its ghost rule) is formed
-// by rhs_tile_compute, which needs the whole psi tile.  The caller
-// synchronises the block afterwards.
+// (periodic: psi and q wrapped around; closed, where no tensor map exists:
+// the three fields bounds-checked, zero outside the domain, as a TMA box
+// reads them) and, where no tensor map exists, interior tiles by
+// element-wise asynchronous copies (all three fields together).  A closed
+// edge tile's ghost values of q (which need the whole psi tile) and of the
+// chain are formed by rhs_tile_compute.  The caller synchronises the block
+// afterwards.
 template <typename T, bool COMP, int R, bool EDGE>
 __device__ __forceinline__ void rhs_tile_fetch(const StepArgs<T>& a, int i0, int j0, int k, const RhsIn<T>& in) {
   constexpr int W = TW, HH = TY + 2 * R;
@@ -1066,12 +1068,32 @@ __device__ __forceinline__ void rhs_tile_fetch(const StepArgs<T>& a, int i0, int
       qs[y * W + xx + XO] = qL[(size_t)wrap_index(j0 + y - 1, ny) * pitch + wrap_index(i0 + xx, nx)];
     }
   } else if (EDGE) {
+    // closed basin: what a TMA box with zero fill holds (the compute step
+    // then writes the ghost values)
     for (int w = tid; w < HH * (TX + 2 * R); w += NT) {
       const int y = w / (TX + 2 * R), xx = w - y * (TX + 2 * R) - R;
       const int gi = i0 + xx, gj = j0 + y - R;
       T v = T(0);
       if (gi >= 0 && gi < nx && gj >= 0 && gj < ny) v = psiL[(size_t)gj * pitch + gi];
       ps[y * W + xx + XO] = v;
+    }
+    for (int w = tid; w < QH * QW; w += NT) {
+      const int y = w / QW, xx = w - y * QW - 1;
+      const int gi = i0 + xx, gj = j0 + y - 1;
+      T v = T(0);
+      if (gi >= 0 && gi < nx && gj >= 0 && gj < ny) v = qL[(size_t)gj * pitch + gi];
+      qs[y * W + xx + XO] = v;
+    }
+    if (COMP && a.zeta_mode == 1 && a.nsweep >= 1) {
+      constexpr int W1 = TX + 2 * R - 2, H1 = HH - 2;
+      const T* zL = a.zeta + (size_t)k * a.lstride;
+      for (int w = tid; w < W1 * H1; w += NT) {
+        const int yr = w / W1, xr = w - yr * W1;
+        const int gi = i0 + xr + 1 - R, gj = j0 + yr + 1 - R;
+        T v = T(0);
+        if (gi >= 0 && gi < nx && gj >= 0 && gj < ny) v = zL[(size_t)gj * pitch + gi];
+        in.zt[yr * W + xr + 1 - R + XO] = v;
+      }
     }
   } else {
     const T* src = psiL + (size_t)(j0 - R) * pitch + (i0 - R);
@@ -1182,16 +1204,17 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile_compute(const
       if (!EDGE || (gi < nx && gj < ny)) hv[h] = zetaL[(size_t)gj * pitch + gi];
     }
   }
-  // q with one ghost point: adjust_bc(q, 1, psi), src/domain.h:308-348
+  // q with one ghost point: adjust_bc(q, 1, psi), src/domain.h:308-348; the
+  // interior values arrived with the tile (zero outside the domain)
   if (EDGE && !per) {
     for (int w = tid; w < QH * QW; w += NT) {
       const int y = w / QW, x = w - y * QW;
       const int xx = x - 1, yy = y - 1;
       const int gi = i0 + xx, gj = j0 + yy;
       const bool inx = gi >= 0 && gi < nx, iny = gj >= 0 && gj < ny;
+      if (inx && iny) continue;
       T v = T(0);
-      if (inx && iny) v = qL[(size_t)gj * pitch + gi];
-      else if (iny && gi == -1) v = cbc * PS(xx + 1, yy);
+      if (iny && gi == -1) v = cbc * PS(xx + 1, yy);
       else if (iny && gi == nx) v = cbc * PS(xx - 1, yy);
       else if (inx && gj == -1) v = cbc * PS(xx, yy + 1);
       else if (inx && gj == ny) v = cbc * PS(xx, yy - 1);
@@ -1235,7 +1258,7 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile_compute(const
           T v = T(0);
           if (inx && iny) {
             if (s == 1 && zm) {
-              v = d2 * zetaL[(size_t)gj * pitch + gi];
+              v = d2 * in.zt[o - W];  // the zeta tile, one row up
             } else {
               const T sum = (Lp[o + 1] + Lp[o - 1]) + (Lp[o + W] + Lp[o - W]);
               v = fmaT(T(-4), Lp[o], sum);
@@ -1455,11 +1478,15 @@ __device__ __forceinline__ void body_rhs_tiles(const StepArgs<T>& a, int ntx, in
     j0 = (r % nty) * TY;
     k = r / nty;
   };
+  // interior tiles, and closed-basin edge tiles (the box's zero fill is the
+  // value outside the domain), arrive by TMA; periodic edge tiles wrap
+  const bool per = a.periodic != 0;
   // prologue: the first tile's boxes into buffer 0
   if (NB == 2 && tm && tid == 0 && (int)blockIdx.x < ntiles) {
     int i0, j0, k;
     tile_of((int)blockIdx.x, i0, j0, k);
-    if (!rhs_edge_tile(i0, j0, R, a.nx, a.ny)) rhs_tile_tma<T, COMP, R>(a, i0, j0, k, rhs_in<T, R>(base, 0), tm, &bar[0]);
+    if (!per || !rhs_edge_tile(i0, j0, R, a.nx, a.ny))
+      rhs_tile_tma<T, COMP, R>(a, i0, j0, k, rhs_in<T, R>(base, 0), tm, &bar[0]);
   }
   decltype(absbits_native(T(0))) mymax = 0;
   int it = 0;
@@ -1475,11 +1502,11 @@ __device__ __forceinline__ void body_rhs_tiles(const StepArgs<T>& a, int ntx, in
       // __syncthreads of the previous iteration)
       int i1, j1, k1;
       tile_of(t + step, i1, j1, k1);
-      if (!rhs_edge_tile(i1, j1, R, a.nx, a.ny))
+      if (!per || !rhs_edge_tile(i1, j1, R, a.nx, a.ny))
         rhs_tile_tma<T, COMP, R>(a, i1, j1, k1, rhs_in<T, R>(base, cur ^ 1), tm, &bar[cur ^ 1]);
     }
     bool ok = true;
-    if (edge) {
+    if (edge && (per || !tm)) {
       rhs_tile_fetch<T, COMP, R, true>(a, i0, j0, k, in);
     } else if (!tm) {
       rhs_tile_fetch<T, COMP, R, false>(a, i0, j0, k, in);
@@ -1513,7 +1540,7 @@ __device__ __forceinline__ void body_rhs(const StepArgs<T>& a, int bx, int by, i
   const RhsIn<T> in = rhs_in<T, R>(smem_raw, 0);
   T* wk = rhs_work<T, R>(smem_raw, 1);
   bool ok = true;
-  if (edge) {
+  if (edge && (a.periodic || !tm)) {
     rhs_tile_fetch<T, COMP, R, true>(a, i0, j0, k, in);
   } else if (!tm) {
     rhs_tile_fetch<T, COMP, R, false>(a, i0, j0, k, in);
