@@ -86,13 +86,15 @@ size_t row_budget(size_t elem, int M, int nl) {
 // a fixed group size rather than a byte budget (each group re-reads the
 // row's spectral data, while larger groups cost occupancy).  With the zeta
 // rows: 3 layers, 5 for rows of 512 and less or more than 10 layers
-// (1024^2 x 20 FP32: 0.477 -> 0.430 ms); without: 2, 4 for more than 10
-// layers on rows of 1024 and less; within 110 KiB of work buffers.  QGW_INV_GROUP overrides the size.
-int inv_group(int zeta, int M, int nl) {
+// (1024^2 x 20 FP32: 0.477 -> 0.430 ms), 4 where the rows transform in place
+// (one buffer per row; 1024^2 x 10 FP32: 0.127 -> 0.114 ms); without: 2, 4
+// for more than 10 layers on rows of 1024 and less; within 110 KiB of work
+// buffers.  QGW_INV_GROUP overrides the size.
+int inv_group(int zeta, int M, int nl, int bufs) {
   const char* e = std::getenv("QGW_INV_GROUP");
   const int v = e ? std::atoi(e) : 0;
   if (v >= 1 && v <= 16) return v;
-  if (zeta) return (M <= 512 || nl > 10) ? 5 : 3;
+  if (zeta) return (M <= 512 || nl > 10) ? 5 : bufs == 1 ? 4 : 3;
   return (nl > 10 && M <= 1024) ? 4 : 2;
 }
 
@@ -300,7 +302,7 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
     else if (sizeof(T) == 8) a.G1 = mode_group_fma(r->nl, Mx, sizeof(T), budget, 16);
     else a.G1 = mode_group(r->nl, Mx, sizeof(T), budget, 1, 16, 16, bufs_x);
   }
-  a.G3 = mode_group(r->nl, Mx, sizeof(T), 110 * 1024, 1, 16, inv_group(0, Mx, r->nl), bufs_x);
+  a.G3 = mode_group(r->nl, Mx, sizeof(T), 110 * 1024, 1, 16, inv_group(0, Mx, r->nl, bufs_x), bufs_x);
   a.CT = 0;
   a.low_k64 = 8;
   // 16-byte column vectors: rows 16-byte aligned and a whole number of
@@ -332,7 +334,7 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
     if ((rc = dalloc(r, &a.spec2, field))) return rc;
     if ((rc = dalloc(r, &a.zeta, field))) return rc;
     // K3 transforms psi and zeta rows of each mode: two rows per mode
-    a.G3 = mode_group(r->nl, Mx, sizeof(T), 110 * 1024, 2, 8, inv_group(1, Mx, r->nl), bufs_x);
+    a.G3 = mode_group(r->nl, Mx, sizeof(T), 110 * 1024, 2, 8, inv_group(1, Mx, r->nl, bufs_x), bufs_x);
     // symbol of the 5-point Laplacian: DST-I basis sin^2(pi k / 2(n+1));
     // periodic Fourier basis sin^2(pi k / N)
     std::vector<double> sx(r->nx, 0.0), sy(r->ny);
@@ -415,6 +417,7 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   for (int g = 1; g <= 4; ++g) a.fc[qgw::FC_GH1 + g - 1] = (float)a.gh[g];
   a.fc[qgw::FC_NORM] = (float)r->norm;
   a.fc[qgw::FC_NUHS] = (float)nuh;
+  a.fc[qgw::FC_NUHD2] = (float)(a.nuh_scaled * r->Delta * r->Delta);
   a.fc[qgw::FC_LX2] = (float)a.lx2;
   a.fc[qgw::FC_LY2] = (float)a.ly2;
   float* fi;

@@ -389,8 +389,12 @@ __device__ __forceinline__ void dst_row_warp_f32(float* row, const DstTables<flo
 #pragma unroll
   for (int u = 0; u < W::IPL; ++u) W::p1_fft(lane + 32 * u, v[u], tb.twd, Z);
   __syncwarp();
+  {
+    C2<float> w2[8];
+    W::p2_twiddles(lane % W::S1, tb.twd, w2);
 #pragma unroll
-  for (int u = 0; u < W::IPL; ++u) W::p2(lane + 32 * u, tb.twd, Z);
+    for (int u = 0; u < W::IPL; ++u) W::p2(lane + 32 * u, w2, Z);
+  }
   __syncwarp();
 #pragma unroll
   for (int u = 0; u < 2; ++u) W::p3(lane + 32 * u, Z);

@@ -74,8 +74,14 @@ template <int LGH> struct WarpDst {
     QGW_UNROLL
     for (int k2 = 0; k2 < 8; ++k2) Z[pc<float>(n1 + S0 * k2)] = v[k2];
   }
-  // pass-2 item it < S0: block it / S1, offset it % S1
-  QGW_HD static void p2(int it, const C2<float>* __restrict__ twd, C2<float>* Z) {
+  // pass-2 twiddles of offset n1 < S1 (w[k2], k2 = 1..7): the items of a
+  // lane (it = lane + 32 u) share their offset it % S1 = lane % S1
+  QGW_HD static void p2_twiddles(int n1, const C2<float>* __restrict__ twd, C2<float>* w) {
+    QGW_UNROLL
+    for (int k2 = 1; k2 < 8; ++k2) w[k2] = twd[7 * S0 + (k2 - 1) * S1 + n1];
+  }
+  // pass-2 item it < S0: block it / S1, offset it % S1 (twiddles w)
+  QGW_HD static void p2(int it, const C2<float>* w, C2<float>* Z) {
     const int b = it / S1, n1 = it - b * S1;
     const int base = b * (H / 8) + n1;
     C2<float> v[8];
@@ -83,7 +89,7 @@ template <int LGH> struct WarpDst {
     for (int n2 = 0; n2 < 8; ++n2) v[n2] = Z[pc<float>(base + S1 * n2)];
     dft8(v);
     QGW_UNROLL
-    for (int k2 = 1; k2 < 8; ++k2) v[k2] = cmul(v[k2], twd[7 * S0 + (k2 - 1) * S1 + n1]);
+    for (int k2 = 1; k2 < 8; ++k2) v[k2] = cmul(v[k2], w[k2]);
     QGW_UNROLL
     for (int k2 = 0; k2 < 8; ++k2) Z[pc<float>(base + S1 * k2)] = v[k2];
   }

@@ -134,7 +134,7 @@ template <typename T> struct StepArgs {
   const float* sy2f;
   // FP32 copies of the RHS and Helmholtz constants (compensated path), made
   // on the host: a double -> float conversion runs on the FP64 pipe
-  float fc[16];
+  float fc[20];
   const float* iRd2f;
   int CT;                          // (unused by the kernels; kept for layout)
   int vec_cols;                    // rows are 16-byte aligned: 16-byte column loads
@@ -186,6 +186,7 @@ enum FcIndex {
   FC_LX2,
   FC_LY2,
   FC_NUHS,        // nu_hyper itself (zeta_mode 2: the field is scaled)
+  FC_NUHD2,       // nuh_scaled * Delta^2 (zeta_mode 1 interior tiles: the chain from the raw zeta)
   FC_COUNT
 };
 static_assert(FC_COUNT <= (int)(sizeof(StepArgs<float>::fc) / sizeof(float)), "fc holds every constant");

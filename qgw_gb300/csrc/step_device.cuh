@@ -1187,7 +1187,7 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile_compute(const
   const T cbc = pick<T>(a.cbc, a.fc[FC_CBC]);
   const T m_inv12 = pick<T>(-a.inv12d2, a.fc[FC_MINV12]), b2d = pick<T>(a.b2d, a.fc[FC_B2D]);
   const T nu_d2 = pick<T>(a.nu_d2, a.fc[FC_NUD2]), nuh = pick<T>(a.nuh_scaled, a.fc[FC_NUH]);
-  const T nuhs = pick<T>(0.0, a.fc[FC_NUHS]);
+  const T nuhs = pick<T>(0.0, a.fc[FC_NUHS]), nuhd2 = pick<T>(0.0, a.fc[FC_NUHD2]);
   const T drag = pick<T>(a.drag_d2, a.fc[FC_DRAG]), topo_c = pick<T>(-(a.inv12d2 * a.topo_fac), a.fc[FC_TOPOC]);
 #define PS(x, y) ps[((y) + R) * W + (x) + XO]
 #define QS(x, y) qs[((y) + 1) * W + (x) + XO]
@@ -1227,11 +1227,15 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile_compute(const
   // sweep is the spectral zeta.  Unrolled over s so that every region
   // width is a compile-time constant.  Region of sweep s: tile rows
   // yy = s-R .. TY+R-s-1 (smem row yy + R), columns xx likewise (xx + XO).
-  const T* Lp = ps;
+  // Interior tiles in zeta mode 1 take the zeta tile itself as the first
+  // sweep's output (fold): the chain then runs on zeta = L psi / Delta^2
+  // rather than L psi, and the factor Delta^2 moves into the coefficient.
+  const bool fold = !EDGE && zm && ksweep >= 1;
+  const T* Lp = fold ? in.zt - W : ps;  // zt's row 0 is the first sweep's first row
   T* Lc = L0;
 #pragma unroll
   for (int s = 1; s <= R; ++s) {
-    if (s <= ksweep) {
+    if (s <= ksweep && !(s == 1 && fold)) {
       __syncthreads();
       const int Ws = TX + 2 * R - 2 * s, Hs = HH - 2 * s;
       const int cx = s - R + XO;  // smem column of the region's first point
@@ -1269,24 +1273,25 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile_compute(const
           else if (inx && gj == ny) v = ghs * PS(xx, yy - 1);
           Lc[o] = v;
         }
-      } else if (s == 1 && zm) {
-        // the raw zeta arrived in in.zt, one row up (its row 0 is the
-        // region's first row): scale it into L0 (== Lc)
-        const T* zt = in.zt;
-        for (int w = tid; w < Ws * Hs; w += NT) {
-          const int yr = w / Ws, xr = w - yr * Ws;
-          const int o = (yr + s) * W + xr + cx;
-          Lc[o] = d2 * zt[o - W];
-        }
       } else {
         // two vertically adjacent points per item (Hs is even), sharing
-        // their column of four values; same arithmetic per point
-        for (int w = tid; w < Ws * (Hs / 2); w += NT) {
-          const int yp = w / Ws, xr = w - yp * Ws;
+        // their column of four values; same arithmetic per point.  The
+        // region's first 32 columns go one row pair per warp (each warp's
+        // accesses in one row: no bank conflicts), its last Ws - 32 columns
+        // (Ws >= 32) after them.
+        auto pair = [&](int yp, int xr) {
           const int o = (2 * yp + s) * W + xr + cx;
           const T c0 = Lp[o - W], c1 = Lp[o], c2 = Lp[o + W], c3 = Lp[o + 2 * W];
           Lc[o] = fmaT(T(-4), c1, (Lp[o + 1] + Lp[o - 1]) + (c2 + c0));
           Lc[o + W] = fmaT(T(-4), c2, (Lp[o + W + 1] + Lp[o + W - 1]) + (c3 + c1));
+        };
+        static_assert(TX == 32, "one warp per row of the region's first 32 columns");
+        for (int w = tid; w < 32 * (Hs / 2); w += NT) pair(w >> 5, w & 31);
+        if (Ws > 32) {
+          for (int w = tid; w < (Ws - 32) * (Hs / 2); w += NT) {
+            const int yp = w / (Ws - 32);
+            pair(yp, 32 + w - yp * (Ws - 32));
+          }
         }
       }
       Lp = Lc;
@@ -1314,7 +1319,7 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile_compute(const
       f = fmaT(nu_d2, lq, f);
     }
     if (zm2) f = fmaT(nuhs, hchain, f);
-    else if (a.nsweep > 0) f = fmaT(nuh, Lp[(y + R) * W + x + XO], f);
+    else if (a.nsweep > 0) f = fmaT(fold ? nuhd2 : nuh, Lp[(y + R) * W + x + XO], f);
     // surface wind (src/dynamics.h:66) and bottom drag + topography (:67-69)
     if (k == 0 && a.has_wind) f += a.wind[gj];
     if (bottom) {

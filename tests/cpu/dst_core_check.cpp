@@ -94,8 +94,11 @@ static void run_warp(int howmany, float* data) {
     }
     for (int lane = 0; lane < 32; ++lane)
       for (int u = 0; u < IPL; ++u) W::p1_fft(lane + 32 * u, v[lane][u], TWD, Z);
-    for (int lane = 0; lane < 32; ++lane)
-      for (int u = 0; u < IPL; ++u) W::p2(lane + 32 * u, TWD, Z);
+    for (int lane = 0; lane < 32; ++lane) {
+      C2<float> w2[8];
+      W::p2_twiddles(lane % W::S1, TWD, w2);
+      for (int u = 0; u < IPL; ++u) W::p2(lane + 32 * u, w2, Z);
+    }
     for (int lane = 0; lane < 32; ++lane)
       for (int u = 0; u < 2; ++u) W::p3(lane + 32 * u, Z);
     C2<float>* N = (C2<float>*)B;
