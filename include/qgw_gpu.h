@@ -234,6 +234,25 @@ int qgw_kernels_per_step(qgw_run* run);
  * inverse y-DST), ms4[2] rows inverse (x-DST + back-projection), ms4[3] RHS. */
 int qgw_profile_kernels(qgw_run* run, int nsteps, float* ms4);
 
+/* Work-tile shape of a run's step kernels (no counterpart in the
+ * reference, which has no tiles): rhs_tile_rows, the RHS tile height (16 or
+ * 32 rows); col_tile, columns per tile of the column transform (FP32: 8 or
+ * 4, FP64: 4 or 2); row_group_fwd and row_group_inv, modes (layers) per
+ * block of the forward and inverse row kernels (1..16, balanced over the
+ * run's layers; the inverse kernel takes at most 8 when it also transforms
+ * zeta).  0 keeps a value.  No choice changes the arithmetic: a run's
+ * results are bitwise the same for every shape.  QGW_ERR_PARAM when a value
+ * is not one of these or the shape needs more shared memory than the
+ * device has (the run keeps its shape). */
+typedef struct {
+  int rhs_tile_rows;
+  int col_tile;
+  int row_group_fwd;
+  int row_group_inv;
+} qgw_shape;
+int qgw_set_shape(qgw_run* run, const qgw_shape* shape);
+int qgw_get_shape(qgw_run* run, qgw_shape* shape);
+
 /* PV inversion without any allocation (no counterpart in the reference,
  * whose invert_pv, src/elliptic.h:76-155, allocates nothing only because its
  * work array is a global made at start-up).  For callers that cannot
@@ -268,8 +287,10 @@ int qgw_probe_fp_rates(double* fp64_tflops, double* fp32_tflops);
  * over all members' work items, the four launches of a step captured once
  * as a CUDA graph (use_graph != 0) and replayed.  A member's result is
  * bitwise the same alone and in any ensemble.  qgw_ensemble_tune chooses
- * each stage's persistent grid size in turn, timing whole steps for every
- * candidate; the trial steps advance the state, so set q afterwards.  No reference
+ * the members' work-tile shape (RHS tile height, column-tile width, modes
+ * per row-kernel block; qgw_set_shape) and then each stage's persistent
+ * grid size, one choice at a time, timing whole steps for every candidate;
+ * the trial steps advance the state, so set q afterwards.  No reference
  * counterpart: the reference runs one configuration per process. */
 typedef struct qgw_ensemble qgw_ensemble;
 int qgw_ensemble_create(int nmembers, const qgw_params* params, int precision, qgw_ensemble** out);
@@ -283,6 +304,10 @@ int qgw_ensemble_step(qgw_ensemble* ens, int nsteps, const int* max_steps, int u
                       qgw_step_info* infos);
 int qgw_ensemble_tune(qgw_ensemble* ens, int trial_steps, float* best_ms);
 int qgw_ensemble_grids(qgw_ensemble* ens, int* blocks_per_sm);
+/* qgw_set_shape for every member (one shape for the whole ensemble; the
+ * member table is rebuilt), and member i's shape (the tuner's choice). */
+int qgw_ensemble_set_shape(qgw_ensemble* ens, const qgw_shape* shape);
+int qgw_ensemble_shape(qgw_ensemble* ens, int i, qgw_shape* shape);
 /* qgw_set_forcing_records for member i (the member table is rebuilt). */
 int qgw_ensemble_set_forcing_records(qgw_ensemble* ens, int i, const double* records, int nrec);
 

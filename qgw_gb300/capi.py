@@ -21,7 +21,7 @@ from typing import Dict, Optional
 
 import numpy as np
 
-from .params import QgwBudget, QgwParams, QgwStepInfo, QgwTime, halo_shape, to_struct
+from .params import QgwBudget, QgwParams, QgwShape, QgwStepInfo, QgwTime, halo_shape, to_struct
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libqgw_gpu.so")
@@ -46,7 +46,8 @@ EXPORTS = [
     "qgw_invert_pv_noalloc", "qgw_nc_create", "qgw_nc_write", "qgw_nc_close", "qgw_nc_read",
     "qgw_ensemble_create", "qgw_ensemble_destroy", "qgw_ensemble_size", "qgw_ensemble_member",
     "qgw_ensemble_set_q", "qgw_ensemble_set_time", "qgw_ensemble_get", "qgw_ensemble_step",
-    "qgw_ensemble_tune", "qgw_ensemble_grids",
+    "qgw_ensemble_tune", "qgw_ensemble_grids", "qgw_ensemble_set_shape", "qgw_ensemble_shape",
+    "qgw_set_shape", "qgw_get_shape",
     "qgw_pool_create", "qgw_pool_submit", "qgw_pool_poll", "qgw_pool_fetch", "qgw_pool_stats",
     "qgw_pool_destroy",
 ]
@@ -114,6 +115,10 @@ def load(path: str = LIB_PATH):
     lib.qgw_ensemble_step.argtypes = [V, I, P(I), I, P(QgwStepInfo)]
     lib.qgw_ensemble_tune.argtypes = [V, I, P(ctypes.c_float)]
     lib.qgw_ensemble_grids.argtypes = [V, P(I)]
+    lib.qgw_ensemble_set_shape.argtypes = [V, P(QgwShape)]
+    lib.qgw_ensemble_shape.argtypes = [V, I, P(QgwShape)]
+    lib.qgw_set_shape.argtypes = [V, P(QgwShape)]
+    lib.qgw_get_shape.argtypes = [V, P(QgwShape)]
     LL = ctypes.c_longlong
     lib.qgw_pool_create.argtypes = [ctypes.c_size_t, I, P(V)]
     lib.qgw_pool_submit.argtypes = [V, pp, D, I, I, P(LL)]
@@ -241,11 +246,24 @@ class Ensemble:
                "qgw_ensemble_set_forcing_records")
 
     def tune(self, trial_steps: int = 3):
+        """Tune the work-tile shape, then each stage's persistent grid;
+        returns (step ms after each stage's grid choice, blocks per SM)."""
         ms = (ctypes.c_float * 4)()
         _check(self.lib.qgw_ensemble_tune(self.h, int(trial_steps), ms), "qgw_ensemble_tune")
         g = (ctypes.c_int * 4)()
         _check(self.lib.qgw_ensemble_grids(self.h, g), "qgw_ensemble_grids")
         return list(ms), list(g)
+
+    def set_shape(self, **kw):
+        """One work-tile shape for every member (keys of QgwShape; 0 or absent keeps a value)."""
+        sh = QgwShape(**{k: int(v) for k, v in kw.items()})
+        _check(self.lib.qgw_ensemble_set_shape(self.h, ctypes.byref(sh)), "qgw_ensemble_set_shape")
+
+    def get_shape(self, i: int = 0) -> dict:
+        """Member i's work-tile shape."""
+        sh = QgwShape()
+        _check(self.lib.qgw_ensemble_shape(self.h, int(i), ctypes.byref(sh)), "qgw_ensemble_shape")
+        return sh.as_dict()
 
 
 class Pool:
@@ -438,6 +456,17 @@ class Run:
 
     def stream(self) -> int:
         return int(self.lib.qgw_stream(self.h) or 0)
+
+    def set_shape(self, **kw):
+        """Work-tile shape of the step kernels (keys of QgwShape; 0 or absent keeps a value)."""
+        sh = QgwShape(**{k: int(v) for k, v in kw.items()})
+        _check(self.lib.qgw_set_shape(self.h, ctypes.byref(sh)), "qgw_set_shape")
+
+    def get_shape(self) -> dict:
+        """The work-tile shape of the step kernels."""
+        sh = QgwShape()
+        _check(self.lib.qgw_get_shape(self.h, ctypes.byref(sh)), "qgw_get_shape")
+        return sh.as_dict()
 
     def profile_kernels(self, nsteps: int):
         ms = (ctypes.c_float * 4)()

@@ -162,6 +162,30 @@ bool encode_tile_map(CUtensorMap* m, const T* base, const qgw_run* r, int rows) 
   return e == CUDA_SUCCESS;
 }
 
+// The RHS kernel's tensor maps for the run's tile height (boxes of TY + 2R
+// psi rows, TY + 2 q rows, TY + 2R - 2 zeta rows), or element-wise copies
+// when the driver cannot encode them, or when QGW_RHS_TILE_LOADS=copies asks
+// for that path.
+template <typename T>
+void encode_rhs_maps(const qgw_run* r, StepArgs<T>& a) {
+  std::memset(a.tm, 0, sizeof(a.tm));
+  a.use_tma = 0;
+  const char* loads = std::getenv("QGW_RHS_TILE_LOADS");
+  if (!tmap_encoder() || (loads && !std::strcmp(loads, "copies"))) return;
+  int R, ty;
+  if constexpr (sizeof(T) == 8) {
+    R = qgw::rhs_halo_of_f64(a);
+    ty = qgw::rhs_tile_y_f64(a);
+  } else {
+    R = qgw::rhs_halo_of_f32c(a);
+    ty = qgw::rhs_tile_y_f32c(a);
+  }
+  const int HH = ty + 2 * R;
+  bool ok = encode_tile_map<T>(&a.tm[0], a.psi, r, HH) && encode_tile_map<T>(&a.tm[1], a.q, r, ty + 2);
+  if (ok && a.zeta_mode == 1 && a.nsweep >= 1) ok = encode_tile_map<T>(&a.tm[2], a.zeta, r, HH - 2);
+  a.use_tma = ok ? 1 : 0;
+}
+
 template <typename T>
 int setup_args(qgw_run* r, StepArgs<T>& a) {
   const qgw_params& p = r->p;
@@ -414,7 +438,10 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   a.fc[qgw::FC_NUH] = (float)a.nuh_scaled;
   a.fc[qgw::FC_DRAG] = (float)a.drag_d2;
   a.fc[qgw::FC_TOPOC] = (float)(-(a.inv12d2 * a.topo_fac));
-  for (int g = 1; g <= 4; ++g) a.fc[qgw::FC_GH1 + g - 1] = (float)a.gh[g];
+  for (int g = 1; g <= 4; ++g) {
+    a.fc[qgw::FC_GH1 + g - 1] = (float)a.gh[g];
+    a.fc[qgw::FC_GHD1 + g - 1] = (float)(a.gh[g] / (r->Delta * r->Delta));
+  }
   a.fc[qgw::FC_NORM] = (float)r->norm;
   a.fc[qgw::FC_NUHS] = (float)nuh;
   a.fc[qgw::FC_NUHD2] = (float)(a.nuh_scaled * r->Delta * r->Delta);
@@ -423,24 +450,15 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   float* fi;
   if ((rc = upload<float>(r, &fi, r->iRd2))) return rc;
   a.iRd2f = fi;
-  // TMA tensor maps of the RHS kernel's interior tiles (psi with halo R, q
-  // with halo 1, in zeta mode 1 zeta over the first sweep's region; zeta
-  // mode 2 reads its field point by point); element-wise asynchronous copies
-  // when the driver cannot encode them, or when QGW_RHS_TILE_LOADS=copies
-  // asks for that path
-  std::memset(a.tm, 0, sizeof(a.tm));
-  a.use_tma = 0;
+  // TMA tensor maps of the RHS kernel's tiles (psi with halo R, q with halo
+  // 1, in zeta mode 1 zeta over the first sweep's region; zeta mode 2 reads
+  // its field point by point)
   a.rhs_grid = 0;
-  const char* loads = std::getenv("QGW_RHS_TILE_LOADS");
-  if (tmap_encoder() && !(loads && !std::strcmp(loads, "copies"))) {
-    int R;
-    if constexpr (sizeof(T) == 8) R = qgw::rhs_halo_of_f64(a);
-    else R = qgw::rhs_halo_of_f32c(a);
-    const int HH = qgw::rhs_tile_y() + 2 * R;
-    bool ok = encode_tile_map<T>(&a.tm[0], a.psi, r, HH) && encode_tile_map<T>(&a.tm[1], a.q, r, qgw::rhs_tile_y() + 2);
-    if (ok && a.zeta_mode == 1 && a.nsweep >= 1) ok = encode_tile_map<T>(&a.tm[2], a.zeta, r, HH - 2);
-    a.use_tma = ok ? 1 : 0;
-  }
+  // work-tile shape: RHS tiles of 16 rows (QGW_RHS_TILE_ROWS=32: 32 rows),
+  // the default column-tile width (a.CT = 0); qgw_set_shape changes them
+  a.rhs_ty = 16;
+  if (const char* e = std::getenv("QGW_RHS_TILE_ROWS")) a.rhs_ty = std::atoi(e) == 32 ? 32 : 16;
+  encode_rhs_maps<T>(r, a);
   // QGW_TEST_FIRST_WAIT_ITERS (tests of the timeout path only) lowers the
   // limit of the first wait for a tile's TMA bytes, down to 0 polls; the
   // second wait keeps the full limit, so the bytes still land before the
@@ -453,11 +471,72 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   return QGW_OK;
 }
 
+// Work-tile shape of a run (qgw_set_shape): validated on a copy of the
+// run's arguments, whose shared-memory needs must fit the device, then
+// applied.  None of the choices changes any arithmetic.
+template <typename T>
+int set_shape(qgw_run* r, StepArgs<T>& a, const qgw_shape& sh) {
+  StepArgs<T> b = a;
+  if (sh.rhs_tile_rows) {
+    if (sh.rhs_tile_rows != 16 && sh.rhs_tile_rows != 32) return QGW_ERR_PARAM;
+    b.rhs_ty = sh.rhs_tile_rows;
+  }
+  const int ctd = 32 / (int)sizeof(T);
+  if (sh.col_tile) {
+    if (sh.col_tile != ctd && sh.col_tile != ctd / 2) return QGW_ERR_PARAM;
+    b.CT = sh.col_tile == ctd ? 0 : sh.col_tile;
+  }
+  const bool per = a.periodic != 0;
+  const int Mx = per ? r->nx : r->nx + 1;
+  const int bufs_x = (!per && qgw::warp_dst_len(Mx / 2, (int)sizeof(T))) ? 1 : 2;
+  const size_t any = (size_t)1 << 30;  // the device's limit is checked below
+  if (sh.row_group_fwd) {
+    if (sh.row_group_fwd < 1 || sh.row_group_fwd > 16) return QGW_ERR_PARAM;
+    b.G1 = mode_group(r->nl, Mx, sizeof(T), any, 1, 16, sh.row_group_fwd, bufs_x);
+  }
+  if (sh.row_group_inv) {
+    if (sh.row_group_inv < 1 || sh.row_group_inv > 16) return QGW_ERR_PARAM;
+    const bool zm = a.zeta_mode != 0;
+    b.G3 = mode_group(r->nl, Mx, sizeof(T), any, zm ? 2 : 1, zm ? 8 : 16, sh.row_group_inv, bufs_x);
+  }
+  if (b.rhs_ty != a.rhs_ty) encode_rhs_maps<T>(r, b);
+  cudaError_t e;
+  if constexpr (sizeof(T) == 8) e = qgw::prepare_f64(b);
+  else e = qgw::prepare_f32c(b);
+  if (e == cudaErrorInvalidValue) return QGW_ERR_PARAM;  // beyond the device's shared memory
+  if (e != cudaSuccess) return QGW_ERR_CUDA;
+  if constexpr (sizeof(T) == 8) b.rhs_grid = qgw::rhs_grid_f64(b);
+  else b.rhs_grid = qgw::rhs_grid_f32c(b);
+  a = b;
+  return QGW_OK;
+}
+
+template <typename T>
+void get_shape(const StepArgs<T>& a, qgw_shape* sh) {
+  sh->rhs_tile_rows = a.rhs_ty == 32 ? 32 : 16;
+  sh->col_tile = a.CT ? a.CT : 32 / (int)sizeof(T);
+  sh->row_group_fwd = a.G1;
+  sh->row_group_inv = a.G3;
+}
+
 }  // namespace
 
 extern "C" {
 
 int qgw_abi_version(void) { return QGW_ABI_VERSION; }
+
+int qgw_set_shape(qgw_run* r, const qgw_shape* sh) {
+  if (!r || !sh) return QGW_ERR_PARAM;
+  if (cudaStreamSynchronize(r->stream) != cudaSuccess) return QGW_ERR_CUDA;
+  return r->precision == QGW_FP64 ? set_shape<double>(r, r->a64, *sh) : set_shape<float>(r, r->a32, *sh);
+}
+
+int qgw_get_shape(qgw_run* r, qgw_shape* sh) {
+  if (!r || !sh) return QGW_ERR_PARAM;
+  if (r->precision == QGW_FP64) get_shape<double>(r->a64, sh);
+  else get_shape<float>(r->a32, sh);
+  return QGW_OK;
+}
 
 const char* qgw_strerror(int s) {
   switch (s) {

@@ -47,6 +47,10 @@ int stage_occupancy(const qgw::EnsembleCore* e, int stage, size_t smem) {
   return e->precision == QGW_FP64 ? qgw::ens_blocks_per_sm_f64(stage, smem) : qgw::ens_blocks_per_sm_f32c(stage, smem);
 }
 
+// occupancy stage of the RHS kernel of halo radius r at the ensemble's tile
+// height (3 + r for 16 rows, 7 + r for 32)
+int rhs_stage(const qgw::EnsembleCore* e, int r) { return (e->sm.rhs_ty == 32 ? 7 : 3) + r; }
+
 // persistent grid of each stage: bps blocks per SM, never more than can be
 // resident at once (blocks beyond that would wait for a second wave); bps 0
 // gives one block per work item
@@ -61,7 +65,7 @@ void set_grids(qgw::EnsembleCore* e) {
     e->grid[s] = std::max(1, stage_grid(e, e->total[s], e->bps[s], stage_occupancy(e, s, e->sm.bytes[s])));
   e->grid[3] = 0;
   for (int r = 1; r <= 4; ++r) {
-    e->rhs_grid[r] = stage_grid(e, e->rhs_total[r], e->bps[3], stage_occupancy(e, 3 + r, e->sm.rhs_bytes[r]));
+    e->rhs_grid[r] = stage_grid(e, e->rhs_total[r], e->bps[3], stage_occupancy(e, rhs_stage(e, r), e->sm.rhs_bytes[r]));
     e->grid[3] += e->rhs_grid[r];
   }
 }
@@ -69,7 +73,7 @@ void set_grids(qgw::EnsembleCore* e) {
 // member table, per-stage work lists and shared-memory sizes
 int build_tables(qgw::EnsembleCore* e) {
   const int n = (int)e->members.size();
-  const int tx = qgw::rhs_tile_x(), ty = qgw::rhs_tile_y();
+  const int tx = qgw::rhs_tile_x();
   const size_t L = (size_t)n + 1;
   std::vector<int> lists(3 * L + 4 + 4 * (L + 4), 0);
   int* rows = lists.data();
@@ -80,6 +84,7 @@ int build_tables(qgw::EnsembleCore* e) {
   for (int i = 0; i < n; ++i) {
     const qgw_run* r = e->members[i];
     const int R = e->precision == QGW_FP64 ? qgw::rhs_halo_of_f64(r->a64) : qgw::rhs_halo_of_f32c(r->a32);
+    const int ty = e->precision == QGW_FP64 ? qgw::rhs_tile_y_f64(r->a64) : qgw::rhs_tile_y_f32c(r->a32);
     const int tiles = ((r->nx + tx - 1) / tx) * ((r->ny + ty - 1) / ty) * r->nl;
     rows[i + 1] = rows[i] + r->ny;
     const int ctiles = e->precision == QGW_FP64 ? qgw::col_tiles_f64(r->a64) : qgw::col_tiles_f32c(r->a32);
@@ -303,13 +308,32 @@ int qgw_ensemble_step(qgw_ensemble* ens, int nsteps, const int* max_steps, int u
   return bad ? QGW_ERR_NAN : QGW_OK;
 }
 
-// Autotuner: coordinate descent over the persistent grid of each stage
-// (blocks per SM from a candidate list), each candidate timed over
-// `trial_steps` whole steps, so that every stage is measured in the context
-// of the others (caches, the member states the step leaves behind).  Runs
-// on the current state and then restores the members' time scalars; the
-// trial steps advance q, so callers re-set q before the time loop.
-// best_ms[4] (optional) receives the step time after each stage's choice.
+// The same work-tile shape for every member (qgw_set_shape), then the
+// member table rebuilt; a member that refuses the shape leaves every member
+// at its previous one.
+static int ensemble_set_shape(qgw::EnsembleCore* e, const qgw_shape& sh) {
+  const int n = (int)e->members.size();
+  std::vector<qgw_shape> old(n);
+  for (int i = 0; i < n; ++i) qgw_get_shape(e->members[i], &old[i]);
+  for (int i = 0; i < n; ++i) {
+    const int rc = qgw_set_shape(e->members[i], &sh);
+    if (rc) {
+      for (int j = 0; j < i; ++j) qgw_set_shape(e->members[j], &old[j]);
+      return rc;
+    }
+  }
+  return qgw::ens_core_build(e);
+}
+
+// Autotuner, coordinate descent timed over `trial_steps` whole steps per
+// candidate (each choice measured in the context of the others: caches,
+// the member states the step leaves behind): first the work-tile shape of
+// every member -- RHS tile height, column-tile width, modes per block of the
+// forward and of the inverse row kernels -- then the persistent grid of
+// each stage (blocks per SM).  Runs on the current state and then restores
+// the members' time scalars; the trial steps advance q, so callers re-set
+// q before the time loop.  best_ms[4] (optional) receives the step time
+// after each stage's grid choice.
 int qgw_ensemble_tune(qgw_ensemble* ens, int trial_steps, float* best_ms) {
   if (!ens || trial_steps < 1) return QGW_ERR_PARAM;
   qgw::EnsembleCore* e = &ens->core;
@@ -320,11 +344,52 @@ int qgw_ensemble_tune(qgw_ensemble* ens, int trial_steps, float* best_ms) {
   for (int i = 0; i < n; ++i) qgw_get_time(e->members[i], &saved[i]);
   std::vector<int> ms(n, 0);
   CK(cudaMemcpyAsync(e->d_maxsteps, ms.data(), sizeof(int) * n, cudaMemcpyHostToDevice, e->stream));
-  const int cands[] = {0, 1, 2, 3, 4, 5, 6, 8};  // 0: one block per work item
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   drop_graph(e);
+  // mean step time of the current configuration
+  auto trial = [&](float* out) -> int {
+    if (e->precision == QGW_FP64) qgw::ens_begin_f64(e->e64, e->d_maxsteps, e->stream);
+    else qgw::ens_begin_f32c(e->e32, e->d_maxsteps, e->stream);
+    launch_step(e, 15);  // warm-up
+    CK(cudaEventRecord(e0, e->stream));
+    for (int t = 0; t < trial_steps; ++t) launch_step(e, 15);
+    CK(cudaEventRecord(e1, e->stream));
+    CK(cudaEventSynchronize(e1));
+    float msr = 0;
+    CK(cudaEventElapsedTime(&msr, e0, e1));
+    *out = msr / trial_steps;
+    return QGW_OK;
+  };
+  int rc;
+  {
+    const int ctd = e->precision == QGW_FP64 ? 4 : 8;
+    const std::vector<int> cand[4] = {{16, 32}, {ctd, ctd / 2}, {2, 4, 8, 16}, {2, 3, 4, 5}};
+    qgw_shape cur{};
+    qgw_get_shape(e->members[0], &cur);
+    int* field[4] = {&cur.rhs_tile_rows, &cur.col_tile, &cur.row_group_fwd, &cur.row_group_inv};
+    for (int f = 0; f < 4; ++f) {
+      float best = 1e30f;
+      int best_v = *field[f];
+      for (int v : cand[f]) {
+        qgw_shape sh{};
+        int* sf[4] = {&sh.rhs_tile_rows, &sh.col_tile, &sh.row_group_fwd, &sh.row_group_inv};
+        *sf[f] = v;
+        if (ensemble_set_shape(e, sh) != QGW_OK) continue;  // e.g. beyond the shared memory
+        float msr;
+        if ((rc = trial(&msr))) return rc;
+        if (msr < best) { best = msr; best_v = v; }
+      }
+      qgw_shape sh{};
+      int* sf[4] = {&sh.rhs_tile_rows, &sh.col_tile, &sh.row_group_fwd, &sh.row_group_inv};
+      *sf[f] = best_v;
+      if ((rc = ensemble_set_shape(e, sh))) return rc;
+      *field[f] = best_v;
+    }
+    drop_graph(e);
+  }
+  const int cands[] = {0, 1, 2, 3, 4, 5, 6, 8};  // 0: one block per work item
   for (int s = 0; s < 4; ++s) {
     float best = 1e30f;
     int best_b = e->bps[s];
@@ -332,21 +397,13 @@ int qgw_ensemble_tune(qgw_ensemble* ens, int trial_steps, float* best_ms) {
     if (s < 3) occ = stage_occupancy(e, s, e->sm.bytes[s]);
     else
       for (int r = 1; r <= 4; ++r)
-        if (e->rhs_total[r] > 0) occ = std::max(occ, stage_occupancy(e, 3 + r, e->sm.rhs_bytes[r]));
+        if (e->rhs_total[r] > 0) occ = std::max(occ, stage_occupancy(e, rhs_stage(e, r), e->sm.rhs_bytes[r]));
     for (int b : cands) {
       if (b > occ) break;  // same grid as the resident maximum
       e->bps[s] = b;
       set_grids(e);
-      if (e->precision == QGW_FP64) qgw::ens_begin_f64(e->e64, e->d_maxsteps, e->stream);
-      else qgw::ens_begin_f32c(e->e32, e->d_maxsteps, e->stream);
-      launch_step(e, 15);  // warm-up
-      CK(cudaEventRecord(e0, e->stream));
-      for (int t = 0; t < trial_steps; ++t) launch_step(e, 15);
-      CK(cudaEventRecord(e1, e->stream));
-      CK(cudaEventSynchronize(e1));
-      float msr = 0;
-      CK(cudaEventElapsedTime(&msr, e0, e1));
-      msr /= trial_steps;
+      float msr;
+      if ((rc = trial(&msr))) return rc;
       if (msr < best) { best = msr; best_b = b; }
     }
     e->bps[s] = best_b;
@@ -394,6 +451,19 @@ int qgw_ensemble_set_forcing_records(qgw_ensemble* ens, int i, const double* rec
   CK(cudaStreamSynchronize(e->stream));
   const int rc = qgw_set_forcing_records(e->members[i], rec, nrec);
   return rc ? rc : qgw::ens_core_build(e);  // the member table holds the record pointers
+}
+
+int qgw_ensemble_set_shape(qgw_ensemble* ens, const qgw_shape* sh) {
+  qgw::EnsembleCore* e = ens ? &ens->core : nullptr;
+  if (!e || !sh) return QGW_ERR_PARAM;
+  CK(cudaStreamSynchronize(e->stream));
+  return ensemble_set_shape(e, *sh);
+}
+
+int qgw_ensemble_shape(qgw_ensemble* ens, int i, qgw_shape* sh) {
+  qgw::EnsembleCore* e = ens ? &ens->core : nullptr;
+  if (!e || !sh || i < 0 || i >= (int)e->members.size()) return QGW_ERR_PARAM;
+  return qgw_get_shape(e->members[i], sh);
 }
 
 int qgw_ensemble_grids(qgw_ensemble* ens, int* bps4) {

@@ -13,13 +13,16 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 3) k_rows_fwd(StepArg
   __shared__ __align__(16) T cst[NLMAX * GMAX];
   body_rows_fwd<T, COMP, PER>(a, step_mode, blockIdx.x, smem_raw, tot, cst);
 }
-template <typename T, bool COMP, bool PER>
+// CT: columns per tile (closed basin; the periodic kernel takes two complex
+// columns whatever CT)
+template <typename T, bool COMP, bool PER, int CT>
 __global__ void __launch_bounds__(NT, 3) k_cols(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
   if (PER) body_cols_per<T, COMP>(a, step_mode, blockIdx.x, blockIdx.y, smem_raw);
-  else body_cols<T, COMP>(a, step_mode, blockIdx.x, blockIdx.y, smem_raw, tot);
+  else body_cols<T, COMP, CT>(a, step_mode, blockIdx.x, blockIdx.y, smem_raw, tot);
 }
+template <typename T> constexpr int CTD = ColsPer<T>::value;
 template <typename T, bool COMP, bool PER>
 __global__ void __launch_bounds__(NT, 3) k_rows_inv(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -31,7 +34,7 @@ __global__ void __launch_bounds__(NT, 3) k_rows_inv(StepArgs<T> a, int step_mode
 // ntx x nty x nl tiles (body_rhs_tiles); the FP64 path launches one block
 // per tile (its tiles keep the FP64 pipe busy, and blocks that each load
 // one tile overlap one another's loads without a second buffer).
-template <typename T, bool COMP, int R>
+template <typename T, bool COMP, int R, int TY>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 4) k_rhs(const __grid_constant__ StepArgs<T> a, int ntx,
                                                                     int nty) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -43,7 +46,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 4) k_rhs(const __grid
     mbar_init(&bar[1]);
   }
   __syncthreads();
-  body_rhs_tiles<T, COMP, R, rhs_nbuf<T>()>(a, ntx, nty, base, a.use_tma ? &a.tm[0] : nullptr, bar);
+  body_rhs_tiles<T, COMP, R, TY, rhs_nbuf<T>()>(a, ntx, nty, base, a.use_tma ? &a.tm[0] : nullptr, bar);
 }
 
 // ------------------------------------------------------- small kernels
@@ -327,20 +330,24 @@ static cudaError_t set_attrs(const StepArgs<T>& a) {
   const int lim = optin - (int)static_tot;
   if ((e = cudaFuncSetAttribute(k_rows_fwd<T, COMP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
   if ((e = cudaFuncSetAttribute(k_rows_inv<T, COMP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
-  if ((e = cudaFuncSetAttribute(k_cols<T, COMP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
+  if ((e = cudaFuncSetAttribute(k_cols<T, COMP, false, CTD<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
+    return e;
+  if ((e = cudaFuncSetAttribute(k_cols<T, COMP, false, CTD<T> / 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
+    return e;
   if ((e = cudaFuncSetAttribute(k_rows_fwd<T, COMP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
   if ((e = cudaFuncSetAttribute(k_rows_inv<T, COMP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
-  if ((e = cudaFuncSetAttribute(k_cols<T, COMP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
+  if ((e = cudaFuncSetAttribute(k_cols<T, COMP, true, CTD<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
+    return e;
   if ((e = cudaFuncSetAttribute(k_forc_cols<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
   if ((e = cudaFuncSetAttribute(k_forc_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
   const int rl = optin - 1024;
-  if ((e = cudaFuncSetAttribute(k_rhs<T, COMP, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, rl)) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(k_rhs<T, COMP, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, rl)) != cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(k_rhs<T, COMP, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, rl)) != cudaSuccess)
-    return e;
-  return cudaFuncSetAttribute(k_rhs<T, COMP, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, rl);
+  const void* rhs_kernels[] = {(const void*)k_rhs<T, COMP, 1, 16>, (const void*)k_rhs<T, COMP, 2, 16>,
+                               (const void*)k_rhs<T, COMP, 3, 16>, (const void*)k_rhs<T, COMP, 4, 16>,
+                               (const void*)k_rhs<T, COMP, 1, 32>, (const void*)k_rhs<T, COMP, 2, 32>,
+                               (const void*)k_rhs<T, COMP, 3, 32>, (const void*)k_rhs<T, COMP, 4, 32>};
+  for (const void* f : rhs_kernels)
+    if ((e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, rl)) != cudaSuccess) return e;
+  return cudaSuccess;
 }
 
 template <typename T, bool COMP>
@@ -351,8 +358,9 @@ static void launch_k1(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
 template <typename T, bool COMP>
 static void launch_k2(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
   const dim3 grid(col_tiles(a), a.nl);
-  if (a.periodic) k_cols<T, COMP, true><<<grid, NT, smem_cols<T, COMP>(a), s>>>(a, step_mode);
-  else k_cols<T, COMP, false><<<grid, NT, smem_cols<T, COMP>(a), s>>>(a, step_mode);
+  if (a.periodic) k_cols<T, COMP, true, CTD<T>><<<grid, NT, smem_cols<T, COMP>(a), s>>>(a, step_mode);
+  else if (col_width(a) == CTD<T>) k_cols<T, COMP, false, CTD<T>><<<grid, NT, smem_cols<T, COMP>(a), s>>>(a, step_mode);
+  else k_cols<T, COMP, false, CTD<T> / 2><<<grid, NT, smem_cols<T, COMP>(a), s>>>(a, step_mode);
 }
 template <typename T, bool COMP>
 static void launch_k3(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
@@ -361,7 +369,7 @@ static void launch_k3(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
 }
 // tiles of the RHS kernel along x and y
 template <typename T> static int rhs_ntx(const StepArgs<T>& a) { return (a.nx + TX - 1) / TX; }
-template <typename T> static int rhs_nty(const StepArgs<T>& a) { return (a.ny + TY - 1) / TY; }
+template <typename T> static int rhs_nty(const StepArgs<T>& a) { return (a.ny + rhs_ty(a) - 1) / rhs_ty(a); }
 
 template <typename T, bool COMP>
 static void launch_rhs(const StepArgs<T>& a, cudaStream_t s) {
@@ -369,11 +377,24 @@ static void launch_rhs(const StepArgs<T>& a, cudaStream_t s) {
   const int grid = (a.rhs_grid > 0 && a.rhs_grid < ntiles) ? a.rhs_grid : ntiles;
   const dim3 blk(32, 8);
   const size_t sm = smem_rhs_tiles(a);
+  const bool t32 = rhs_ty(a) == 32;
   switch (rhs_halo(a)) {
-    case 1: k_rhs<T, COMP, 1><<<grid, blk, sm, s>>>(a, ntx, nty); break;
-    case 2: k_rhs<T, COMP, 2><<<grid, blk, sm, s>>>(a, ntx, nty); break;
-    case 3: k_rhs<T, COMP, 3><<<grid, blk, sm, s>>>(a, ntx, nty); break;
-    default: k_rhs<T, COMP, 4><<<grid, blk, sm, s>>>(a, ntx, nty); break;
+    case 1:
+      if (t32) k_rhs<T, COMP, 1, 32><<<grid, blk, sm, s>>>(a, ntx, nty);
+      else k_rhs<T, COMP, 1, 16><<<grid, blk, sm, s>>>(a, ntx, nty);
+      break;
+    case 2:
+      if (t32) k_rhs<T, COMP, 2, 32><<<grid, blk, sm, s>>>(a, ntx, nty);
+      else k_rhs<T, COMP, 2, 16><<<grid, blk, sm, s>>>(a, ntx, nty);
+      break;
+    case 3:
+      if (t32) k_rhs<T, COMP, 3, 32><<<grid, blk, sm, s>>>(a, ntx, nty);
+      else k_rhs<T, COMP, 3, 16><<<grid, blk, sm, s>>>(a, ntx, nty);
+      break;
+    default:
+      if (t32) k_rhs<T, COMP, 4, 32><<<grid, blk, sm, s>>>(a, ntx, nty);
+      else k_rhs<T, COMP, 4, 16><<<grid, blk, sm, s>>>(a, ntx, nty);
+      break;
   }
 }
 
@@ -385,13 +406,12 @@ static int rhs_grid(const StepArgs<T>& a) {
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
   const size_t sm = smem_rhs_tiles(a);
-  cudaError_t e;
-  switch (rhs_halo(a)) {
-    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rhs<T, COMP, 1>, NT, sm); break;
-    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rhs<T, COMP, 2>, NT, sm); break;
-    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rhs<T, COMP, 3>, NT, sm); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rhs<T, COMP, 4>, NT, sm); break;
-  }
+  const int h = rhs_halo(a);
+  const void* f = rhs_ty(a) == 32 ? (h == 1 ? (const void*)k_rhs<T, COMP, 1, 32> : h == 2 ? (const void*)k_rhs<T, COMP, 2, 32>
+                                     : h == 3 ? (const void*)k_rhs<T, COMP, 3, 32> : (const void*)k_rhs<T, COMP, 4, 32>)
+                                  : (h == 1 ? (const void*)k_rhs<T, COMP, 1, 16> : h == 2 ? (const void*)k_rhs<T, COMP, 2, 16>
+                                     : h == 3 ? (const void*)k_rhs<T, COMP, 3, 16> : (const void*)k_rhs<T, COMP, 4, 16>);
+  const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, NT, sm);
   return (e == cudaSuccess && per > 0) ? per * sms : 0;
 }
 
@@ -483,7 +503,8 @@ int cols_per_tile_f64() { return ColsPer<double>::value; }
 int cols_per_tile_f32c() { return ColsPer<float>::value; }
 int rhs_tile_x() { return TX; }
 int rhs_box_width() { return TW; }
-int rhs_tile_y() { return TY; }
+int rhs_tile_y_f64(const StepArgs<double>& a) { return rhs_ty(a); }
+int rhs_tile_y_f32c(const StepArgs<float>& a) { return rhs_ty(a); }
 
 size_t smem_bytes_rows_f64(const StepArgs<double>& a) { return smem_rows<double, false>(a); }
 size_t smem_bytes_cols_f64(const StepArgs<double>& a) { return smem_cols<double, false>(a); }

@@ -46,7 +46,8 @@ void enqueue_budget_f32c(const StepArgs<float>& a, const double* wts, double* pa
 
 // ensembles (one persistent launch per stage over all members)
 // dynamic shared memory per stage; the RHS stage per halo radius R (rhs_bytes[R], 0: no member)
-struct EnsSmem { size_t bytes[4]; size_t rhs_bytes[5]; };
+// and the (ensemble-wide) RHS tile height and column-tile width
+struct EnsSmem { size_t bytes[4]; size_t rhs_bytes[5]; int rhs_ty; int ct; };
 cudaError_t ens_prepare_f64();
 cudaError_t ens_prepare_f32c();
 EnsSmem ens_smem_f64(const StepArgs<double>* host_members, int n);
@@ -82,7 +83,9 @@ int cols_per_tile_f32c();
 int rhs_tile_x();
 // TMA box width (columns) of the RHS kernel's interior tiles
 int rhs_box_width();
-int rhs_tile_y();
+// RHS tile height of a run (16 or 32 rows)
+int rhs_tile_y_f64(const StepArgs<double>& a);
+int rhs_tile_y_f32c(const StepArgs<float>& a);
 
 size_t smem_bytes_rows_f64(const StepArgs<double>& a);
 size_t smem_bytes_cols_f64(const StepArgs<double>& a);

@@ -5,6 +5,9 @@
 
 namespace qgw {
 
+// default columns per K2 tile (the alternative is half as many)
+template <typename T> constexpr int CTE = ColsPer<T>::value;
+
 // --------------------------------------------------- ensemble wrappers
 // Persistent launches over all members of an ensemble: work item w of a
 // stage belongs to member mi with start[mi] <= w < start[mi+1]; each block
@@ -69,9 +72,8 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 2) k_rows_fwd_ens(Ens
     __syncthreads();
   }
 }
-template <typename T, bool COMP, bool PER>
+template <typename T, bool COMP, bool PER, int CT>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 2) k_cols_ens(EnsArgs<T> e, int step_mode) {
-  constexpr int CT = ColsPer<T>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
   __shared__ StepArgs<T> sa;
@@ -81,7 +83,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 2) k_cols_ens(EnsArgs
     const int local = ens_item(e, e.start_cols, item, &sa, &cur);
     const int ntx = PER ? (sa.gx.H + 2) / 2 : (sa.nx + CT - 1) / CT;
     if (PER) body_cols_per<T, COMP>(sa, step_mode, local % ntx, local / ntx, smem_raw);
-    else body_cols<T, COMP>(sa, step_mode, local % ntx, local / ntx, smem_raw, tot);
+    else body_cols<T, COMP, CT>(sa, step_mode, local % ntx, local / ntx, smem_raw, tot);
     __syncthreads();
   }
 }
@@ -102,7 +104,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 2) k_rows_inv_ens(Ens
 // RHS stage of an ensemble: one launch per halo radius R over the members
 // with that radius (the work list of the launch gives the others no items),
 // so each launch runs the same specialised body as a single run.
-template <typename T, bool COMP, int R>
+template <typename T, bool COMP, int R, int TY>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 3) k_rhs_ens(EnsArgs<T> e) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ StepArgs<T> sa;
@@ -120,11 +122,21 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 3) k_rhs_ens(EnsArgs<
     // the tensor maps are read from the member table in global memory (TMA
     // takes them from the parameter, constant or global space, not shared);
     // only thread 0, which wrote cur, issues the copies
-    body_rhs<T, COMP, R>(sa, bx, by, bz, total, base, sa.use_tma ? &e.members[cur].tm[0] : nullptr, &bar, &phase);
+    body_rhs<T, COMP, R, TY>(sa, bx, by, bz, total, base, sa.use_tma ? &e.members[cur].tm[0] : nullptr, &bar, &phase);
     __syncthreads();
   }
 }
 
+
+// the RHS ensemble kernel of halo radius r and tile height ty
+template <typename T, bool COMP>
+static const void* rhs_ens_kernel(int r, int ty) {
+  if (ty == 32)
+    return r == 1 ? (const void*)k_rhs_ens<T, COMP, 1, 32> : r == 2 ? (const void*)k_rhs_ens<T, COMP, 2, 32>
+         : r == 3 ? (const void*)k_rhs_ens<T, COMP, 3, 32> : (const void*)k_rhs_ens<T, COMP, 4, 32>;
+  return r == 1 ? (const void*)k_rhs_ens<T, COMP, 1, 16> : r == 2 ? (const void*)k_rhs_ens<T, COMP, 2, 16>
+       : r == 3 ? (const void*)k_rhs_ens<T, COMP, 3, 16> : (const void*)k_rhs_ens<T, COMP, 4, 16>;
+}
 
 template <typename T>
 __global__ void k_begin_ens(EnsArgs<T> e, double t_out, double tend, const int* max_steps) {
@@ -202,17 +214,24 @@ static cudaError_t set_attrs_ens() {
     return e;
   if ((e = cudaFuncSetAttribute(k_rows_inv_ens<T, COMP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
     return e;
-  if ((e = cudaFuncSetAttribute(k_cols_ens<T, COMP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
+  if ((e = cudaFuncSetAttribute(k_cols_ens<T, COMP, false, CTE<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
+    return e;
+  if ((e = cudaFuncSetAttribute(k_cols_ens<T, COMP, false, CTE<T> / 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                lim)))
+    return e;
   if ((e = cudaFuncSetAttribute(k_rows_fwd_ens<T, COMP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
     return e;
   if ((e = cudaFuncSetAttribute(k_rows_inv_ens<T, COMP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
     return e;
-  if ((e = cudaFuncSetAttribute(k_cols_ens<T, COMP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
+  if ((e = cudaFuncSetAttribute(k_cols_ens<T, COMP, true, CTE<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
+    return e;
   const int rl = optin - (int)(sizeof(StepArgs<T>) + 1024);
-  if ((e = cudaFuncSetAttribute(k_rhs_ens<T, COMP, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, rl))) return e;
-  if ((e = cudaFuncSetAttribute(k_rhs_ens<T, COMP, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, rl))) return e;
-  if ((e = cudaFuncSetAttribute(k_rhs_ens<T, COMP, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, rl))) return e;
-  return cudaFuncSetAttribute(k_rhs_ens<T, COMP, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, rl);
+  for (int t = 0; t < 2; ++t)
+    for (int r = 1; r <= 4; ++r)
+      if ((e = cudaFuncSetAttribute(rhs_ens_kernel<T, COMP>(r, t ? 32 : 16), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    rl)))
+        return e;
+  return cudaSuccess;
 }
 
 template <typename T, bool COMP>
@@ -225,8 +244,17 @@ static EnsSmem ens_smem(const StepArgs<T>* host_members, int n) {
     s.bytes[2] = std::max(s.bytes[2], smem_rows_inv<T, COMP>(a));
     s.bytes[3] = std::max(s.bytes[3], smem_rhs<T>(a));
     s.rhs_bytes[rhs_halo(a)] = smem_rhs<T>(a);
+    s.rhs_ty = rhs_ty(a);  // the same for every member of an ensemble
+    s.ct = col_width(a);
   }
   return s;
+}
+
+// the closed-basin column stage at the ensemble's column-tile width
+template <typename T, bool COMP>
+static void launch_cols_ens(const EnsArgs<T>& e, const EnsSmem& sm, int grid, int step_mode, cudaStream_t s) {
+  if (sm.ct == CTE<T> / 2) k_cols_ens<T, COMP, false, CTE<T> / 2><<<grid, NT, sm.bytes[1], s>>>(e, step_mode);
+  else k_cols_ens<T, COMP, false, CTE<T>><<<grid, NT, sm.bytes[1], s>>>(e, step_mode);
 }
 
 template <typename T, bool COMP>
@@ -234,31 +262,32 @@ static void ens_step(const EnsArgs<T>& e, const EnsArgs<T>* er, const EnsSmem& s
                      int which_mask, int periodic, cudaStream_t s) {
   if (periodic) {
     if (which_mask & 1) k_rows_fwd_ens<T, COMP, true><<<grid[0], NT, sm.bytes[0], s>>>(e, 1);
-    if (which_mask & 2) k_cols_ens<T, COMP, true><<<grid[1], NT, sm.bytes[1], s>>>(e, 1);
+    if (which_mask & 2) k_cols_ens<T, COMP, true, CTE<T>><<<grid[1], NT, sm.bytes[1], s>>>(e, 1);
     if (which_mask & 4) k_rows_inv_ens<T, COMP, true><<<grid[2], NT, sm.bytes[2], s>>>(e, 1);
   } else {
     if (which_mask & 1) k_rows_fwd_ens<T, COMP, false><<<grid[0], NT, sm.bytes[0], s>>>(e, 1);
-    if (which_mask & 2) k_cols_ens<T, COMP, false><<<grid[1], NT, sm.bytes[1], s>>>(e, 1);
+    if (which_mask & 2) launch_cols_ens<T, COMP>(e, sm, grid[1], 1, s);
     if (which_mask & 4) k_rows_inv_ens<T, COMP, false><<<grid[2], NT, sm.bytes[2], s>>>(e, 1);
   }
   if (which_mask & 8) {
     const dim3 blk(32, 8);
-    if (rgrid[1] > 0) k_rhs_ens<T, COMP, 1><<<rgrid[1], blk, sm.rhs_bytes[1], s>>>(er[1]);
-    if (rgrid[2] > 0) k_rhs_ens<T, COMP, 2><<<rgrid[2], blk, sm.rhs_bytes[2], s>>>(er[2]);
-    if (rgrid[3] > 0) k_rhs_ens<T, COMP, 3><<<rgrid[3], blk, sm.rhs_bytes[3], s>>>(er[3]);
-    if (rgrid[4] > 0) k_rhs_ens<T, COMP, 4><<<rgrid[4], blk, sm.rhs_bytes[4], s>>>(er[4]);
+    for (int r = 1; r <= 4; ++r)
+      if (rgrid[r] > 0) {
+        void* args[] = {(void*)&er[r]};
+        cudaLaunchKernel(rhs_ens_kernel<T, COMP>(r, sm.rhs_ty), dim3(rgrid[r]), blk, args, sm.rhs_bytes[r], s);
+      }
   }
 }
 template <typename T, bool COMP>
 static void ens_invert(const EnsArgs<T>& e, const EnsSmem& sm, const int* grid, int periodic, cudaStream_t s) {
   if (periodic) {
     k_rows_fwd_ens<T, COMP, true><<<grid[0], NT, sm.bytes[0], s>>>(e, 0);
-    k_cols_ens<T, COMP, true><<<grid[1], NT, sm.bytes[1], s>>>(e, 0);
+    k_cols_ens<T, COMP, true, CTE<T>><<<grid[1], NT, sm.bytes[1], s>>>(e, 0);
     k_rows_inv_ens<T, COMP, true><<<grid[2], NT, sm.bytes[2], s>>>(e, 0);
     return;
   }
   k_rows_fwd_ens<T, COMP, false><<<grid[0], NT, sm.bytes[0], s>>>(e, 0);
-  k_cols_ens<T, COMP, false><<<grid[1], NT, sm.bytes[1], s>>>(e, 0);
+  launch_cols_ens<T, COMP>(e, sm, grid[1], 0, s);
   k_rows_inv_ens<T, COMP, false><<<grid[2], NT, sm.bytes[2], s>>>(e, 0);
 }
 
@@ -268,13 +297,14 @@ static int ens_occupancy(int stage, size_t smem) {
   cudaError_t e = cudaSuccess;
   // the periodic variants have the same register and shared-memory needs
   if (stage == 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_rows_fwd_ens<T, COMP, false>, NT, smem);
-  if (stage == 1) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_cols_ens<T, COMP, false>, NT, smem);
+  if (stage == 1) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_cols_ens<T, COMP, false, CTE<T>>, NT, smem);
   if (stage == 2) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_rows_inv_ens<T, COMP, false>, NT, smem);
-  // stage 3 + R: the RHS kernel of halo radius R
-  if (stage == 4) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_rhs_ens<T, COMP, 1>, NT, smem);
-  if (stage == 5) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_rhs_ens<T, COMP, 2>, NT, smem);
-  if (stage == 6) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_rhs_ens<T, COMP, 3>, NT, smem);
-  if (stage == 7) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_rhs_ens<T, COMP, 4>, NT, smem);
+  // stage 3 + R: the RHS kernel of halo radius R (both tile heights have the
+  // same register needs; smem gives the difference)
+  if (stage >= 4 && stage <= 7)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, rhs_ens_kernel<T, COMP>(stage - 3, 16), NT, smem);
+  if (stage >= 8 && stage <= 11)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, rhs_ens_kernel<T, COMP>(stage - 7, 32), NT, smem);
   return e == cudaSuccess && b > 0 ? b : 1;
 }
 int ens_blocks_per_sm_f64(int stage, size_t smem) { return ens_occupancy<double, false>(stage, smem); }

@@ -134,7 +134,7 @@ template <typename T> struct StepArgs {
   const float* sy2f;
   // FP32 copies of the RHS and Helmholtz constants (compensated path), made
   // on the host: a double -> float conversion runs on the FP64 pipe
-  float fc[20];
+  float fc[24];
   const float* iRd2f;
   int CT;                          // (unused by the kernels; kept for layout)
   int vec_cols;                    // rows are 16-byte aligned: 16-byte column loads
@@ -151,7 +151,8 @@ template <typename T> struct StepArgs {
   // the element-wise asynchronous copies instead
   CUtensorMap tm[3];
   int use_tma;
-  int rhs_grid;                    // blocks of the persistent RHS kernel (0: one per tile)
+  int rhs_grid;
+  int rhs_ty;  // RHS tile height: 16 (default) or 32 rows                    // blocks of the persistent RHS kernel (0: one per tile)
   // iterations of the first bounded wait for a tile's TMA bytes (normally
   // kWaitIters; lowered only by tests, to make that wait run out -- the
   // second wait, which lets the bytes land before the block moves on, always
@@ -186,8 +187,9 @@ enum FcIndex {
   FC_LX2,
   FC_LY2,
   FC_NUHS,        // nu_hyper itself (zeta_mode 2: the field is scaled)
-  FC_NUHD2,       // nuh_scaled * Delta^2 (zeta_mode 1 interior tiles: the chain from the raw zeta)
-  FC_COUNT
+  FC_NUHD2,       // nuh_scaled * Delta^2 (zeta_mode 1: the chain runs on L psi / Delta^2)
+  FC_GHD1,        // gh[1..4] / Delta^2 (its ghost factors)
+  FC_COUNT = FC_GHD1 + 4
 };
 static_assert(FC_COUNT <= (int)(sizeof(StepArgs<float>::fc) / sizeof(float)), "fc holds every constant");
 

@@ -38,15 +38,19 @@ namespace qgw {
 constexpr int NT = 256;          // threads per block in every step kernel
 constexpr int GMAX = 16;         // max rows of one batched DST in a block
 constexpr int NLMAX = 32;        // max layers on the GPU path
-constexpr int TX = 32, TY = 16;  // RHS tile (interior points)
+constexpr int TX = 32, TYD = 16;  // RHS tile (interior points): width, default height (16 or 32)
 constexpr double TEPS = 1e-9;    // src/timestep.h:16
 constexpr double HUGEV = 1e30;   // src/qg.c:43
 
 // columns per block of the column kernel (one or two 16-byte vectors per row):
 // four, so that the three work buffers of the compensated path leave room
 // for four blocks per SM
-// columns per K2 tile: 32-byte rows of FP32 (8) and FP64 (4) values
+// columns per K2 tile: 32-byte rows of FP32 (8) and FP64 (4) values by
+// default, 16-byte rows (half as many columns) as the alternative
 template <typename T> struct ColsPer { static constexpr int value = 32 / (int)sizeof(T); };
+template <typename T> __host__ __device__ inline int col_width(const StepArgs<T>& a) {
+  return a.CT == ColsPer<T>::value / 2 ? a.CT : ColsPer<T>::value;
+}
 
 // --------------------------------------------------------------- DST block
 // Batched DST-I of nrows rows (row r at A + r*ld, padded input format) by
@@ -544,10 +548,9 @@ __device__ __forceinline__ void store_cols(T* __restrict__ dst, const T* v) {
   }
 }
 
-template <typename T, bool COMP>
+template <typename T, bool COMP, int CT>
 __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, int bx, int m, unsigned char* smem_raw,
                                           T* tot) {
-  constexpr int CT = ColsPer<T>::value;
   DevState* st = a.state;
   if (step_mode && !st->active) return;
   const int k0 = bx * CT;
@@ -996,11 +999,6 @@ __device__ __forceinline__ int wrap_index(int g, int n) {
   return r < 0 ? r + n : r;
 }
 
-// RHS tile of TX x TY points of one layer; block (32, 8); R = halo radius
-// of psi (the number of hyperviscosity sweeps, at least 1).  EDGE: the tile
-// plus its halo touches a wall, so loads are bounds-checked and ghost values
-// follow adjust_bc; interior tiles (the vast majority) skip all of that.
-// Returns this thread's CFL maximum |dpsi| as bits in the arithmetic width.
 // Shared-memory layout of the RHS tile: psi-shaped arrays (psi, the two
 // chain buffers) have HH = TY + 2R rows of TW = TX + 8 columns, tile column
 // xx at TW offset TOX = 4 (xx = -4..TX+3, the span of one TMA box starting at
@@ -1015,7 +1013,7 @@ template <typename T> __host__ __device__ constexpr int tile_round(int n) {
 // with halo R, q with halo 1 and, in zeta mode 1, the raw zeta of the first
 // sweep's region) followed by the work buffers (the chain's ping-pong and,
 // for FP64, the centred differences).  Every array starts 128-byte aligned.
-template <typename T, int R> struct RhsShape {
+template <typename T, int R, int TY> struct RhsShape {
   static constexpr int HH = TY + 2 * R, QH = TY + 2, QW = TX + 2;
   static constexpr int TS = tile_round<T>(TW * HH), QS = tile_round<T>(TW * QH), ZS = tile_round<T>(TW * (HH - 2));
   static constexpr int IS = TS + QS + ZS;  // one input buffer
@@ -1028,13 +1026,13 @@ template <typename T> struct RhsIn {
   T* qs;  // QH x TW: q with halo 1
   T* zt;  // (HH - 2) x TW: zeta over the first sweep's region (zeta mode 1)
 };
-template <typename T, int R> __device__ __forceinline__ RhsIn<T> rhs_in(unsigned char* base, int b) {
-  using S = RhsShape<T, R>;
+template <typename T, int R, int TY> __device__ __forceinline__ RhsIn<T> rhs_in(unsigned char* base, int b) {
+  using S = RhsShape<T, R, TY>;
   T* p = (T*)base + (size_t)b * S::IS;
   return RhsIn<T>{p, p + S::TS, p + S::TS + S::QS};
 }
-template <typename T, int R> __device__ __forceinline__ T* rhs_work(unsigned char* base, int nb) {
-  return (T*)base + (size_t)nb * RhsShape<T, R>::IS;
+template <typename T, int R, int TY> __device__ __forceinline__ T* rhs_work(unsigned char* base, int nb) {
+  return (T*)base + (size_t)nb * RhsShape<T, R, TY>::IS;
 }
 
 // Loads of one tile that do not go through TMA, into `in`: edge tiles
@@ -1045,7 +1043,7 @@ template <typename T, int R> __device__ __forceinline__ T* rhs_work(unsigned cha
 // edge tile's ghost values of q (which need the whole psi tile) and of the
 // chain are formed by rhs_tile_compute.  The caller synchronises the block
 // afterwards.
-template <typename T, bool COMP, int R, bool EDGE>
+template <typename T, bool COMP, int R, int TY, bool EDGE>
 __device__ __forceinline__ void rhs_tile_fetch(const StepArgs<T>& a, int i0, int j0, int k, const RhsIn<T>& in) {
   constexpr int W = TW, HH = TY + 2 * R;
   constexpr int QW = TX + 2, QH = TY + 2;
@@ -1122,7 +1120,7 @@ __device__ __forceinline__ void rhs_tile_fetch(const StepArgs<T>& a, int i0, int
 // and, in zeta mode 1, zeta over the first sweep's region (HH - 2 rows), each
 // TW columns from x = i0 - 4; the mbarrier `bar` collects the bytes.  The
 // caller has synchronised the block since the buffers were last read.
-template <typename T, bool COMP, int R>
+template <typename T, bool COMP, int R, int TY>
 __device__ __forceinline__ void rhs_tile_tma(const StepArgs<T>& a, int i0, int j0, int k, const RhsIn<T>& in,
                                              const CUtensorMap* tm, unsigned long long* bar) {
   constexpr int W = TW, HH = TY + 2 * R, QH = TY + 2;
@@ -1157,14 +1155,14 @@ __device__ __forceinline__ bool rhs_tile_wait(const StepArgs<T>& a, unsigned lon
 // skip all of that.  The tile's inputs are in `in` and the block has been
 // synchronised since they arrived; `wk` holds the work buffers.  Returns
 // this thread's CFL maximum |dpsi| as bits in the arithmetic width.
-template <typename T, bool COMP, int R, bool EDGE>
+template <typename T, bool COMP, int R, int TY, bool EDGE>
 __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile_compute(const StepArgs<T>& a, int i0, int j0,
                                                                             int k, int step_index,
                                                                             const RhsIn<T>& in, T* wk) {
   constexpr int W = TW, HH = TY + 2 * R;
   constexpr int QW = TX + 2, QH = TY + 2;
   constexpr int XO = TOX;  // column of tile x = 0
-  constexpr int TS = RhsShape<T, R>::TS;
+  constexpr int TS = RhsShape<T, R, TY>::TS;
   T* ps = in.ps;              // HH x W, psi with halo R
   T* qs = in.qs;              // QH x W
   T* L0 = wk;                 // chain ping-pong
@@ -1193,14 +1191,18 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile_compute(const
 #define QS(x, y) qs[((y) + 1) * W + (x) + XO]
   const int tid = tx + ty * 32;
   const bool per = a.periodic != 0;
-  // zeta mode 2: the chain value at this thread's two points (x = tx,
-  // y = 2 ty + h; the FP32 Jacobian's mapping), loaded first so that its
+  // zeta mode 2: the chain value at this thread's points (x = tx, y = 16 b
+  // + 2 ty + h; the FP32 Jacobian's mapping), loaded first so that its
   // latency overlaps the tile's shared-memory work
-  T hv[2] = {T(0), T(0)};
+  static_assert(TY % 16 == 0, "tiles of 16-row bands");
+  constexpr int NBAND = TY / 16;
+  T hv[2 * NBAND];
+#pragma unroll
+  for (int h = 0; h < 2 * NBAND; ++h) hv[h] = T(0);
   if (zm2) {
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int gi = i0 + tx, gj = j0 + 2 * ty + h;
+    for (int h = 0; h < 2 * NBAND; ++h) {
+      const int gi = i0 + tx, gj = j0 + 16 * (h >> 1) + 2 * ty + (h & 1);
       if (!EDGE || (gi < nx && gj < ny)) hv[h] = zetaL[(size_t)gj * pitch + gi];
     }
   }
@@ -1227,15 +1229,18 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile_compute(const
   // sweep is the spectral zeta.  Unrolled over s so that every region
   // width is a compile-time constant.  Region of sweep s: tile rows
   // yy = s-R .. TY+R-s-1 (smem row yy + R), columns xx likewise (xx + XO).
-  // Interior tiles in zeta mode 1 take the zeta tile itself as the first
-  // sweep's output (fold): the chain then runs on zeta = L psi / Delta^2
-  // rather than L psi, and the factor Delta^2 moves into the coefficient.
-  const bool fold = !EDGE && zm && ksweep >= 1;
-  const T* Lp = fold ? in.zt - W : ps;  // zt's row 0 is the first sweep's first row
+  // Zeta mode 1 runs the chain on zeta = L psi / Delta^2 rather than L psi
+  // (fold): an interior tile takes the zeta tile itself as the first
+  // sweep's output, edge tiles divide their ghost values by Delta^2, and
+  // the factor Delta^2 moves into the coefficient.  Every point's value is
+  // then the same whatever tile holds it (the tile shape never changes the
+  // result).
+  const bool fold = zm && ksweep >= 1;
+  const T* Lp = (fold && !EDGE) ? in.zt - W : ps;  // zt's row 0 is the first sweep's first row
   T* Lc = L0;
 #pragma unroll
   for (int s = 1; s <= R; ++s) {
-    if (s <= ksweep && !(s == 1 && fold)) {
+    if (s <= ksweep && !(s == 1 && fold && !EDGE)) {
       __syncthreads();
       const int Ws = TX + 2 * R - 2 * s, Hs = HH - 2 * s;
       const int cx = s - R + XO;  // smem column of the region's first point
@@ -1245,14 +1250,15 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile_compute(const
           const int yr = w / Ws, xr = w - yr * Ws;
           const int o = (yr + s) * W + xr + cx;
           if (s == 1 && zm) {
-            Lc[o] = d2 * zetaL[(size_t)wrap_index(j0 + yr + s - R, ny) * pitch + wrap_index(i0 + xr + s - R, nx)];
+            Lc[o] = zetaL[(size_t)wrap_index(j0 + yr + s - R, ny) * pitch + wrap_index(i0 + xr + s - R, nx)];
           } else {
             const T sum = (Lp[o + 1] + Lp[o - 1]) + (Lp[o + W] + Lp[o - W]);
             Lc[o] = fmaT(T(-4), Lp[o], sum);
           }
         }
       } else if (EDGE) {
-        const T ghs = pick<T>(a.gh[s], a.fc[FC_GH1 + s - 1]);
+        // ghost factor of sweep s (divided by Delta^2 in zeta mode 1)
+        const T ghs = pick<T>(a.gh[s], a.fc[(fold ? FC_GHD1 : FC_GH1) + s - 1]);
         for (int w = tid; w < Ws * Hs; w += NT) {
           const int yr = w / Ws, xr = w - yr * Ws;
           const int xx = xr + s - R, yy = yr + s - R;
@@ -1262,7 +1268,7 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile_compute(const
           T v = T(0);
           if (inx && iny) {
             if (s == 1 && zm) {
-              v = d2 * in.zt[o - W];  // the zeta tile, one row up
+              v = in.zt[o - W];  // the zeta tile, one row up
             } else {
               const T sum = (Lp[o + 1] + Lp[o - 1]) + (Lp[o + W] + Lp[o - W]);
               v = fmaT(T(-4), Lp[o], sum);
@@ -1356,8 +1362,10 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile_compute(const
     // FP32: the Arakawa Jacobian (jacobian_lev, src/domain.h:17-27)
     // straight from the tiles, two vertically adjacent points per thread
     // sharing their 4 x 3 neighbourhoods (FP32 arithmetic is cheap; the
-    // instructions that move data are not)
-    const int y0 = 2 * ty;
+    // instructions that move data are not), in each 16-row band of the tile
+#pragma unroll
+    for (int band = 0; band < NBAND; ++band) {
+    const int y0 = 16 * band + 2 * ty;
     T P[4][3], Q[4][3];
 #pragma unroll
     for (int r = 0; r < 4; ++r)
@@ -1383,7 +1391,8 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile_compute(const
       J = fmaT(-Q[r - 1][1], P[r - 1][2] - P[r - 1][0], J);
       J = fmaT(-Q[r][2], P[r + 1][2] - P[r - 1][2], J);
       J = fmaT(Q[r][0], P[r + 1][0] - P[r - 1][0], J);
-      finish(y, J, dxp, dyp, hv[h]);
+      finish(y, J, dxp, dyp, hv[2 * band + h]);
+    }
     }
   } else {
     // FP64: centred differences shared between neighbouring Jacobian
@@ -1455,8 +1464,8 @@ __device__ __forceinline__ void rhs_block_done(DevState* st, unsigned long long 
 }
 
 // the tile at (i0, j0) plus its psi halo R touches a wall (or wraps)
-__device__ __forceinline__ bool rhs_edge_tile(int i0, int j0, int R, int nx, int ny) {
-  return i0 < R || j0 < R || i0 + TX + R > nx || j0 + TY + R > ny;
+__device__ __forceinline__ bool rhs_edge_tile(int i0, int j0, int R, int ty, int nx, int ny) {
+  return i0 < R || j0 < R || i0 + TX + R > nx || j0 + ty + R > ny;
 }
 
 // The RHS stage of one run: tiles t = blockIdx.x, blockIdx.x + gridDim.x,
@@ -1464,12 +1473,12 @@ __device__ __forceinline__ bool rhs_edge_tile(int i0, int j0, int R, int nx, int
 // input buffers, the next interior tile's TMA boxes are issued before the
 // current tile is computed, so that its copy overlaps the computation.
 // NB == 1: one tile per block, loaded and then computed.
-template <typename T, bool COMP, int R, int NB>
+template <typename T, bool COMP, int R, int TY, int NB>
 __device__ __forceinline__ void body_rhs_tiles(const StepArgs<T>& a, int ntx, int nty, unsigned char* base,
                                                const CUtensorMap* tm, unsigned long long* bar) {
   DevState* st = a.state;
   if (!st->active) return;
-  T* wk = rhs_work<T, R>(base, NB);
+  T* wk = rhs_work<T, R, TY>(base, NB);
   // mbarrier parities of the two buffers (two scalars: an array indexed by
   // the loop's buffer number would live in local memory)
   unsigned int ph0 = 0u, ph1 = 0u;
@@ -1490,8 +1499,8 @@ __device__ __forceinline__ void body_rhs_tiles(const StepArgs<T>& a, int ntx, in
   if (NB == 2 && tm && tid == 0 && (int)blockIdx.x < ntiles) {
     int i0, j0, k;
     tile_of((int)blockIdx.x, i0, j0, k);
-    if (!per || !rhs_edge_tile(i0, j0, R, a.nx, a.ny))
-      rhs_tile_tma<T, COMP, R>(a, i0, j0, k, rhs_in<T, R>(base, 0), tm, &bar[0]);
+    if (!per || !rhs_edge_tile(i0, j0, R, TY, a.nx, a.ny))
+      rhs_tile_tma<T, COMP, R, TY>(a, i0, j0, k, rhs_in<T, R, TY>(base, 0), tm, &bar[0]);
   }
   decltype(absbits_native(T(0))) mymax = 0;
   int it = 0;
@@ -1499,30 +1508,30 @@ __device__ __forceinline__ void body_rhs_tiles(const StepArgs<T>& a, int ntx, in
     const int cur = NB == 2 ? (it & 1) : 0;
     int i0, j0, k;
     tile_of(t, i0, j0, k);
-    const bool edge = rhs_edge_tile(i0, j0, R, a.nx, a.ny);
-    const RhsIn<T> in = rhs_in<T, R>(base, cur);
+    const bool edge = rhs_edge_tile(i0, j0, R, TY, a.nx, a.ny);
+    const RhsIn<T> in = rhs_in<T, R, TY>(base, cur);
     if (NB == 2 && tm && tid == 0 && t + step < ntiles) {
       // the next tile's boxes into the other buffer (last read by the
       // previous tile, which every thread has finished: the trailing
       // __syncthreads of the previous iteration)
       int i1, j1, k1;
       tile_of(t + step, i1, j1, k1);
-      if (!per || !rhs_edge_tile(i1, j1, R, a.nx, a.ny))
-        rhs_tile_tma<T, COMP, R>(a, i1, j1, k1, rhs_in<T, R>(base, cur ^ 1), tm, &bar[cur ^ 1]);
+      if (!per || !rhs_edge_tile(i1, j1, R, TY, a.nx, a.ny))
+        rhs_tile_tma<T, COMP, R, TY>(a, i1, j1, k1, rhs_in<T, R, TY>(base, cur ^ 1), tm, &bar[cur ^ 1]);
     }
     bool ok = true;
     if (edge && (per || !tm)) {
-      rhs_tile_fetch<T, COMP, R, true>(a, i0, j0, k, in);
+      rhs_tile_fetch<T, COMP, R, TY, true>(a, i0, j0, k, in);
     } else if (!tm) {
-      rhs_tile_fetch<T, COMP, R, false>(a, i0, j0, k, in);
+      rhs_tile_fetch<T, COMP, R, TY, false>(a, i0, j0, k, in);
     } else {
-      if (NB == 1 && tid == 0) rhs_tile_tma<T, COMP, R>(a, i0, j0, k, in, tm, &bar[0]);
+      if (NB == 1 && tid == 0) rhs_tile_tma<T, COMP, R, TY>(a, i0, j0, k, in, tm, &bar[0]);
       ok = cur ? rhs_tile_wait(a, &bar[1], &ph1) : rhs_tile_wait(a, &bar[0], &ph0);
     }
     __syncthreads();
     if (ok) {
-      const auto m = edge ? rhs_tile_compute<T, COMP, R, true>(a, i0, j0, k, si, in, wk)
-                          : rhs_tile_compute<T, COMP, R, false>(a, i0, j0, k, si, in, wk);
+      const auto m = edge ? rhs_tile_compute<T, COMP, R, TY, true>(a, i0, j0, k, si, in, wk)
+                          : rhs_tile_compute<T, COMP, R, TY, false>(a, i0, j0, k, si, in, wk);
       mymax = m > mymax ? m : mymax;
     }
     __syncthreads();
@@ -1532,32 +1541,32 @@ __device__ __forceinline__ void body_rhs_tiles(const StepArgs<T>& a, int ntx, in
 
 // One RHS tile (bx, by, layer k) of an ensemble member, in one input
 // buffer; `total` blocks share the member's CFL reduction.
-template <typename T, bool COMP, int R>
+template <typename T, bool COMP, int R, int TY>
 __device__ __forceinline__ void body_rhs(const StepArgs<T>& a, int bx, int by, int k, unsigned int total,
                                          unsigned char* smem_raw, const CUtensorMap* tm,
                                          unsigned long long* bar, unsigned int* phase) {
   DevState* st = a.state;
   if (!st->active) return;
   const int i0 = bx * TX, j0 = by * TY;
-  const bool edge = rhs_edge_tile(i0, j0, R, a.nx, a.ny);
+  const bool edge = rhs_edge_tile(i0, j0, R, TY, a.nx, a.ny);
   const int si = st->step_index;
   const int tid = threadIdx.x + threadIdx.y * 32;
-  const RhsIn<T> in = rhs_in<T, R>(smem_raw, 0);
-  T* wk = rhs_work<T, R>(smem_raw, 1);
+  const RhsIn<T> in = rhs_in<T, R, TY>(smem_raw, 0);
+  T* wk = rhs_work<T, R, TY>(smem_raw, 1);
   bool ok = true;
   if (edge && (a.periodic || !tm)) {
-    rhs_tile_fetch<T, COMP, R, true>(a, i0, j0, k, in);
+    rhs_tile_fetch<T, COMP, R, TY, true>(a, i0, j0, k, in);
   } else if (!tm) {
-    rhs_tile_fetch<T, COMP, R, false>(a, i0, j0, k, in);
+    rhs_tile_fetch<T, COMP, R, TY, false>(a, i0, j0, k, in);
   } else {
-    if (tid == 0) rhs_tile_tma<T, COMP, R>(a, i0, j0, k, in, tm, bar);
+    if (tid == 0) rhs_tile_tma<T, COMP, R, TY>(a, i0, j0, k, in, tm, bar);
     ok = rhs_tile_wait(a, bar, phase);
   }
   __syncthreads();
   decltype(absbits_native(T(0))) mymax = 0;
   if (ok) {
-    mymax = edge ? rhs_tile_compute<T, COMP, R, true>(a, i0, j0, k, si, in, wk)
-                 : rhs_tile_compute<T, COMP, R, false>(a, i0, j0, k, si, in, wk);
+    mymax = edge ? rhs_tile_compute<T, COMP, R, TY, true>(a, i0, j0, k, si, in, wk)
+                 : rhs_tile_compute<T, COMP, R, TY, false>(a, i0, j0, k, si, in, wk);
   }
   rhs_block_done(st, widen_absbits<T>(mymax), total, a.Delta, a.cfl);
 }
@@ -1590,14 +1599,14 @@ static size_t smem_cols(const StepArgs<T>& a) {
   // ([A] and [B] without the second field)
   const bool zm = COMP && a.zeta_mode;
   const size_t rows = a.periodic ? (size_t)(zm ? 3 : 2) * 2
-                                 : (size_t)(zm ? 2 : 1) * dst_bufs(a, a.gy) * ColsPer<T>::value;
+                                 : (size_t)(zm ? 2 : 1) * dst_bufs(a, a.gy) * col_width(a);
   return rows * padded_len<T>(a.gy.M) * sizeof(T);
 }
 // column tiles of one mode: four real columns (DST) or two complex columns
 // k = 0..nx/2 (periodic)
 template <typename T>
 static int col_tiles(const StepArgs<T>& a) {
-  return a.periodic ? (a.gx.H + 2) / 2 : (a.nx + ColsPer<T>::value - 1) / ColsPer<T>::value;
+  return a.periodic ? (a.gx.H + 2) / 2 : (a.nx + col_width(a) - 1) / col_width(a);
 }
 template <typename T, bool COMP>
 static size_t smem_rows_inv(const StepArgs<T>& a) {
@@ -1605,27 +1614,34 @@ static size_t smem_rows_inv(const StepArgs<T>& a) {
 }
 // dynamic shared memory of the RHS kernels for halo radius r and nb input
 // buffers (RhsShape)
-template <typename T>
-static size_t smem_rhs_r(int r, int nb = 1) {
+template <typename T, int TY>
+static size_t smem_rhs_rt(int r, int nb) {
   switch (r) {
-    case 1: return RhsShape<T, 1>::bytes(nb);
-    case 2: return RhsShape<T, 2>::bytes(nb);
-    case 3: return RhsShape<T, 3>::bytes(nb);
-    default: return RhsShape<T, 4>::bytes(nb);
+    case 1: return RhsShape<T, 1, TY>::bytes(nb);
+    case 2: return RhsShape<T, 2, TY>::bytes(nb);
+    case 3: return RhsShape<T, 3, TY>::bytes(nb);
+    default: return RhsShape<T, 4, TY>::bytes(nb);
   }
+}
+template <typename T>
+static size_t smem_rhs_r(int r, int nb = 1, int ty = TYD) {
+  return ty == 32 ? smem_rhs_rt<T, 32>(r, nb) : smem_rhs_rt<T, 16>(r, nb);
 }
 // halo radius of the RHS tiles: the Laplacian sweeps they run (none in zeta
 // mode 2, where the whole chain is spectral), at least 1 (the Jacobian)
 template <typename T>
 static int rhs_halo(const StepArgs<T>& a) { return (a.nsweep > 0 && a.zeta_mode != 2) ? a.nsweep : 1; }
+// the run's RHS tile height (16 or 32 rows)
 template <typename T>
-static size_t smem_rhs(const StepArgs<T>& a) { return smem_rhs_r<T>(rhs_halo(a)); }
+static int rhs_ty(const StepArgs<T>& a) { return a.rhs_ty == 32 ? 32 : 16; }
+template <typename T>
+static size_t smem_rhs(const StepArgs<T>& a) { return smem_rhs_r<T>(rhs_halo(a), 1, rhs_ty(a)); }
 // input buffers of the single-run RHS kernel: FP32 double-buffers its
 // persistent loop, FP64 runs one tile per block
 template <typename T>
 constexpr int rhs_nbuf() { return sizeof(T) == 4 ? 2 : 1; }
 template <typename T>
-static size_t smem_rhs_tiles(const StepArgs<T>& a) { return smem_rhs_r<T>(rhs_halo(a), rhs_nbuf<T>()); }
+static size_t smem_rhs_tiles(const StepArgs<T>& a) { return smem_rhs_r<T>(rhs_halo(a), rhs_nbuf<T>(), rhs_ty(a)); }
 
 constexpr int RHS_RMAX = 4;  // n_hyper <= 6
 

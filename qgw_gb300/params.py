@@ -55,6 +55,14 @@ class QgwStepInfo(ctypes.Structure):
                 ("stop_reason", ctypes.c_int), ("nonfinite", ctypes.c_int)]
 
 
+class QgwShape(ctypes.Structure):
+    """Work-tile shape of a run's step kernels (qgw_shape)."""
+    _fields_ = [(k, ctypes.c_int) for k in ("rhs_tile_rows", "col_tile", "row_group_fwd", "row_group_inv")]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
 class QgwBudget(ctypes.Structure):
     _fields_ = [(k, ctypes.c_double) for k in ("ke", "energy", "enstrophy", "wind_work")]
 
