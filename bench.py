@@ -494,8 +494,9 @@ def run_variants(args, capi, configs, torch, max_over_ranks, world):
 def run_ensemble(args, capi, configs, torch, barrier, max_over_ranks, world):
     """The batched form: uneven members (grids 128^2..1024^2, 2..10 layers,
     random wind amplitude, distinct noise seeds), all FP32-compensated, one
-    launch per step stage over all members, replayed as a CUDA graph, grids
-    chosen by the autotuner."""
+    launch per step stage over all members, replayed as a CUDA graph, the
+    work-tile shape (RHS tile height, column-tile width, modes per row-kernel
+    block) and then each stage's persistent grid chosen by the autotuner."""
     members = configs.ensemble_members(args.ensemble_members)
     ens = capi.Ensemble([configs.public(p) for p in members], capi.FP32C)
     q0s = [configs.noise_ic(p, p["_seed"]) for p in members]
@@ -506,7 +507,9 @@ def run_ensemble(args, capi, configs, torch, barrier, max_over_ranks, world):
             ens.fix_dt(i, p["dt"])
 
     reset()
+    default_shape = ens.get_shape(0)
     tuned_ms, grids = ens.tune(3)
+    shapes = [ens.get_shape(i) for i in range(len(members))]
     reset()
     ens.step(3)
     stream = torch.cuda.ExternalStream(0)
@@ -531,7 +534,11 @@ def run_ensemble(args, capi, configs, torch, barrier, max_over_ranks, world):
     del stream
     return {"value": world * lgp * args.ensemble_steps / wall, "unit": "lgp-steps/s", "members": len(members),
             "lgp_per_step": lgp, "steps": args.ensemble_steps, "ms_per_step": wall / args.ensemble_steps * 1e3,
-            "grids_blocks_per_sm": grids, "tuned_stage_ms": tuned_ms, "graph": True, "dtype": "f32 (q hi+lo)",
+            "grids_blocks_per_sm": grids, "tuned_stage_ms": tuned_ms,
+            "tile_shape": {"default": default_shape, "tuned_members": shapes,
+                           "searched": {"rhs_tile_rows": [16, 32], "col_tile": [8, 4],
+                                        "row_group_fwd": [2, 4, 8, 16], "row_group_inv": [2, 3, 4, 5]}},
+            "graph": True, "dtype": "f32 (q hi+lo)",
             "largest_member_alone_equals_in_mix": same,
             "timing": "host wall clock around qgw_ensemble_step (graph replays + flush + state read-back)"}
 
