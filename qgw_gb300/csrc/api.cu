@@ -450,6 +450,15 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   float* fi;
   if ((rc = upload<float>(r, &fi, r->iRd2))) return rc;
   a.iRd2f = fi;
+  // column tiles of 32-byte rows, or 16-byte rows where the former's
+  // buffers would pass 200 KiB of shared memory (long columns with the
+  // second spectral field: FP32 NY = 2048 in zeta mode)
+  {
+    size_t need;
+    if constexpr (sizeof(T) == 8) need = qgw::smem_bytes_cols_f64(a);
+    else need = qgw::smem_bytes_cols_f32c(a);
+    if (need > (size_t)200 * 1024) a.CT = (32 / (int)sizeof(T)) / 2;
+  }
   // TMA tensor maps of the RHS kernel's tiles (psi with halo R, q with halo
   // 1, in zeta mode 1 zeta over the first sweep's region; zeta mode 2 reads
   // its field point by point)

@@ -231,9 +231,40 @@ void ens_core_free_tables(EnsembleCore* e) {
   e->d_maxsteps = nullptr;
 }
 
+// The batched kernels take the column-tile width and the RHS tile height
+// as template arguments, one for all members: where members differ (a run
+// whose long columns forced the narrower tile, a member set alone), every
+// member takes the narrower width and, if their heights differ, 16 rows.
+// No shape changes a result.
+static int uniform_shape(EnsembleCore* e) {
+  if (e->members.empty()) return QGW_OK;
+  qgw_shape first{};
+  qgw_get_shape(e->members[0], &first);
+  int ct = first.col_tile, ty = first.rhs_tile_rows;
+  bool mixed = false;
+  for (qgw_run* r : e->members) {
+    qgw_shape sh{};
+    qgw_get_shape(r, &sh);
+    if (sh.col_tile != ct || sh.rhs_tile_rows != ty) mixed = true;
+    ct = std::min(ct, sh.col_tile);
+    if (sh.rhs_tile_rows != ty) ty = 16;
+  }
+  if (!mixed) return QGW_OK;
+  qgw_shape want{};
+  want.col_tile = ct;
+  want.rhs_tile_rows = ty;
+  for (qgw_run* r : e->members) {
+    const int rc = qgw_set_shape(r, &want);
+    if (rc) return rc;
+  }
+  return QGW_OK;
+}
+
 int ens_core_build(EnsembleCore* e) {
   const cudaError_t pe = e->precision == QGW_FP64 ? ens_prepare_f64() : ens_prepare_f32c();
   if (pe != cudaSuccess) return cuda_fail(pe);
+  const int rc = uniform_shape(e);
+  if (rc) return rc;
   return build_tables(e);
 }
 

@@ -155,3 +155,23 @@ def test_ensemble_tuner_picks_a_shape(qgwlib):
         psi_a, q_a = alone(qgwlib, p, 1, q0, 5)
         assert np.array_equal(q, q_a) and np.array_equal(psi, psi_a), i
     ens.close()
+
+
+def test_ensemble_of_mixed_column_widths(qgwlib):
+    """A 2048^2 FP32c member takes 16-byte column tiles (its 32-byte-row
+    buffers would pass the shared memory a block can have) while a small
+    member defaults to 32-byte ones: the ensemble gives both the narrower
+    width and each member still equals its run alone bitwise."""
+    ps = [C.cfg2(2048, 2), C.cfg2(128, 5)]
+    q0s = [C.noise_ic(p, 1100 + i) for i, p in enumerate(ps)]
+    ens = qgwlib.Ensemble(ps, 1)
+    assert [ens.get_shape(i)["col_tile"] for i in range(2)] == [4, 4]
+    for i, (p, q0) in enumerate(zip(ps, q0s)):
+        ens.set_q(i, q0)
+        ens.fix_dt(i, p["dt"])
+    ens.step(3)
+    for i, (p, q0) in enumerate(zip(ps, q0s)):
+        psi, q = ens.get(i)
+        psi_a, q_a = alone(qgwlib, p, 1, q0, 3)
+        assert np.array_equal(q, q_a) and np.array_equal(psi, psi_a), i
+    ens.close()

@@ -367,6 +367,27 @@ def test_fp32c_vs_fp64_100_steps(qgwlib, nx, nl):
     assert rel(psi32, psi64) <= TOL32C, rel(psi32, psi64)
 
 
+def test_fp32c_2048_columns(qgwlib):
+    """NX = NY = 2048 in zeta mode: the column tiles fall back to 16-byte
+    rows (their 32-byte-row buffers would pass the shared memory a block can
+    have), and the FP32c step still tracks the FP64 one.  The bounds are
+    looser than at 1024^2: at the same dt the biharmonic chain's grid-scale
+    factor is 2^6 = 64 times larger on the finer grid and amplifies FP32
+    round-off (q: 1.1e-5 after 10 steps), and psi of a white-noise q is
+    dominated by its lowest modes, which receive the FP32 transforms'
+    round-off relative to the whole of q (a relative error that grows with
+    the number of modes: 1.0e-4 after 10 steps)."""
+    p = C.cfg2(2048, 2)
+    q0 = C.noise_ic(p, 35)
+    r = qgwlib.Run(p, 1)
+    assert r.get_shape()["col_tile"] == 4
+    r.close()
+    psi64, q64, _ = gpu_run(qgwlib, p, q0, 10, 600.0, precision=0)
+    psi32, q32, _ = gpu_run(qgwlib, p, q0, 10, 600.0, precision=1)
+    assert rel(q32, q64) <= 2 * TOL32C, rel(q32, q64)
+    assert rel(psi32, psi64) <= 2e-4, rel(psi32, psi64)
+
+
 def test_budget_matches_numpy(qgwlib):
     p = C.cfg1(128)
     q0 = C.noise_ic(p, 9)
