@@ -30,7 +30,8 @@ CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unknown-pragmas", "-pth
 def cuda_include() -> str:
     return os.path.join(os.path.dirname(os.path.dirname(nvcc())), "include")
 
-CU_SOURCES = ["kernels.cu", "kernels_ens.cu", "api.cu", "ensemble.cu", "probe.cu", "noalloc.cu"]
+CU_SOURCES = ["kernels.cu", "kernels_f32c.cu", "kernels_ens.cu", "kernels_ens_f32c.cu", "api.cu", "ensemble.cu", "probe.cu",
+              "noalloc.cu"]
 CXX_SOURCES = ["host.cpp", "ncio.cpp", "serve.cpp"]
 
 

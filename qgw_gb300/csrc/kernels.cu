@@ -3,32 +3,42 @@
 // side they share with the ensemble kernels is step_device.cuh.
 #include "step_device.cuh"
 
+// The FP64 and the FP32c instantiations compile as two translation units
+// (in parallel): this file compiled directly is part 1 (the FP64 kernels and
+// the precision-free helpers), kernels_f32c.cu includes it as part 2 (the
+// FP32c kernels).  The few non-template kernels are static to each unit.
+#ifndef QGW_KERNELS_PART
+#define QGW_KERNELS_PART 1
+#endif
+
 namespace qgw {
 
 // ------------------------------------------------- single-run wrappers
-template <typename T, bool COMP, bool PER>
+// HL: 0, or the half-length whose transform alone the kernel holds (512:
+// the 1024-point rows and columns of the common grid)
+template <typename T, bool COMP, bool PER, int HL>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 3) k_rows_fwd(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
   __shared__ __align__(16) T cst[NLMAX * GMAX];
-  body_rows_fwd<T, COMP, PER>(a, step_mode, blockIdx.x, smem_raw, tot, cst);
+  body_rows_fwd<T, COMP, PER, HL>(a, step_mode, blockIdx.x, smem_raw, tot, cst);
 }
 // CT: columns per tile (closed basin; the periodic kernel takes two complex
 // columns whatever CT)
-template <typename T, bool COMP, bool PER, int CT>
+template <typename T, bool COMP, bool PER, int CT, int HL>
 __global__ void __launch_bounds__(NT, 3) k_cols(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
   if (PER) body_cols_per<T, COMP>(a, step_mode, blockIdx.x, blockIdx.y, smem_raw);
-  else body_cols<T, COMP, CT>(a, step_mode, blockIdx.x, blockIdx.y, smem_raw, tot);
+  else body_cols<T, COMP, CT, HL>(a, step_mode, blockIdx.x, blockIdx.y, smem_raw, tot);
 }
 template <typename T> constexpr int CTD = ColsPer<T>::value;
-template <typename T, bool COMP, bool PER>
+template <typename T, bool COMP, bool PER, int HL>
 __global__ void __launch_bounds__(NT, 3) k_rows_inv(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
   __shared__ __align__(16) T cst[NLMAX * GMAX];
-  body_rows_inv<T, COMP, PER>(a, step_mode, blockIdx.x, smem_raw, tot, cst);
+  body_rows_inv<T, COMP, PER, HL>(a, step_mode, blockIdx.x, smem_raw, tot, cst);
 }
 // The RHS of a step: a persistent grid (a.rhs_grid blocks) over the
 // ntx x nty x nl tiles (body_rhs_tiles); the FP64 path launches one block
@@ -50,7 +60,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 4) k_rhs(const __grid
 }
 
 // ------------------------------------------------------- small kernels
-__global__ void k_begin(DevState* st, double t_out, double tend) { begin_state(st, t_out, tend, 0); }
+static __global__ void k_begin(DevState* st, double t_out, double tend) { begin_state(st, t_out, tend, 0); }
 
 template <typename T, bool COMP>
 // (a.qout: also writes the final q, joined to FP64, into the caller's array
@@ -113,7 +123,7 @@ __global__ void __launch_bounds__(NT) k_flush(StepArgs<T> a) {
   }
 }
 
-__global__ void k_end(DevState* st) { st->pending = 0; }
+static __global__ void k_end(DevState* st) { st->pending = 0; }
 
 // --------------------------------------------------- stochastic forcing
 // F1: new ring amplitudes after each completed step (calc_forc,
@@ -254,7 +264,7 @@ __global__ void __launch_bounds__(256) k_pack(const T* __restrict__ src, const T
 }
 
 // FP32c <-> FP64 conversions for the boundary copies
-__global__ void k_split_f64(const double* src, float* hi, float* lo, size_t n) {
+static __global__ void k_split_f64(const double* src, float* hi, float* lo, size_t n) {
   for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < n; w += (size_t)gridDim.x * blockDim.x) {
     const double x = src[w];
     const float h = (float)x;
@@ -262,7 +272,7 @@ __global__ void k_split_f64(const double* src, float* hi, float* lo, size_t n) {
     lo[w] = (float)(x - (double)h);
   }
 }
-__global__ void k_join_f64(const float* hi, const float* lo, double* dst, size_t n) {
+static __global__ void k_join_f64(const float* hi, const float* lo, double* dst, size_t n) {
   for (size_t w = blockIdx.x * (size_t)blockDim.x + threadIdx.x; w < n; w += (size_t)gridDim.x * blockDim.x)
     dst[w] = (double)hi[w] + (lo ? (double)lo[w] : 0.0);
 }
@@ -303,7 +313,7 @@ __global__ void __launch_bounds__(NT) k_budget_partial(StepArgs<T> a, const doub
   if (threadIdx.x < 4) part[blockIdx.x * 4 + threadIdx.x] = red[threadIdx.x][0];
 }
 
-__global__ void k_budget_final(const double* part, int nblk, double scale, double* out) {
+static __global__ void k_budget_final(const double* part, int nblk, double scale, double* out) {
   if (threadIdx.x < 4) {
     double s = 0;
     for (int b = 0; b < nblk; ++b) s += part[b * 4 + threadIdx.x];
@@ -328,16 +338,15 @@ static cudaError_t set_attrs(const StepArgs<T>& a) {
       smem_rhs<T>(a) + 1024 > (size_t)optin || smem_rhs_tiles<T>(a) + 1024 > (size_t)optin)
     return cudaErrorInvalidValue;
   const int lim = optin - (int)static_tot;
-  if ((e = cudaFuncSetAttribute(k_rows_fwd<T, COMP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
-  if ((e = cudaFuncSetAttribute(k_rows_inv<T, COMP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
-  if ((e = cudaFuncSetAttribute(k_cols<T, COMP, false, CTD<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
-    return e;
-  if ((e = cudaFuncSetAttribute(k_cols<T, COMP, false, CTD<T> / 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
-    return e;
-  if ((e = cudaFuncSetAttribute(k_rows_fwd<T, COMP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
-  if ((e = cudaFuncSetAttribute(k_rows_inv<T, COMP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
-  if ((e = cudaFuncSetAttribute(k_cols<T, COMP, true, CTD<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
-    return e;
+  const void* transforms[] = {
+      (const void*)k_rows_fwd<T, COMP, false, 0>,         (const void*)k_rows_fwd<T, COMP, false, 512>,
+      (const void*)k_rows_inv<T, COMP, false, 0>,         (const void*)k_rows_inv<T, COMP, false, 512>,
+      (const void*)k_cols<T, COMP, false, CTD<T>, 0>,     (const void*)k_cols<T, COMP, false, CTD<T>, 512>,
+      (const void*)k_cols<T, COMP, false, CTD<T> / 2, 0>, (const void*)k_cols<T, COMP, false, CTD<T> / 2, 512>,
+      (const void*)k_rows_fwd<T, COMP, true, 0>,          (const void*)k_rows_inv<T, COMP, true, 0>,
+      (const void*)k_cols<T, COMP, true, CTD<T>, 0>};
+  for (const void* f : transforms)
+    if ((e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
   if ((e = cudaFuncSetAttribute(k_forc_cols<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
   if ((e = cudaFuncSetAttribute(k_forc_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
   const int rl = optin - 1024;
@@ -352,20 +361,28 @@ static cudaError_t set_attrs(const StepArgs<T>& a) {
 
 template <typename T, bool COMP>
 static void launch_k1(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
-  if (a.periodic) k_rows_fwd<T, COMP, true><<<dim3(a.ny), NT, smem_rows<T, COMP>(a), s>>>(a, step_mode);
-  else k_rows_fwd<T, COMP, false><<<dim3(a.ny), NT, smem_rows<T, COMP>(a), s>>>(a, step_mode);
+  const size_t sm = smem_rows<T, COMP>(a);
+  if (a.periodic) k_rows_fwd<T, COMP, true, 0><<<dim3(a.ny), NT, sm, s>>>(a, step_mode);
+  else if (a.gx.H == 512) k_rows_fwd<T, COMP, false, 512><<<dim3(a.ny), NT, sm, s>>>(a, step_mode);
+  else k_rows_fwd<T, COMP, false, 0><<<dim3(a.ny), NT, sm, s>>>(a, step_mode);
 }
 template <typename T, bool COMP>
 static void launch_k2(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
   const dim3 grid(col_tiles(a), a.nl);
-  if (a.periodic) k_cols<T, COMP, true, CTD<T>><<<grid, NT, smem_cols<T, COMP>(a), s>>>(a, step_mode);
-  else if (col_width(a) == CTD<T>) k_cols<T, COMP, false, CTD<T>><<<grid, NT, smem_cols<T, COMP>(a), s>>>(a, step_mode);
-  else k_cols<T, COMP, false, CTD<T> / 2><<<grid, NT, smem_cols<T, COMP>(a), s>>>(a, step_mode);
+  const size_t sm = smem_cols<T, COMP>(a);
+  const bool wide = col_width(a) == CTD<T>, h512 = a.gy.H == 512;
+  if (a.periodic) k_cols<T, COMP, true, CTD<T>, 0><<<grid, NT, sm, s>>>(a, step_mode);
+  else if (wide && h512) k_cols<T, COMP, false, CTD<T>, 512><<<grid, NT, sm, s>>>(a, step_mode);
+  else if (wide) k_cols<T, COMP, false, CTD<T>, 0><<<grid, NT, sm, s>>>(a, step_mode);
+  else if (h512) k_cols<T, COMP, false, CTD<T> / 2, 512><<<grid, NT, sm, s>>>(a, step_mode);
+  else k_cols<T, COMP, false, CTD<T> / 2, 0><<<grid, NT, sm, s>>>(a, step_mode);
 }
 template <typename T, bool COMP>
 static void launch_k3(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
-  if (a.periodic) k_rows_inv<T, COMP, true><<<dim3(a.ny), NT, smem_rows_inv<T, COMP>(a), s>>>(a, step_mode);
-  else k_rows_inv<T, COMP, false><<<dim3(a.ny), NT, smem_rows_inv<T, COMP>(a), s>>>(a, step_mode);
+  const size_t sm = smem_rows_inv<T, COMP>(a);
+  if (a.periodic) k_rows_inv<T, COMP, true, 0><<<dim3(a.ny), NT, sm, s>>>(a, step_mode);
+  else if (a.gx.H == 512) k_rows_inv<T, COMP, false, 512><<<dim3(a.ny), NT, sm, s>>>(a, step_mode);
+  else k_rows_inv<T, COMP, false, 0><<<dim3(a.ny), NT, sm, s>>>(a, step_mode);
 }
 // tiles of the RHS kernel along x and y
 template <typename T> static int rhs_ntx(const StepArgs<T>& a) { return (a.nx + TX - 1) / TX; }
@@ -440,77 +457,107 @@ static void launch_one(const StepArgs<T>& a, int which, cudaStream_t s) {
 }
 
 // ---- entry points used by api.cu (see kernels.h)
-cudaError_t prepare_f64(const StepArgs<double>& a) { return set_attrs<double, false>(a); }
-cudaError_t prepare_f32c(const StepArgs<float>& a) { return set_attrs<float, true>(a); }
-int rhs_grid_f64(const StepArgs<double>&) { return 0; }  // one block per tile
-int rhs_grid_f32c(const StepArgs<float>& a) { return rhs_grid<float, true>(a); }
-
-void enqueue_begin(DevState* st, double t_out, double tend, cudaStream_t s) { k_begin<<<1, 1, 0, s>>>(st, t_out, tend); }
-
-void enqueue_step_f64(const StepArgs<double>& a, cudaStream_t s) {
-  launch_invert<double, false>(a, 1, s);
-  launch_rhs<double, false>(a, s);
-  launch_forcing<double>(a, s);
-}
-void enqueue_step_f32c(const StepArgs<float>& a, cudaStream_t s) {
-  launch_invert<float, true>(a, 1, s);
-  launch_rhs<float, true>(a, s);
-  launch_forcing<float>(a, s);
-}
-void enqueue_forcing_f64(const StepArgs<double>& a, cudaStream_t s) { launch_forcing<double>(a, s); }
-void enqueue_forcing_f32c(const StepArgs<float>& a, cudaStream_t s) { launch_forcing<float>(a, s); }
-void enqueue_invert_f64(const StepArgs<double>& a, cudaStream_t s) { launch_invert<double, false>(a, 0, s); }
-void enqueue_invert_f32c(const StepArgs<float>& a, cudaStream_t s) { launch_invert<float, true>(a, 0, s); }
-void enqueue_flush_f64(const StepArgs<double>& a, cudaStream_t s) { launch_flush<double, false>(a, s); }
-void enqueue_flush_f32c(const StepArgs<float>& a, cudaStream_t s) { launch_flush<float, true>(a, s); }
-void enqueue_step_kernel_f64(const StepArgs<double>& a, int which, cudaStream_t s) { launch_one<double, false>(a, which, s); }
-void enqueue_step_kernel_f32c(const StepArgs<float>& a, int which, cudaStream_t s) { launch_one<float, true>(a, which, s); }
-
-void enqueue_unpack_f64(const double* full, double* q, int nx, int ny, int nl, int pitch, cudaStream_t s) {
-  k_unpack<double, false><<<152 * 8, 256, 0, s>>>(full, q, nullptr, nx, ny, nl, pitch);
-}
-void enqueue_unpack_split(const double* full, float* hi, float* lo, int nx, int ny, int nl, int pitch,
-                          cudaStream_t s) {
-  k_unpack<float, true><<<152 * 8, 256, 0, s>>>(full, hi, lo, nx, ny, nl, pitch);
-}
-void enqueue_pack_f64(const double* src, double* full, int nx, int ny, int nl, int pitch, cudaStream_t s) {
-  k_pack<double><<<152 * 8, 256, 0, s>>>(src, nullptr, full, nx, ny, nl, pitch);
-}
-void enqueue_pack_join(const float* hi, const float* lo, double* full, int nx, int ny, int nl, int pitch,
-                       cudaStream_t s) {
-  k_pack<float><<<152 * 8, 256, 0, s>>>(hi, lo, full, nx, ny, nl, pitch);
-}
-
-void enqueue_split_f64(const double* src, float* hi, float* lo, size_t n, cudaStream_t s) {
-  k_split_f64<<<1024, 256, 0, s>>>(src, hi, lo, n);
-}
-void enqueue_join_f64(const float* hi, const float* lo, double* dst, size_t n, cudaStream_t s) {
-  k_join_f64<<<1024, 256, 0, s>>>(hi, lo, dst, n);
-}
-
 template <typename T>
 static void budget_impl(const StepArgs<T>& a, const double* wts, double* part, int nblk, double scale, double* out,
                         cudaStream_t s) {
   k_budget_partial<T><<<nblk, NT, 0, s>>>(a, wts, part);
   k_budget_final<<<1, 32, 0, s>>>(part, nblk, scale, out);
 }
+
+#if QGW_KERNELS_PART == 1
+void enqueue_begin(DevState* st, double t_out, double tend, cudaStream_t s) { k_begin<<<1, 1, 0, s>>>(st, t_out, tend); }
+
+void enqueue_unpack_split(const double* full, float* hi, float* lo, int nx, int ny, int nl, int pitch,
+                          cudaStream_t s) {
+  k_unpack<float, true><<<152 * 8, 256, 0, s>>>(full, hi, lo, nx, ny, nl, pitch);
+}
+
+void enqueue_pack_join(const float* hi, const float* lo, double* full, int nx, int ny, int nl, int pitch,
+                       cudaStream_t s) {
+  k_pack<float><<<152 * 8, 256, 0, s>>>(hi, lo, full, nx, ny, nl, pitch);
+}
+
+int rhs_tile_x() { return TX; }
+
+int rhs_box_width() { return TW; }
+
+cudaError_t prepare_f64(const StepArgs<double>& a) { return set_attrs<double, false>(a); }
+
+int rhs_grid_f64(const StepArgs<double>&) { return 0; }  // one block per tile
+
+void enqueue_step_f64(const StepArgs<double>& a, cudaStream_t s) {
+  launch_invert<double, false>(a, 1, s);
+  launch_rhs<double, false>(a, s);
+  launch_forcing<double>(a, s);
+}
+
+void enqueue_forcing_f64(const StepArgs<double>& a, cudaStream_t s) { launch_forcing<double>(a, s); }
+
+void enqueue_invert_f64(const StepArgs<double>& a, cudaStream_t s) { launch_invert<double, false>(a, 0, s); }
+
+void enqueue_flush_f64(const StepArgs<double>& a, cudaStream_t s) { launch_flush<double, false>(a, s); }
+
+void enqueue_step_kernel_f64(const StepArgs<double>& a, int which, cudaStream_t s) { launch_one<double, false>(a, which, s); }
+
+void enqueue_unpack_f64(const double* full, double* q, int nx, int ny, int nl, int pitch, cudaStream_t s) {
+  k_unpack<double, false><<<152 * 8, 256, 0, s>>>(full, q, nullptr, nx, ny, nl, pitch);
+}
+
+void enqueue_pack_f64(const double* src, double* full, int nx, int ny, int nl, int pitch, cudaStream_t s) {
+  k_pack<double><<<152 * 8, 256, 0, s>>>(src, nullptr, full, nx, ny, nl, pitch);
+}
+
+void enqueue_split_f64(const double* src, float* hi, float* lo, size_t n, cudaStream_t s) {
+  k_split_f64<<<1024, 256, 0, s>>>(src, hi, lo, n);
+}
+
+void enqueue_join_f64(const float* hi, const float* lo, double* dst, size_t n, cudaStream_t s) {
+  k_join_f64<<<1024, 256, 0, s>>>(hi, lo, dst, n);
+}
+
 void enqueue_budget_f64(const StepArgs<double>& a, const double* w, double* part, int nblk, double scale, double* out,
                         cudaStream_t s) { budget_impl<double>(a, w, part, nblk, scale, out, s); }
+
+int cols_per_tile_f64() { return ColsPer<double>::value; }
+
+int rhs_tile_y_f64(const StepArgs<double>& a) { return rhs_ty(a); }
+
+size_t smem_bytes_rows_f64(const StepArgs<double>& a) { return smem_rows<double, false>(a); }
+
+size_t smem_bytes_cols_f64(const StepArgs<double>& a) { return smem_cols<double, false>(a); }
+
+size_t smem_bytes_rhs_f64(const StepArgs<double>& a) { return smem_rhs_tiles<double>(a); }
+#else
+cudaError_t prepare_f32c(const StepArgs<float>& a) { return set_attrs<float, true>(a); }
+
+int rhs_grid_f32c(const StepArgs<float>& a) { return rhs_grid<float, true>(a); }
+
+void enqueue_step_f32c(const StepArgs<float>& a, cudaStream_t s) {
+  launch_invert<float, true>(a, 1, s);
+  launch_rhs<float, true>(a, s);
+  launch_forcing<float>(a, s);
+}
+
+void enqueue_forcing_f32c(const StepArgs<float>& a, cudaStream_t s) { launch_forcing<float>(a, s); }
+
+void enqueue_invert_f32c(const StepArgs<float>& a, cudaStream_t s) { launch_invert<float, true>(a, 0, s); }
+
+void enqueue_flush_f32c(const StepArgs<float>& a, cudaStream_t s) { launch_flush<float, true>(a, s); }
+
+void enqueue_step_kernel_f32c(const StepArgs<float>& a, int which, cudaStream_t s) { launch_one<float, true>(a, which, s); }
+
 void enqueue_budget_f32c(const StepArgs<float>& a, const double* w, double* part, int nblk, double scale, double* out,
                          cudaStream_t s) { budget_impl<float>(a, w, part, nblk, scale, out, s); }
 
-int cols_per_tile_f64() { return ColsPer<double>::value; }
 int cols_per_tile_f32c() { return ColsPer<float>::value; }
-int rhs_tile_x() { return TX; }
-int rhs_box_width() { return TW; }
-int rhs_tile_y_f64(const StepArgs<double>& a) { return rhs_ty(a); }
+
 int rhs_tile_y_f32c(const StepArgs<float>& a) { return rhs_ty(a); }
 
-size_t smem_bytes_rows_f64(const StepArgs<double>& a) { return smem_rows<double, false>(a); }
-size_t smem_bytes_cols_f64(const StepArgs<double>& a) { return smem_cols<double, false>(a); }
-size_t smem_bytes_rhs_f64(const StepArgs<double>& a) { return smem_rhs_tiles<double>(a); }
 size_t smem_bytes_rows_f32c(const StepArgs<float>& a) { return smem_rows<float, true>(a); }
+
 size_t smem_bytes_cols_f32c(const StepArgs<float>& a) { return smem_cols<float, true>(a); }
+
 size_t smem_bytes_rhs_f32c(const StepArgs<float>& a) { return smem_rhs_tiles<float>(a); }
+#endif  // QGW_KERNELS_PART
 
 }  // namespace qgw

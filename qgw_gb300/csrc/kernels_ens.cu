@@ -3,6 +3,13 @@
 // they share with the single-run kernels is step_device.cuh.
 #include "step_device.cuh"
 
+// The FP64 and the FP32c instantiations compile as two translation units:
+// this file compiled directly is part 1 (FP64 and the precision-free
+// helpers), kernels_ens_f32c.cu includes it as part 2 (FP32c).
+#ifndef QGW_ENS_PART
+#define QGW_ENS_PART 1
+#endif
+
 namespace qgw {
 
 // default columns per K2 tile (the alternative is half as many)
@@ -307,43 +314,46 @@ static int ens_occupancy(int stage, size_t smem) {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, rhs_ens_kernel<T, COMP>(stage - 7, 32), NT, smem);
   return e == cudaSuccess && b > 0 ? b : 1;
 }
+#if QGW_ENS_PART == 1
 int ens_blocks_per_sm_f64(int stage, size_t smem) { return ens_occupancy<double, false>(stage, smem); }
-int ens_blocks_per_sm_f32c(int stage, size_t smem) { return ens_occupancy<float, true>(stage, smem); }
 int rhs_halo_of_f64(const StepArgs<double>& a) { return rhs_halo(a); }
 int col_tiles_f64(const StepArgs<double>& a) { return col_tiles(a); }
-int col_tiles_f32c(const StepArgs<float>& a) { return col_tiles(a); }
-int rhs_halo_of_f32c(const StepArgs<float>& a) { return rhs_halo(a); }
-
 cudaError_t ens_prepare_f64() { return set_attrs_ens<double, false>(); }
-cudaError_t ens_prepare_f32c() { return set_attrs_ens<float, true>(); }
 EnsSmem ens_smem_f64(const StepArgs<double>* m, int n) { return ens_smem<double, false>(m, n); }
-EnsSmem ens_smem_f32c(const StepArgs<float>* m, int n) { return ens_smem<float, true>(m, n); }
 void ens_begin_f64(const EnsArgs<double>& e, const int* max_steps, cudaStream_t s) {
   k_begin_ens<double><<<(e.n + 63) / 64, 64, 0, s>>>(e, 0.0, 0.0, max_steps);
-}
-void ens_begin_f32c(const EnsArgs<float>& e, const int* max_steps, cudaStream_t s) {
-  k_begin_ens<float><<<(e.n + 63) / 64, 64, 0, s>>>(e, 0.0, 0.0, max_steps);
 }
 void ens_step_f64(const EnsArgs<double>& e, const EnsArgs<double>* er, const EnsSmem& sm, const int* grid,
                   const int* rgrid, int mask, int periodic, cudaStream_t s) {
   ens_step<double, false>(e, er, sm, grid, rgrid, mask, periodic, s);
 }
-void ens_step_f32c(const EnsArgs<float>& e, const EnsArgs<float>* er, const EnsSmem& sm, const int* grid,
-                   const int* rgrid, int mask, int periodic, cudaStream_t s) {
-  ens_step<float, true>(e, er, sm, grid, rgrid, mask, periodic, s);
-}
 void ens_invert_f64(const EnsArgs<double>& e, const EnsSmem& sm, const int* grid, int periodic, cudaStream_t s) {
   ens_invert<double, false>(e, sm, grid, periodic, s);
-}
-void ens_invert_f32c(const EnsArgs<float>& e, const EnsSmem& sm, const int* grid, int periodic, cudaStream_t s) {
-  ens_invert<float, true>(e, sm, grid, periodic, s);
 }
 void ens_flush_f64(const EnsArgs<double>& e, int grid, cudaStream_t s) {
   k_flush_ens<double, false><<<grid, NT, 0, s>>>(e);
   k_end_ens<double><<<(e.n + 63) / 64, 64, 0, s>>>(e);
 }
+#else
+int ens_blocks_per_sm_f32c(int stage, size_t smem) { return ens_occupancy<float, true>(stage, smem); }
+int col_tiles_f32c(const StepArgs<float>& a) { return col_tiles(a); }
+int rhs_halo_of_f32c(const StepArgs<float>& a) { return rhs_halo(a); }
+cudaError_t ens_prepare_f32c() { return set_attrs_ens<float, true>(); }
+EnsSmem ens_smem_f32c(const StepArgs<float>* m, int n) { return ens_smem<float, true>(m, n); }
+void ens_begin_f32c(const EnsArgs<float>& e, const int* max_steps, cudaStream_t s) {
+  k_begin_ens<float><<<(e.n + 63) / 64, 64, 0, s>>>(e, 0.0, 0.0, max_steps);
+}
+void ens_step_f32c(const EnsArgs<float>& e, const EnsArgs<float>* er, const EnsSmem& sm, const int* grid,
+                   const int* rgrid, int mask, int periodic, cudaStream_t s) {
+  ens_step<float, true>(e, er, sm, grid, rgrid, mask, periodic, s);
+}
+void ens_invert_f32c(const EnsArgs<float>& e, const EnsSmem& sm, const int* grid, int periodic, cudaStream_t s) {
+  ens_invert<float, true>(e, sm, grid, periodic, s);
+}
 void ens_flush_f32c(const EnsArgs<float>& e, int grid, cudaStream_t s) {
   k_flush_ens<float, true><<<grid, NT, 0, s>>>(e);
   k_end_ens<float><<<(e.n + 63) / 64, 64, 0, s>>>(e);
 }
+#endif  // QGW_ENS_PART
+
 }  // namespace qgw

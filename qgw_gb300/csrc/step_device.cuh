@@ -105,9 +105,16 @@ __device__ __forceinline__ T* dst_block_generic(T* A, T* B, int nrows, int ld, c
 // use the compile-time specialisations of dst_fixed.cuh (FP32 M = 512 and
 // 1024: one warp per row, in place, the result in A), others (mixed radix
 // 2, 3, 5, 7) the generic loops.
-template <typename T>
+// HL != 0: a kernel specialised for half-length HL (its launcher checked the
+// run's length), whose code then holds that transform alone -- the step
+// kernels of the common lengths keep their instruction stream small.
+template <typename T, int HL = 0>
 __device__ __forceinline__ T* dst_block(T* A, T* B, int nrows, int ld, const DstGeom& g, const DstTables<T>& tb,
                                         T* tot) {
+  if constexpr (HL == 512) {
+    if constexpr (sizeof(T) == 4) return dst_block_warp_f32<9>(A, nrows, ld, tb);
+    else return dst_block_fixed<T, 9>(A, B, nrows, ld, tb);
+  }
   switch (g.H) {
     case 64: return dst_block_fixed<T, 6>(A, B, nrows, ld, tb);
     case 128: return dst_block_fixed<T, 7>(A, B, nrows, ld, tb);
@@ -424,7 +431,7 @@ __device__ __forceinline__ void project_fwd(const StepArgs<T>& a, int j, bool up
 
 // PER: doubly periodic basin -- real FFT of the row instead of the DST-I;
 // the spectral row holds X_0..X_H as (re, im) pairs (nx + 2 reals).
-template <typename T, bool COMP, bool PER>
+template <typename T, bool COMP, bool PER, int HL = 0>
 __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mode, int j, unsigned char* smem_raw,
                                               T* tot, T* cst) {
   DevState* st = a.state;
@@ -491,7 +498,7 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
 #undef QGW_PF_GB
 #undef QGW_PF
     __syncthreads();
-    T* O = PER ? rfft_block<T>(A, B, G, ld, a.gx, a.tx) : dst_block<T>(A, B, G, ld, a.gx, a.tx, tot);
+    T* O = PER ? rfft_block<T>(A, B, G, ld, a.gx, a.tx) : dst_block<T, HL>(A, B, G, ld, a.gx, a.tx, tot);
     // spectral row: the real FFT's X_0..X_H as (re, im) pairs from index 0,
     // or the DST's Y_1..Y_{M-1} from index 1
     const int nout = PER ? a.nx + 2 : a.nx, yo = PER ? 0 : 1;
@@ -548,7 +555,7 @@ __device__ __forceinline__ void store_cols(T* __restrict__ dst, const T* v) {
   }
 }
 
-template <typename T, bool COMP, int CT>
+template <typename T, bool COMP, int CT, int HL = 0>
 __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, int bx, int m, unsigned char* smem_raw,
                                           T* tot) {
   DevState* st = a.state;
@@ -600,7 +607,7 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
     }
   }
   __syncthreads();
-  T* O = dst_block<T>(A, B, CT, ld, a.gy, a.ty, tot);
+  T* O = dst_block<T, HL>(A, B, CT, ld, a.gy, a.ty, tot);
   T* C = O + (size_t)CT * ld;  // the second field's rows (zeta mode)
   const double iRd2 = a.iRd2[m];
   // power of the 5-point symbol in the second field: L psi (zeta mode 1) or
@@ -673,7 +680,7 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
   }
   __syncthreads();
   T* Oth = (O == A) ? B : A;
-  T* O2 = dst_block<T>(O, Oth, zm ? 2 * CT : CT, ld, a.gy, a.ty, tot);
+  T* O2 = dst_block<T, HL>(O, Oth, zm ? 2 * CT : CT, ld, a.gy, a.ty, tot);
   T* S2 = zm ? a.spec2 + (size_t)m * a.lstride : nullptr;
   T v[CT];
   for (int jj = threadIdx.x - 1; jj < ny; jj += NT) {
@@ -860,7 +867,7 @@ __device__ __forceinline__ void project_spec(const StepArgs<T>& a, int j, int G,
   }
 }
 
-template <typename T, bool COMP, bool PER>
+template <typename T, bool COMP, bool PER, int HL = 0>
 __device__ __forceinline__ void body_rows_inv(const StepArgs<T>& a, int step_mode, int j, unsigned char* smem_raw,
                                               T* tot, T* cst) {
   DevState* st = a.state;
@@ -900,7 +907,7 @@ __device__ __forceinline__ void body_rows_inv(const StepArgs<T>& a, int step_mod
     }
     __syncthreads();
     const int nrow = zm ? 2 * G : G;
-    T* O = PER ? irfft_block<T>(A, B, nrow, ld, a.gx, a.tx) : dst_block<T>(A, B, nrow, ld, a.gx, a.tx, tot);
+    T* O = PER ? irfft_block<T>(A, B, nrow, ld, a.gx, a.tx) : dst_block<T, HL>(A, B, nrow, ld, a.gx, a.tx, tot);
     // periodic: x_{2m+1} is minus the imaginary part of the backward FFT
     // (x_i at index i); DST: x_{i+1} at index i + 1
     const T odd = PER ? T(-1) : T(1);
