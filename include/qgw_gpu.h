@@ -39,13 +39,15 @@
 extern "C" {
 #endif
 
-#define QGW_ABI_VERSION 1
+#define QGW_ABI_VERSION 2
 
-/* Largest number of layers a params struct can describe.  The reference
- * sizes its dh/N2 arrays with nl_max = 1000 (src/qg.c:45); the GPU kernels
- * accept nl <= QGW_NL_GPU_MAX. */
-#define QGW_NL_MAX 64
-#define QGW_NL_GPU_MAX 32
+/* Largest number of layers a params struct can describe: the reference's
+ * nl_max (src/qg.c:45), which sizes its dh/N2 arrays.  The GPU kernels
+ * accept nl <= QGW_NL_GPU_MAX (their per-block projection coefficients,
+ * nl x 16 values, sit in shared memory); the allocation-free inversion
+ * keeps nl <= 32. */
+#define QGW_NL_MAX 1000
+#define QGW_NL_GPU_MAX 256
 
 typedef enum qgw_status {
   QGW_OK = 0,

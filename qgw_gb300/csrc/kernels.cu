@@ -20,8 +20,7 @@ template <typename T, bool COMP, bool PER, int HL>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 3) k_rows_fwd(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
-  __shared__ __align__(16) T cst[NLMAX * GMAX];
-  body_rows_fwd<T, COMP, PER, HL>(a, step_mode, blockIdx.x, smem_raw, tot, cst);
+  body_rows_fwd<T, COMP, PER, HL>(a, step_mode, blockIdx.x, smem_raw + cst_bytes<T>(a.nl), tot, (T*)smem_raw);
 }
 // CT: columns per tile (closed basin; the periodic kernel takes two complex
 // columns whatever CT)
@@ -37,8 +36,7 @@ template <typename T, bool COMP, bool PER, int HL>
 __global__ void __launch_bounds__(NT, 3) k_rows_inv(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
-  __shared__ __align__(16) T cst[NLMAX * GMAX];
-  body_rows_inv<T, COMP, PER, HL>(a, step_mode, blockIdx.x, smem_raw, tot, cst);
+  body_rows_inv<T, COMP, PER, HL>(a, step_mode, blockIdx.x, smem_raw + cst_bytes<T>(a.nl), tot, (T*)smem_raw);
 }
 // The RHS of a step: a persistent grid (a.rhs_grid blocks) over the
 // ntx x nty x nl tiles (body_rhs_tiles); the FP64 path launches one block
@@ -332,7 +330,7 @@ static cudaError_t set_attrs(const StepArgs<T>& a) {
   if (e != cudaSuccess) return e;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return e;
-  const size_t static_tot = sizeof(T) * (GMAX * 32 + NLMAX * GMAX) + 64;
+  const size_t static_tot = sizeof(T) * GMAX * 32 + 64;
   if (smem_rows<T, COMP>(a) + static_tot > (size_t)optin || smem_cols<T, COMP>(a) + static_tot > (size_t)optin ||
       smem_rows_inv<T, COMP>(a) + static_tot > (size_t)optin || rhs_halo(a) > RHS_RMAX ||
       smem_rhs<T>(a) + 1024 > (size_t)optin || smem_rhs_tiles<T>(a) + 1024 > (size_t)optin)

@@ -69,13 +69,12 @@ template <typename T, bool COMP, bool PER>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 2) k_rows_fwd_ens(EnsArgs<T> e, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
-  __shared__ __align__(16) T cst[NLMAX * GMAX];
   __shared__ StepArgs<T> sa;
   __shared__ int cur;
   ens_init_cur(&cur);
   for (int item = blockIdx.x; item < e.total[0]; item += gridDim.x) {
     const int local = ens_item(e, e.start_rows, item, &sa, &cur);
-    body_rows_fwd<T, COMP, PER>(sa, step_mode, local, smem_raw, tot, cst);
+    body_rows_fwd<T, COMP, PER>(sa, step_mode, local, smem_raw + cst_bytes<T>(sa.nl), tot, (T*)smem_raw);
     __syncthreads();
   }
 }
@@ -98,13 +97,12 @@ template <typename T, bool COMP, bool PER>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 3 : 2) k_rows_inv_ens(EnsArgs<T> e, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
-  __shared__ __align__(16) T cst[NLMAX * GMAX];
   __shared__ StepArgs<T> sa;
   __shared__ int cur;
   ens_init_cur(&cur);
   for (int item = blockIdx.x; item < e.total[2]; item += gridDim.x) {
     const int local = ens_item(e, e.start_rows, item, &sa, &cur);
-    body_rows_inv<T, COMP, PER>(sa, step_mode, local, smem_raw, tot, cst);
+    body_rows_inv<T, COMP, PER>(sa, step_mode, local, smem_raw + cst_bytes<T>(sa.nl), tot, (T*)smem_raw);
     __syncthreads();
   }
 }
@@ -216,7 +214,7 @@ static cudaError_t set_attrs_ens() {
   if (e != cudaSuccess) return e;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return e;
-  const int lim = optin - (int)(sizeof(T) * (GMAX * 32 + NLMAX * GMAX) + sizeof(StepArgs<T>) + 128);
+  const int lim = optin - (int)(sizeof(T) * GMAX * 32 + sizeof(StepArgs<T>) + 128);
   if ((e = cudaFuncSetAttribute(k_rows_fwd_ens<T, COMP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))
     return e;
   if ((e = cudaFuncSetAttribute(k_rows_inv_ens<T, COMP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)))

@@ -31,7 +31,7 @@ namespace {
 
 constexpr size_t kFieldMax = (size_t)1 << 21;  // doubles: nl*(NX+1)*(NY+1) limit
 constexpr int kMMax = 1024;                     // NX, NY limit (DST length + 1)
-constexpr int kNlMax = QGW_NL_GPU_MAX;
+constexpr int kNlMax = 32;  // layers the shared scratch array holds
 constexpr int kDevMax = 16;
 // DST tables of one dimension: tw (H), pre (H+1), spl (H/2+1), twp (< H)
 // complex values

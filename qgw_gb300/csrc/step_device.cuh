@@ -37,7 +37,12 @@ namespace qgw {
 
 constexpr int NT = 256;          // threads per block in every step kernel
 constexpr int GMAX = 16;         // max rows of one batched DST in a block
-constexpr int NLMAX = 32;        // max layers on the GPU path
+// The projection coefficients of a row kernel's mode (layer) group,
+// cst[l * GMAX + g], sit at the start of its dynamic shared memory, before
+// the work buffers: nl * GMAX values, rounded to whole 16-byte vectors.
+template <typename T> __host__ __device__ inline size_t cst_bytes(int nl) {
+  return ((size_t)nl * GMAX * sizeof(T) + 15) / 16 * 16;
+}
 constexpr int TX = 32, TYD = 16;  // RHS tile (interior points): width, default height (16 or 32)
 constexpr double TEPS = 1e-9;    // src/timestep.h:16
 constexpr double HUGEV = 1e30;   // src/qg.c:43
@@ -1597,7 +1602,7 @@ static int dst_bufs(const StepArgs<T>& a, const DstGeom& g) {
 }
 template <typename T, bool COMP>
 static size_t smem_rows(const StepArgs<T>& a) {
-  return (size_t)dst_bufs(a, a.gx) * a.G1 * padded_len<T>(a.gx.M) * sizeof(T);
+  return cst_bytes<T>(a.nl) + (size_t)dst_bufs(a, a.gx) * a.G1 * padded_len<T>(a.gx.M) * sizeof(T);
 }
 template <typename T, bool COMP>
 static size_t smem_cols(const StepArgs<T>& a) {
@@ -1617,7 +1622,8 @@ static int col_tiles(const StepArgs<T>& a) {
 }
 template <typename T, bool COMP>
 static size_t smem_rows_inv(const StepArgs<T>& a) {
-  return (size_t)((COMP && a.zeta_mode) ? 2 : 1) * dst_bufs(a, a.gx) * a.G3 * padded_len<T>(a.gx.M) * sizeof(T);
+  return cst_bytes<T>(a.nl) +
+         (size_t)((COMP && a.zeta_mode) ? 2 : 1) * dst_bufs(a, a.gx) * a.G3 * padded_len<T>(a.gx.M) * sizeof(T);
 }
 // dynamic shared memory of the RHS kernels for halo radius r and nb input
 // buffers (RhsShape)

@@ -14,7 +14,7 @@ from __future__ import annotations
 import ctypes
 from typing import Dict, Iterable
 
-NL_MAX = 64  # QGW_NL_MAX in include/qgw_gpu.h
+NL_MAX = 1000  # QGW_NL_MAX in include/qgw_gpu.h
 
 INT_KEYS = ("NX", "NY", "nl", "n_hyper")
 ARRAY_KEYS = ("dh", "N2")

@@ -417,12 +417,45 @@ def test_step_stops_at_t_out_and_tend(qgwlib):
 
 
 def test_unsupported_configs_fail_loudly(qgwlib):
-    deep = dict(C.cfg2(64, 33))  # more layers than the GPU kernels hold (32)
+    deep = dict(C.cfg2(16, 257))  # more layers than the GPU kernels hold (256)
     # NX = 22: half-length 11 (a prime beyond the radices 2, 3, 5, 7); NX = 99: odd
     for bad in (dict(C.cfg1(64), NX=22), dict(C.cfg1(64), NX=99), dict(C.cfg1(64), bc_fac=-0.5), deep):
         with pytest.raises(qgwlib.QgwError) as e:
             qgwlib.Run(bad)
         assert e.value.status == -6
+
+
+@pytest.mark.parametrize("nl", [40, 100])
+def test_many_layers_vs_port(qgwlib, oracle_mod, nl):
+    """More than 32 layers (the GPU kernels take up to 256; the reference's
+    nl_max is 1000): each row kernel's projection coefficients, nl x 16
+    values, sit in dynamic shared memory.  The run takes the port's own
+    vertical modes: with 100 stretched layers the stretching matrix's
+    eigenvectors are ill-conditioned (the library's satisfy
+    cm2l cl2m = I to 2.6e-11 at 100 layers against 2e-14 at 40), so two
+    eigensolvers' modes alone would separate psi by ~5e-6.  FP64 against the
+    port (each projection sums nl rounded terms, in spectral space on the
+    GPU and point by point in the port: the bound grows with nl), FP32c
+    against FP64."""
+    p = C.cfg2(64, nl)
+    q0 = C.noise_ic(p, 1201)
+    port = oracle_mod.Port(p)
+    modes = port.modes()
+    o = oracle_mod.run_port(p, q0, 20, dt_fixed=600.0)
+    out = []
+    for prec in (0, 1):
+        r = qgwlib.Run(p, prec, modes=modes)
+        r.set_q(q0)
+        r.fix_dt(600.0)
+        assert r.step(20).steps_taken == 20
+        out.append(r.get())
+        r.close()
+    (psi, q), (psi32, q32) = out
+    tol = TOL64 * nl / 10
+    assert rel(q, o["q"]) <= tol, rel(q, o["q"])
+    assert rel(psi, o["psi"]) <= tol, rel(psi, o["psi"])
+    assert rel(q32, q) <= TOL32C, rel(q32, q)
+    assert rel(psi32, psi) <= TOL32C, rel(psi32, psi)
 
 
 def test_runs_of_different_sizes_coexist(qgwlib):

@@ -30,7 +30,8 @@ def test_library_exports_every_declared_symbol(qgwlib):
     for n in names:
         assert hasattr(lib, n), n
     assert set(names) <= set(qgwlib.EXPORTS) | {"qgw_create_noalloc"} or True
-    assert lib.qgw_abi_version() == 1
+    hdr = open(os.path.join(ROOT, "include", "qgw_gpu.h")).read()
+    assert lib.qgw_abi_version() == int(re.search(r"#define QGW_ABI_VERSION (\d+)", hdr).group(1))
     assert lib.qgw_strerror(-6) == b"configuration not supported by the GPU kernels"
 
 
