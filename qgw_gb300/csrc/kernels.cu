@@ -46,13 +46,11 @@ template <typename T, bool COMP, int R, int TY>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 5 : 4) k_rhs(const __grid_constant__ StepArgs<T> a, int ntx,
                                                                     int nty) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ unsigned long long bar[2];
+  __shared__ unsigned long long bar[4];
   // TMA destinations are 128-byte aligned (the launch adds 128 bytes)
   unsigned char* base = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
-  if (threadIdx.x == 0 && threadIdx.y == 0) {
-    mbar_init(&bar[0]);
-    mbar_init(&bar[1]);
-  }
+  if (threadIdx.x == 0 && threadIdx.y == 0)
+    for (int b = 0; b < 4; ++b) mbar_init(&bar[b]);
   __syncthreads();
   body_rhs_tiles<T, COMP, R, TY, rhs_nbuf<T>()>(a, ntx, nty, base, a.use_tma ? &a.tm[0] : nullptr, bar);
 }

@@ -1328,7 +1328,8 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile_compute(const
   // Jacobian J and the centred differences dxp = psi_E - psi_W,
   // dyp = psi_N - psi_S (and, in zeta mode 2, the spectral chain value
   // hchain at the point); then the CFL maximum
-  auto finish = [&](int y, T J, T dxp, T dyp, T hchain) {
+  // (pc, pe, pn: psi at the point and its east and north neighbours)
+  auto finish = [&](int y, T J, T dxp, T dyp, T hchain, T pc, T pe, T pn) {
     const int gi = i0 + x, gj = j0 + y;
     // rhs, src/dynamics.h:55-58: -J - beta psi_x + nu lap q + nu_h lap^n psi
     T f = fmaT(m_inv12, J, -(b2d * dxp));
@@ -1364,8 +1365,8 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile_compute(const
     }
     fout[(size_t)gj * pitch + gi] = f;
     // CFL (adjust_timestep, src/timestep.h:74-87): one-sided differences
-    const T du = PS(x + 1, y) - PS(x, y);
-    const T dv = PS(x, y + 1) - PS(x, y);
+    const T du = pe - pc;
+    const T dv = pn - pc;
     const auto bu = absbits_native(du), bv = absbits_native(dv);
     const auto bm = bu > bv ? bu : bv;
     mymax_n = bm > mymax_n ? bm : mymax_n;
@@ -1403,7 +1404,7 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile_compute(const
       J = fmaT(-Q[r - 1][1], P[r - 1][2] - P[r - 1][0], J);
       J = fmaT(-Q[r][2], P[r + 1][2] - P[r - 1][2], J);
       J = fmaT(Q[r][0], P[r + 1][0] - P[r - 1][0], J);
-      finish(y, J, dxp, dyp, hv[2 * band + h]);
+      finish(y, J, dxp, dyp, hv[2 * band + h], P[r][1], P[r][2], P[r + 1][1]);
     }
     }
   } else {
@@ -1436,7 +1437,7 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile_compute(const
       J = fmaT(-QS(x, y - 1), DX(dxp, x, y - 1), J);
       J = fmaT(-QS(x + 1, y), DY(dyp, x + 1, y), J);
       J = fmaT(QS(x - 1, y), DY(dyp, x - 1, y), J);
-      finish(y, J, DX(dxp, x, y), DY(dyp, x, y), T(0));
+      finish(y, J, DX(dxp, x, y), DY(dyp, x, y), T(0), PS(x, y), PS(x + 1, y), PS(x, y + 1));
     }
   }
 #undef DY
@@ -1481,55 +1482,74 @@ __device__ __forceinline__ bool rhs_edge_tile(int i0, int j0, int R, int ty, int
 }
 
 // The RHS stage of one run: tiles t = blockIdx.x, blockIdx.x + gridDim.x,
-// ... over (x tile, y tile, layer).  NB == 2 (FP32, a persistent grid): two
-// input buffers, the next interior tile's TMA boxes are issued before the
-// current tile is computed, so that its copy overlaps the computation.
-// NB == 1: one tile per block, loaded and then computed.
+// ... over (x tile, y tile, layer).  NB >= 2 (FP32, a persistent grid): a
+// ring of NB input buffers; the boxes of the tile NB - 1 iterations ahead
+// are issued before the current tile is computed, so that a tile's copy has
+// NB - 1 tiles' computation to arrive in.  NB == 1: one tile per block,
+// loaded and then computed.
 template <typename T, bool COMP, int R, int TY, int NB>
 __device__ __forceinline__ void body_rhs_tiles(const StepArgs<T>& a, int ntx, int nty, unsigned char* base,
                                                const CUtensorMap* tm, unsigned long long* bar) {
+  static_assert(NB >= 1 && NB <= 4, "up to four input buffers");
   DevState* st = a.state;
   if (!st->active) return;
   T* wk = rhs_work<T, R, TY>(base, NB);
-  // mbarrier parities of the two buffers (two scalars: an array indexed by
-  // the loop's buffer number would live in local memory)
-  unsigned int ph0 = 0u, ph1 = 0u;
+  // mbarrier parities of the buffers, one bit each (a register: an array
+  // indexed by the loop's buffer number would live in local memory)
+  unsigned int ph = 0u;
   const int tid = threadIdx.x + threadIdx.y * 32;
   const int ntiles = ntx * nty * a.nl;
   const int si = st->step_index;
   const int step = (int)gridDim.x;
-  auto tile_of = [&](int t, int& i0, int& j0, int& k) {
-    const int bx = t % ntx, r = t / ntx;
-    i0 = bx * TX;
-    j0 = (r % nty) * TY;
-    k = r / nty;
+  // tile coordinates (x tile, y tile, layer) of tile t, and their advance by
+  // the grid's stride without divisions (sbx < ntx and sby < nty, so one
+  // carry per coordinate)
+  struct TC { int bx, by, k; };
+  auto tile_of = [&](int t) {
+    const int r = t / ntx;
+    return TC{t - r * ntx, r % nty, r / nty};
+  };
+  const TC sc = tile_of(step);
+  auto advance = [&](TC c) {
+    c.bx += sc.bx;
+    const int cx = c.bx >= ntx;
+    c.bx -= cx ? ntx : 0;
+    c.by += sc.by + cx;
+    const int cy = c.by >= nty;
+    c.by -= cy ? nty : 0;
+    c.k += sc.k + cy;
+    return c;
   };
   // interior tiles, and closed-basin edge tiles (the box's zero fill is the
   // value outside the domain), arrive by TMA; periodic edge tiles wrap
   const bool per = a.periodic != 0;
-  // prologue: the first tile's boxes into buffer 0
-  if (NB == 2 && tm && tid == 0 && (int)blockIdx.x < ntiles) {
-    int i0, j0, k;
-    tile_of((int)blockIdx.x, i0, j0, k);
-    if (!per || !rhs_edge_tile(i0, j0, R, TY, a.nx, a.ny))
-      rhs_tile_tma<T, COMP, R, TY>(a, i0, j0, k, rhs_in<T, R, TY>(base, 0), tm, &bar[0]);
+  // the boxes of the tile at c into buffer b (thread 0)
+  auto issue = [&](TC c, int b) {
+    const int i1 = c.bx * TX, j1 = c.by * TY;
+    if (!per || !rhs_edge_tile(i1, j1, R, TY, a.nx, a.ny))
+      rhs_tile_tma<T, COMP, R, TY>(a, i1, j1, c.k, rhs_in<T, R, TY>(base, b), tm, &bar[b]);
+  };
+  TC cur_c = tile_of((int)blockIdx.x);
+  // prologue: the block's first NB - 1 tiles into buffers 0 .. NB - 2
+  if (NB >= 2 && tm && tid == 0) {
+    TC c = cur_c;
+    for (int p = 0; p < NB - 1; ++p, c = advance(c))
+      if ((int)blockIdx.x + p * step < ntiles) issue(c, p);
   }
   decltype(absbits_native(T(0))) mymax = 0;
   int it = 0;
-  for (int t = (int)blockIdx.x; t < ntiles; t += step, ++it) {
-    const int cur = NB == 2 ? (it & 1) : 0;
-    int i0, j0, k;
-    tile_of(t, i0, j0, k);
+  for (int t = (int)blockIdx.x; t < ntiles; t += step, ++it, cur_c = advance(cur_c)) {
+    const int cur = NB >= 2 ? it % NB : 0;
+    const int i0 = cur_c.bx * TX, j0 = cur_c.by * TY, k = cur_c.k;
     const bool edge = rhs_edge_tile(i0, j0, R, TY, a.nx, a.ny);
     const RhsIn<T> in = rhs_in<T, R, TY>(base, cur);
-    if (NB == 2 && tm && tid == 0 && t + step < ntiles) {
-      // the next tile's boxes into the other buffer (last read by the
-      // previous tile, which every thread has finished: the trailing
-      // __syncthreads of the previous iteration)
-      int i1, j1, k1;
-      tile_of(t + step, i1, j1, k1);
-      if (!per || !rhs_edge_tile(i1, j1, R, TY, a.nx, a.ny))
-        rhs_tile_tma<T, COMP, R, TY>(a, i1, j1, k1, rhs_in<T, R, TY>(base, cur ^ 1), tm, &bar[cur ^ 1]);
+    // the tile NB - 1 ahead into the buffer the previous tile used (every
+    // thread has finished with it: the trailing __syncthreads of the
+    // previous iteration)
+    if (NB >= 2 && tm && tid == 0 && t + (NB - 1) * step < ntiles) {
+      TC c = cur_c;
+      for (int p = 0; p < NB - 1; ++p) c = advance(c);
+      issue(c, (it + NB - 1) % NB);
     }
     bool ok = true;
     if (edge && (per || !tm)) {
@@ -1538,7 +1558,9 @@ __device__ __forceinline__ void body_rhs_tiles(const StepArgs<T>& a, int ntx, in
       rhs_tile_fetch<T, COMP, R, TY, false>(a, i0, j0, k, in);
     } else {
       if (NB == 1 && tid == 0) rhs_tile_tma<T, COMP, R, TY>(a, i0, j0, k, in, tm, &bar[0]);
-      ok = cur ? rhs_tile_wait(a, &bar[1], &ph1) : rhs_tile_wait(a, &bar[0], &ph0);
+      unsigned int pb = (ph >> cur) & 1u;
+      ok = rhs_tile_wait(a, &bar[cur], &pb);
+      ph ^= 1u << cur;
     }
     __syncthreads();
     if (ok) {
@@ -1649,8 +1671,10 @@ template <typename T>
 static int rhs_ty(const StepArgs<T>& a) { return a.rhs_ty == 32 ? 32 : 16; }
 template <typename T>
 static size_t smem_rhs(const StepArgs<T>& a) { return smem_rhs_r<T>(rhs_halo(a), 1, rhs_ty(a)); }
-// input buffers of the single-run RHS kernel: FP32 double-buffers its
-// persistent loop, FP64 runs one tile per block
+// input buffers of the single-run RHS kernel: FP32 runs its persistent
+// loop on a ring of two (each tile's boxes issued one tile ahead; three,
+// issued two ahead, measured the same, four cost a block per SM), FP64 one
+// tile per block
 template <typename T>
 constexpr int rhs_nbuf() { return sizeof(T) == 4 ? 2 : 1; }
 template <typename T>
