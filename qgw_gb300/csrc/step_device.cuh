@@ -1167,7 +1167,10 @@ __device__ __forceinline__ bool rhs_tile_wait(const StepArgs<T>& a, unsigned lon
 // skip all of that.  The tile's inputs are in `in` and the block has been
 // synchronised since they arrived; `wk` holds the work buffers.  Returns
 // this thread's CFL maximum |dpsi| as bits in the arithmetic width.
-template <typename T, bool COMP, int R, int TY, bool EDGE>
+// Z1: the run is in zeta mode 1 with R = nsweep sweeps (the compensated
+// path's common case), which the compiler then knows: the sweep count, the
+// chain's units and the buffers each sweep reads and writes.
+template <typename T, bool COMP, int R, int TY, bool EDGE, bool Z1 = false>
 __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile_compute(const StepArgs<T>& a, int i0, int j0,
                                                                             int k, int step_index,
                                                                             const RhsIn<T>& in, T* wk) {
@@ -1188,9 +1191,9 @@ __device__ __forceinline__ decltype(absbits_native(T(0))) rhs_tile_compute(const
   const T* qL = a.q + (size_t)k * a.lstride;
   // zeta mode 1: the spectral L psi starts the chain and gives the drag;
   // zeta mode 2: the field is the whole chain L^nsweep psi (no sweeps here)
-  const bool zm = COMP && a.zeta_mode == 1;
-  const bool zm2 = COMP && a.zeta_mode == 2;
-  const int ksweep = zm2 ? 0 : a.nsweep;  // Laplacian sweeps run on the tile
+  const bool zm = Z1 || (COMP && a.zeta_mode == 1);
+  const bool zm2 = !Z1 && COMP && a.zeta_mode == 2;
+  const int ksweep = Z1 ? R : zm2 ? 0 : a.nsweep;  // Laplacian sweeps run on the tile
   const T* zetaL = (COMP && a.zeta_mode) ? a.zeta + (size_t)k * a.lstride : nullptr;
   // every double parameter converted once (conversions run on the FP64 pipe)
   const T d2 = pick<T>(a.Delta * a.Delta, a.fc[FC_D2]);
@@ -1536,6 +1539,9 @@ __device__ __forceinline__ void body_rhs_tiles(const StepArgs<T>& a, int ntx, in
     for (int p = 0; p < NB - 1; ++p, c = advance(c))
       if ((int)blockIdx.x + p * step < ntiles) issue(c, p);
   }
+  // interior tiles of the compensated path's zeta mode 1 with R sweeps run
+  // the compile-time form
+  const bool z1 = COMP && a.zeta_mode == 1 && a.nsweep == R;
   decltype(absbits_native(T(0))) mymax = 0;
   int it = 0;
   for (int t = (int)blockIdx.x; t < ntiles; t += step, ++it, cur_c = advance(cur_c)) {
@@ -1565,6 +1571,7 @@ __device__ __forceinline__ void body_rhs_tiles(const StepArgs<T>& a, int ntx, in
     __syncthreads();
     if (ok) {
       const auto m = edge ? rhs_tile_compute<T, COMP, R, TY, true>(a, i0, j0, k, si, in, wk)
+                     : z1 ? rhs_tile_compute<T, COMP, R, TY, false, true>(a, i0, j0, k, si, in, wk)
                           : rhs_tile_compute<T, COMP, R, TY, false>(a, i0, j0, k, si, in, wk);
       mymax = m > mymax ? m : mymax;
     }
