@@ -453,7 +453,9 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
   const T* f1 = a.fab + s1 * fs;
   const T* f2 = a.fab + s2 * fs;
   const int tid = threadIdx.x;
-  const int GB = group_width(a.G1);
+  // FP32 groups of 9..12 modes run at width 12 (three 16-byte coefficient
+  // vectors), the common 10-layer case without six idle accumulators
+  const int GB = (sizeof(T) == 4 && a.G1 > 8 && a.G1 <= 12) ? 12 : group_width(a.G1);
   if (!PER) prefetch_tables_l1(a.tx, a.gx.M);
   const T* frow = (ab3 && a.fr.on) ? a.fr.field + (size_t)j * a.pitch : nullptr;
   const T sqdt = frow ? (T)sqrt(st->dt) : T(0);
@@ -488,6 +490,12 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
     case 2: QGW_PF(2, F); break;     \
     case 4: QGW_PF(4, F); break;     \
     case 8: QGW_PF(8, F); break;     \
+    case 12:                         \
+      if constexpr (sizeof(T) == 4) {\
+        QGW_PF(12, F);               \
+        break;                       \
+      }                              \
+      [[fallthrough]];               \
     default: QGW_PF(16, F); break;   \
   }
     // the compensated path has registers for one forced loop only
