@@ -16,6 +16,7 @@
 #include "../../include/qgw_gpu.h"
 #include "dst_tables.h"
 #include "dst_warp.h"
+#include "dst_blue.h"
 #include "host.h"
 #include "kernels.h"
 #include "qgw_device.cuh"
@@ -202,14 +203,20 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   // real FFT of length NX along x (a complex FFT of NX/2: M = NX) and
   // complex FFT of length NY along y (M = 2 NY)
   const int Mx = per ? r->nx : r->nx + 1, My = per ? 2 * r->ny : r->ny + 1;
-  a.gx = qgw::make_geom(Mx);
-  a.gy = qgw::make_geom(My);
+  a.gx = per ? qgw::make_geom(Mx) : qgw::make_geom_any(Mx);
+  a.gy = per ? qgw::make_geom(My) : qgw::make_geom_any(My);
   int rc;
   // transform tables for x and y
   for (int dim = 0; dim < 2; ++dim) {
-    const int M = dim == 0 ? Mx : My;
-    qgw::DstTablesHost th = qgw::build_dst_tables(M);
-    T *tw, *pre, *spl, *twp, *sj, *twd, *sjp;
+    const qgw::DstGeom& g = dim == 0 ? a.gx : a.gy;
+    // the chirp-z form's FFT is L = g.H points: its tables are those of a
+    // half-length FFT of L (the DST tables of 2L), plus the chirp tables
+    qgw::DstTablesHost th = qgw::build_dst_tables(g.blue ? 2 * g.H : g.M);
+    std::vector<double> bcv(2, 0.0), bzv(2, 0.0);
+    if (g.blue) qgw::build_blue_tables(g, bcv, bzv);
+    T *tw, *pre, *spl, *twp, *sj, *twd, *sjp, *bc, *bz;
+    if ((rc = upload<T>(r, &bc, bcv))) return rc;
+    if ((rc = upload<T>(r, &bz, bzv))) return rc;
     if ((rc = upload<T>(r, &tw, th.tw))) return rc;
     if ((rc = upload<T>(r, &pre, th.pre))) return rc;
     if ((rc = upload<T>(r, &spl, th.spl))) return rc;
@@ -225,6 +232,8 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
     t.sj = sj;
     t.twd = (const qgw::C2<T>*)twd;
     t.sjp = (const qgw::C2<T>*)sjp;
+    t.bc = (const qgw::C2<T>*)bc;
+    t.bz = (const qgw::C2<T>*)bz;
   }
   T *cl, *cm;
   if ((rc = upload<T>(r, &cl, r->cl2m))) return rc;
@@ -316,17 +325,19 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   a.has_topo = 0;
   a.has_wind = p.tau0 != 0;
   // work buffers per row of the row kernels' transforms (one: in place)
-  const int bufs_x = (!per && qgw::warp_dst_len(Mx / 2, (int)sizeof(T))) ? 1 : 2;
+  const int bufs_x = (!per && !a.gx.blue && qgw::warp_dst_len(a.gx.H, (int)sizeof(T))) ? 1 : 2;
+  // reals per row buffer (the chirp-z form holds L complex values)
+  const int Mrow = a.gx.blue ? 2 * a.gx.H : Mx;
   {
     // QGW_ROW_GROUP overrides the modes per forward-rows block (tuning knob)
     const char* e = std::getenv("QGW_ROW_GROUP");
     const int want = e ? std::atoi(e) : 0;
-    const size_t budget = row_budget(sizeof(T), Mx, r->nl);
-    if (want >= 1 && want <= 16) a.G1 = mode_group(r->nl, Mx, sizeof(T), budget, 1, 16, want, bufs_x);
-    else if (sizeof(T) == 8) a.G1 = mode_group_fma(r->nl, Mx, sizeof(T), budget, 16);
-    else a.G1 = mode_group(r->nl, Mx, sizeof(T), budget, 1, 16, 16, bufs_x);
+    const size_t budget = row_budget(sizeof(T), Mrow, r->nl);
+    if (want >= 1 && want <= 16) a.G1 = mode_group(r->nl, Mrow, sizeof(T), budget, 1, 16, want, bufs_x);
+    else if (sizeof(T) == 8) a.G1 = mode_group_fma(r->nl, Mrow, sizeof(T), budget, 16);
+    else a.G1 = mode_group(r->nl, Mrow, sizeof(T), budget, 1, 16, 16, bufs_x);
   }
-  a.G3 = mode_group(r->nl, Mx, sizeof(T), 110 * 1024, 1, 16, inv_group(0, Mx, r->nl, bufs_x), bufs_x);
+  a.G3 = mode_group(r->nl, Mrow, sizeof(T), 110 * 1024, 1, 16, inv_group(0, Mrow, r->nl, bufs_x), bufs_x);
   a.CT = 0;
   a.low_k64 = 8;
   // 16-byte column vectors: rows 16-byte aligned and a whole number of
@@ -358,7 +369,7 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
     if ((rc = dalloc(r, &a.spec2, field))) return rc;
     if ((rc = dalloc(r, &a.zeta, field))) return rc;
     // K3 transforms psi and zeta rows of each mode: two rows per mode
-    a.G3 = mode_group(r->nl, Mx, sizeof(T), 110 * 1024, 2, 8, inv_group(1, Mx, r->nl, bufs_x), bufs_x);
+    a.G3 = mode_group(r->nl, Mrow, sizeof(T), 110 * 1024, 2, 8, inv_group(1, Mrow, r->nl, bufs_x), bufs_x);
     // symbol of the 5-point Laplacian: DST-I basis sin^2(pi k / 2(n+1));
     // periodic Fourier basis sin^2(pi k / N)
     std::vector<double> sx(r->nx, 0.0), sy(r->ny);
@@ -452,7 +463,9 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   a.iRd2f = fi;
   // column tiles of 32-byte rows, or 16-byte rows where the former's
   // buffers would pass 200 KiB of shared memory (long columns with the
-  // second spectral field: FP32 NY = 2048 in zeta mode)
+  // second spectral field: FP32 NY = 2048 in zeta mode) and for the chirp-z
+  // form's columns (its kernel is built for the narrower tiles alone)
+  if (a.gy.blue) a.CT = (32 / (int)sizeof(T)) / 2;
   {
     size_t need;
     if constexpr (sizeof(T) == 8) need = qgw::smem_bytes_cols_f64(a);
@@ -493,11 +506,12 @@ int set_shape(qgw_run* r, StepArgs<T>& a, const qgw_shape& sh) {
   const int ctd = 32 / (int)sizeof(T);
   if (sh.col_tile) {
     if (sh.col_tile != ctd && sh.col_tile != ctd / 2) return QGW_ERR_PARAM;
+    if (a.gy.blue && sh.col_tile != ctd / 2) return QGW_ERR_PARAM;  // the chirp-z columns' one width
     b.CT = sh.col_tile == ctd ? 0 : sh.col_tile;
   }
   const bool per = a.periodic != 0;
-  const int Mx = per ? r->nx : r->nx + 1;
-  const int bufs_x = (!per && qgw::warp_dst_len(Mx / 2, (int)sizeof(T))) ? 1 : 2;
+  const int bufs_x = (!per && !a.gx.blue && qgw::warp_dst_len(a.gx.H, (int)sizeof(T))) ? 1 : 2;
+  const int Mx = a.gx.blue ? 2 * a.gx.H : per ? r->nx : r->nx + 1;  // reals per row buffer
   const size_t any = (size_t)1 << 30;  // the device's limit is checked below
   if (sh.row_group_fwd) {
     if (sh.row_group_fwd < 1 || sh.row_group_fwd > 16) return QGW_ERR_PARAM;
@@ -597,11 +611,13 @@ int qgw_create(const qgw_params* pin, const double* cl2m, const double* cm2l, co
     const int n_rec = (int)std::floor(p.dt_forc_period / p.dt_forc);
     if (n_rec < 1 || n_rec * p.dt_forc != p.dt_forc_period) return QGW_ERR_PARAM;
   }
-  // transform lengths: closed DST-I of M = NX, NY; periodic real FFT of NX and
-  // complex FFT of NY (M = 2 NY); M even, M/2 a product of 2, 3, 5 and 7
+  // transform lengths: closed DST-I of M = NX, NY (any M >= 4: the
+  // half-length FFT where M is even with M/2 a product of 2, 3, 5 and 7,
+  // else the chirp-z form); periodic real FFT of NX and complex FFT of NY
+  // (M = 2 NY), which take only the former
   if (p.NX > 8192 || p.NY > 8192) return QGW_ERR_UNSUPPORTED;
-  if (!qgw::transform_length_ok(p.NX) || !qgw::transform_length_ok(per ? 2 * p.NY : p.NY))
-    return QGW_ERR_UNSUPPORTED;
+  if (p.NX < 4 || p.NY < 4) return QGW_ERR_UNSUPPORTED;
+  if (per && (!qgw::transform_length_ok(p.NX) || !qgw::transform_length_ok(2 * p.NY))) return QGW_ERR_UNSUPPORTED;
   if (p.nl < 1 || p.nl > QGW_NL_GPU_MAX) return QGW_ERR_UNSUPPORTED;
   if (!(p.Lx > 0) || !(p.cfl > 0)) return QGW_ERR_PARAM;
   qgw_run* r = new qgw_run();
@@ -686,6 +702,9 @@ int qgw_create(const qgw_params* pin, const double* cl2m, const double* cm2l, co
   if (cudaMemcpyAsync(r->d_state, &s, sizeof(s), cudaMemcpyHostToDevice, r->stream) != cudaSuccess)
     return fail(QGW_ERR_CUDA);
   cudaError_t e = precision == QGW_FP64 ? qgw::prepare_f64(r->a64) : qgw::prepare_f32c(r->a32);
+  // a configuration whose work buffers pass the device's shared memory (the
+  // chirp-z form's rows of long, odd or prime-sized grids) is refused
+  if (e == cudaErrorInvalidValue) return fail(QGW_ERR_UNSUPPORTED);
   if (e != cudaSuccess) return fail(cuda_fail(e));
   // persistent grid of the RHS kernel (after the shared-memory limits are set)
   if (precision == QGW_FP64) r->a64.rhs_grid = qgw::rhs_grid_f64(r->a64);

@@ -87,13 +87,16 @@ template <typename T> QGW_HD int padded_len(int M) {
 
 // Static shape of one DST length.
 struct DstGeom {
-  int M;          // DST length + 1 (even, >= 4)
-  int H;          // M / 2, complex FFT length
+  int M;          // DST length + 1 (>= 4; even unless blue)
+  int H;          // complex FFT length: M / 2, or (blue) the chirp-z transform's L
   int npass;      // Stockham passes
   int radix[12];  // radix of each pass: 8s, then 4 or 2, then 3s, 5s, 7s; first pass has Ns = 1
   int chunk;      // prefix-sum chunk length (values per work item)
   int nchunk;     // ceil(H / chunk) (<= 32)
   int ok;         // 1 when H factors into 2, 3, 5 and 7
+  int blue;       // 1: a length the half-length FFT cannot take (M odd, or M/2 with a
+                  // prime factor above 7), run as a chirp-z (Bluestein) transform of
+                  // power-of-two length L = H (dst_blue.h)
 };
 
 inline DstGeom make_geom(int M) {
@@ -113,8 +116,29 @@ inline DstGeom make_geom(int M) {
   return g;
 }
 
-// Lengths the transforms support: even, half-length a product of 2, 3, 5, 7
+// Lengths the half-length transforms take: even, half-length a product of
+// 2, 3, 5, 7
 inline bool transform_length_ok(int M) { return M >= 4 && make_geom(M).ok == 1; }
+
+// Geometry of the chirp-z form of DST length M >= 4: L the smallest power of
+// two >= 2M - 1 (the cyclic convolution of M values with a chirp of 2M - 1
+// values); make_geom_any: the half-length form where it applies, else this
+inline DstGeom make_geom_blue(int M) {
+  int L = 1;
+  while (L < 2 * M - 1) L *= 2;
+  DstGeom g = make_geom(2 * L);  // the radices of an L-point FFT
+  g.M = M;
+  g.blue = 1;
+  g.chunk = 0;
+  g.nchunk = 0;
+  return g;
+}
+inline DstGeom make_geom_any(int M) { return transform_length_ok(M) ? make_geom(M) : make_geom_blue(M); }
+// reals of one row buffer of a transform: M (padded) for the half-length
+// form, L complex values for the chirp-z form
+template <typename T> QGW_HD int row_len(const DstGeom& g) {
+  return g.blue ? padded_len<T>(2 * g.H) : padded_len<T>(g.M);
+}
 
 // Twiddles of the Stockham passes with Ns > 1 in the order the passes read
 // them: pass (R, Ns) holds w_H^(q k H/(Ns R)) at (Ns - R0) + (q-1) Ns + k for
@@ -153,6 +177,8 @@ template <typename T> struct DstTables {
   const T* sj;  // s_j = sin(pi j/M), j <= H (the merged pre-processing pass)
   const C2<T>* twd;  // the one-warp transform (dst_warp.h, H = 256, 512): DIF twiddles
   const C2<T>* sjp;  // and (s_{2m}, s_{2m+1}), m < H
+  const C2<T>* bc;   // chirp-z form (dst_blue.h): c_m = exp(i pi m^2 / 2M), m < M
+  const C2<T>* bz;   // and the L-point FFT of the conjugate chirp
 };
 
 // Work-item loop of a block over nrows rows of n items each: f(r, i) for

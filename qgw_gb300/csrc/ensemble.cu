@@ -263,6 +263,12 @@ static int uniform_shape(EnsembleCore* e) {
 int ens_core_build(EnsembleCore* e) {
   const cudaError_t pe = e->precision == QGW_FP64 ? ens_prepare_f64() : ens_prepare_f32c();
   if (pe != cudaSuccess) return cuda_fail(pe);
+  // the batched kernels hold the half-length transforms only: a member whose
+  // grid needs the chirp-z form runs alone
+  for (qgw_run* r : e->members) {
+    const bool blue = e->precision == QGW_FP64 ? (r->a64.gx.blue || r->a64.gy.blue) : (r->a32.gx.blue || r->a32.gy.blue);
+    if (blue) return QGW_ERR_UNSUPPORTED;
+  }
   const int rc = uniform_shape(e);
   if (rc) return rc;
   return build_tables(e);

@@ -339,6 +339,8 @@ static cudaError_t set_attrs(const StepArgs<T>& a) {
       (const void*)k_rows_inv<T, COMP, false, 0>,         (const void*)k_rows_inv<T, COMP, false, 512>,
       (const void*)k_cols<T, COMP, false, CTD<T>, 0>,     (const void*)k_cols<T, COMP, false, CTD<T>, 512>,
       (const void*)k_cols<T, COMP, false, CTD<T> / 2, 0>, (const void*)k_cols<T, COMP, false, CTD<T> / 2, 512>,
+      (const void*)k_rows_fwd<T, COMP, false, -1>,        (const void*)k_rows_inv<T, COMP, false, -1>,
+      (const void*)k_cols<T, COMP, false, CTD<T> / 2, -1>,
       (const void*)k_rows_fwd<T, COMP, true, 0>,          (const void*)k_rows_inv<T, COMP, true, 0>,
       (const void*)k_cols<T, COMP, true, CTD<T>, 0>};
   for (const void* f : transforms)
@@ -359,6 +361,7 @@ template <typename T, bool COMP>
 static void launch_k1(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
   const size_t sm = smem_rows<T, COMP>(a);
   if (a.periodic) k_rows_fwd<T, COMP, true, 0><<<dim3(a.ny), NT, sm, s>>>(a, step_mode);
+  else if (a.gx.blue) k_rows_fwd<T, COMP, false, -1><<<dim3(a.ny), NT, sm, s>>>(a, step_mode);
   else if (a.gx.H == 512) k_rows_fwd<T, COMP, false, 512><<<dim3(a.ny), NT, sm, s>>>(a, step_mode);
   else k_rows_fwd<T, COMP, false, 0><<<dim3(a.ny), NT, sm, s>>>(a, step_mode);
 }
@@ -366,8 +369,9 @@ template <typename T, bool COMP>
 static void launch_k2(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
   const dim3 grid(col_tiles(a), a.nl);
   const size_t sm = smem_cols<T, COMP>(a);
-  const bool wide = col_width(a) == CTD<T>, h512 = a.gy.H == 512;
+  const bool wide = col_width(a) == CTD<T>, h512 = a.gy.H == 512 && !a.gy.blue;
   if (a.periodic) k_cols<T, COMP, true, CTD<T>, 0><<<grid, NT, sm, s>>>(a, step_mode);
+  else if (a.gy.blue) k_cols<T, COMP, false, CTD<T> / 2, -1><<<grid, NT, sm, s>>>(a, step_mode);
   else if (wide && h512) k_cols<T, COMP, false, CTD<T>, 512><<<grid, NT, sm, s>>>(a, step_mode);
   else if (wide) k_cols<T, COMP, false, CTD<T>, 0><<<grid, NT, sm, s>>>(a, step_mode);
   else if (h512) k_cols<T, COMP, false, CTD<T> / 2, 512><<<grid, NT, sm, s>>>(a, step_mode);
@@ -377,6 +381,7 @@ template <typename T, bool COMP>
 static void launch_k3(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
   const size_t sm = smem_rows_inv<T, COMP>(a);
   if (a.periodic) k_rows_inv<T, COMP, true, 0><<<dim3(a.ny), NT, sm, s>>>(a, step_mode);
+  else if (a.gx.blue) k_rows_inv<T, COMP, false, -1><<<dim3(a.ny), NT, sm, s>>>(a, step_mode);
   else if (a.gx.H == 512) k_rows_inv<T, COMP, false, 512><<<dim3(a.ny), NT, sm, s>>>(a, step_mode);
   else k_rows_inv<T, COMP, false, 0><<<dim3(a.ny), NT, sm, s>>>(a, step_mode);
 }

@@ -87,6 +87,14 @@ int admit_one(qgw_pool* pl, const std::shared_ptr<Request>& r) {
   qgw_run* run = nullptr;
   int rc = qgw_create(&r->p, nullptr, nullptr, nullptr, nullptr, r->precision, &run);
   if (rc) return rc;
+  // the pool batches runs through the ensemble kernels, which hold the
+  // half-length transforms only (odd or prime-sized grids run alone)
+  const bool blue = r->precision == QGW_FP64 ? (run->a64.gx.blue || run->a64.gy.blue)
+                                             : (run->a32.gx.blue || run->a32.gy.blue);
+  if (blue) {
+    qgw_destroy(run);
+    return QGW_ERR_UNSUPPORTED;
+  }
   if ((rc = qgw_set_q(run, r->q0.data()))) {
     qgw_destroy(run);
     return rc;

@@ -28,6 +28,7 @@
 
 #include <algorithm>
 
+#include "dst_blue.h"
 #include "dst_fixed.cuh"
 #include "periodic.cuh"
 #include "kernels.h"
@@ -106,13 +107,35 @@ __device__ __forceinline__ T* dst_block_generic(T* A, T* B, int nrows, int ld, c
   return dst;
 }
 
+// Chirp-z DST-I (dst_blue.h) of nrows rows in A (x_j at index j), B the
+// second buffer, both of row_len = L complex values: chirp, L-point FFT,
+// multiply by the chirp's transform (conjugated), FFT, output Y_k at index
+// k; returns the buffer that holds the output.  g.H = L, g's radices are
+// L's, tb.tw holds L's twiddles.
+template <typename T>
+__device__ __forceinline__ T* dst_block_blue(T* A, T* B, int nrows, int ld, const DstGeom& g, const DstTables<T>& tb) {
+  const int M = g.M, L = g.H;
+  block_items(nrows, L, [&](int r, int m) { blue_chirp_item<T>(A + r * ld, (C2<T>*)(B + r * ld), m, M, tb.bc); });
+  __syncthreads();
+  T* O = cfft_block<T>(B, A, nrows, ld, g, tb.tw, nullptr);
+  block_items(nrows, L, [&](int r, int k) { blue_mul_item<T>((C2<T>*)(O + r * ld), k, tb.bz); });
+  __syncthreads();
+  T* D = cfft_block<T>(O, O == A ? B : A, nrows, ld, g, tb.tw, nullptr);
+  T* out = D == A ? B : A;
+  const T invL = T(1) / T(L);  // a power of two: exact
+  block_items(nrows, M, [&](int r, int k) { blue_out_item<T>((const C2<T>*)(D + r * ld), out + r * ld, k, invL, tb.bc); });
+  __syncthreads();
+  return out;
+}
+
 // Block DST of any supported length: the power-of-two lengths M = 128..2048
 // use the compile-time specialisations of dst_fixed.cuh (FP32 M = 512 and
 // 1024: one warp per row, in place, the result in A), others (mixed radix
 // 2, 3, 5, 7) the generic loops.
 // HL != 0: a kernel specialised for half-length HL (its launcher checked the
 // run's length), whose code then holds that transform alone -- the step
-// kernels of the common lengths keep their instruction stream small.
+// kernels of the common lengths keep their instruction stream small; HL = -1:
+// the chirp-z form (the lengths the half-length FFT cannot take).
 template <typename T, int HL = 0>
 __device__ __forceinline__ T* dst_block(T* A, T* B, int nrows, int ld, const DstGeom& g, const DstTables<T>& tb,
                                         T* tot) {
@@ -120,6 +143,7 @@ __device__ __forceinline__ T* dst_block(T* A, T* B, int nrows, int ld, const Dst
     if constexpr (sizeof(T) == 4) return dst_block_warp_f32<9>(A, nrows, ld, tb);
     else return dst_block_fixed<T, 9>(A, B, nrows, ld, tb);
   }
+  if constexpr (HL == -1) return dst_block_blue<T>(A, B, nrows, ld, g, tb);
   switch (g.H) {
     case 64: return dst_block_fixed<T, 6>(A, B, nrows, ld, tb);
     case 128: return dst_block_fixed<T, 7>(A, B, nrows, ld, tb);
@@ -441,7 +465,7 @@ __device__ __forceinline__ void body_rows_fwd(const StepArgs<T>& a, int step_mod
                                               T* tot, T* cst) {
   DevState* st = a.state;
   if (step_mode && !st->active) return;
-  const int ld = padded_len<T>(a.gx.M);
+  const int ld = row_len<T>(a.gx);
   T* A = (T*)smem_raw;
   T* B = A + (size_t)a.G1 * ld;
   const bool ab3 = step_mode && st->pending;
@@ -575,7 +599,7 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
   if (step_mode && !st->active) return;
   const int k0 = bx * CT;
   const int CTb = min(CT, a.nx - k0);
-  const int ld = padded_len<T>(a.gy.M);
+  const int ld = row_len<T>(a.gy);
   const bool zm = COMP && a.zeta_mode;
   // Two pairs of CT-row buffers, [A | C] and [B | D]: the forward DST runs on
   // A with B as work buffer; the divide overwrites its output O with psi_hat
@@ -728,7 +752,7 @@ __device__ __forceinline__ void body_cols_per(const StepArgs<T>& a, int step_mod
   if (step_mode && !st->active) return;
   const int H = a.gx.H;  // x: complex columns k = 0..H
   const int k0 = bx * CC;
-  const int ld = padded_len<T>(a.gy.M);
+  const int ld = row_len<T>(a.gy);
   T* A = (T*)smem_raw;
   T* B = A + (size_t)CC * ld;
   T* C = B + (size_t)CC * ld;  // zeta mode only
@@ -885,7 +909,7 @@ __device__ __forceinline__ void body_rows_inv(const StepArgs<T>& a, int step_mod
                                               T* tot, T* cst) {
   DevState* st = a.state;
   if (step_mode && !st->active) return;
-  const int ld = padded_len<T>(a.gx.M);
+  const int ld = row_len<T>(a.gx);
   const bool zm = COMP && a.zeta_mode;
   const int Gb = a.G3;
   T* A = (T*)smem_raw;
@@ -1635,11 +1659,11 @@ __device__ __forceinline__ void begin_state(DevState* st, double t_out, double t
 // in place (the one-warp DST)
 template <typename T>
 static int dst_bufs(const StepArgs<T>& a, const DstGeom& g) {
-  return (!a.periodic && warp_dst_len(g.H, (int)sizeof(T))) ? 1 : 2;
+  return (!a.periodic && !g.blue && warp_dst_len(g.H, (int)sizeof(T))) ? 1 : 2;
 }
 template <typename T, bool COMP>
 static size_t smem_rows(const StepArgs<T>& a) {
-  return cst_bytes<T>(a.nl) + (size_t)dst_bufs(a, a.gx) * a.G1 * padded_len<T>(a.gx.M) * sizeof(T);
+  return cst_bytes<T>(a.nl) + (size_t)dst_bufs(a, a.gx) * a.G1 * row_len<T>(a.gx) * sizeof(T);
 }
 template <typename T, bool COMP>
 static size_t smem_cols(const StepArgs<T>& a) {
@@ -1649,7 +1673,7 @@ static size_t smem_cols(const StepArgs<T>& a) {
   const bool zm = COMP && a.zeta_mode;
   const size_t rows = a.periodic ? (size_t)(zm ? 3 : 2) * 2
                                  : (size_t)(zm ? 2 : 1) * dst_bufs(a, a.gy) * col_width(a);
-  return rows * padded_len<T>(a.gy.M) * sizeof(T);
+  return rows * row_len<T>(a.gy) * sizeof(T);
 }
 // column tiles of one mode: four real columns (DST) or two complex columns
 // k = 0..nx/2 (periodic)
@@ -1660,7 +1684,7 @@ static int col_tiles(const StepArgs<T>& a) {
 template <typename T, bool COMP>
 static size_t smem_rows_inv(const StepArgs<T>& a) {
   return cst_bytes<T>(a.nl) +
-         (size_t)((COMP && a.zeta_mode) ? 2 : 1) * dst_bufs(a, a.gx) * a.G3 * padded_len<T>(a.gx.M) * sizeof(T);
+         (size_t)((COMP && a.zeta_mode) ? 2 : 1) * dst_bufs(a, a.gx) * a.G3 * row_len<T>(a.gx) * sizeof(T);
 }
 // dynamic shared memory of the RHS kernels for halo radius r and nb input
 // buffers (RhsShape)

@@ -6,6 +6,7 @@
 #include <cstring>
 #include "../../qgw_gb300/csrc/dst_tables.h"
 #include "../../qgw_gb300/csrc/dst_warp.h"
+#include "../../qgw_gb300/csrc/dst_blue.h"
 
 using namespace qgw;
 
@@ -129,6 +130,48 @@ extern "C" int dst_warp_run_f32(int M, int howmany, float* data) {
   else return 0;
   return 1;
 }
+
+// The chirp-z form (dst_blue.h) of any length M >= 4, its phases as loops:
+// chirp, L-point FFT (the Stockham items), multiply, FFT, output.
+template <typename T>
+static void run_blue(int M, int howmany, T* data) {
+  const DstGeom g = make_geom_blue(M);
+  const int L = g.H;
+  DstTablesHost th = build_dst_tables(2 * L);  // twiddles of the L-point FFT
+  std::vector<double> bcd, bzd;
+  build_blue_tables(g, bcd, bzd);
+  std::vector<T> tw(th.tw.begin(), th.tw.end()), bc(bcd.begin(), bcd.end()), bz(bzd.begin(), bzd.end());
+  const C2<T>* TW = (const C2<T>*)tw.data();
+  const C2<T>* BC = (const C2<T>*)bc.data();
+  const C2<T>* BZ = (const C2<T>*)bz.data();
+  const int ld = padded_len<T>(2 * L);
+  std::vector<T> A(ld), B(ld);
+  auto fft = [&](T* src, T* dst) -> T* {
+    int Ns = 1;
+    for (int p = 0; p < g.npass; ++p) {
+      const int R = g.radix[p];
+      for (int b = 0; b < L / R; ++b) stockham_dispatch<T>(R, (const C2<T>*)src, (C2<T>*)dst, b, Ns, L, TW);
+      Ns *= R;
+      T* t = src; src = dst; dst = t;
+    }
+    return src;
+  };
+  for (int r = 0; r < howmany; ++r) {
+    T* x = data + (size_t)r * (M - 1);
+    for (int j = 0; j < ld; ++j) A[j] = B[j] = T(777);
+    for (int j = 0; j < M - 1; ++j) A[pr<T>(j + 1)] = x[j];
+    A[pr<T>(0)] = T(12345);  // index 0 must never be read
+    for (int m = 0; m < L; ++m) blue_chirp_item<T>(A.data(), (C2<T>*)B.data(), m, M, BC);
+    T* O = fft(B.data(), A.data());
+    for (int k = 0; k < L; ++k) blue_mul_item<T>((C2<T>*)O, k, BZ);
+    T* D = fft(O, O == A.data() ? B.data() : A.data());
+    T* out = D == A.data() ? B.data() : A.data();
+    for (int k = 0; k < M; ++k) blue_out_item<T>((const C2<T>*)D, out, k, T(1) / T(L), BC);
+    for (int j = 0; j < M - 1; ++j) x[j] = out[pr<T>(j + 1)];
+  }
+}
+extern "C" void dst_blue_run_f64(int M, int howmany, double* data) { run_blue<double>(M, howmany, data); }
+extern "C" void dst_blue_run_f32(int M, int howmany, float* data) { run_blue<float>(M, howmany, data); }
 
 extern "C" void dst_core_run_f64(int M, int howmany, double* data) { run<double>(M, howmany, data); }
 extern "C" void dst_core_run_f32(int M, int howmany, float* data) { run<float>(M, howmany, data); }

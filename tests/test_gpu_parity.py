@@ -418,11 +418,40 @@ def test_step_stops_at_t_out_and_tend(qgwlib):
 
 def test_unsupported_configs_fail_loudly(qgwlib):
     deep = dict(C.cfg2(16, 257))  # more layers than the GPU kernels hold (256)
-    # NX = 22: half-length 11 (a prime beyond the radices 2, 3, 5, 7); NX = 99: odd
-    for bad in (dict(C.cfg1(64), NX=22), dict(C.cfg1(64), NX=99), dict(C.cfg1(64), bc_fac=-0.5), deep):
+    # periodic basins take the half-length FFT only: NX = 22 (half-length 11,
+    # a prime beyond the radices 2, 3, 5, 7) and odd NX are refused there
+    per = [dict(C.cfg1(22), bc_fac=-1.0), dict(C.cfg1(99), bc_fac=-1.0)]
+    for bad in per + [dict(C.cfg1(64), bc_fac=-0.5), deep]:
         with pytest.raises(qgwlib.QgwError) as e:
             qgwlib.Run(bad)
         assert e.value.status == -6
+
+
+@pytest.mark.parametrize("case", ["nx22", "nx99_ny70", "nx64_ny26_hyper"])
+def test_chirp_z_grids_vs_port(qgwlib, oracle_mod, case):
+    """Closed-basin grids the half-length FFT cannot take run the chirp-z
+    (Bluestein) DST-I: NX = 22 (M/2 = 11, prime), NX = 99 (odd) with
+    NY = 70 (a half-length grid in y), NY = 26 (M/2 = 13) with the
+    biharmonic chain.  FP64 against the port (whose DST of these lengths is
+    the direct sum), FP32c against FP64."""
+    p = {"nx22": C.cfg1(22), "nx99_ny70": dict(C.cfg1(99), NY=70),
+         "nx64_ny26_hyper": dict(C.cfg2(64, 5), NY=26)}[case]
+    q0 = C.noise_ic(p, 1301)
+    o = oracle_mod.run_port(p, q0, 20, dt_fixed=p["dt"])
+    psi, q, _ = gpu_run(qgwlib, p, q0, 20, p["dt"])
+    assert rel(q, o["q"]) <= TOL64, rel(q, o["q"])
+    assert rel(psi, o["psi"]) <= TOL64, rel(psi, o["psi"])
+    psi32, q32, _ = gpu_run(qgwlib, p, q0, 20, p["dt"], precision=1)
+    assert rel(q32, q) <= TOL32C, rel(q32, q)
+    assert rel(psi32, psi) <= TOL32C, rel(psi32, psi)
+
+
+def test_chirp_z_grids_run_alone(qgwlib):
+    """The batched kernels hold the half-length transforms only: an ensemble
+    with a chirp-z member is refused (the member runs alone)."""
+    with pytest.raises(qgwlib.QgwError) as e:
+        qgwlib.Ensemble([C.cfg1(64), C.cfg1(22)], 0)
+    assert e.value.status == -6
 
 
 @pytest.mark.parametrize("nl", [40, 100])

@@ -153,6 +153,8 @@ def dstcore(tmp_path_factory):
     lib.dst_core_run_f64.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
     lib.dst_core_run_f32.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
     lib.dst_warp_run_f32.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    lib.dst_blue_run_f64.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    lib.dst_blue_run_f32.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
     return lib
 
 
@@ -184,6 +186,21 @@ def test_warp_dst_on_host(dstcore, M):
         yf = row.astype(np.float32).copy()
         assert dstcore.dst_warp_run_f32(M, 1, yf.ctypes.data) == 1
         assert np.linalg.norm(yf - ref) <= 1e-5 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("M", [5, 9, 22, 23, 26, 99, 101, 998, 1001, 64, 1024])
+def test_chirp_z_dst_on_host(dstcore, M):
+    """The chirp-z (Bluestein) DST-I of lengths the half-length FFT cannot
+    take (odd M; M/2 = 11, 13, 499) -- and of two it can, as a check of the
+    form itself -- against scipy's DST-I."""
+    x = np.random.default_rng(M + 7).standard_normal((3, M - 1))
+    ref = sf.dst(x, type=1, axis=1)
+    y = x.copy()
+    dstcore.dst_blue_run_f64(M, 3, y.ctypes.data)
+    assert np.linalg.norm(y - ref) <= 1e-14 * np.linalg.norm(ref), np.linalg.norm(y - ref) / np.linalg.norm(ref)
+    yf = x.astype(np.float32)
+    dstcore.dst_blue_run_f32(M, 3, yf.ctypes.data)
+    assert np.linalg.norm(yf - ref) <= 2e-6 * np.linalg.norm(ref), np.linalg.norm(yf - ref) / np.linalg.norm(ref)
 
 
 def test_supported_transform_lengths(dstcore):
