@@ -142,9 +142,13 @@ int qgw_topo(const qgw_params* p, double* topo);
  * analytic shelf of qgw_topo() when h_topo != 0); otherwise it is a
  * (ny+2, nx+2) reference-layout array.  The time scalars start as the
  * reference's init_timestep leaves them (src/timestep.h:56-67), or at the
- * fixed dt when p->dt > 0.  q starts at zero.  Grids: NX and NY even, up to
- * 8192, with NX/2 and NY/2 products of 2, 3, 5 and 7 (the transforms'
- * radices); periodic grids square; 1..32 layers.  Anything else returns
+ * fixed dt when p->dt > 0.  q starts at zero.  Grids: 4 <= NX, NY <= 8192.
+ * Closed basins take any size: where NX or NY is even with NX/2 (NY/2) a
+ * product of 2, 3, 5 and 7 the transform is a half-length FFT, otherwise a
+ * chirp-z transform of power-of-two length (slower; such runs are refused by
+ * ensembles and the serving pool).  Periodic grids square, NX even with NX/2
+ * a product of 2, 3, 5 and 7.  1..QGW_NL_GPU_MAX layers.  Anything else, or
+ * a grid whose kernels need more shared memory than a block has, returns
  * QGW_ERR_UNSUPPORTED. */
 int qgw_create(const qgw_params* p, const double* cl2m, const double* cm2l,
                const double* iRd2, const double* topo, int precision,
@@ -267,8 +271,8 @@ int qgw_get_shape(qgw_run* run, qgw_shape* shape);
  * it.  cl2m, cm2l, iRd2 are host arrays (e.g. from qgw_eigmode).  Scratch
  * is one file-scope device array of 32 MiB held by every GPU that loads the
  * library.  Accepted: closed basins (bc_fac >= 0; the periodic basin is
- * QGW_ERR_UNSUPPORTED here) on grids the run path accepts (NX, NY even, NX/2
- * and NY/2 products of 2, 3, 5 and 7) with 4 <= NX, NY <= 1024, 1 <= nl <= 32
+ * QGW_ERR_UNSUPPORTED here) on the half-length grids of the run path (NX,
+ * NY even, NX/2 and NY/2 products of 2, 3, 5 and 7) with 4 <= NX, NY <= 1024, 1 <= nl <= 32
  * and nl*(NX+1)*(NY+1) <= 2097152; anything else returns
  * QGW_ERR_UNSUPPORTED.  A launch error already pending in the calling thread
  * makes the call return QGW_ERR_CUDA without clearing it.  The first call on
