@@ -464,13 +464,18 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   // column tiles of 32-byte rows, or 16-byte rows where the former's
   // buffers would pass 200 KiB of shared memory (long columns with the
   // second spectral field: FP32 NY = 2048 in zeta mode) and for the chirp-z
-  // form's columns (its kernel is built for the narrower tiles alone)
-  if (a.gy.blue) a.CT = (32 / (int)sizeof(T)) / 2;
+  // form's columns (its kernel is built for the narrower tiles alone), whose
+  // long buffers (two per column) take one column per tile where 16-byte rows
+  // would pass 200 KiB (chirp-z lengths above 512 in FP32c, 1024 in FP64)
   {
-    size_t need;
-    if constexpr (sizeof(T) == 8) need = qgw::smem_bytes_cols_f64(a);
-    else need = qgw::smem_bytes_cols_f32c(a);
-    if (need > (size_t)200 * 1024) a.CT = (32 / (int)sizeof(T)) / 2;
+    auto need = [&]() -> size_t {
+      if constexpr (sizeof(T) == 8) return qgw::smem_bytes_cols_f64(a);
+      else return qgw::smem_bytes_cols_f32c(a);
+    };
+    const size_t limit = (size_t)200 * 1024;
+    if (a.gy.blue) a.CT = (32 / (int)sizeof(T)) / 2;
+    if (need() > limit) a.CT = (32 / (int)sizeof(T)) / 2;
+    if (a.gy.blue && need() > limit) a.CT = 1;
   }
   // TMA tensor maps of the RHS kernel's tiles (psi with halo R, q with halo
   // 1, in zeta mode 1 zeta over the first sweep's region; zeta mode 2 reads
@@ -481,6 +486,11 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   a.rhs_ty = 16;
   if (const char* e = std::getenv("QGW_RHS_TILE_ROWS")) a.rhs_ty = std::atoi(e) == 32 ? 32 : 16;
   encode_rhs_maps<T>(r, a);
+  // K3 over rows x layer groups in FP64 (measured at 1024^2 x 10: 0.575 ->
+  // 0.552 ms); the FP32c kernel keeps one block per row (0.109 against 0.123
+  // ms split).  QGW_INV_SPLIT=0/1 overrides.
+  a.inv_split = sizeof(T) == 8;
+  if (const char* e = std::getenv("QGW_INV_SPLIT")) a.inv_split = std::atoi(e) != 0;
   // QGW_TEST_FIRST_WAIT_ITERS (tests of the timeout path only) lowers the
   // limit of the first wait for a tile's TMA bytes, down to 0 polls; the
   // second wait keeps the full limit, so the bytes still land before the
@@ -505,9 +515,13 @@ int set_shape(qgw_run* r, StepArgs<T>& a, const qgw_shape& sh) {
   }
   const int ctd = 32 / (int)sizeof(T);
   if (sh.col_tile) {
-    if (sh.col_tile != ctd && sh.col_tile != ctd / 2) return QGW_ERR_PARAM;
-    if (a.gy.blue && sh.col_tile != ctd / 2) return QGW_ERR_PARAM;  // the chirp-z columns' one width
-    b.CT = sh.col_tile == ctd ? 0 : sh.col_tile;
+    if (a.gy.blue) {
+      // the chirp-z columns keep the width chosen at creation
+      if (sh.col_tile != a.CT) return QGW_ERR_PARAM;
+    } else {
+      if (sh.col_tile != ctd && sh.col_tile != ctd / 2) return QGW_ERR_PARAM;
+      b.CT = sh.col_tile == ctd ? 0 : sh.col_tile;
+    }
   }
   const bool per = a.periodic != 0;
   const int bufs_x = (!per && !a.gx.blue && qgw::warp_dst_len(a.gx.H, (int)sizeof(T))) ? 1 : 2;

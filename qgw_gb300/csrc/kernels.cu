@@ -32,11 +32,14 @@ __global__ void __launch_bounds__(NT, 3) k_cols(StepArgs<T> a, int step_mode) {
   else body_cols<T, COMP, CT, HL>(a, step_mode, blockIdx.x, blockIdx.y, smem_raw, tot);
 }
 template <typename T> constexpr int CTD = ColsPer<T>::value;
+// FP32: four blocks per SM (64 registers; at 1024^2 x 10 the kernel drops
+// from 0.109 to 0.101 ms); FP64 keeps three (64 registers spill there)
 template <typename T, bool COMP, bool PER, int HL>
-__global__ void __launch_bounds__(NT, 3) k_rows_inv(StepArgs<T> a, int step_mode) {
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 4 : 3) k_rows_inv(StepArgs<T> a, int step_mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ T tot[GMAX * 32];
-  body_rows_inv<T, COMP, PER, HL>(a, step_mode, blockIdx.x, smem_raw + cst_bytes<T>(a.nl), tot, (T*)smem_raw);
+  body_rows_inv<T, COMP, PER, HL>(a, step_mode, blockIdx.x, smem_raw + cst_bytes<T>(a.nl), tot, (T*)smem_raw,
+                                  gridDim.y > 1 ? (int)blockIdx.y : -1);
 }
 // The RHS of a step: a persistent grid (a.rhs_grid blocks) over the
 // ntx x nty x nl tiles (body_rhs_tiles); the FP64 path launches one block
@@ -340,7 +343,7 @@ static cudaError_t set_attrs(const StepArgs<T>& a) {
       (const void*)k_cols<T, COMP, false, CTD<T>, 0>,     (const void*)k_cols<T, COMP, false, CTD<T>, 512>,
       (const void*)k_cols<T, COMP, false, CTD<T> / 2, 0>, (const void*)k_cols<T, COMP, false, CTD<T> / 2, 512>,
       (const void*)k_rows_fwd<T, COMP, false, -1>,        (const void*)k_rows_inv<T, COMP, false, -1>,
-      (const void*)k_cols<T, COMP, false, CTD<T> / 2, -1>,
+      (const void*)k_cols<T, COMP, false, CTD<T> / 2, -1>, (const void*)k_cols<T, COMP, false, 1, -1>,
       (const void*)k_rows_fwd<T, COMP, true, 0>,          (const void*)k_rows_inv<T, COMP, true, 0>,
       (const void*)k_cols<T, COMP, true, CTD<T>, 0>};
   for (const void* f : transforms)
@@ -371,6 +374,7 @@ static void launch_k2(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
   const size_t sm = smem_cols<T, COMP>(a);
   const bool wide = col_width(a) == CTD<T>, h512 = a.gy.H == 512 && !a.gy.blue;
   if (a.periodic) k_cols<T, COMP, true, CTD<T>, 0><<<grid, NT, sm, s>>>(a, step_mode);
+  else if (a.gy.blue && col_width(a) == 1) k_cols<T, COMP, false, 1, -1><<<grid, NT, sm, s>>>(a, step_mode);
   else if (a.gy.blue) k_cols<T, COMP, false, CTD<T> / 2, -1><<<grid, NT, sm, s>>>(a, step_mode);
   else if (wide && h512) k_cols<T, COMP, false, CTD<T>, 512><<<grid, NT, sm, s>>>(a, step_mode);
   else if (wide) k_cols<T, COMP, false, CTD<T>, 0><<<grid, NT, sm, s>>>(a, step_mode);
@@ -380,10 +384,13 @@ static void launch_k2(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
 template <typename T, bool COMP>
 static void launch_k3(const StepArgs<T>& a, int step_mode, cudaStream_t s) {
   const size_t sm = smem_rows_inv<T, COMP>(a);
-  if (a.periodic) k_rows_inv<T, COMP, true, 0><<<dim3(a.ny), NT, sm, s>>>(a, step_mode);
-  else if (a.gx.blue) k_rows_inv<T, COMP, false, -1><<<dim3(a.ny), NT, sm, s>>>(a, step_mode);
-  else if (a.gx.H == 512) k_rows_inv<T, COMP, false, 512><<<dim3(a.ny), NT, sm, s>>>(a, step_mode);
-  else k_rows_inv<T, COMP, false, 0><<<dim3(a.ny), NT, sm, s>>>(a, step_mode);
+  // rows x layer groups: a row's groups read the same spectral rows, so
+  // splitting them over blocks adds no traffic and evens out the SMs' loads
+  const dim3 grid(a.ny, a.inv_split ? (a.nl + a.G3 - 1) / a.G3 : 1);
+  if (a.periodic) k_rows_inv<T, COMP, true, 0><<<grid, NT, sm, s>>>(a, step_mode);
+  else if (a.gx.blue) k_rows_inv<T, COMP, false, -1><<<grid, NT, sm, s>>>(a, step_mode);
+  else if (a.gx.H == 512) k_rows_inv<T, COMP, false, 512><<<grid, NT, sm, s>>>(a, step_mode);
+  else k_rows_inv<T, COMP, false, 0><<<grid, NT, sm, s>>>(a, step_mode);
 }
 // tiles of the RHS kernel along x and y
 template <typename T> static int rhs_ntx(const StepArgs<T>& a) { return (a.nx + TX - 1) / TX; }

@@ -151,8 +151,11 @@ template <typename T> struct StepArgs {
   // the element-wise asynchronous copies instead
   CUtensorMap tm[3];
   int use_tma;
-  int rhs_grid;
-  int rhs_ty;  // RHS tile height: 16 (default) or 32 rows                    // blocks of the persistent RHS kernel (0: one per tile)
+  int rhs_grid;  // blocks of the persistent RHS kernel (0: one per tile)
+  int rhs_ty;    // RHS tile height: 16 (default) or 32 rows
+  // K3 grid: 1 = one block per (row, layer group), 0 = one block per row
+  // that runs the row's layer groups in turn (same arithmetic per layer)
+  int inv_split;
   // iterations of the first bounded wait for a tile's TMA bytes (normally
   // kWaitIters; lowered only by tests, to make that wait run out -- the
   // second wait, which lets the bytes land before the block moves on, always

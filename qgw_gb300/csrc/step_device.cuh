@@ -48,14 +48,13 @@ constexpr int TX = 32, TYD = 16;  // RHS tile (interior points): width, default 
 constexpr double TEPS = 1e-9;    // src/timestep.h:16
 constexpr double HUGEV = 1e30;   // src/qg.c:43
 
-// columns per block of the column kernel (one or two 16-byte vectors per row):
-// four, so that the three work buffers of the compensated path leave room
-// for four blocks per SM
 // columns per K2 tile: 32-byte rows of FP32 (8) and FP64 (4) values by
-// default, 16-byte rows (half as many columns) as the alternative
+// default, 16-byte rows (half as many columns) as the alternative, and one
+// column per tile for the chirp-z columns whose two buffers per column leave
+// no room for more
 template <typename T> struct ColsPer { static constexpr int value = 32 / (int)sizeof(T); };
 template <typename T> __host__ __device__ inline int col_width(const StepArgs<T>& a) {
-  return a.CT == ColsPer<T>::value / 2 ? a.CT : ColsPer<T>::value;
+  return (a.CT == ColsPer<T>::value / 2 || a.CT == 1) ? a.CT : ColsPer<T>::value;
 }
 
 // --------------------------------------------------------------- DST block
@@ -620,7 +619,9 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
   // Thread t takes the points jj = t - 1 + u NT (tile index jj + 1 = t +
   // u NT), so that each warp's shared-memory accesses cover whole 128-byte
   // pad periods (one wavefront per access).
-  const bool vec = a.vec_cols != 0;
+  // (a one-column tile, narrower than a vector, reads element by element)
+  constexpr bool VEC = CT * sizeof(T) % 16 == 0;
+  const bool vec = VEC && a.vec_cols != 0;
   for (int j0 = threadIdx.x - 1; j0 < ny; j0 += RB * NT) {
     T vv[RB][CT];
 #pragma unroll
@@ -628,9 +629,13 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
       const int jj = j0 + u * NT;
       if (jj >= 0 && jj < ny) {
         const T* src = S + (size_t)jj * a.pitch + k0;
-        if (vec) load_cols_stream<T, CT>(src, vv[u]);
-        else
-          for (int c = 0; c < CT; ++c) vv[u][c] = c < CTb ? src[c] : T(0);
+        if constexpr (VEC) {
+          if (vec) {
+            load_cols_stream<T, CT>(src, vv[u]);
+            continue;
+          }
+        }
+        for (int c = 0; c < CT; ++c) vv[u][c] = c < CTb ? src[c] : T(0);
       }
     }
 #pragma unroll
@@ -670,9 +675,13 @@ __device__ __forceinline__ void body_cols(const StepArgs<T>& a, int step_mode, i
       if (jj < 0 || jj >= ny) continue;
       if (!COMP) {
         const T* hrow = (const T*)(a.hinv + (size_t)m * a.lstride + (size_t)jj * a.pitch + k0);
-        if (vec) load_cols<T, CT>(hrow, h4[u]);
-        else
-          for (int c = 0; c < CT; ++c) h4[u][c] = c < CTb ? hrow[c] : T(0);
+        if constexpr (VEC) {
+          if (vec) {
+            load_cols<T, CT>(hrow, h4[u]);
+            continue;
+          }
+        }
+        for (int c = 0; c < CT; ++c) h4[u][c] = c < CTb ? hrow[c] : T(0);
       } else {
         ksq4[u] = a.Ksqf[jj];
         sy4[u] = zm ? a.sy2f[jj] : 0.f;
@@ -904,9 +913,11 @@ __device__ __forceinline__ void project_spec(const StepArgs<T>& a, int j, int G,
   }
 }
 
+// only >= 0: this block takes layer group `only` of row j alone (a K3 grid
+// of rows x groups); only < 0: it takes every group of the row in turn
 template <typename T, bool COMP, bool PER, int HL = 0>
 __device__ __forceinline__ void body_rows_inv(const StepArgs<T>& a, int step_mode, int j, unsigned char* smem_raw,
-                                              T* tot, T* cst) {
+                                              T* tot, T* cst, int only = -1) {
   DevState* st = a.state;
   if (step_mode && !st->active) return;
   const int ld = row_len<T>(a.gx);
@@ -918,7 +929,8 @@ __device__ __forceinline__ void body_rows_inv(const StepArgs<T>& a, int step_mod
   if (!PER) prefetch_tables_l1(a.tx, a.gx.M);
   // ceil(nl / Gb) layer groups of balanced sizes (at most Gb each)
   const int ng = (a.nl + Gb - 1) / Gb, gq = a.nl / ng, gr = a.nl - gq * ng;
-  for (int gi = 0, l0 = 0; gi < ng; l0 += gq + (gi < gr), ++gi) {
+  const int g_begin = only < 0 ? 0 : only, g_end = only < 0 ? ng : min(only + 1, ng);
+  for (int gi = g_begin, l0 = g_begin * gq + min(g_begin, gr); gi < g_end; l0 += gq + (gi < gr), ++gi) {
     const int G = gq + (gi < gr);
     for (int w = threadIdx.x; w < a.nl * GMAX; w += NT) {
       const int m = w / GMAX, g = w - m * GMAX;

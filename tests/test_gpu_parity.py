@@ -421,21 +421,30 @@ def test_unsupported_configs_fail_loudly(qgwlib):
     # periodic basins take the half-length FFT only: NX = 22 (half-length 11,
     # a prime beyond the radices 2, 3, 5, 7) and odd NX are refused there
     per = [dict(C.cfg1(22), bc_fac=-1.0), dict(C.cfg1(99), bc_fac=-1.0)]
-    for bad in per + [dict(C.cfg1(64), bc_fac=-0.5), deep]:
+    # a chirp-z length above 2048 (NX = 2050: convolution length 8192): one
+    # row's two buffers exceed a block's shared memory
+    long_chirp = dict(C.cfg1(2050), NY=64)
+    for bad in per + [dict(C.cfg1(64), bc_fac=-0.5), deep, long_chirp]:
         with pytest.raises(qgwlib.QgwError) as e:
             qgwlib.Run(bad)
         assert e.value.status == -6
 
 
-@pytest.mark.parametrize("case", ["nx22", "nx99_ny70", "nx64_ny26_hyper"])
+@pytest.mark.parametrize("case", ["nx22", "nx99_ny70", "nx64_ny26_hyper", "nx64_ny514_hyper",
+                                  "nx32_ny1030_hyper"])
 def test_chirp_z_grids_vs_port(qgwlib, oracle_mod, case):
     """Closed-basin grids the half-length FFT cannot take run the chirp-z
     (Bluestein) DST-I: NX = 22 (M/2 = 11, prime), NX = 99 (odd) with
     NY = 70 (a half-length grid in y), NY = 26 (M/2 = 13) with the
-    biharmonic chain.  FP64 against the port (whose DST of these lengths is
-    the direct sum), FP32c against FP64."""
+    biharmonic chain.  NY = 514 (M/2 = 257, convolution length 2048) and
+    NY = 1030 (M/2 = 515 = 5 * 103, length 4096) run the chirp-z columns one
+    column per tile (FP32c at 514, both precisions at 1030), the width their
+    two buffers per column leave room for.  FP64 against the port (whose DST
+    of these lengths is the direct sum), FP32c against FP64."""
     p = {"nx22": C.cfg1(22), "nx99_ny70": dict(C.cfg1(99), NY=70),
-         "nx64_ny26_hyper": dict(C.cfg2(64, 5), NY=26)}[case]
+         "nx64_ny26_hyper": dict(C.cfg2(64, 5), NY=26),
+         "nx64_ny514_hyper": dict(C.cfg2(64, 5), NY=514),
+         "nx32_ny1030_hyper": dict(C.cfg2(32, 5), NY=1030)}[case]
     q0 = C.noise_ic(p, 1301)
     o = oracle_mod.run_port(p, q0, 20, dt_fixed=p["dt"])
     psi, q, _ = gpu_run(qgwlib, p, q0, 20, p["dt"])

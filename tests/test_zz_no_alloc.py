@@ -103,14 +103,16 @@ def test_noalloc_set_ups_alternate(qgwlib):
         _noalloc_vs_library(qgwlib, torch, p, 20 + k)
 
 
-@pytest.mark.parametrize("case", ["oversize", "periodic", "prime_half_length"])
+@pytest.mark.parametrize("case", ["oversize", "periodic", "prime_half_length", "odd"])
 def test_noalloc_rejects_what_it_cannot_hold(qgwlib, case):
     """QGW_ERR_UNSUPPORTED before any device work (the array arguments are
     never touched): 10 * 1025^2 doubles exceed the scratch array; the
-    periodic basin; NX = 2 * 11, a half-length the transforms do not take."""
+    periodic basin; NX = 2 * 11 and NY = 99, lengths that the run path takes
+    as chirp-z transforms and the allocation-free path does not hold."""
     lib = qgwlib.load()
     p = {"oversize": C.cfg2(1024, 10), "periodic": dict(C.cfg1(64), bc_fac=-1.0),
-         "prime_half_length": dict(C.cfg1(64), NX=22)}[case]
+         "prime_half_length": dict(C.cfg1(64), NX=22),
+         "odd": dict(C.cfg1(64), NY=99)}[case]
     s = to_struct(p)
     cl, cm, ird = qgwlib.eigmode(p)
     fn = lib.qgw_invert_pv_noalloc
