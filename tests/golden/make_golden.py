@@ -116,6 +116,13 @@ def cases():
     p["dh"] = [float(f"{x:.6g}") for x in p["dh"]]
     p["N2"] = [float(f"{x:.6g}") for x in p["N2"]]
     out.append(("cfg2_nx32_nl20_hyper", p, 40, 600.0, None))
+    # lengths whose half-length FFT would need a radix above 7, or that are
+    # odd (FFTW plans them; the GPU runs them as chirp-z transforms): 22^2
+    # (half-length 11), 45 x 26 with hyperviscosity (odd; half-length 13)
+    out.append(("chirp_z_nx22", C.cfg1(22), 40, 1200.0, None))
+    p = C.cfg2(45, 5)
+    p["NY"] = 26
+    out.append(("chirp_z_nx45_ny26_hyper", p, 40, 600.0, None))
     return out
 
 
