@@ -244,7 +244,8 @@ int qgw_profile_kernels(qgw_run* run, int nsteps, float* ms4);
 /* Work-tile shape of a run's step kernels (no counterpart in the
  * reference, which has no tiles): rhs_tile_rows, the RHS tile height (16 or
  * 32 rows); col_tile, columns per tile of the column transform (FP32: 8 or
- * 4, FP64: 4 or 2); row_group_fwd and row_group_inv, modes (layers) per
+ * 4, FP64: 4 or 2; a chirp-z NY keeps the width chosen at creation, 4 or 1
+ * in FP32 and 2 or 1 in FP64); row_group_fwd and row_group_inv, modes (layers) per
  * block of the forward and inverse row kernels (1..16, balanced over the
  * run's layers; the inverse kernel takes at most 8 when it also transforms
  * zeta).  0 keeps a value.  No choice changes the arithmetic: a run's
