@@ -63,6 +63,23 @@ def test_pool_admission_by_footprint(qgwlib):
     pool.close()
 
 
+def test_pool_refuses_chirp_z_grids(qgwlib):
+    """The pool batches runs through the ensemble kernels, which hold the
+    half-length transforms only: a request on a grid that needs the chirp-z
+    transform (NX = 22, half-length 11) ends with QGW_ERR_UNSUPPORTED, and
+    the requests around it still complete."""
+    pool = qgwlib.Pool(steps_per_tick=4)
+    ok = C.cfg1(64)
+    chirp = C.cfg1(22)
+    a = pool.submit(ok, C.noise_ic(ok, 3), 0, 8)
+    b = pool.submit(chirp, C.noise_ic(chirp, 4), 0, 8)
+    c = pool.submit(ok, C.noise_ic(ok, 5), 1, 8)
+    assert pool.poll(a, wait_ms=60000) == 0
+    assert pool.poll(b, wait_ms=60000) == -6  # QGW_ERR_UNSUPPORTED
+    assert pool.poll(c, wait_ms=60000) == 0
+    pool.close()
+
+
 def test_pool_concurrent_submitters(qgwlib):
     pool = qgwlib.Pool(steps_per_tick=16)
     out = {}
