@@ -464,9 +464,10 @@ int setup_args(qgw_run* r, StepArgs<T>& a) {
   // column tiles of 32-byte rows, or 16-byte rows where the former's
   // buffers would pass 200 KiB of shared memory (long columns with the
   // second spectral field: FP32 NY = 2048 in zeta mode) and for the chirp-z
-  // form's columns (its kernel is built for the narrower tiles alone), whose
-  // long buffers (two per column) take one column per tile where 16-byte rows
-  // would pass 200 KiB (chirp-z lengths above 512 in FP32c, 1024 in FP64)
+  // form's columns (its kernels are built for 16-byte tiles and for one
+  // column per tile), whose long buffers (two per column) take one column per
+  // tile where 16-byte rows would pass 200 KiB (chirp-z lengths above 512 in
+  // FP32c, 1024 in FP64)
   {
     auto need = [&]() -> size_t {
       if constexpr (sizeof(T) == 8) return qgw::smem_bytes_cols_f64(a);

@@ -854,13 +854,15 @@ __device__ __forceinline__ void body_cols_per(const StepArgs<T>& a, int step_mod
 }
 
 // ------------------------------------------------------------------ K3
-// One block per row j; LAYER groups in turn.  The mode -> layer projection
-// is linear and acts point by point, so it commutes with the x-DST: each
-// group first forms the spectral rows of its layers, sum_m cm2l[l][m] *
-// spec_m (and of zeta from spec2 in zeta mode), then inverse-transforms them
-// and writes psi_l (zeta_l) once.  The spectral rows of row j are re-read by
-// each group (from cache); nothing is accumulated in global memory.  Column
-// i goes to index i + xo of its row (xo = 1: the DST's input format).
+// One block per row j with its LAYER groups in turn, or (a grid of rows x
+// groups, the FP64 default) one block per group of row j.  The mode -> layer
+// projection is linear and acts point by point, so it commutes with the
+// x-DST: each group first forms the spectral rows of its layers,
+// sum_m cm2l[l][m] * spec_m (and of zeta from spec2 in zeta mode), then
+// inverse-transforms them and writes psi_l (zeta_l) once.  The spectral rows
+// of row j are re-read by each group (from cache); nothing is accumulated in
+// global memory.  Column i goes to index i + xo of its row (xo = 1: the
+// DST's input format).
 template <typename T, bool ZM, int GB>
 __device__ __forceinline__ void project_spec(const StepArgs<T>& a, int j, int G, T* A, int ld, const T* cst,
                                              int ncols, int xo) {
