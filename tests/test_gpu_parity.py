@@ -455,6 +455,24 @@ def test_chirp_z_grids_vs_port(qgwlib, oracle_mod, case):
     assert rel(psi32, psi) <= TOL32C, rel(psi32, psi)
 
 
+@pytest.mark.parametrize("case", ["nx8_ny6", "nx5_ny7_chirp", "periodic_nx8"])
+def test_smallest_grids_vs_port(qgwlib, oracle_mod, case):
+    """Grids far below one RHS tile (32 x 16 points): 8 x 6 (half-lengths 4
+    and 3), 5 x 7 (odd: chirp-z transforms of length 16 in both directions)
+    and the periodic 8^2 basin, the smallest the real FFT takes.  FP64
+    against the port, FP32c against FP64."""
+    p = {"nx8_ny6": dict(C.cfg1(8), NY=6), "nx5_ny7_chirp": dict(C.cfg1(5), NY=7),
+         "periodic_nx8": dict(C.cfg1(8), bc_fac=-1.0)}[case]
+    q0 = C.noise_ic(p, 1402)
+    o = oracle_mod.run_port(p, q0, 20, dt_fixed=p["dt"])
+    psi, q, _ = gpu_run(qgwlib, p, q0, 20, p["dt"])
+    assert rel(q, o["q"]) <= TOL64, rel(q, o["q"])
+    assert rel(psi, o["psi"]) <= TOL64, rel(psi, o["psi"])
+    psi32, q32, _ = gpu_run(qgwlib, p, q0, 20, p["dt"], precision=1)
+    assert rel(q32, q) <= TOL32C, rel(q32, q)
+    assert rel(psi32, psi) <= TOL32C, rel(psi32, psi)
+
+
 def test_chirp_z_grids_run_alone(qgwlib):
     """The batched kernels hold the half-length transforms only: an ensemble
     with a chirp-z member is refused (the member runs alone)."""

@@ -204,8 +204,9 @@ def test_chirp_z_dst_on_host(dstcore, M):
 
 
 def test_supported_transform_lengths(dstcore):
-    """Even lengths whose half factors into 2, 3, 5 and 7 run on the GPU; the
-    rest is refused (QGW_ERR_UNSUPPORTED at qgw_create)."""
+    """Even lengths whose half factors into 2, 3, 5 and 7 take the half-length
+    FFT; closed basins run the rest as chirp-z transforms, and the periodic
+    basin refuses them (QGW_ERR_UNSUPPORTED at qgw_create)."""
     def smooth(n):
         for f in (2, 3, 5, 7):
             while n % f == 0:
