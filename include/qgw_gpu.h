@@ -124,7 +124,10 @@ int qgw_params_read(qgw_params* p, const char* path);
 /* Vertical modes of the stretching matrix: replaces compute_eigmode,
  * src/eigmode.h:87-271 (LAPACKE_dgeev there, the implicit-QL
  * symmetric-tridiagonal solver here; the Flierl normalisation makes both
- * give the same result).  cl2m, cm2l are nl*nl row-major, iRd2 has nl entries. */
+ * give the same result, up to the sign of a mode trapped at depth, whose
+ * surface value -- the sign rule -- is at round-off level; such a flip of a
+ * mode's cm2l column and cl2m row together changes no result).  cl2m, cm2l
+ * are nl*nl row-major, iRd2 has nl entries. */
 int qgw_eigmode(const qgw_params* p, double* cl2m, double* cm2l, double* iRd2);
 
 /* Maximum and initial time step: replaces check_timestep,

@@ -197,7 +197,24 @@ extern "C" int qgw_eigmode(const qgw_params* p, double* cl2m, double* cm2l, doub
     if (!(up * lo > 0)) return QGW_ERR_EIGEN;
     e[l] = (up < 0 ? -1.0 : 1.0) * std::sqrt(up * lo);
   }
-  if (qgw_host::tql2(nl, d.data(), e.data(), z.data())) return QGW_ERR_EIGEN;
+  // The QL iteration keeps its accuracy on a strongly graded matrix only
+  // with the large entries last.  Thin, strongly stratified upper layers put
+  // them first (many stretched layers: couplings falling by 1e6..1e10 from
+  // top to bottom), so where the couplings fall by more than 1e3 the matrix
+  // is solved in reversed layer order and the vectors are mapped back.
+  const bool reverse = std::fabs(e[1]) > 1e3 * std::fabs(e[nl - 1]);
+  if (reverse) {
+    std::vector<double> dr(nl), er(nl, 0.0);
+    for (int i = 0; i < nl; ++i) dr[i] = d[nl - 1 - i];
+    for (int i = 1; i < nl; ++i) er[i] = e[nl - i];
+    if (qgw_host::tql2(nl, dr.data(), er.data(), z.data())) return QGW_ERR_EIGEN;
+    d = dr;
+    std::vector<double> zr(z);
+    for (int k = 0; k < nl; ++k)
+      for (int m = 0; m < nl; ++m) z[(size_t)k * nl + m] = zr[(size_t)(nl - 1 - k) * nl + m];
+  } else if (qgw_host::tql2(nl, d.data(), e.data(), z.data())) {
+    return QGW_ERR_EIGEN;
+  }
   // ascending order
   std::vector<int> ord(nl);
   for (int m = 0; m < nl; ++m) ord[m] = m;

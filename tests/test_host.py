@@ -94,6 +94,77 @@ def test_eigmode_matches_oracle(qgwlib, oracle_mod, nl):
     assert np.allclose(ird, oird, rtol=1e-11, atol=0)
 
 
+def _stretching(p):
+    """The stretching matrix of compute_eigmode (src/eigmode.h:107-119)."""
+    nl = p["nl"]
+    dh, n2, f0 = np.asarray(p["dh"], float), np.asarray(p["N2"], float), p["f0"]
+    dhc = 0.5 * (dh[:-1] + dh[1:])
+    g = np.zeros((nl, nl))
+    for l in range(nl):
+        if l < nl - 1:
+            g[l, l + 1] = -f0 ** 2 / (n2[l] * dhc[l] * dh[l])
+        if l > 0:
+            g[l, l - 1] = -f0 ** 2 / (n2[l - 1] * dhc[l - 1] * dh[l])
+        g[l, l] = -g[l].sum()
+    return g
+
+
+def _sign_free(cl, cm, ocl, ocm):
+    """Modes up to the sign of each mode.  The reference fixes a mode's sign
+    by its surface value (src/eigmode.h:210); a mode trapped at depth has a
+    surface value at round-off level (1e-17 .. 1e-27), whose sign any two
+    eigensolvers may choose differently.  A flip of column m of cm2l and row
+    m of cl2m together leaves every projection pair unchanged."""
+    s = np.sign(np.sum(cm * ocm, axis=0))
+    s[s == 0] = 1
+    return cl * s[:, None], cm * s[None, :]
+
+
+@pytest.mark.parametrize("nl", [40, 64, 100])
+def test_eigmode_many_graded_layers_matches_oracle(qgwlib, oracle_mod, nl):
+    """Many layers of the stretched profile (dh_k = dh_0 1.3^k): the top
+    layers get thin and strongly stratified, and the couplings fall by 1e3
+    to 1e10 from top to bottom; the solver then runs in reversed layer order
+    and keeps the oracle's Jacobi accuracy."""
+    p = C.basin_params(64, nl)
+    cl, cm, ird = qgwlib.eigmode(p)
+    ocl, ocm, oird = oracle_mod.Port(p).modes()
+    cl, cm = _sign_free(cl, cm, ocl, ocm)
+    assert np.abs(ird - oird).max() <= 1e-12 * oird.max()
+    assert np.all(np.diff(ird) > 0) and ird[0] == 0.0
+    assert np.abs(cm - ocm).max() <= 1e-11 * np.abs(ocm).max()
+    assert np.abs(cl - ocl).max() <= 1e-11 * np.abs(ocl).max()
+    assert np.abs(cl @ cm - np.eye(nl)).max() <= 1e-13
+
+
+@pytest.mark.parametrize("nl", [64, 128, 256])
+@pytest.mark.parametrize("profile", ["uniform", "stretched"])
+def test_eigmode_many_layers_invariants(qgwlib, oracle_mod, nl, profile):
+    """Up to the kernels' 256 layers on ocean-like profiles (uniform or
+    2%-per-layer stretched thicknesses, N2 decaying with depth): the vectors
+    solve the stretching problem, the two projections invert each other, and
+    the projection pairs agree with the oracle's (at 64 layers)."""
+    p = C.basin_params(64, nl)
+    w = np.ones(nl) if profile == "uniform" else 1.02 ** np.arange(nl)
+    dh = 4000.0 * w / w.sum()
+    z = np.cumsum(dh)[:-1]
+    p["dh"] = dh.tolist()
+    p["N2"] = (1e-5 * np.exp(-z / 800.0) + 1e-7).tolist()
+    cl, cm, ird = qgwlib.eigmode(p)
+    g = _stretching(p)
+    res = np.linalg.norm(g @ cm - cm * ird[None, :], axis=0) / np.linalg.norm(cm, axis=0)
+    assert res.max() <= 1e-13 * ird.max()
+    assert np.abs(cl @ cm - np.eye(nl)).max() <= 1e-13
+    assert np.all(np.diff(ird) > 0) and ird[0] == 0.0
+    if nl == 64:
+        ocl, ocm, oird = oracle_mod.Port(p).modes()
+        assert np.abs(ird - oird).max() <= 1e-12 * oird.max()
+        wts = np.random.default_rng(nl).standard_normal(nl)
+        a = cm @ np.diag(wts) @ cl
+        b = ocm @ np.diag(wts) @ ocl
+        assert np.abs(a - b).max() <= 1e-11 * np.abs(b).max()
+
+
 TIMESTEP_CASES = [
     C.cfg1(256), C.cfg2(1024),
     dict(C.cfg1(64), tau0=0.0), dict(C.cfg1(64), sigma_f=0.0), dict(C.cfg1(64), tau0=0.0, sigma_f=0.0),
