@@ -148,12 +148,14 @@ int qgw_topo(const qgw_params* p, double* topo);
  * fixed dt when p->dt > 0.  q starts at zero.  Grids: 4 <= NX, NY <= 8192.
  * Closed basins take any size: where NX or NY is even with NX/2 (NY/2) a
  * product of 2, 3, 5 and 7 the transform is a half-length FFT, otherwise a
- * chirp-z transform of power-of-two length (slower; up to 2048 points, whose
- * buffers still fit a block's shared memory; such runs are refused by
- * ensembles and the serving pool).  Periodic grids square, NX even with NX/2
- * a product of 2, 3, 5 and 7.  1..QGW_NL_GPU_MAX layers.  Anything else, or
- * a grid whose kernels need more shared memory than a block has, returns
- * QGW_ERR_UNSUPPORTED. */
+ * chirp-z transform of power-of-two length (slower; up to 2048 points;
+ * such runs are refused by ensembles and the serving pool).  Periodic grids
+ * square, NX even with NX/2 a product of 2, 3, 5 and 7.  1..QGW_NL_GPU_MAX
+ * layers.  The column kernel holds whole columns in shared memory, which
+ * bounds NY: closed basins NY <= 6300 (FP32C with hyperviscosity or bottom
+ * drag, whose second spectral field doubles the buffers: NY <= 3150);
+ * periodic NX = NY <= 3150 (FP64), 4200 (FP32C with that field) or 6300.
+ * Anything else returns QGW_ERR_UNSUPPORTED. */
 int qgw_create(const qgw_params* p, const double* cl2m, const double* cm2l,
                const double* iRd2, const double* topo, int precision,
                qgw_run** out);
